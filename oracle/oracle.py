@@ -1,0 +1,233 @@
+"""ctypes front end of the CPU oracle (oracle.c).
+
+Test infrastructure only: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py, never by the product package.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_U8 = C.POINTER(C.c_ubyte)
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc, a second or two)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "oracle.c"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_eam_from_knots.restype = C.c_void_p
+        L.orc_eam_from_knots.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D, _D, _D]
+        L.orc_eam_read_setfl.restype = C.c_void_p
+        L.orc_eam_read_setfl.argtypes = [C.c_char_p]
+        L.orc_eam_free.argtypes = [C.c_void_p]
+        L.orc_eam_info.argtypes = [C.c_void_p, _I, _I, _I, _D, _D]
+        L.orc_eam_tables.argtypes = [C.c_void_p, _D, _D, _D, _D]
+        L.orc_sys_new.restype = C.c_void_p
+        L.orc_sys_new.argtypes = [C.c_int, _D, _D, _U8, _D, C.c_double, C.c_void_p]
+        L.orc_sys_free.argtypes = [C.c_void_p]
+        for nm in ("orc_sys_set_x", "orc_sys_get_x", "orc_sys_set_v", "orc_sys_get_v", "orc_sys_get_f"):
+            getattr(L, nm).argtypes = [C.c_void_p, _D]
+        L.orc_sys_set_pair_wise.argtypes = [C.c_void_p, C.c_int]
+        L.orc_sys_nghost.argtypes = [C.c_void_p]
+        L.orc_sys_nrebuild.argtypes = [C.c_void_p]
+        L.orc_sys_init_dynamic.argtypes = [C.c_void_p]
+        L.orc_sys_update.argtypes = [C.c_void_p]
+        L.orc_sys_neighbors.restype = C.c_long
+        L.orc_sys_neighbors.argtypes = [C.c_void_p, _I, _I]
+        L.orc_sys_force.restype = C.c_double
+        L.orc_sys_force.argtypes = [C.c_void_p, _D]
+        L.orc_sys_force_full.restype = C.c_double
+        L.orc_sys_force_full.argtypes = [C.c_void_p, _D, C.c_int]
+        L.orc_sys_energy.restype = C.c_double
+        L.orc_sys_energy.argtypes = [C.c_void_p]
+        L.orc_sys_get_rho.argtypes = [C.c_void_p, _D, _D]
+        L.orc_md_nvt_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_int, C.c_int, C.c_int, _D, _D]
+        L.orc_lbfgs_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_double, C.c_double, C.c_int, _D]
+        L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+def _err():
+    return lib().orc_last_error().decode()
+
+
+class Eam:
+    """Spline tables built exactly as ImportEAM does (import_eam.h:348-613)."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise RuntimeError("oracle: " + _err())
+        self.h = handle
+        ne, nr, nrho = C.c_int(), C.c_int(), C.c_int()
+        dr, drho = C.c_double(), C.c_double()
+        lib().orc_eam_info(self.h, C.byref(ne), C.byref(nr), C.byref(nrho), C.byref(dr), C.byref(drho))
+        self.nelem, self.nr, self.nrho = ne.value, nr.value, nrho.value
+        self.dr, self.drho = dr.value, drho.value
+
+    @classmethod
+    def setfl(cls, path):
+        return cls(lib().orc_eam_read_setfl(os.fsencode(path)))
+
+    @classmethod
+    def knots(cls, nr, nrho, dr, drho, F, rho, rphi):
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        rphi = np.ascontiguousarray(rphi, dtype=np.float64)
+        ne = F.shape[0]
+        return cls(lib().orc_eam_from_knots(ne, nr, nrho, dr, drho, _dp(F), _dp(rho), _dp(rphi)))
+
+    def tables(self):
+        ne, nr, nrho = self.nelem, self.nr, self.nrho
+        F = np.zeros((ne, nrho, 4))
+        rho = np.zeros((ne, ne, nr, 4))
+        rphi = np.zeros((ne, ne, nr, 4))
+        cut = np.zeros((ne, ne))
+        lib().orc_eam_tables(self.h, _dp(F), _dp(rho), _dp(rphi), _dp(cut))
+        return F, rho, rphi, cut
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_eam_free(self.h)
+            self.h = None
+
+
+class System:
+    """One periodic cell on one rank (AtomsMD + ForceFieldEAM + DynamicMD)."""
+
+    def __init__(self, eam, H, x, elem, masses, skin=0.5, pair_wise=True):
+        self.eam = eam
+        H = np.ascontiguousarray(H, dtype=np.float64).reshape(3, 3)
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        self.elem = np.ascontiguousarray(elem, dtype=np.uint8)
+        self.masses = np.ascontiguousarray(masses, dtype=np.float64)
+        self.n = x.shape[0]
+        self.h = lib().orc_sys_new(self.n, _dp(H), _dp(x), self.elem.ctypes.data_as(_U8),
+                                   _dp(self.masses), skin, eam.h)
+        lib().orc_sys_set_pair_wise(self.h, 1 if pair_wise else 0)
+        self.initialized = False
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_sys_free(self.h)
+            self.h = None
+
+    def _get(self, fn):
+        a = np.zeros((self.n, 3))
+        fn(self.h, _dp(a))
+        return a
+
+    @property
+    def x(self):
+        return self._get(lib().orc_sys_get_x)
+
+    @x.setter
+    def x(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        lib().orc_sys_set_x(self.h, _dp(v))
+
+    @property
+    def v(self):
+        return self._get(lib().orc_sys_get_v)
+
+    @v.setter
+    def v(self, val):
+        val = np.ascontiguousarray(val, dtype=np.float64).reshape(-1, 3)
+        lib().orc_sys_set_v(self.h, _dp(val))
+
+    @property
+    def f(self):
+        return self._get(lib().orc_sys_get_f)
+
+    def init_dynamic(self):
+        if lib().orc_sys_init_dynamic(self.h) != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+
+    def force(self):
+        """ForceFieldMD::force_calc: returns (pe, virial F_H voigt[6]); forces in .f"""
+        if not self.initialized:
+            self.init_dynamic()
+        out = np.zeros(7)
+        lib().orc_sys_force(self.h, _dp(out))
+        return out[0], out[1:].copy()
+
+    def force_full(self, nthreads=1):
+        if not self.initialized:
+            self.init_dynamic()
+        out = np.zeros(7)
+        lib().orc_sys_force_full(self.h, _dp(out), int(nthreads))
+        return out[0], out[1:].copy()
+
+    def energy(self):
+        if not self.initialized:
+            self.init_dynamic()
+        return lib().orc_sys_energy(self.h)
+
+    def rho_dF(self):
+        rho = np.zeros(self.n)
+        dF = np.zeros(self.n)
+        lib().orc_sys_get_rho(self.h, _dp(rho), _dp(dF))
+        return rho, dF
+
+    def neighbors(self):
+        """Full/half list as a list (per local atom) of sorted (owner, n0, n1, n2) tuples."""
+        cnt = np.zeros(self.n, dtype=np.int32)
+        tot = lib().orc_sys_neighbors(self.h, cnt.ctypes.data_as(_I), None)
+        ent = np.zeros((tot, 4), dtype=np.int32)
+        lib().orc_sys_neighbors(self.h, cnt.ctypes.data_as(_I), ent.ctypes.data_as(_I))
+        return cnt, ent
+
+    def nvt_run(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None):
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        eta_a = np.zeros(max(L, 1)) if eta is None else np.ascontiguousarray(eta, dtype=np.float64)
+        thermo = np.zeros((nsteps + 1, 14))
+        r = lib().orc_md_nvt_run(self.h, T, dt, kB, t_relax, L, niters, nsteps, _dp(eta_a), _dp(thermo))
+        if r < 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return thermo, eta_a, r
+
+    def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=10000):
+        st = np.zeros(6)
+        r = lib().orc_lbfgs_run(self.h, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+
+def create_temp(elem, masses, T, kB, seed):
+    """AtomsMD::create_T restated (Park-Miller); seed 0 is rejected."""
+    elem = np.ascontiguousarray(elem, dtype=np.uint8)
+    masses = np.ascontiguousarray(masses, dtype=np.float64)
+    v = np.zeros((elem.shape[0], 3))
+    if lib().orc_create_temp(elem.shape[0], elem.ctypes.data_as(_U8), _dp(masses), T, kB, seed, _dp(v)):
+        raise ValueError("oracle: " + _err())
+    return v
