@@ -1,0 +1,339 @@
+"""EAM MD throughput benchmark (atom-steps/s).
+
+Workload: the 2,048,000-atom random 50/50 A/B alloy (FCC 80^3, a = 3.615 A,
+seed 1, 0.05 A Gaussian noise, 600 K velocities) on the analytic EAM of
+mapp4py_gb300.synth (setfl, nr = nrho = 5000, cutoff 5.5 A), NVT with the
+Nose-Hoover chain, dt = 1 fs, skin 0.5 A, mixed precision (FP32 pair math,
+FP64 state and reductions).  One step = one MD step of the whole cell.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Each rank runs its own replica of the cell on its own GPU (the path has no
+data exchange between cells); value = atoms * steps * N / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EAM MD atom-steps/s"
+N_CELLS = (80, 80, 80)
+T_K = 600.0
+KERNELS_PER_STEP = 13  # step_open, kick_drift, com_skin, 7 rebuild-chain, density, force, kick2
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(name):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary
+    (a line 'dram_bytes_per_launch: <bytes>' in profiles/<name>.md)."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while timing."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_cell():
+    from mapp4py_gb300 import synth
+
+    return synth.alloy(N_CELLS, xB=0.5, sigma=0.05, T=T_K, seed=1)
+
+
+def write_potential(d):
+    from mapp4py_gb300 import synth
+
+    return synth.write_setfl(os.path.join(d, "AB.setfl"), ("A", "B"))
+
+
+def cpu_baseline(path, cell, threads, steps=5, natoms_cap=256000):
+    """The oracle's multi-threaded restatement on a bounded sample: the
+    first FCC 40^3 block (256,000 atoms) of the same alloy, same noise and
+    temperature, `steps` NVT steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from mapp4py_gb300 import synth
+
+    c = synth.alloy((40, 40, 40), xB=0.5, sigma=0.05, T=T_K, seed=1)
+    e = O.Eam.setfl(path)
+    o = O.System(e, c.H, c.x, c.elem, c.masses, skin=0.5, pair_wise=False)
+    o.v = c.v
+    o.nvt_run(T_K, synth.FS, synth.KB, steps, threads=threads)
+    secs = o.loop_seconds
+    return {"value": c.natoms * steps / secs, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d NVT steps of a 256,000-atom (FCC 40^3) block of the same alloy, full-list OpenMP "
+                      "restatement of ForceFieldEAM/MDNVT, step loop only" % steps}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as d:
+        path = write_potential(d)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        from mapp4py_gb300 import synth
+
+        c = synth.alloy((40, 40, 40), xB=0.5, sigma=0.05, T=T_K, seed=1)
+        e = O.Eam.setfl(path)
+        o = O.System(e, c.H, c.x, c.elem, c.masses, skin=0.5, pair_wise=False)
+        o.v = c.v
+        if args.warmup:
+            o.nvt_run(T_K, synth.FS, synth.KB, args.warmup, threads=threads)
+        o.nvt_run(T_K, synth.FS, synth.KB, args.steps, threads=threads)
+        secs = o.loop_seconds
+    value = c.natoms * args.steps / secs
+    sample = ("each step: one NVT step of a 256,000-atom (FCC 40^3) block of the 2,048,000-atom alloy; "
+              "the reference does not build here (MPI and Python<=3.10 C-API), so this is the oracle's "
+              "OpenMP restatement")
+    line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "EAM NVT MD, A/B alloy FCC 40^3 sample of 80^3",
+                                            "natoms": int(c.natoms), "seq_len": None, "global_batch": None},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    from mapp4py_gb300 import _lib, md, synth
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    K, W = args.steps, args.warmup
+    tmp = tempfile.TemporaryDirectory()
+    path = write_potential(tmp.name)
+    cell = make_cell()
+    N = cell.natoms
+    ff = _lib.ForceField.setfl(path)
+    prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
+    sysm = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, skin=0.5, precision=prec)
+    sysm.set_v(cell.v)
+    dt = synth.FS
+    sysm.nvt_begin(T_K, dt, synth.KB, W + K, t_relax=100.0 * dt, L=3, niters=1)
+    stream = torch.cuda.ExternalStream(sysm.stream())
+    sysm.nvt_steps(W)
+    sysm.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local_rank)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sysm.nvt_steps(K)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    sysm.nvt_end(K + W)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * K * world / (ms / 1000.0)
+    st = sysm.stats()
+    kbar = st["mean_row_x1000"] / 1000.0
+
+    # dominant kernels timed alone with CUDA events on the library's stream
+    def time_kernel(what, reps=20):
+        for _ in range(3):
+            sysm.enqueue(what)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            sysm.enqueue(what)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    sysm.enqueue(0)
+    t_density = time_kernel(0)
+    t_force = time_kernel(1)
+    # algorithmic bytes per launch (per atom: the row of 4*K entries plus the
+    # atom's own streams; neighbour gathers are served by L2)
+    if prec == _lib.MIXED:
+        b_force = N * (4 * kbar + 16 + 4 + 1 + 4 + 24)   # row, p32, dF32, elem, count, f (FP64)
+        b_density = N * (4 * kbar + 16 + 1 + 4 + 8 + 8 + 4)  # row, p32, elem, count, rho, dF, dF32
+    else:
+        b_force = N * (4 * kbar + 24 + 8 + 1 + 4 + 4 + 24)   # row, x, dF, elem, count, bins, f
+        b_density = N * (4 * kbar + 24 + 1 + 4 + 4 + 8 + 8)
+    peak, peak_kind = peaks()
+    achieved = b_force / (t_force / 1000.0) / 1e9
+    prof = "k_force_mixed_alloy_2048000" if prec == _lib.MIXED else "k_force_fp64_alloy_2048000"
+    traffic = traffic_from_profiles(prof)
+    roof = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "bytes_per_launch": b_force, "ms_per_launch": t_force,
+            "density_kernel": {"ms_per_launch": t_density, "bytes_per_launch": b_density,
+                               "achieved": b_density / (t_density / 1000.0) / 1e9},
+            "step_bytes_per_atom": 8 * kbar + 305, "mean_row": kbar,
+            "step_frac": (8 * kbar + 305) * value / world / 1e9 / peak}
+
+    # end to end: md.nvt(T,dt).run(atoms, 1) per step through the public API,
+    # positions and velocities in pinned host memory, copied in and out
+    E = max(1, min(K, args.e2e_steps))
+    xh = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    vh = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    xh[:] = cell.x
+    vh[:] = cell.v
+    at = md.atoms(cell.H, xh, cell.elem, elems=("A", "B"), masses=cell.masses, x_d=vh)
+    at.x, at.x_d = xh, vh  # keep the pinned buffers
+    at.kB = synth.KB
+    at.precision = args.precision
+    at.ff = ff
+    nv = md.nvt(T_K, dt)
+    nv.ntally = 0
+    nv.run(at, 1)  # warm-up call (system creation)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(E):
+        nv.run(at, 1)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([te], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    e2e = {"value": N * E * world / te, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * N,
+           "d2h_bytes_per_step": 72 * N, "steps": E,
+           "call": "mapp4py_gb300.md.nvt(600,1fs).run(atoms,1): x,v in; x,v,f out; neighbour build + "
+                   "opening force call + one step per call, as MDNVT::run"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "data": "synthetic",
+                "config": {"workload": "EAM NVT MD, 2,048,000-atom A/B alloy (FCC 80^3, seed 1)",
+                           "natoms": N, "precision": args.precision, "dt_fs": 1.0, "T_K": T_K,
+                           "l2": "inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6),
+                           "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None},
+                "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * K,
+                "neighbor": {"rebuilds_in_run": st["rebuilds"], "max_row": st["max_row"], "capacity": st["capacity"]}}
+        if not args.no_cpu and world == 1:
+            try:
+                line["cpu_baseline"] = cpu_baseline(path, cell, os.cpu_count() or 1)
+            except Exception as ex:  # reported, not fatal
+                line["cpu_baseline"] = {"value": None, "error": str(ex)}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    tmp.cleanup()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="mapp", choices=["mapp", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = env_int("RANK", 0)
+    world = env_int("WORLD_SIZE", args.gpus)
+    local_rank = env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * mappg.h -- C ABI of libmappg, the GB300 (sm_103a) EAM molecular-dynamics
+ * and minimization engine.  It replaces the force-field and driver path of
+ * MAPP (sinamoeini/mapp4py): ForceFieldEAM behind the ForceFieldMD contract,
+ * its neighbour list, the NVT (Nose-Hoover chain) integrator and the L-BFGS
+ * minimizer with back-tracking line search.
+ *
+ * Conventions
+ *   - Every call returns 0 on success and a negative status on failure;
+ *     mappg_last_error() returns the message of the last failure on the
+ *     calling thread.  No C++ exception crosses this boundary.
+ *   - Units are MAPP's: Angstrom, eV, amu; time in A*sqrt(amu/eV).
+ *   - Boxes are 3x3 row-major, lower triangular, rows are the cell vectors
+ *     (x = s*H with s the fractional coordinate), as Atoms::H.
+ *   - Per-atom arrays are row-major [natoms][3] doubles in the caller's atom
+ *     order; element indices are unsigned char as MAPP's elem_type.
+ *   - Virial arrays are Voigt ordered (xx, xy, xz, yy, yz, zz) and hold
+ *     F_H = sum over pairs of fpair*dx(x)dx, the quantity ForceFieldMD keeps
+ *     in F_H (ff_md.cpp:125-144); the stress is S_pe = -F_H/volume.
+ *   - One handle is used by one host thread at a time.  Each system owns
+ *     its device buffers and one CUDA stream.
+ */
+#ifndef MAPPG_H
+#define MAPPG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MAPPG_OK 0
+#define MAPPG_ERR_ARG -1      /* invalid argument                          */
+#define MAPPG_ERR_CUDA -2     /* CUDA runtime failure                      */
+#define MAPPG_ERR_FILE -3     /* potential file missing or malformed       */
+#define MAPPG_ERR_GEOM -4     /* box too thin for cutoff + skin            */
+#define MAPPG_ERR_NBR -5      /* neighbour capacity exceeded               */
+#define MAPPG_ERR_NAN -6      /* non-finite position, force or energy      */
+#define MAPPG_ERR_TIMEOUT -7  /* a bounded device wait gave up             */
+#define MAPPG_ERR_UNSUPP -8   /* feature outside this engine's scope       */
+
+#define MAPPG_FP64 0  /* FP64 everywhere (the reference's arithmetic)       */
+#define MAPPG_MIXED 1 /* FP32 pair math, FP64 state and global reductions   */
+
+typedef struct mappg_ff mappg_ff;
+typedef struct mappg_sys mappg_sys;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* mappg_last_error(void);
+
+/* Device name and SM count of the current CUDA device. */
+int mappg_device_info(char* name, int name_len, int* sm_count);
+
+/* ---------------------------------------------------------------- tables */
+
+/* Read a DYNAMO setfl file.  Replaces ImportEAM::setfl (import_eam.h:348-613)
+ * called by the Python constructor ff_eam_setfl (ff_eam.cpp:668-698).
+ * nelems/elems select and order elements as the reference's optional element
+ * list does; nelems = 0 keeps the file's order.  Splines are built as
+ * ImportEAM::interpolate (import_eam.cpp:62-83) and the cutoff as
+ * set_cuttoff (import_eam.h:52-64). */
+int mappg_ff_setfl(const char* path, int nelems, const char* const* elems, mappg_ff** out);
+
+/* Read a Finnis-Sinclair (eam/fs) file.  Replaces ImportEAM::fs
+ * (import_eam.h:617-901) behind ff_eam_fs (ff_eam.cpp:700-801). */
+int mappg_ff_fs(const char* path, int nelems, const char* const* elems, mappg_ff** out);
+
+/* Read one DYNAMO funcfl file per element.  Replaces ImportEAM::funcfl
+ * (import_eam.h:68-346) behind ff_eam_funcfl (ff_eam.cpp:594-666). */
+int mappg_ff_funcfl(int nfiles, const char* const* paths, mappg_ff** out);
+
+/* Tables from raw knot values (no file): F [nelem][nrho], rho
+ * [nelem][nelem][nr] with rho[i][j] the reference's rho_arr[i][j], rphi
+ * [nelem][nelem][nr] (only i >= j is read).  Same spline and cutoff rules as
+ * mappg_ff_setfl. */
+int mappg_ff_from_knots(int nelem, int nr, int nrho, double dr, double drho, const double* F,
+                        const double* rho, const double* rphi, mappg_ff** out);
+
+/* Table dimensions. */
+int mappg_ff_info(const mappg_ff* ff, int* nelem, int* nr, int* nrho, double* dr, double* drho);
+
+/* Host copies of the spline coefficients ([..][4] each, NULL to skip) and
+ * of the derived cutoffs [nelem][nelem]. */
+int mappg_ff_tables(const mappg_ff* ff, double* F, double* rho, double* rphi, double* cut);
+
+/* Element name i (as read from the file, "" for knot tables). */
+int mappg_ff_element_name(const mappg_ff* ff, int i, char* buf, int len);
+
+void mappg_ff_destroy(mappg_ff* ff);
+
+/* ---------------------------------------------------------------- system */
+
+/* One periodic cell resident on the GPU.  Replaces the AtomsMD state that
+ * ForceFieldEAM, NeighborMD and DynamicMD work on (atoms.h:462-580,
+ * atoms_md.h:6-60).  masses has one entry per element.  skin is the
+ * neighbour skin (Atoms skin, default 0.5).  precision is MAPPG_FP64 or
+ * MAPPG_MIXED. */
+int mappg_sys_create(const mappg_ff* ff, int natoms, const double* H, const double* x,
+                     const unsigned char* elem, const double* masses, double skin, int precision,
+                     mappg_sys** out);
+void mappg_sys_destroy(mappg_sys* sys);
+
+int mappg_sys_natoms(const mappg_sys* sys);
+int mappg_sys_set_x(mappg_sys* sys, const double* x);
+int mappg_sys_get_x(mappg_sys* sys, double* x);
+int mappg_sys_set_v(mappg_sys* sys, const double* v);
+int mappg_sys_get_v(mappg_sys* sys, double* v);
+int mappg_sys_get_f(mappg_sys* sys, double* f);
+int mappg_sys_set_box(mappg_sys* sys, const double* H);
+
+/* Wrap positions into the cell, bin them and build the full neighbour list
+ * within cut+skin.  Replaces DynamicMD::init's x2s_lcl / Update::list /
+ * NeighborMD::create_list (dynamic_md.cpp:34-53, neighbor_md.cpp:82-152);
+ * ghosts are replaced by periodic image shifts stored with each entry. */
+int mappg_sys_build(mappg_sys* sys);
+
+/* Skin test and rebuild when any atom moved more than skin/2 since the last
+ * build (DynamicMD::decide/update_w_x, dynamic_md.cpp:90-105,
+ * dynamic_md.h:37-68).  *rebuilt (may be NULL) tells which happened. */
+int mappg_sys_update(mappg_sys* sys, int* rebuilt);
+
+/* Forces, energy and virial (ForceFieldMD::force_calc / derivative,
+ * ff_md.cpp:125-179 over ForceFieldEAM::__force_calc, ff_eam.cpp:65-240).
+ * Builds the neighbour list first if none exists.  Forces stay on the device
+ * (read them with mappg_sys_get_f).  pe, virial6 may be NULL. */
+int mappg_sys_force(mappg_sys* sys, double* pe, double* virial6);
+
+/* Energy only (ForceFieldMD::value, ff_md.cpp:148-155 over
+ * ForceFieldEAM::__energy_calc, ff_eam.cpp:244-318). */
+int mappg_sys_energy(mappg_sys* sys, double* pe);
+
+/* Per-atom host density rho and F'(rho) from the last force call. */
+int mappg_sys_get_rho(mappg_sys* sys, double* rho, double* dF);
+
+/* The current full neighbour list in the caller's atom order: counts[i]
+ * entries for atom i, each written as 4 ints (neighbour atom, image shift
+ * n0, n1, n2) so that the neighbour sits at x_j + n*H.  Pass entries = NULL
+ * to get *total only. */
+int mappg_sys_neighbors(mappg_sys* sys, int* counts, int* entries, long long* total);
+
+/* Counters: [0] rebuilds, [1] neighbour capacity per atom, [2] max list
+ * length, [3] mean list length*1000, [4] bins, [5] precision. */
+int mappg_sys_stats(mappg_sys* sys, long long* out6);
+
+/* Gaussian velocities sqrt(kB*T/m) per component (AtomsMD::create_T,
+ * atoms_md.cpp:130-162) from the Park-Miller generator and polar Box-Muller
+ * of Random (random.cpp:32-68), seeded with seed.  Seed 0, on which the
+ * reference's generator never returns, is rejected.  v is [natoms][3]. */
+int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
+                      double* v);
+
+/* ---------------------------------------------------------------- drivers */
+
+/* md.nvt(T,dt).run(atoms,nsteps): velocity Verlet with the Nose-Hoover
+ * chain of ThermostatNHC (MDNVT::run, md_nvt.cpp:383-480,
+ * thermostat.cpp:47-143), including the lazy velocity rescale and the
+ * centre-of-mass displacement removal.  NVE is t_relax = +inf.  eta (L
+ * doubles, may be NULL) carries the chain state in and out.  thermo (may be
+ * NULL) receives nsteps+1 rows of 14 doubles: pe, T, mvv[6] (xx,xy,xz,yy,yz,
+ * zz), virial[6].  Velocities must have been set. */
+int mappg_nvt_run(mappg_sys* sys, double T, double dt, double kB, double t_relax, int L,
+                  int niters, int nsteps, double* eta, double* thermo);
+
+/* The same run in three parts, for callers that time or interleave the
+ * steps: mappg_nvt_begin does MDNVT::init and the opening force call (a
+ * neighbour build, then the step is captured as a CUDA graph) for a run of
+ * nsteps steps; mappg_nvt_steps enqueues steps on the system's stream
+ * without waiting; mappg_nvt_end waits, applies the pending velocity scale,
+ * returns eta and (if record_thermo was set) the thermo rows, and checks the
+ * run's error flags. */
+int mappg_nvt_begin(mappg_sys* sys, double T, double dt, double kB, double t_relax, int L, int niters,
+                    long long nsteps, const double* eta, int record_thermo);
+int mappg_nvt_steps(mappg_sys* sys, long long nsteps);
+int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
+
+/* The system's CUDA stream (a cudaStream_t) and a wait on it. */
+int mappg_sys_stream(mappg_sys* sys, void** stream);
+int mappg_sys_sync(mappg_sys* sys);
+
+/* Enqueue one kernel launch on the system's stream without waiting, for
+ * timing: 0 density + embedding, 1 force/virial (uses the last F'(rho)),
+ * 2 energy only, 3 neighbour rebuild. */
+int mappg_sys_enqueue(mappg_sys* sys, int what);
+
+/* md.min_lbfgs(m,e_tol,max_dx,ls=ls_bt(c,rho,min_alpha)).run(atoms,nsteps)
+ * (MinLBFGS::__run, min_l-bfgs.h:113-219; LineSearchBackTrack::min,
+ * ls.h:711-769) with an added stop at max|F| < f_tol (f_tol <= 0 disables
+ * it).  stats (6 doubles): iterations, pe, max|F|, stop code, energy calls,
+ * force calls.  Stop codes follow ls.h:9-22 (4 = energy tolerance, 5 = max
+ * iterations) plus 100 = force tolerance. */
+int mappg_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f_tol, double c,
+                    double rho, double min_alpha, int nsteps, double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAPPG_H */

@@ -1,0 +1,322 @@
+"""ctypes binding of libmappg.so (include/mappg.h).
+
+The library is built in-tree (mapp4py_gb300/build.py).  Loading fails loudly
+when it is missing: there is no CPU fallback for the EAM path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmappg.so")
+
+FP64 = 0
+MIXED = 1
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_U8 = C.POINTER(C.c_ubyte)
+_LL = C.POINTER(C.c_longlong)
+_VP = C.c_void_p
+
+# every exported entry point and its argument types (include/mappg.h)
+SIGNATURES = {
+    "mappg_last_error": (C.c_char_p, []),
+    "mappg_device_info": (C.c_int, [C.c_char_p, C.c_int, _I]),
+    "mappg_ff_setfl": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
+    "mappg_ff_fs": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
+    "mappg_ff_funcfl": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
+    "mappg_ff_from_knots": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D, _D, _D,
+                                      C.POINTER(_VP)]),
+    "mappg_ff_info": (C.c_int, [_VP, _I, _I, _I, _D, _D]),
+    "mappg_ff_tables": (C.c_int, [_VP, _D, _D, _D, _D]),
+    "mappg_ff_element_name": (C.c_int, [_VP, C.c_int, C.c_char_p, C.c_int]),
+    "mappg_ff_destroy": (None, [_VP]),
+    "mappg_sys_create": (C.c_int, [_VP, C.c_int, _D, _D, _U8, _D, C.c_double, C.c_int, C.POINTER(_VP)]),
+    "mappg_sys_destroy": (None, [_VP]),
+    "mappg_sys_natoms": (C.c_int, [_VP]),
+    "mappg_sys_set_x": (C.c_int, [_VP, _D]),
+    "mappg_sys_get_x": (C.c_int, [_VP, _D]),
+    "mappg_sys_set_v": (C.c_int, [_VP, _D]),
+    "mappg_sys_get_v": (C.c_int, [_VP, _D]),
+    "mappg_sys_get_f": (C.c_int, [_VP, _D]),
+    "mappg_sys_set_box": (C.c_int, [_VP, _D]),
+    "mappg_sys_build": (C.c_int, [_VP]),
+    "mappg_sys_update": (C.c_int, [_VP, _I]),
+    "mappg_sys_force": (C.c_int, [_VP, _D, _D]),
+    "mappg_sys_energy": (C.c_int, [_VP, _D]),
+    "mappg_sys_get_rho": (C.c_int, [_VP, _D, _D]),
+    "mappg_sys_neighbors": (C.c_int, [_VP, _I, _I, _LL]),
+    "mappg_sys_stats": (C.c_int, [_VP, _LL]),
+    "mappg_create_temp": (C.c_int, [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]),
+    "mappg_nvt_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                _D, _D]),
+    "mappg_nvt_begin": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                  C.c_longlong, _D, C.c_int]),
+    "mappg_nvt_steps": (C.c_int, [_VP, C.c_longlong]),
+    "mappg_nvt_end": (C.c_int, [_VP, _D, _D]),
+    "mappg_sys_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "mappg_sys_sync": (C.c_int, [_VP]),
+    "mappg_sys_enqueue": (C.c_int, [_VP, C.c_int]),
+    "mappg_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.c_int, _D]),
+}
+
+_lib = None
+
+
+class MappgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("libmappg error %d: %s" % (code, msg))
+        self.code = code
+
+
+def load(path=None):
+    """Load libmappg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError("libmappg.so is not built (run mapp4py_gb300.build.build()); "
+                          "the EAM path has no CPU fallback")
+    L = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        raise MappgError(rc, load().mappg_last_error().decode(errors="replace"))
+    return rc
+
+
+def dptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def cstrings(items):
+    arr = (C.c_char_p * max(1, len(items)))()
+    for i, s in enumerate(items):
+        arr[i] = os.fsencode(s) if not isinstance(s, bytes) else s
+    return arr
+
+
+class ForceField:
+    """EAM tables on the device (one mappg_ff handle)."""
+
+    def __init__(self, handle, kind):
+        self.h = handle
+        self.kind = kind
+        L = load()
+        ne, nr, nrho = C.c_int(), C.c_int(), C.c_int()
+        dr, drho = C.c_double(), C.c_double()
+        check(L.mappg_ff_info(self.h, C.byref(ne), C.byref(nr), C.byref(nrho), C.byref(dr), C.byref(drho)))
+        self.nelem, self.nr, self.nrho, self.dr, self.drho = ne.value, nr.value, nrho.value, dr.value, drho.value
+        names = []
+        buf = C.create_string_buffer(256)
+        for i in range(self.nelem):
+            check(L.mappg_ff_element_name(self.h, i, buf, 256))
+            names.append(buf.value.decode())
+        self.names = names
+
+    @classmethod
+    def setfl(cls, path, elems=None):
+        out = _VP()
+        elems = list(elems or [])
+        check(load().mappg_ff_setfl(os.fsencode(path), len(elems), cstrings(elems), C.byref(out)))
+        return cls(out, "setfl")
+
+    @classmethod
+    def fs(cls, path, elems=None):
+        out = _VP()
+        elems = list(elems or [])
+        check(load().mappg_ff_fs(os.fsencode(path), len(elems), cstrings(elems), C.byref(out)))
+        return cls(out, "fs")
+
+    @classmethod
+    def funcfl(cls, paths):
+        out = _VP()
+        paths = list(paths)
+        check(load().mappg_ff_funcfl(len(paths), cstrings(paths), C.byref(out)))
+        return cls(out, "funcfl")
+
+    @classmethod
+    def knots(cls, nr, nrho, dr, drho, F, rho, rphi):
+        F, rho, rphi = f64(F), f64(rho), f64(rphi)
+        out = _VP()
+        check(load().mappg_ff_from_knots(F.shape[0], nr, nrho, dr, drho, dptr(F), dptr(rho), dptr(rphi),
+                                         C.byref(out)))
+        return cls(out, "knots")
+
+    def tables(self):
+        ne, nr, nrho = self.nelem, self.nr, self.nrho
+        F = np.zeros((ne, nrho, 4))
+        rho = np.zeros((ne, ne, nr, 4))
+        rphi = np.zeros((ne, ne, nr, 4))
+        cut = np.zeros((ne, ne))
+        check(load().mappg_ff_tables(self.h, dptr(F), dptr(rho), dptr(rphi), dptr(cut)))
+        return F, rho, rphi, cut
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.mappg_ff_destroy(self.h)
+            self.h = None
+
+
+class System:
+    """One periodic cell resident on the GPU (one mappg_sys handle)."""
+
+    def __init__(self, ff, H, x, elem, masses, skin=0.5, precision=FP64):
+        self.ff = ff
+        H = f64(H, (3, 3))
+        x = f64(x, (-1, 3))
+        self.elem = np.ascontiguousarray(elem, dtype=np.uint8)
+        masses = f64(masses)
+        self.n = x.shape[0]
+        out = _VP()
+        check(load().mappg_sys_create(ff.h, self.n, dptr(H), dptr(x), self.elem.ctypes.data_as(_U8),
+                                      dptr(masses), float(skin), int(precision), C.byref(out)))
+        self.h = out
+        self.precision = precision
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.mappg_sys_destroy(self.h)
+            self.h = None
+
+    def _get(self, fn, out=None):
+        a = np.empty((self.n, 3)) if out is None else out
+        check(fn(self.h, dptr(a)))
+        return a
+
+    def set_x(self, x):
+        check(load().mappg_sys_set_x(self.h, dptr(f64(x, (-1, 3)))))
+
+    def get_x(self, out=None):
+        return self._get(load().mappg_sys_get_x, out)
+
+    def set_v(self, v):
+        check(load().mappg_sys_set_v(self.h, dptr(f64(v, (-1, 3)))))
+
+    def get_v(self, out=None):
+        return self._get(load().mappg_sys_get_v, out)
+
+    def get_f(self, out=None):
+        return self._get(load().mappg_sys_get_f, out)
+
+    def set_box(self, H):
+        check(load().mappg_sys_set_box(self.h, dptr(f64(H, (3, 3)))))
+
+    def build(self):
+        check(load().mappg_sys_build(self.h))
+
+    def update(self):
+        r = C.c_int(0)
+        check(load().mappg_sys_update(self.h, C.byref(r)))
+        return bool(r.value)
+
+    def force(self):
+        pe = C.c_double()
+        vir = np.zeros(6)
+        check(load().mappg_sys_force(self.h, C.byref(pe), dptr(vir)))
+        return pe.value, vir
+
+    def energy(self):
+        pe = C.c_double()
+        check(load().mappg_sys_energy(self.h, C.byref(pe)))
+        return pe.value
+
+    def rho_dF(self):
+        rho = np.zeros(self.n)
+        dF = np.zeros(self.n)
+        check(load().mappg_sys_get_rho(self.h, dptr(rho), dptr(dF)))
+        return rho, dF
+
+    def neighbors(self):
+        cnt = np.zeros(self.n, dtype=np.int32)
+        tot = C.c_longlong()
+        check(load().mappg_sys_neighbors(self.h, cnt.ctypes.data_as(_I), None, C.byref(tot)))
+        ent = np.zeros((tot.value, 4), dtype=np.int32)
+        check(load().mappg_sys_neighbors(self.h, cnt.ctypes.data_as(_I), ent.ctypes.data_as(_I), C.byref(tot)))
+        return cnt, ent
+
+    def stats(self):
+        out = np.zeros(6, dtype=np.int64)
+        check(load().mappg_sys_stats(self.h, out.ctypes.data_as(_LL)))
+        keys = ("rebuilds", "capacity", "max_row", "mean_row_x1000", "bins", "precision")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def nvt_run(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False):
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        eta_a = np.zeros(max(L, 1)) if eta is None else f64(eta).copy()
+        th = np.zeros((nsteps + 1, 14)) if thermo else None
+        check(load().mappg_nvt_run(self.h, float(T), float(dt), float(kB), float(t_relax), int(L), int(niters),
+                                   int(nsteps), dptr(eta_a), dptr(th) if th is not None else None))
+        return th, eta_a
+
+    def nvt_begin(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False):
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        eta_a = np.zeros(max(L, 1)) if eta is None else f64(eta).copy()
+        self._run = (L, nsteps, thermo)
+        check(load().mappg_nvt_begin(self.h, float(T), float(dt), float(kB), float(t_relax), int(L), int(niters),
+                                     int(nsteps), dptr(eta_a), 1 if thermo else 0))
+
+    def nvt_steps(self, nsteps):
+        check(load().mappg_nvt_steps(self.h, int(nsteps)))
+
+    def nvt_end(self, steps_done=None):
+        L, nsteps, thermo = self._run
+        n = nsteps if steps_done is None else steps_done
+        eta = np.zeros(max(L, 1))
+        th = np.zeros((n + 1, 14)) if thermo else None
+        check(load().mappg_nvt_end(self.h, dptr(eta), dptr(th) if th is not None else None))
+        return th, eta
+
+    def stream(self):
+        p = _VP()
+        check(load().mappg_sys_stream(self.h, C.byref(p)))
+        return p.value or 0
+
+    def sync(self):
+        check(load().mappg_sys_sync(self.h))
+
+    def enqueue(self, what):
+        check(load().mappg_sys_enqueue(self.h, int(what)))
+
+    def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000):
+        st = np.zeros(6)
+        check(load().mappg_lbfgs_run(self.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
+                                     float(rho), float(min_alpha), int(nsteps), dptr(st)))
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+
+def create_temp(elem, masses, T, kB, seed):
+    elem = np.ascontiguousarray(elem, dtype=np.uint8)
+    v = np.zeros((elem.shape[0], 3))
+    check(load().mappg_create_temp(elem.shape[0], elem.ctypes.data_as(_U8), dptr(f64(masses)), float(T),
+                                   float(kB), int(seed), dptr(v)))
+    return v
+
+
+def device_info():
+    buf = C.create_string_buffer(256)
+    sm = C.c_int()
+    check(load().mappg_device_info(buf, 256, C.byref(sm)))
+    return buf.value.decode(), sm.value

@@ -1,0 +1,566 @@
+// extern "C" entry points of libmappg (declared in include/mappg.h).
+// Every entry point catches all exceptions, records the message for
+// mappg_last_error() and returns a negative status.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "system.h"
+
+namespace mappg {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+const char* get_error() { return g_err.c_str(); }
+
+void sys_alloc(mappg_sys* s, const double* x_host);
+void sys_alloc_bins(mappg_sys* s);
+void sys_alloc_nbr(mappg_sys* s, int maxnbr);
+void sys_free(mappg_sys* s);
+void sys_upload(mappg_sys* s, const double* host, double* dev);
+void sys_download(mappg_sys* s, const double* dev, double* host);
+void sys_build(mappg_sys* s);
+void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total);
+void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
+             double* thermo);
+void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
+               double min_alpha, int nsteps, double* stats);
+void lb_update(mappg_sys* s);
+void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
+               const double* eta, bool thermo);
+void nvt_steps(mappg_sys* s, long long nsteps);
+void nvt_end(mappg_sys* s, double* eta, double* thermo);
+void nvt_free(mappg_sys* s);
+
+template <class F>
+static int guard(F&& f) {
+    try {
+        f();
+        return MAPPG_OK;
+    } catch (const Error& e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return MAPPG_ERR_ARG;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return MAPPG_ERR_ARG;
+    } catch (...) {
+        set_error("unknown failure");
+        return MAPPG_ERR_ARG;
+    }
+}
+
+void upload_tables(mappg_ff* ff) {
+    HostTables& t = ff->host;
+    DevTables& d = ff->dev;
+    const int ne = t.nelem;
+    d.nelem = ne;
+    d.nr = t.nr;
+    d.nrho = t.nrho;
+    d.dr_inv = 1.0 / t.dr;
+    d.drho_inv = 1.0 / t.drho;
+    d.rho_max = (double)t.nrho * t.drho;
+    d.max_cut = 0.0;
+    for (int i = 0; i < ne * ne; i++) {
+        d.cut[i] = t.cut[i];
+        d.max_cut = std::max(d.max_cut, t.cut[i]);
+    }
+    MAPPG_CUDA(cudaGetDevice(&ff->device));
+    size_t nrt = (size_t)ne * ne * t.nr, nFt = (size_t)ne * t.nrho;
+    auto up64 = [](double4** dst, const std::vector<double>& src, size_t n) {
+        MAPPG_CUDA(cudaMalloc(dst, sizeof(double4) * n));
+        MAPPG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(double4) * n, cudaMemcpyHostToDevice));
+    };
+    auto up32 = [](float4** dst, const std::vector<double>& src, size_t n) {
+        std::vector<float> f(4 * n);
+        for (size_t k = 0; k < 4 * n; k++) f[k] = (float)src[k];
+        MAPPG_CUDA(cudaMalloc(dst, sizeof(float4) * n));
+        MAPPG_CUDA(cudaMemcpy(*dst, f.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    };
+    up64(&d.rho64, t.rho, nrt);
+    up64(&d.rphi64, t.rphi, nrt);
+    up64(&d.F64, t.F, nFt);
+    up32(&d.rho32, t.rho, nrt);
+    up32(&d.rphi32, t.rphi, nrt);
+    up32(&d.F32, t.F, nFt);
+}
+
+void free_tables(mappg_ff* ff) {
+    DevTables& d = ff->dev;
+    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.rphi32, d.F32};
+    for (void* q : p)
+        if (q) cudaFree(q);
+}
+
+}  // namespace mappg
+
+using namespace mappg;
+
+// tables reach the device when the first system uses them, so the host-side
+// readers work (and can be tested) without a GPU
+static mappg_ff* finish_ff(mappg_ff* ff) { return ff; }
+
+static void ensure_uploaded(const mappg_ff* cff) {
+    mappg_ff* ff = const_cast<mappg_ff*>(cff);
+    if (ff->dev.rho64) return;
+    try {
+        upload_tables(ff);
+    } catch (...) {
+        free_tables(ff);
+        ff->dev = DevTables();
+        throw;
+    }
+}
+
+extern "C" {
+
+const char* mappg_last_error(void) { return get_error(); }
+
+int mappg_device_info(char* name, int name_len, int* sm_count) {
+    return guard([&] {
+        int dev;
+        MAPPG_CUDA(cudaGetDevice(&dev));
+        cudaDeviceProp p;
+        MAPPG_CUDA(cudaGetDeviceProperties(&p, dev));
+        if (name && name_len > 0) {
+            strncpy(name, p.name, name_len - 1);
+            name[name_len - 1] = 0;
+        }
+        if (sm_count) *sm_count = p.multiProcessorCount;
+    });
+}
+
+int mappg_ff_setfl(const char* path, int nelems, const char* const* elems, mappg_ff** out) {
+    return guard([&] {
+        if (!path || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        mappg_ff* ff = new mappg_ff();
+        try {
+            read_setfl(path, nelems, elems, ff->host);
+        } catch (...) {
+            delete ff;
+            throw;
+        }
+        *out = finish_ff(ff);
+    });
+}
+
+int mappg_ff_fs(const char* path, int nelems, const char* const* elems, mappg_ff** out) {
+    return guard([&] {
+        if (!path || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        mappg_ff* ff = new mappg_ff();
+        try {
+            read_fs(path, nelems, elems, ff->host);
+        } catch (...) {
+            delete ff;
+            throw;
+        }
+        *out = finish_ff(ff);
+    });
+}
+
+int mappg_ff_funcfl(int nfiles, const char* const* paths, mappg_ff** out) {
+    return guard([&] {
+        if (!paths || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        mappg_ff* ff = new mappg_ff();
+        try {
+            read_funcfl(nfiles, paths, ff->host);
+        } catch (...) {
+            delete ff;
+            throw;
+        }
+        *out = finish_ff(ff);
+    });
+}
+
+int mappg_ff_from_knots(int nelem, int nr, int nrho, double dr, double drho, const double* F, const double* rho,
+                        const double* rphi, mappg_ff** out) {
+    return guard([&] {
+        if (!F || !rho || !rphi || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (nr < 5 || nrho < 5) throw Error{MAPPG_ERR_ARG, "nr and nrho must be at least 5"};
+        if (!(dr > 0.0) || !(drho > 0.0)) throw Error{MAPPG_ERR_ARG, "dr and drho must be positive"};
+        mappg_ff* ff = new mappg_ff();
+        try {
+            HostTables& t = ff->host;
+            t.alloc(nelem, nr, nrho, dr, drho);
+            t.names.assign(nelem, "");
+            for (int i = 0; i < nelem; i++)
+                for (int k = 0; k < nrho; k++) t.F_at(i)[4 * k] = F[(size_t)i * nrho + k];
+            for (int i = 0; i < nelem; i++)
+                for (int j = 0; j < nelem; j++)
+                    for (int k = 0; k < nr; k++) t.rho_at(i, j)[4 * k] = rho[((size_t)i * nelem + j) * nr + k];
+            for (int i = 0; i < nelem; i++)
+                for (int j = 0; j <= i; j++)
+                    for (int k = 0; k < nr; k++) t.rphi_at(i, j)[4 * k] = rphi[((size_t)i * nelem + j) * nr + k];
+            t.finish_splines(true);
+        } catch (...) {
+            delete ff;
+            throw;
+        }
+        *out = finish_ff(ff);
+    });
+}
+
+int mappg_ff_info(const mappg_ff* ff, int* nelem, int* nr, int* nrho, double* dr, double* drho) {
+    return guard([&] {
+        if (!ff) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (nelem) *nelem = ff->host.nelem;
+        if (nr) *nr = ff->host.nr;
+        if (nrho) *nrho = ff->host.nrho;
+        if (dr) *dr = ff->host.dr;
+        if (drho) *drho = ff->host.drho;
+    });
+}
+
+int mappg_ff_tables(const mappg_ff* ff, double* F, double* rho, double* rphi, double* cut) {
+    return guard([&] {
+        if (!ff) throw Error{MAPPG_ERR_ARG, "null handle"};
+        const HostTables& t = ff->host;
+        if (F) memcpy(F, t.F.data(), sizeof(double) * t.F.size());
+        if (rho) memcpy(rho, t.rho.data(), sizeof(double) * t.rho.size());
+        if (rphi) memcpy(rphi, t.rphi.data(), sizeof(double) * t.rphi.size());
+        if (cut) memcpy(cut, t.cut.data(), sizeof(double) * t.cut.size());
+    });
+}
+
+int mappg_ff_element_name(const mappg_ff* ff, int i, char* buf, int len) {
+    return guard([&] {
+        if (!ff || !buf || len < 1) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (i < 0 || i >= ff->host.nelem) throw Error{MAPPG_ERR_ARG, "element index out of range"};
+        const std::string& nm = i < (int)ff->host.names.size() ? ff->host.names[i] : std::string();
+        strncpy(buf, nm.c_str(), len - 1);
+        buf[len - 1] = 0;
+    });
+}
+
+void mappg_ff_destroy(mappg_ff* ff) {
+    if (!ff) return;
+    free_tables(ff);
+    delete ff;
+}
+
+int mappg_sys_create(const mappg_ff* ff, int natoms, const double* H, const double* x, const unsigned char* elem,
+                     const double* masses, double skin, int precision, mappg_sys** out) {
+    return guard([&] {
+        if (!ff || !H || !x || !elem || !masses || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (natoms < 1 || natoms >= (1 << (31 - kCodeBits))) throw Error{MAPPG_ERR_ARG, "natoms out of range"};
+        if (precision != MAPPG_FP64 && precision != MAPPG_MIXED) throw Error{MAPPG_ERR_ARG, "unknown precision mode"};
+        if (!(skin >= 0.0)) throw Error{MAPPG_ERR_ARG, "skin must be >= 0"};
+        const int ne = ff->host.nelem;
+        for (int i = 0; i < natoms; i++)
+            if (elem[i] >= ne) throw Error{MAPPG_ERR_ARG, "element index beyond the force field's elements"};
+        for (int e = 0; e < ne; e++)
+            if (!(masses[e] > 0.0)) throw Error{MAPPG_ERR_ARG, "masses must be positive"};
+        for (int i = 0; i < 3 * natoms; i++)
+            if (!std::isfinite(x[i])) throw Error{MAPPG_ERR_NAN, "non-finite position"};
+        ensure_uploaded(ff);
+        mappg_sys* s = new mappg_sys();
+        try {
+            s->ff = ff;
+            s->n = natoms;
+            s->precision = precision;
+            s->ne = ne;
+            s->skin = skin;
+            for (int e = 0; e < ne; e++) s->masses[e] = masses[e];
+            // ForceFieldMD::pre_init (ff_md.cpp:80-94) and max_cut = cut + skin
+            double mc = 0.0;
+            for (int i = 0; i < ne; i++)
+                for (int j = 0; j < ne; j++) {
+                    double c = ff->host.cut[i * ne + j];
+                    mc = std::max(mc, c);
+                    s->cut_sq[i * ne + j] = c * c;
+                    double ck = c + skin;
+                    s->cut_sk_sq[i * ne + j] = ck * ck;
+                }
+            s->max_cut = mc + skin;
+            MAPPG_CUDA(cudaGetDevice(&s->device));
+            cudaDeviceProp p;
+            MAPPG_CUDA(cudaGetDeviceProperties(&p, s->device));
+            s->sm_count = p.multiProcessorCount;
+            sys_set_box(s, H);
+            sys_alloc(s, x);
+            sys_alloc_bins(s);
+            // row capacity from the mean density, refined by the first build
+            double dens = natoms / s->box.vol;
+            double est = dens * 4.18879 * s->max_cut * s->max_cut * s->max_cut;
+            int cap = ((int)(est * 1.35) + 32 + 31) / 32 * 32;
+            sys_alloc_nbr(s, std::min(cap, 4096));
+            sys_upload(s, x, s->x);
+            std::vector<uint8_t> es(natoms);
+            for (int i = 0; i < natoms; i++) es[i] = elem[s->host_id[i]];
+            MAPPG_CUDA(cudaMemcpyAsync(s->elem, es.data(), natoms, cudaMemcpyHostToDevice, s->stream));
+            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        } catch (...) {
+            sys_free(s);
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+void mappg_sys_destroy(mappg_sys* s) {
+    if (!s) return;
+    nvt_free(s);
+    sys_free(s);
+    delete s;
+}
+
+int mappg_sys_natoms(const mappg_sys* s) { return s ? s->n : 0; }
+
+int mappg_sys_set_x(mappg_sys* s, const double* x) {
+    return guard([&] {
+        if (!s || !x) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sys_upload(s, x, s->x);
+        s->built = false;
+        s->forces_valid = false;
+    });
+}
+
+int mappg_sys_get_x(mappg_sys* s, double* x) {
+    return guard([&] {
+        if (!s || !x) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sys_download(s, s->x, x);
+    });
+}
+
+int mappg_sys_set_v(mappg_sys* s, const double* v) {
+    return guard([&] {
+        if (!s || !v) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sys_upload(s, v, s->v);
+        s->have_v = true;
+    });
+}
+
+int mappg_sys_get_v(mappg_sys* s, double* v) {
+    return guard([&] {
+        if (!s || !v) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sys_download(s, s->v, v);
+    });
+}
+
+int mappg_sys_get_f(mappg_sys* s, double* f) {
+    return guard([&] {
+        if (!s || !f) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sys_download(s, s->f, f);
+    });
+}
+
+int mappg_sys_set_box(mappg_sys* s, const double* H) {
+    return guard([&] {
+        if (!s || !H) throw Error{MAPPG_ERR_ARG, "null argument"};
+        int nb_old = s->nbins;
+        sys_set_box(s, H);
+        if (s->nbins != nb_old) sys_alloc_bins(s);
+        s->built = false;
+    });
+}
+
+int mappg_sys_build(mappg_sys* s) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        sys_build(s);
+    });
+}
+
+int mappg_sys_update(mappg_sys* s, int* rebuilt) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->built) {
+            sys_build(s);
+            if (rebuilt) *rebuilt = 1;
+            return;
+        }
+        long long before;
+        MAPPG_CUDA(cudaMemcpyAsync(&before, &s->sc->nrebuild, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+        lb_update(s);
+        check_build(s);
+        long long after;
+        MAPPG_CUDA(cudaMemcpyAsync(&after, &s->sc->nrebuild, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (rebuilt) *rebuilt = after != before;
+    });
+}
+
+int mappg_sys_force(mappg_sys* s, double* pe, double* virial6) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->built) sys_build(s);
+        launch_force(s);
+        DevScalars h;
+        MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (pe) *pe = h.energy;
+        if (virial6)
+            for (int k = 0; k < 6; k++) virial6[k] = h.virial[k];
+        s->forces_valid = true;
+        if (!std::isfinite(h.energy)) throw Error{MAPPG_ERR_NAN, "non-finite energy"};
+    });
+}
+
+int mappg_sys_energy(mappg_sys* s, double* pe) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->built) sys_build(s);
+        launch_energy(s);
+        double e;
+        MAPPG_CUDA(cudaMemcpyAsync(&e, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (pe) *pe = e;
+    });
+}
+
+int mappg_sys_get_rho(mappg_sys* s, double* rho, double* dF) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        std::vector<double> a(s->n), b(s->n);
+        MAPPG_CUDA(cudaMemcpyAsync(a.data(), s->rho, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(b.data(), s->dF, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        for (int i = 0; i < s->n; i++) {
+            int u = s->host_id[i];
+            if (rho) rho[u] = a[i];
+            if (dF) dF[u] = b[i];
+        }
+    });
+}
+
+int mappg_sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->built) sys_build(s);
+        sys_neighbors(s, counts, entries, total);
+    });
+}
+
+int mappg_sys_stats(mappg_sys* s, long long* out6) {
+    return guard([&] {
+        if (!s || !out6) throw Error{MAPPG_ERR_ARG, "null argument"};
+        DevScalars h;
+        MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        out6[0] = h.nrebuild;
+        out6[1] = s->maxnbr;
+        out6[2] = h.maxrow;
+        out6[3] = s->n ? (long long)(1000.0 * (double)h.sumrow / s->n) : 0;
+        out6[4] = s->nbins;
+        out6[5] = s->precision;
+    });
+}
+
+int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
+                      double* v) {
+    return guard([&] {
+        if (!elem || !masses || !v || natoms < 0) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (seed == 0) throw Error{MAPPG_ERR_ARG, "seed 0 never yields a Gaussian sample"};
+        if (!(kB == kB)) throw Error{MAPPG_ERR_ARG, "boltzmann constant should be set prior to create_temp"};
+        int sd = seed;
+        auto uniform = [&sd]() {
+            int first = sd / 127773, second = sd % 127773;
+            int rnd = 16807 * second - 2836 * first;
+            sd = rnd > 0 ? rnd : rnd + 2147483647;
+            return sd * 1.0 / 2147483647;
+        };
+        bool gchk = false;
+        double reserved = 0.0;
+        for (int i = 0; i < natoms; i++) {
+            double fac = sqrt(kB * T / masses[elem[i]]);
+            for (int j = 0; j < 3; j++) {
+                double g;
+                if (gchk) {
+                    gchk = false;
+                    g = reserved;
+                } else {
+                    gchk = true;
+                    double u = 0.0, w = 0.0, s2 = 1.0;
+                    while (s2 >= 1.0) {
+                        u = 2.0 * uniform() - 1.0;
+                        w = 2.0 * uniform() - 1.0;
+                        s2 = u * u + w * w;
+                    }
+                    double r = sqrt(-2.0 * log(s2) / s2);
+                    reserved = w * r;
+                    g = u * r;
+                }
+                v[3 * (size_t)i + j] = g * fac;
+            }
+        }
+    });
+}
+
+int mappg_nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps,
+                  double* eta, double* thermo) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
+        nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo);
+    });
+}
+
+int mappg_nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters,
+                    long long nsteps, const double* eta, int record_thermo) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, record_thermo != 0);
+    });
+}
+
+int mappg_nvt_steps(mappg_sys* s, long long nsteps) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
+        nvt_steps(s, nsteps);
+    });
+}
+
+int mappg_nvt_end(mappg_sys* s, double* eta, double* thermo) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        nvt_end(s, eta, thermo);
+    });
+}
+
+int mappg_sys_stream(mappg_sys* s, void** stream) {
+    return guard([&] {
+        if (!s || !stream) throw Error{MAPPG_ERR_ARG, "null argument"};
+        *stream = (void*)s->stream;
+    });
+}
+
+int mappg_sys_sync(mappg_sys* s) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
+
+int mappg_sys_enqueue(mappg_sys* s, int what) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (!s->built) throw Error{MAPPG_ERR_ARG, "build the neighbour list first"};
+        switch (what) {
+            case 0: launch_density_only(s); break;
+            case 1: launch_force_only(s); break;
+            case 2: launch_energy(s); break;
+            case 3:
+                request_rebuild(s);
+                launch_rebuild_chain(s);
+                break;
+            default: throw Error{MAPPG_ERR_ARG, "unknown kernel selector"};
+        }
+    });
+}
+
+int mappg_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c, double rho,
+                    double min_alpha, int nsteps, double* stats) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats);
+    });
+}
+
+}  // extern "C"

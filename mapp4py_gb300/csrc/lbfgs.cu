@@ -1,0 +1,460 @@
+// L-BFGS minimization with back-tracking line search on the device:
+// md.min_lbfgs(m,e_tol,max_dx,ls=ls_bt(c,rho,min_alpha)).run(atoms,nsteps).
+//
+// The iteration is MinLBFGS::__run (min_l-bfgs.h:113-219) over the line-
+// search object MinMDHandler<false,true> (min_cg.h:215-309) and
+// LineSearchBackTrack::min (ls.h:711-769):
+//   x0 = x; h = f0 = f; two-loop recursion over the m most recent (s, y);
+//   f.h < 0 -> h = f, history dropped; Armijo back-tracking from
+//   alpha = min(max_dx/max|h|, 1); force call; stop on the energy tolerance,
+//   on max|F| < f_tol (added), or on the iteration limit; history update
+//   s0 = alpha*h, y0 = f0 - f, rho0 = 1/(s0.y0), gamma = s0.y0/(y0.y0).
+// All vectors live on the device in the system's SoA layout.  The recursion
+// keeps its scalars on the device: each kernel reads the coefficient it
+// needs, applies its update and reduces the next dot product in the same
+// pass, so the host only reads the line-search energies and f.h.  Dot
+// products are FP64 with a fixed reduction order.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "system.h"
+
+namespace mappg {
+
+void sys_build(mappg_sys* s);
+void lb_update(mappg_sys* s);
+
+// device scalars of the recursion (one block of doubles)
+struct LbScal {
+    double dot[2 * 64 + 8];  // dot products, one slot per use
+    double rho[64];
+    double alpha[64];
+    double gamma;
+    double fh, hh, hmax, fmax;
+};
+
+__device__ __forceinline__ void warp_sum(double& t) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+}
+
+template <int K>
+__device__ bool lb_block(double (&v)[K], double* partials, unsigned* counter, bool is_max = false) {
+    __shared__ double red[32][K];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double u = __shfl_xor_sync(0xffffffffu, t, o);
+            t = is_max ? fmax(t, u) : t + u;
+        }
+        if (lane == 0) red[w][k] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = is_max ? 0.0 : 0.0;
+        for (int q = 0; q < nw; q++) t = is_max ? fmax(t, red[q][threadIdx.x]) : t + red[q][threadIdx.x];
+        partials[blockIdx.x * kRedSlots + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    return last;
+}
+
+template <int K>
+__device__ void lb_final(const double* partials, int nblk, double (&tot)[K], bool is_max = false) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double t = 0.0;
+        for (int b = lane; b < nblk; b += 32) t = is_max ? fmax(t, partials[b * kRedSlots + k]) : t + partials[b * kRedSlots + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double u = __shfl_xor_sync(0xffffffffu, t, o);
+            t = is_max ? fmax(t, u) : t + u;
+        }
+        tot[k] = t;
+    }
+}
+
+// h <- h + coef*y, then dot = s.h (s may be null: no dot).  coef is read
+// from the device: mode 0: coef = 0 (plain dot); mode 1: alpha_i =
+// -rho_i*dot_in, stored; mode 2: beta = -alpha_i - rho_i*dot_in; mode 3:
+// coef applies as a scale: h <- gamma*h
+__global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__ h, const double* __restrict__ y,
+                                                     const double* __restrict__ s, LbScal* L, int mode, int idx,
+                                                     int dot_in, int dot_out, double* partials, unsigned* counter) {
+    double coef = 0.0;
+    if (mode == 1) {
+        coef = -L->rho[idx] * L->dot[dot_in];
+        if (blockIdx.x == 0 && threadIdx.x == 0) L->alpha[idx] = coef;
+    } else if (mode == 2) {
+        coef = -L->alpha[idx] - L->rho[idx] * L->dot[dot_in];
+    } else if (mode == 3) {
+        coef = L->gamma;
+    }
+    double acc = 0.0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
+        double hv = h[q];
+        if (mode == 1 || mode == 2)
+            hv = hv + coef * y[q];
+        else if (mode == 3)
+            hv = hv * coef;
+        if (mode) h[q] = hv;
+        if (s) acc += s[q] * hv;
+    }
+    if (!s) return;
+    double v[1] = {acc};
+    if (lb_block<1>(v, partials, counter) && threadIdx.x < 32) {
+        double t[1];
+        lb_final<1>(partials, gridDim.x, t);
+        if (threadIdx.x == 0) {
+            L->dot[dot_out] = t[0];
+            *counter = 0;
+        }
+    }
+}
+
+// dots f.h, h.h and max|h| (line-search preparation) and max|f|
+__global__ void __launch_bounds__(256) k_lb_prep(int N, const double* __restrict__ f, const double* __restrict__ h,
+                                                 LbScal* L, double* partials, unsigned* counter) {
+    double v[2] = {0.0, 0.0};
+    double mx[2] = {0.0, 0.0};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
+        double hv = h[q], fv = f[q];
+        v[0] += fv * hv;
+        v[1] += hv * hv;
+        mx[0] = fmax(mx[0], fabs(hv));
+        mx[1] = fmax(mx[1], fabs(fv));
+    }
+    // sums into slots 0,1 and maxima into slots 2,3 of the same partial row
+    __shared__ double red[32][4];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double t[4] = {v[0], v[1], mx[0], mx[1]};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double u = __shfl_xor_sync(0xffffffffu, t[k], o);
+            t[k] = k < 2 ? t[k] + u : fmax(t[k], u);
+        }
+        if (lane == 0) red[w][k] = t[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double r = 0.0;
+        for (int q = 0; q < nw; q++) r = threadIdx.x < 2 ? r + red[q][threadIdx.x] : fmax(r, red[q][threadIdx.x]);
+        partials[blockIdx.x * kRedSlots + threadIdx.x] = r;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x < 32) {
+        double s2[2], m2[2];
+        for (int k = 0; k < 2; k++) {
+            double a = 0.0, b = 0.0;
+            for (int bb = lane; bb < (int)gridDim.x; bb += 32) {
+                a += partials[bb * kRedSlots + k];
+                b = fmax(b, partials[bb * kRedSlots + 2 + k]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+            }
+            s2[k] = a;
+            m2[k] = b;
+        }
+        if (threadIdx.x == 0) {
+            L->fh = s2[0];
+            L->hh = s2[1];
+            L->hmax = m2[0];
+            L->fmax = m2[1];
+            *counter = 0;
+        }
+    }
+}
+
+// x = x0 + alpha*h  (MinMDHandler::F, min_cg.h:260-267)
+__global__ void k_lb_trial(int N, double* __restrict__ x, const double* __restrict__ x0, const double* __restrict__ h,
+                           double alpha) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x)
+        x[q] = x0[q] + alpha * h[q];
+}
+
+// s0 = alpha*h, y0 = f0 - f; dots s0.y0, y0.y0 -> rho0, gamma
+__global__ void __launch_bounds__(256) k_lb_hist(int N, double* __restrict__ s0, double* __restrict__ y0,
+                                                 const double* __restrict__ h, const double* __restrict__ f0,
+                                                 const double* __restrict__ f, double alpha, LbScal* L,
+                                                 double* partials, unsigned* counter) {
+    double v[2] = {0.0, 0.0};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
+        double sv = alpha * h[q];
+        double yv = f0[q] - f[q];
+        s0[q] = sv;
+        y0[q] = yv;
+        v[0] += sv * yv;
+        v[1] += yv * yv;
+    }
+    if (lb_block<2>(v, partials, counter) && threadIdx.x < 32) {
+        double t[2];
+        lb_final<2>(partials, gridDim.x, t);
+        if (threadIdx.x == 0) {
+            L->gamma = t[0] / t[1];
+            L->rho[0] = 1.0 / t[0];
+            *counter = 0;
+        }
+    }
+}
+
+__global__ void k_lb_shift_rho(LbScal* L, int m) {
+    for (int i = m - 1; i > 0; i--) L->rho[i] = L->rho[i - 1];
+}
+
+struct LbState {
+    mappg_sys* s;
+    int N, grid;
+    double *f0, *h, *xs;  // xs: the minimizer's x0
+    std::vector<double*> sv, yv;
+    LbScal* L;
+    unsigned* counter;
+};
+
+static double lb_energy(mappg_sys* s) {
+    // skin test and (gated) rebuild, then the energy kernel
+    lb_update(s);
+    launch_energy(s);
+    double e;
+    MAPPG_CUDA(cudaMemcpyAsync(&e, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    return e;
+}
+
+__global__ void k_clear_rebuild(DevScalars* sc) { sc->rebuild = 0; }
+
+void lb_update(mappg_sys* s) {
+    k_clear_rebuild<<<1, 1, 0, s->stream>>>(s->sc);
+    launch_skin_test(s);
+    launch_rebuild_chain(s);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+static void lb_force(mappg_sys* s, double* pe) {
+    launch_force(s);
+    MAPPG_CUDA(cudaMemcpyAsync(pe, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
+               double min_alpha, int nsteps, double* stats) {
+    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
+    if (m < 0 || m > 64) throw Error{MAPPG_ERR_ARG, "m must be in 0..64"};
+    if (!(max_dx > 0.0)) throw Error{MAPPG_ERR_ARG, "max_dx must be positive"};
+    if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
+    if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
+    const int N = 3 * s->n;
+    const int grid = grid_for(s, N, 256);
+    std::vector<void*> owned;
+    auto dalloc = [&](size_t bytes) {
+        void* p = nullptr;
+        MAPPG_CUDA(cudaMalloc(&p, bytes));
+        owned.push_back(p);
+        return p;
+    };
+    struct Guard {
+        std::vector<void*>& o;
+        ~Guard() {
+            for (void* p : o) cudaFree(p);
+        }
+    } guard{owned};
+    double* f0 = (double*)dalloc(sizeof(double) * N);
+    double* h = (double*)dalloc(sizeof(double) * N);
+    double* xs = (double*)dalloc(sizeof(double) * N);
+    std::vector<double*> sv(m), yv(m);
+    for (int i = 0; i < m; i++) {
+        sv[i] = (double*)dalloc(sizeof(double) * N);
+        yv[i] = (double*)dalloc(sizeof(double) * N);
+    }
+    LbScal* L = (LbScal*)dalloc(sizeof(LbScal));
+    unsigned* counter = (unsigned*)dalloc(sizeof(unsigned) * 4);
+    MAPPG_CUDA(cudaMemsetAsync(L, 0, sizeof(LbScal), s->stream));
+    MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * 4, s->stream));
+    const double one = 1.0;  // gamma starts at 1 (min_l-bfgs.h:140)
+    MAPPG_CUDA(cudaMemcpyAsync(&L->gamma, &one, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    cudaStream_t st = s->stream;
+    double* part = s->partials;
+
+    // NewDynamicMD::init then the opening force call
+    sys_build(s);
+    long long n_en = 0, n_fc = 1;
+    double e_curr;
+    lb_force(s, &e_curr);
+    double e_prev, alpha_m = 0.0;
+    int k = 0;
+    int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
+    auto read_prep = [&](double* fh, double* hh, double* hmax, double* fmax_) {
+        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, L, part, counter);
+        MAPPG_CUDA(cudaGetLastError());
+        double buf[4];
+        MAPPG_CUDA(cudaMemcpyAsync(buf, &L->fh, sizeof(buf), cudaMemcpyDeviceToHost, st));
+        MAPPG_CUDA(cudaStreamSynchronize(st));
+        *fh = buf[0];
+        *hh = buf[1];
+        *hmax = buf[2];
+        *fmax_ = buf[3];
+    };
+    double fh, hh, hmax, fmaxv;
+    if (err == LS_S && f_tol > 0.0) {
+        MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        read_prep(&fh, &hh, &hmax, &fmaxv);
+        if (fmaxv < f_tol) err = MIN_S_FTOL;
+    }
+    int istep = 0;
+    for (; err == LS_S; istep++) {
+        MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        MAPPG_CUDA(cudaMemcpyAsync(f0, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        // first loop: alpha_i = -rho_i (s_i.h); h += alpha_i y_i
+        if (k > 0) k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, nullptr, sv[0], L, 0, 0, 0, 0, part, counter);
+        for (int i = 0; i < k; i++) {
+            const double* nxt = (i + 1 < k) ? sv[i + 1] : nullptr;
+            k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, yv[i], nxt, L, 1, i, i, i + 1, part, counter);
+        }
+        // h *= gamma, and the first dot of the second loop y_{k-1}.h
+        k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, nullptr, k > 0 ? yv[k - 1] : nullptr, L, 3, 0, 0, 64, part,
+                                            counter);
+        for (int i = k - 1; i > -1; i--) {
+            const double* nxt = i > 0 ? yv[i - 1] : nullptr;
+            k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, sv[i], nxt, L, 2, i, 64 + (k - 1 - i), 64 + (k - i), part,
+                                                counter);
+        }
+        MAPPG_CUDA(cudaGetLastError());
+        e_prev = e_curr;
+        read_prep(&fh, &hh, &hmax, &fmaxv);
+        if (fh < 0.0) {
+            MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            k = 0;
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+        }
+        // LineSearchBackTrack::min, init_flag 0
+        double dfa = -fh, max_a;
+        int lerr = LS_S;
+        if (hh == 0.0) {
+            max_a = 0.0;
+            dfa = 0.0;
+        } else if (dfa >= 0.0) {
+            max_a = 0.0;
+            dfa = 1.0;
+        } else {
+            max_a = fabs(max_dx / hmax);
+        }
+        if (dfa == 0.0)
+            lerr = LS_F_GRAD0;
+        else if (max_a == 0.0)
+            lerr = LS_MIN_ALPHA;
+        else if (dfa >= 0.0)
+            lerr = LS_F_DOWNHILL;
+        else {
+            max_a = fmin(max_a, 1.0);
+            if (max_a <= min_alpha)
+                lerr = LS_MIN_ALPHA;
+            else {
+                double a = max_a, init_energy = e_curr;
+                while (true) {
+                    double ideal = e_curr + a * c_ls * dfa;
+                    k_lb_trial<<<grid, 256, 0, st>>>(N, s->x, xs, h, a);
+                    double cur = lb_energy(s);
+                    n_en++;
+                    if (cur <= ideal) {
+                        e_curr = cur;
+                        lerr = LS_S;
+                        break;
+                    }
+                    a *= rho_ls;
+                    if (a <= min_alpha) {
+                        e_curr = init_energy;
+                        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+                        lb_update(s);
+                        lerr = LS_MIN_ALPHA;
+                        break;
+                    }
+                }
+                alpha_m = a;
+            }
+        }
+        err = lerr;
+        if (err != LS_S) {
+            istep--;
+            continue;
+        }
+        lb_force(s, &e_curr);
+        n_fc++;
+        if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
+        if (f_tol > 0.0) {
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+            if (fmaxv < f_tol) err = MIN_S_FTOL;
+        }
+        if (istep + 1 == nsteps) err = MIN_F_MAX_ITER;
+        if (err) continue;
+        if (m) {
+            if (k != m) k++;
+            double* ts = sv[k - 1];
+            double* ty = yv[k - 1];
+            for (int i = k - 1; i > 0; i--) {
+                sv[i] = sv[i - 1];
+                yv[i] = yv[i - 1];
+            }
+            sv[0] = ts;
+            yv[0] = ty;
+            k_lb_shift_rho<<<1, 1, 0, st>>>(L, m);
+            k_lb_hist<<<grid, 256, 0, st>>>(N, sv[0], yv[0], h, f0, s->f, alpha_m, L, part, counter);
+            MAPPG_CUDA(cudaGetLastError());
+        } else {
+            // gamma = alpha_m (h.f0 - h.f)/(f.f + f0.f0 - 2 f.f0) on the host
+            std::vector<double> hv(N), fv(N), f0v(N);
+            MAPPG_CUDA(cudaMemcpyAsync(hv.data(), h, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+            MAPPG_CUDA(cudaMemcpyAsync(fv.data(), s->f, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+            MAPPG_CUDA(cudaMemcpyAsync(f0v.data(), f0, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+            MAPPG_CUDA(cudaStreamSynchronize(st));
+            double hf0 = 0, hf = 0, ff = 0, f0f0 = 0, ff0 = 0;
+            for (int q = 0; q < N; q++) {
+                hf0 += hv[q] * f0v[q];
+                hf += hv[q] * fv[q];
+                ff += fv[q] * fv[q];
+                f0f0 += f0v[q] * f0v[q];
+                ff0 += fv[q] * f0v[q];
+            }
+            double g = alpha_m * (hf0 - hf) / (ff + f0f0 - 2.0 * ff0);
+            MAPPG_CUDA(cudaMemcpyAsync(&L->gamma, &g, sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+    }
+    if (f_tol <= 0.0 || err != MIN_S_FTOL) {
+        MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        read_prep(&fh, &hh, &hmax, &fmaxv);
+    }
+    DevScalars hs;
+    MAPPG_CUDA(cudaMemcpyAsync(&hs, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+    MAPPG_CUDA(cudaStreamSynchronize(st));
+    if (hs.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during minimization"};
+    if (hs.bad) throw Error{MAPPG_ERR_NAN, "non-finite value during minimization"};
+    if (stats) {
+        stats[0] = istep;
+        stats[1] = e_curr;
+        stats[2] = fmaxv;
+        stats[3] = err;
+        stats[4] = (double)n_en;
+        stats[5] = (double)n_fc;
+    }
+    s->forces_valid = true;
+}
+
+}  // namespace mappg

@@ -1,0 +1,688 @@
+// Device state of one periodic cell, coordinate transforms, binning and the
+// full neighbour-list build.
+//
+// The list holds, for every atom i, every periodic image j' = x_j + n*H
+// (j' != i) with |x_i - x_j'|^2 < (cut_ij + skin)^2, the same set that
+// NeighborMD::create_list (neighbor_md.cpp:82-152) finds in full mode
+// (pair_wise = false) over the ghost images of Update::list
+// (exchange.h:833-875).  Candidates come from the 27 bins around atom i; an
+// FP32 distance on bin-relative positions settles every pair outside a thin
+// band around the cutoff, and pairs inside the band are decided with the
+// reference's FP64 arithmetic: x = S2X(s) (xmath.h:2636-2658) of the wrapped
+// fractional coordinate, images at S2X(s_j + n), RSQ = d0^2 + (d1^2 + d2^2)
+// (xmath.h:2464-2510), no fused multiply-adds.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "system.h"
+
+namespace mappg {
+
+// ------------------------------------------------------------------ box
+// Atoms::update_H  atoms.cpp:187-194 with the lower-triangular inverse,
+// depth and determinant of xmath.h:1403-1480,2399-2415
+static void box_from_H(Box& b, const double* H9) {
+    memcpy(b.H, H9, sizeof(double) * 9);
+    double(*H)[3] = b.H;
+    double(*B)[3] = b.B;
+    memset(B, 0, sizeof(double) * 9);
+    B[0][0] = 1.0 / H[0][0];
+    B[1][1] = 1.0 / H[1][1];
+    B[1][0] = -B[1][1] * (B[0][0] * H[1][0]);
+    B[2][2] = 1.0 / H[2][2];
+    B[2][1] = -B[2][2] * (B[1][1] * H[2][1]);
+    B[2][0] = -B[2][2] * (B[0][0] * H[2][0] + B[1][0] * H[2][1]);
+    b.vol = H[0][0] * (H[1][1] * H[2][2]);
+    b.depth_inv[0] = sqrt(B[0][0] * B[0][0] + (B[1][0] * B[1][0] + B[2][0] * B[2][0]));
+    b.depth_inv[1] = sqrt(B[1][1] * B[1][1] + B[2][1] * B[2][1]);
+    b.depth_inv[2] = fabs(B[2][2]);
+    b.h6[0] = H[0][0]; b.h6[1] = H[1][0]; b.h6[2] = H[2][0];
+    b.h6[3] = H[1][1]; b.h6[4] = H[2][1]; b.h6[5] = H[2][2];
+    b.b6[0] = B[0][0]; b.b6[1] = B[1][0]; b.b6[2] = B[2][0];
+    b.b6[3] = B[1][1]; b.b6[4] = B[2][1]; b.b6[5] = B[2][2];
+}
+
+void sys_set_box(mappg_sys* s, const double* H) {
+    if (!(H[0] > 0 && H[4] > 0 && H[8] > 0) || H[1] != 0.0 || H[2] != 0.0 || H[5] != 0.0)
+        throw Error{MAPPG_ERR_ARG, "H must be lower triangular with a positive diagonal"};
+    box_from_H(s->box, H);
+    double nbv[3];
+    for (int d = 0; d < 3; d++) {
+        double cs = s->max_cut * s->box.depth_inv[d];
+        if (!(cs < 1.0))
+            throw Error{MAPPG_ERR_GEOM, "box thinner than cutoff+skin along dimension " + std::to_string(d) +
+                                            ": multi-layer periodic images are not supported"};
+        int nb = (int)(1.0 / (cs * (1.0 + 1e-12)));
+        nb = std::max(1, std::min(nb, 1023));
+        s->nb[d] = nb;
+        nbv[d] = 1.0 / nb;
+    }
+    s->nbins = s->nb[0] * s->nb[1] * s->nb[2];
+    // neighbour code c = (d0+1)+3(d1+1)+9(d2+1): the image's bin is atom i's bin + d
+    for (int c = 0; c < 27; c++) {
+        int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
+        for (int k = 0; k < 3; k++) {
+            double o = 0.0, sh = 0.0;
+            for (int q = 0; q < 3; q++) {
+                o -= d[q] * nbv[q] * s->box.H[q][k];
+                sh += d[q] * s->box.H[q][k];
+            }
+            s->off32[c][k] = (float)o;
+            s->shift[c][k] = sh;  // indexed by image code n instead of d
+        }
+        s->off32[c][3] = 0.f;
+    }
+    double pmax = s->skin;
+    for (int q = 0; q < 3; q++) {
+        double l = 0;
+        for (int k = 0; k < 3; k++) l += s->box.H[q][k] * s->box.H[q][k];
+        pmax += sqrt(l) * nbv[q];
+    }
+    double csk = 0;
+    for (int i = 0; i < s->ne * s->ne; i++) csk = std::max(csk, s->cut_sk_sq[i]);
+    s->band = 2e-5 * (csk + pmax * pmax);
+    s->built = false;
+}
+
+int grid_for(mappg_sys* s, long long threads, int block) {
+    long long g = (threads + block - 1) / block;
+    long long cap = (long long)s->sm_count * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    if (g > kMaxBlocks) g = kMaxBlocks;
+    return (int)g;
+}
+
+// ------------------------------------------------------------------ kernels
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+struct Geo {
+    double h6[6], b6[6];
+    double bv[3][3];  // bin vectors H[d]/nb[d]
+    int nb[3];
+};
+
+static Geo make_geo(mappg_sys* s) {
+    Geo g;
+    memcpy(g.h6, s->box.h6, sizeof(g.h6));
+    memcpy(g.b6, s->box.b6, sizeof(g.b6));
+    for (int d = 0; d < 3; d++) {
+        g.nb[d] = s->nb[d];
+        for (int k = 0; k < 3; k++) g.bv[d][k] = s->box.H[d][k] / s->nb[d];
+    }
+    return g;
+}
+
+// one wrap of X2S (xmath.h:2660-2700): ++/-- until in [0,1); bounded
+__device__ __forceinline__ double wrap01(double v, int* bad) {
+    int it = 0;
+    while (v < 0.0 && it < 64) {
+        v = dadd(v, 1.0);
+        it++;
+    }
+    while (v >= 1.0 && it < 64) {
+        v = dsub(v, 1.0);
+        it++;
+    }
+    if (it >= 64 || v != v) {
+        *bad = 1;
+        v = 0.0;
+    }
+    return v;
+}
+
+__device__ __forceinline__ void s2x(const double* h, double s0, double s1, double s2, double& x0, double& x1,
+                                    double& x2) {
+    x0 = dadd(dmul(h[0], s0), dadd(dmul(h[1], s1), dmul(h[2], s2)));
+    x1 = dadd(dmul(h[3], s1), dmul(h[4], s2));
+    x2 = dmul(s2, h[5]);
+}
+
+// rebuild step 1: wrap x into the cell (x2s_lcl then s2x_all), bin, count
+__global__ void k_wrap_bin(int n, double* __restrict__ x, double* __restrict__ s, Geo g, int* __restrict__ binc,
+                           int* __restrict__ binid, int* __restrict__ bin_count, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double x0 = x[i], x1 = x[n + i], x2 = x[2 * n + i];
+        double s0 = dadd(dmul(g.b6[0], x0), dadd(dmul(g.b6[1], x1), dmul(g.b6[2], x2)));
+        s0 = wrap01(s0, &bad);
+        double s1 = dadd(dmul(g.b6[3], x1), dmul(g.b6[4], x2));
+        s1 = wrap01(s1, &bad);
+        double s2 = dmul(x2, g.b6[5]);
+        s2 = wrap01(s2, &bad);
+        s2x(g.h6, s0, s1, s2, x0, x1, x2);
+        x[i] = x0;
+        x[n + i] = x1;
+        x[2 * n + i] = x2;
+        s[i] = s0;
+        s[n + i] = s1;
+        s[2 * n + i] = s2;
+        int b0 = min((int)(s0 * g.nb[0]), g.nb[0] - 1);
+        int b1 = min((int)(s1 * g.nb[1]), g.nb[1] - 1);
+        int b2 = min((int)(s2 * g.nb[2]), g.nb[2] - 1);
+        binc[i] = b0 | (b1 << 10) | (b2 << 20);
+        int b = b0 + g.nb[0] * (b1 + g.nb[1] * b2);
+        binid[i] = b;
+        atomicAdd(&bin_count[b], 1);
+    }
+    if (bad) sc->bad = 1;
+}
+
+// rebuild step 2: exclusive scan of bin counts (one block), counts zeroed
+__global__ void k_scan_bins(int nbins, int* __restrict__ bin_count, int* __restrict__ bin_start, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    __shared__ int part[1024];
+    int t = threadIdx.x, T = blockDim.x;
+    int chunk = (nbins + T - 1) / T;
+    int lo = min(t * chunk, nbins), hi = min(lo + chunk, nbins);
+    int sum = 0;
+    for (int b = lo; b < hi; b++) sum += bin_count[b];
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        int v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - sum;
+    for (int b = lo; b < hi; b++) {
+        int c = bin_count[b];
+        bin_start[b] = run;
+        run += c;
+        bin_count[b] = 0;
+    }
+    if (t == T - 1) bin_start[nbins] = part[T - 1];
+    if (t == 0) {
+        sc->maxrow = 0;
+        sc->sumrow = 0;
+    }
+}
+
+// rebuild step 3: scatter atom indices into their bins (order fixed next)
+__global__ void k_scatter_bins(int n, const int* __restrict__ binid, const int* __restrict__ bin_start,
+                               int* __restrict__ bin_count, int* __restrict__ bin_tmp, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int b = binid[i];
+        int slot = atomicAdd(&bin_count[b], 1);
+        bin_tmp[bin_start[b] + slot] = i;
+    }
+}
+
+// rebuild step 4: one warp per bin ranks its atoms by index (deterministic
+// order), counts zeroed for the next rebuild
+__global__ void k_sort_bins(int nbins, const int* __restrict__ bin_start, const int* __restrict__ bin_tmp,
+                            int* __restrict__ bin_atoms, int* __restrict__ bin_count, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    int lane = threadIdx.x & 31;
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int b = warp; b < nbins; b += nw) {
+        int lo = bin_start[b], hi = bin_start[b + 1];
+        for (int k = lo + lane; k < hi; k += 32) {
+            int a = bin_tmp[k];
+            int r = 0;
+            for (int q = lo; q < hi; q++) r += bin_tmp[q] < a;
+            bin_atoms[lo + r] = a;
+        }
+        if (lane == 0) bin_count[b] = 0;
+    }
+}
+
+// FP32 bin-relative positions (the shadow the mixed kernels gather);
+// gated == true only runs inside a rebuild
+__global__ void k_shadow(int n, const double* __restrict__ x, const int* __restrict__ binc,
+                         const uint8_t* __restrict__ elem, float4* __restrict__ p32, Geo g, int gated,
+                         DevScalars* sc) {
+    if (gated && !sc->rebuild) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int bc = binc[i];
+        double b0 = bc & 1023, b1 = (bc >> 10) & 1023, b2 = (bc >> 20) & 1023;
+        double o0 = b0 * g.bv[0][0] + b1 * g.bv[1][0] + b2 * g.bv[2][0];
+        double o1 = b1 * g.bv[1][1] + b2 * g.bv[2][1];
+        double o2 = b2 * g.bv[2][2];
+        float4 p;
+        p.x = (float)(x[i] - o0);
+        p.y = (float)(x[n + i] - o1);
+        p.z = (float)(x[2 * n + i] - o2);
+        p.w = __int_as_float((int)elem[i]);
+        p32[i] = p;
+    }
+}
+
+struct BuildArgs {
+    int n, maxnbr, ne;
+    const double* x;
+    const double* s;
+    const float4* p32;
+    const int* binc;
+    const int* bin_start;
+    const int* bin_atoms;
+    int* nbr;
+    int* nnbr;
+    double* x0;
+    Geo g;
+    float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
+    double cut_sk_sq[kMaxElem * kMaxElem];
+    float off32[27][4];
+};
+
+// rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
+// candidates, ballots keep the row in (bin, index) order; x0 <- x
+__global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    __shared__ float4 off[27];
+    if (threadIdx.x < 27)
+        off[threadIdx.x] = make_float4(a.off32[threadIdx.x][0], a.off32[threadIdx.x][1], a.off32[threadIdx.x][2], 0.f);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = a.n;
+    int maxrow = 0;
+    long long sumrow = 0;
+    int overflow = 0;
+    for (int i = warp; i < n; i += nw) {
+        float4 pi = a.p32[i];
+        int ei = __float_as_int(pi.w);
+        int bc = a.binc[i];
+        int bi[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
+        double xi0 = a.x[i], xi1 = a.x[n + i], xi2 = a.x[2 * n + i];
+        int cnt = 0;
+        int* row = a.nbr + (size_t)i * a.maxnbr;
+        for (int c = 0; c < 27; c++) {
+            int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
+            int u0 = bi[0] + d0, u1 = bi[1] + d1, u2 = bi[2] + d2;
+            int n0 = u0 < 0 ? -1 : (u0 >= a.g.nb[0] ? 1 : 0);
+            int n1 = u1 < 0 ? -1 : (u1 >= a.g.nb[1] ? 1 : 0);
+            int n2 = u2 < 0 ? -1 : (u2 >= a.g.nb[2] ? 1 : 0);
+            int w0 = u0 - n0 * a.g.nb[0], w1 = u1 - n1 * a.g.nb[1], w2 = u2 - n2 * a.g.nb[2];
+            int b = w0 + a.g.nb[0] * (w1 + a.g.nb[1] * w2);
+            int lo = a.bin_start[b], hi = a.bin_start[b + 1];
+            float4 o = off[c];
+            bool self_img = (n0 | n1 | n2) == 0;
+            for (int k0 = lo; k0 < hi; k0 += 32) {
+                int k = k0 + lane;
+                bool keep = false;
+                int j = 0;
+                if (k < hi) {
+                    j = a.bin_atoms[k];
+                    if (!(self_img && j == i)) {
+                        float4 pj = a.p32[j];
+                        int ej = __float_as_int(pj.w);
+                        float dx = (pi.x - pj.x) + o.x, dy = (pi.y - pj.y) + o.y, dz = (pi.z - pj.z) + o.z;
+                        float r2 = dx * dx + (dy * dy + dz * dz);
+                        int pe = ei * a.ne + ej;
+                        if (r2 < a.lo2[pe]) {
+                            keep = true;
+                        } else if (r2 <= a.hi2[pe]) {
+                            // exact reference predicate on S2X(s_j + n)
+                            double s0 = a.s[j], s1 = a.s[n + j], s2 = a.s[2 * n + j];
+                            if (n0 > 0) s0 = dadd(s0, 1.0);
+                            if (n0 < 0) s0 = dsub(s0, 1.0);
+                            if (n1 > 0) s1 = dadd(s1, 1.0);
+                            if (n1 < 0) s1 = dsub(s1, 1.0);
+                            if (n2 > 0) s2 = dadd(s2, 1.0);
+                            if (n2 < 0) s2 = dsub(s2, 1.0);
+                            double xj0, xj1, xj2;
+                            s2x(a.g.h6, s0, s1, s2, xj0, xj1, xj2);
+                            double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
+                            double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
+                            keep = rsq < a.cut_sk_sq[pe];
+                        }
+                    }
+                }
+                unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    if (pos < a.maxnbr) row[pos] = (j << kCodeBits) | c;
+                }
+                cnt += __popc(m);
+            }
+        }
+        if (lane == 0) {
+            a.nnbr[i] = min(cnt, a.maxnbr);
+            if (cnt > a.maxnbr) overflow = 1;
+            maxrow = max(maxrow, cnt);
+            sumrow += cnt;
+        }
+        if (lane < 3) a.x0[lane * n + i] = lane == 0 ? xi0 : (lane == 1 ? xi1 : xi2);
+    }
+    if (lane == 0) {
+        if (overflow) sc->overflow = 1;
+        if (maxrow) atomicMax(&sc->maxrow, maxrow);
+        if (sumrow) atomicAdd(&sc->sumrow, (unsigned long long)sumrow);
+    }
+}
+
+__global__ void k_rebuild_done(DevScalars* sc) {
+    if (!sc->rebuild) return;
+    sc->nrebuild++;
+}
+
+// skin test of DynamicMD::decide (dynamic_md.cpp:90-105): rebuild when any
+// |x - x0|^2 > skin^2/4, RSQ order, FP64
+__global__ void k_skin(int n, const double* __restrict__ x, const double* __restrict__ x0, double skin_sq,
+                       DevScalars* sc) {
+    int moved = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d0 = dsub(x0[i], x[i]), d1 = dsub(x0[n + i], x[n + i]), d2 = dsub(x0[2 * n + i], x[2 * n + i]);
+        double r = dadd(dmul(d0, d0), dadd(dmul(d1, d1), dmul(d2, d2)));
+        moved |= r > skin_sq;
+    }
+    if (__syncthreads_or(moved) && threadIdx.x == 0) sc->rebuild = 1;
+}
+
+__global__ void k_set_rebuild(DevScalars* sc, int v) {
+    sc->rebuild = v;
+}
+
+// caller order (AoS) <-> bin-sorted order (SoA)
+__global__ void k_gather_aos(int n, const int* __restrict__ id, const double* __restrict__ src,
+                             double* __restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int u = id[i];
+        dst[i] = src[3 * (size_t)u];
+        dst[n + i] = src[3 * (size_t)u + 1];
+        dst[2 * n + i] = src[3 * (size_t)u + 2];
+    }
+}
+
+__global__ void k_scatter_aos(int n, const int* __restrict__ id, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int u = id[i];
+        dst[3 * (size_t)u] = src[i];
+        dst[3 * (size_t)u + 1] = src[n + i];
+        dst[3 * (size_t)u + 2] = src[2 * n + i];
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+void request_rebuild(mappg_sys* s) {
+    k_set_rebuild<<<1, 1, 0, s->stream>>>(s->sc, 1);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+void launch_shadow(mappg_sys* s, bool gated) {
+    Geo g = make_geo(s);
+    k_shadow<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->elem, s->p32, g, gated ? 1 : 0,
+                                                            s->sc);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+void launch_rebuild_chain(mappg_sys* s) {
+    Geo g = make_geo(s);
+    const int B = 256;
+    int gb = grid_for(s, s->n, B);
+    k_wrap_bin<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, g, s->binc, s->binid, s->bin_count, s->sc);
+    k_scan_bins<<<1, 1024, 0, s->stream>>>(s->nbins, s->bin_count, s->bin_start, s->sc);
+    int* bin_tmp = s->bin_atoms + s->n;
+    k_scatter_bins<<<gb, B, 0, s->stream>>>(s->n, s->binid, s->bin_start, s->bin_count, bin_tmp, s->sc);
+    k_sort_bins<<<grid_for(s, (long long)s->nbins * 32, B), B, 0, s->stream>>>(s->nbins, s->bin_start, bin_tmp,
+                                                                               s->bin_atoms, s->bin_count, s->sc);
+    k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->elem, s->p32, g, 1, s->sc);
+    BuildArgs a;
+    a.n = s->n;
+    a.maxnbr = s->maxnbr;
+    a.ne = s->ne;
+    a.x = s->x;
+    a.s = s->s;
+    a.p32 = s->p32;
+    a.binc = s->binc;
+    a.bin_start = s->bin_start;
+    a.bin_atoms = s->bin_atoms;
+    a.nbr = s->nbr;
+    a.nnbr = s->nnbr;
+    a.x0 = s->x0;
+    a.g = g;
+    for (int p = 0; p < s->ne * s->ne; p++) {
+        a.cut_sk_sq[p] = s->cut_sk_sq[p];
+        a.lo2[p] = (float)(s->cut_sk_sq[p] - s->band);
+        a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
+    }
+    memcpy(a.off32, s->off32, sizeof(a.off32));
+    k_build_list<<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
+    k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+void launch_skin_test(mappg_sys* s) {
+    double skin_sq = 0.25 * s->skin * s->skin;
+    k_skin<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->x0, skin_sq, s->sc);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+EamArgs eam_args(mappg_sys* s) {
+    const mappg_ff* ff = s->ff;
+    EamArgs a;
+    memset(&a, 0, sizeof(a));
+    a.n = s->n;
+    a.maxnbr = s->maxnbr;
+    a.ne = s->ne;
+    a.nr = ff->dev.nr;
+    a.nrho = ff->dev.nrho;
+    a.nbr = s->nbr;
+    a.nnbr = s->nnbr;
+    a.elem = s->elem;
+    a.x = s->x;
+    a.p32 = s->p32;
+    a.binc = s->binc;
+    a.rho64 = ff->dev.rho64;
+    a.rphi64 = ff->dev.rphi64;
+    a.F64 = ff->dev.F64;
+    a.rho32 = ff->dev.rho32;
+    a.rphi32 = ff->dev.rphi32;
+    a.F32 = ff->dev.F32;
+    a.dr_inv = ff->dev.dr_inv;
+    a.drho_inv = ff->dev.drho_inv;
+    a.rho_max = ff->dev.rho_max;
+    for (int p = 0; p < s->ne * s->ne; p++) a.cut_sq[p] = s->cut_sq[p];
+    memcpy(a.shift, s->shift, sizeof(a.shift));
+    memcpy(a.off32, s->off32, sizeof(a.off32));
+    for (int d = 0; d < 3; d++) a.nb[d] = s->nb[d];
+    a.rho = s->rho;
+    a.dF = s->dF;
+    a.dF32 = s->dF32;
+    a.f = s->f;
+    a.partials = s->partials;
+    a.sc = s->sc;
+    return a;
+}
+
+// host check after a build: capacity, bad coordinates
+void check_build(mappg_sys* s) {
+    DevScalars h;
+    MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite or far out-of-cell position"};
+    if (h.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded"};
+}
+
+}  // namespace mappg
+
+using namespace mappg;
+
+// ------------------------------------------------------------------ system lifecycle (called from api.cpp)
+namespace mappg {
+
+static void dev_alloc(void** p, size_t bytes) { MAPPG_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 16)); }
+
+void sys_free(mappg_sys* s) {
+    void* ptrs[] = {s->x, s->v, s->f, s->x0, s->s, s->elem, s->id, s->inv, s->p32, s->binc, s->binid,
+                    s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr, s->rho, s->dF, s->dF32,
+                    s->partials, s->sc, s->stage, s->thermo_dev};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+static unsigned long long morton3(unsigned a, unsigned b, unsigned c) {
+    auto spread = [](unsigned long long v) {
+        v &= 0x1fffff;
+        v = (v | v << 32) & 0x1f00000000ffffULL;
+        v = (v | v << 16) & 0x1f0000ff0000ffULL;
+        v = (v | v << 8) & 0x100f00f00f00f00fULL;
+        v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+        v = (v | v << 2) & 0x1249249249249249ULL;
+        return v;
+    };
+    return spread(a) | (spread(b) << 1) | (spread(c) << 2);
+}
+
+void sys_alloc(mappg_sys* s, const double* x_host) {
+    const int n = s->n;
+    MAPPG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    // fixed atom order: Morton order of the initial bins, then caller index
+    std::vector<unsigned long long> key(n);
+    const double* b6 = s->box.b6;
+    for (int u = 0; u < n; u++) {
+        const double* xu = x_host + 3 * (size_t)u;
+        double sv[3] = {b6[0] * xu[0] + (b6[1] * xu[1] + b6[2] * xu[2]), b6[3] * xu[1] + b6[4] * xu[2], xu[2] * b6[5]};
+        unsigned b[3];
+        for (int d = 0; d < 3; d++) {
+            double w = sv[d] - floor(sv[d]);
+            if (!(w >= 0.0 && w < 1.0)) w = 0.0;
+            b[d] = (unsigned)std::min((int)(w * s->nb[d] * 2), 2 * s->nb[d] - 1);
+        }
+        key[u] = morton3(b[0], b[1], b[2]);
+    }
+    s->host_id.resize(n);
+    std::iota(s->host_id.begin(), s->host_id.end(), 0);
+    std::stable_sort(s->host_id.begin(), s->host_id.end(), [&](int a, int b) { return key[a] < key[b]; });
+    std::vector<int> inv(n);
+    for (int i = 0; i < n; i++) inv[s->host_id[i]] = i;
+
+    size_t nd = (size_t)3 * n * sizeof(double);
+    dev_alloc((void**)&s->x, nd);
+    dev_alloc((void**)&s->v, nd);
+    dev_alloc((void**)&s->f, nd);
+    dev_alloc((void**)&s->x0, nd);
+    dev_alloc((void**)&s->s, nd);
+    dev_alloc((void**)&s->stage, nd);
+    dev_alloc((void**)&s->elem, n);
+    dev_alloc((void**)&s->id, sizeof(int) * n);
+    dev_alloc((void**)&s->inv, sizeof(int) * n);
+    dev_alloc((void**)&s->p32, sizeof(float4) * n);
+    dev_alloc((void**)&s->binc, sizeof(int) * n);
+    dev_alloc((void**)&s->binid, sizeof(int) * n);
+    dev_alloc((void**)&s->bin_atoms, sizeof(int) * 2 * (size_t)n);
+    dev_alloc((void**)&s->nnbr, sizeof(int) * n);
+    dev_alloc((void**)&s->rho, sizeof(double) * n);
+    dev_alloc((void**)&s->dF, sizeof(double) * n);
+    dev_alloc((void**)&s->dF32, sizeof(float) * n);
+    dev_alloc((void**)&s->partials, sizeof(double) * kRedSlots * kMaxBlocks);
+    dev_alloc((void**)&s->sc, sizeof(DevScalars));
+    MAPPG_CUDA(cudaMemsetAsync(s->sc, 0, sizeof(DevScalars), s->stream));
+    MAPPG_CUDA(cudaMemsetAsync(s->v, 0, nd, s->stream));
+    MAPPG_CUDA(cudaMemsetAsync(s->f, 0, nd, s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(s->id, s->host_id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(s->inv, inv.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+void sys_alloc_bins(mappg_sys* s) {
+    if (s->bin_count) cudaFree(s->bin_count);
+    if (s->bin_start) cudaFree(s->bin_start);
+    s->bin_count = nullptr;
+    s->bin_start = nullptr;
+    dev_alloc((void**)&s->bin_count, sizeof(int) * s->nbins);
+    dev_alloc((void**)&s->bin_start, sizeof(int) * (s->nbins + 1));
+    MAPPG_CUDA(cudaMemsetAsync(s->bin_count, 0, sizeof(int) * s->nbins, s->stream));
+}
+
+void sys_alloc_nbr(mappg_sys* s, int maxnbr) {
+    if (s->nbr) cudaFree(s->nbr);
+    s->nbr = nullptr;
+    s->maxnbr = maxnbr;
+    dev_alloc((void**)&s->nbr, sizeof(int) * (size_t)s->n * maxnbr);
+}
+
+// upload caller-order AoS doubles into a SoA device array
+void sys_upload(mappg_sys* s, const double* host, double* dev) {
+    MAPPG_CUDA(cudaMemcpyAsync(s->stage, host, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
+    k_gather_aos<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, s->stage, dev);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+void sys_download(mappg_sys* s, const double* dev, double* host) {
+    k_scatter_aos<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, dev, s->stage);
+    MAPPG_CUDA(cudaGetLastError());
+    MAPPG_CUDA(cudaMemcpyAsync(host, s->stage, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+// full build with capacity growth: first build sizes the rows from a count
+void sys_build(mappg_sys* s) {
+    for (int attempt = 0; attempt < 4; attempt++) {
+        request_rebuild(s);
+        MAPPG_CUDA(cudaMemsetAsync(&s->sc->overflow, 0, sizeof(int), s->stream));
+        launch_rebuild_chain(s);
+        DevScalars h;
+        MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite or far out-of-cell position"};
+        if (!h.overflow) {
+            k_set_rebuild<<<1, 1, 0, s->stream>>>(s->sc, 0);
+            s->built = true;
+            return;
+        }
+        int need = (int)h.maxrow;
+        int cap = ((need + need / 4 + 16) + 31) / 32 * 32;
+        sys_alloc_nbr(s, cap);
+    }
+    throw Error{MAPPG_ERR_NBR, "neighbour list capacity could not be sized"};
+}
+
+void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
+    const int n = s->n;
+    std::vector<int> nn(n), bc(n);
+    MAPPG_CUDA(cudaMemcpyAsync(nn.data(), s->nnbr, sizeof(int) * n, cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(bc.data(), s->binc, sizeof(int) * n, cudaMemcpyDeviceToHost, s->stream));
+    std::vector<int> rows;
+    if (entries) {
+        rows.resize((size_t)n * s->maxnbr);
+        MAPPG_CUDA(cudaMemcpyAsync(rows.data(), s->nbr, sizeof(int) * rows.size(), cudaMemcpyDeviceToHost, s->stream));
+    }
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    long long tot = 0;
+    std::vector<long long> off(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        int u = s->host_id[i];
+        if (counts) counts[u] = nn[i];
+        tot += nn[i];
+    }
+    if (total) *total = tot;
+    if (!entries) return;
+    // caller order offsets
+    std::vector<long long> uoff(n + 1, 0);
+    std::vector<int> ucount(n);
+    for (int i = 0; i < n; i++) ucount[s->host_id[i]] = nn[i];
+    for (int u = 0; u < n; u++) uoff[u + 1] = uoff[u] + ucount[u];
+    for (int i = 0; i < n; i++) {
+        int u = s->host_id[i];
+        int b[3] = {bc[i] & 1023, (bc[i] >> 10) & 1023, (bc[i] >> 20) & 1023};
+        int* out = entries + 4 * uoff[u];
+        for (int k = 0; k < nn[i]; k++) {
+            int e = rows[(size_t)i * s->maxnbr + k];
+            int j = e >> kCodeBits, c = e & 31;
+            int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
+            out[4 * k] = s->host_id[j];
+            for (int q = 0; q < 3; q++) {
+                int uq = b[q] + d[q];
+                out[4 * k + 1 + q] = uq < 0 ? -1 : (uq >= s->nb[q] ? 1 : 0);
+            }
+        }
+    }
+}
+
+}  // namespace mappg

@@ -1,0 +1,233 @@
+"""The `mapp4py.md` surface for the EAM path, backed by libmappg on the GPU.
+
+Names, arguments and defaults follow the reference's Python types:
+  md.atoms             AtomsMD (atoms_md.cpp); here built from arrays, with
+                       ff_eam_setfl / ff_eam_funcfl / ff_eam_fs (ff_eam.cpp:594-801),
+                       create_temp (atoms_md.cpp:490-531), kB, skin, H, x, x_d
+  md.nvt(T, dt)        MDNVT (md_nvt.cpp:14-26,493-881): t_relax=100*dt, L=3,
+                       niters=1, ntally=10000, run(atoms, nsteps)
+  md.min_lbfgs(...)    MinLBFGS (min_l-bfgs.cpp:69-127): m=2, e_tol=sqrt(eps),
+                       affine=False, max_dx=1.0, ls=ls_bt(); run(atoms, max_nsteps)
+  ls_bt()              LineSearchBackTrack (ls.cpp:456-461): c=0.4, rho=0.5,
+                       min_alpha=0.0
+Additive: atoms.precision ('fp64' | 'mixed') selects the GPU arithmetic, and
+min_lbfgs.f_tol adds the max|F| stop.
+
+Each run keeps the reference's semantics: positions and velocities are read
+from the atoms object, the neighbour list is rebuilt at the start, and the
+results are written back when the run returns.
+"""
+import math
+import sys
+
+import numpy as np
+
+from . import _lib
+
+_PREC = {"fp64": _lib.FP64, "mixed": _lib.MIXED}
+
+
+class ls_bt:
+    """Back-tracking (Armijo) line search parameters."""
+
+    def __init__(self, c=0.4, rho=0.5, min_alpha=0.0):
+        if not (0.0 < c < 1.0):
+            raise TypeError("c must be in (0,1)")
+        if not (0.0 < rho < 1.0):
+            raise TypeError("rho must be in (0,1)")
+        if min_alpha < 0.0:
+            raise TypeError("min_alpha must be >= 0")
+        self.c, self.rho, self.min_alpha = float(c), float(rho), float(min_alpha)
+
+
+class atoms:
+    """A periodic cell: H (lower-triangular rows), x [N][3], elem [N] indices
+    into elems, masses per element."""
+
+    def __init__(self, H, x, elem, elems=("A",), masses=(63.5,), x_d=None):
+        self.H = np.ascontiguousarray(H, dtype=np.float64).reshape(3, 3)
+        self.x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3).copy()
+        self.elem = np.ascontiguousarray(elem, dtype=np.uint8).copy()
+        if self.elem.shape[0] != self.x.shape[0]:
+            raise TypeError("elem and x sizes differ")
+        self.elems = tuple(elems)
+        self.masses = np.ascontiguousarray(masses, dtype=np.float64)
+        self.x_d = None if x_d is None else np.ascontiguousarray(x_d, dtype=np.float64).reshape(-1, 3).copy()
+        self.f = None
+        self.kB = float("nan")
+        self.skin = 0.5
+        self.precision = "fp64"
+        self.step = 0
+        self.pe = float("nan")
+        self.S_pe = np.full((3, 3), np.nan)
+        self.ff = None
+        self._sys = None
+        self._sys_key = None
+
+    @property
+    def natms(self):
+        return self.x.shape[0]
+
+    @property
+    def vol(self):
+        return float(self.H[0, 0] * self.H[1, 1] * self.H[2, 2])
+
+    # ---------------------------------------------------------- force fields
+    def _remap(self, ff):
+        # the file's elements become the system's; an existing element list
+        # selects and orders them, as the reference's element mapping does
+        self.ff = ff
+        if ff.names and all(ff.names):
+            self.elems = tuple(ff.names)
+        if self.masses.shape[0] != ff.nelem:
+            m = np.full(ff.nelem, self.masses[0] if self.masses.size else 1.0)
+            m[: min(ff.nelem, self.masses.shape[0])] = self.masses[: ff.nelem]
+            self.masses = m
+        self._sys = None
+
+    def ff_eam_setfl(self, setfl_file):
+        elems = list(self.elems) if all(self.elems) else None
+        try:
+            self._remap(_lib.ForceField.setfl(setfl_file, elems))
+        except _lib.MappgError as e:
+            raise TypeError(str(e)) from None
+
+    def ff_eam_fs(self, fs_file):
+        elems = list(self.elems) if all(self.elems) else None
+        try:
+            self._remap(_lib.ForceField.fs(fs_file, elems))
+        except _lib.MappgError as e:
+            raise TypeError(str(e)) from None
+
+    def ff_eam_funcfl(self, funcfl_files, elems=None):
+        if isinstance(funcfl_files, str):
+            funcfl_files = [funcfl_files]
+        try:
+            self._remap(_lib.ForceField.funcfl(funcfl_files))
+        except _lib.MappgError as e:
+            raise TypeError(str(e)) from None
+        if elems is not None:
+            self.elems = tuple(elems)
+
+    def create_temp(self, temp, seed):
+        if math.isnan(self.kB):
+            raise TypeError("boltzmann constant should be set prior to create_temp")
+        self.x_d = _lib.create_temp(self.elem, self.masses, temp, self.kB, seed)
+
+    # ---------------------------------------------------------- device state
+    def _system(self):
+        if self.ff is None:
+            raise TypeError("cannot start without governing equations (force field)")
+        key = (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
+        if self._sys is None or self._sys_key != key:
+            self._sys = None
+            self._sys = _lib.System(self.ff, self.H, self.x, self.elem, self.masses, self.skin,
+                                    _PREC[self.precision])
+            self._sys_key = key
+        return self._sys
+
+
+def _print_thermo(th, step0, ntally, vol):
+    hdr = "%8s %14s %16s %12s %12s %12s" % ("step", "T", "PE", "S[0][0]", "S[1][1]", "S[2][2]")
+    print(hdr)
+    n = th.shape[0] - 1
+    for k in range(n + 1):
+        if k == 0 or k == n or (ntally and k % ntally == 0):
+            r = th[k]
+            # S_part = S_pe - mvv/V with S_pe = -F_H/V
+            s = [-(r[8 + q] + r[2 + q]) / vol for q in (0, 3, 5)]
+            print("%8d %14.6f %16.8f %12.6e %12.6e %12.6e" % (step0 + k, r[1], r[0], s[0], s[1], s[2]))
+    sys.stdout.flush()
+
+
+class nvt:
+    """Canonical MD with a Nose-Hoover chain (NVE: t_relax = inf)."""
+
+    def __init__(self, T, dt):
+        if not (T > 0.0):
+            raise TypeError("T should be greater than 0.0")
+        if not (dt > 0.0):
+            raise TypeError("dt should be greater than 0.0")
+        self.T = float(T)
+        self.dt = float(dt)
+        self.t_relax = 100.0 * self.dt
+        self.L = 3
+        self.niters = 1
+        self.ntally = 10000
+        self.export = None
+        self._eta = np.zeros(3)
+
+    def run(self, atoms, nsteps):
+        if nsteps < 0:
+            raise TypeError("nsteps should be greater than or equal to 0")
+        if atoms.ff is None:
+            raise TypeError("cannot start md without governing equations (force field)")
+        if math.isnan(atoms.kB):
+            raise TypeError("boltzmann constant should be set prior to MD")
+        if self._eta.shape[0] != self.L:
+            self._eta = np.zeros(self.L)
+        s = atoms._system()
+        s.set_x(atoms.x)
+        s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
+        th, self._eta = s.nvt_run(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L,
+                                  niters=self.niters, eta=self._eta, thermo=bool(self.ntally))
+        s.get_x(atoms.x)
+        if atoms.x_d is None:
+            atoms.x_d = np.zeros_like(atoms.x)
+        s.get_v(atoms.x_d)
+        atoms.f = s.get_f()
+        if th is not None:
+            _print_thermo(th, atoms.step, self.ntally, atoms.vol)
+            atoms.pe = float(th[-1, 0])
+            F_H = th[-1, 8:14]
+        else:
+            atoms.pe, F_H = s.force()
+        atoms.S_pe = _voigt_to_matrix(-np.asarray(F_H) / atoms.vol)
+        atoms.step += nsteps
+
+
+def _voigt_to_matrix(v):
+    v = np.asarray(v)
+    return np.array([[v[0], v[1], v[2]], [v[1], v[3], v[4]], [v[2], v[4], v[5]]])
+
+
+class min_lbfgs:
+    """L-BFGS minimization of positions (box degrees of freedom are not in
+    this engine's scope; H_dof must stay all False)."""
+
+    def __init__(self, m=2, e_tol=math.sqrt(sys.float_info.epsilon), H_dof=None, affine=False, max_dx=1.0,
+                 ls=None, f_tol=0.0):
+        if m < 0:
+            raise TypeError("m should be greater than or equal to 0")
+        if e_tol < 0.0:
+            raise TypeError("e_tol should be greater than or equal to 0.0")
+        if not (max_dx > 0.0):
+            raise TypeError("max_dx should be greater than 0.0")
+        if H_dof is not None and np.any(np.asarray(H_dof, dtype=object) == True):  # noqa: E712
+            raise TypeError("box degrees of freedom (H_dof) are not supported by this engine")
+        if affine:
+            raise TypeError("affine minimization is not supported by this engine")
+        self.m = int(m)
+        self.e_tol = float(e_tol)
+        self.max_dx = float(max_dx)
+        self.ls = ls if ls is not None else ls_bt()
+        self.f_tol = float(f_tol)
+        self.ntally = 1000
+        self.export = None
+        self.last = None
+
+    def run(self, atoms, max_nsteps):
+        if max_nsteps < 0:
+            raise TypeError("max_nsteps should be greater than or equal to 0")
+        if not isinstance(self.ls, ls_bt):
+            raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
+        s = atoms._system()
+        s.set_x(atoms.x)
+        r = s.lbfgs_run(m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c,
+                        rho=self.ls.rho, min_alpha=self.ls.min_alpha, nsteps=max_nsteps)
+        s.get_x(atoms.x)
+        atoms.f = s.get_f()
+        atoms.pe = r["pe"]
+        atoms.step += r["niter"]
+        self.last = r
+        return r

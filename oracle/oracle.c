@@ -31,6 +31,13 @@
 #define OMIN(a, b) ((a) < (b) ? (a) : (b))
 #define OMAX(a, b) ((a) > (b) ? (a) : (b))
 
+#include <time.h>
+static double now_seconds(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
 static char orc_err[512];
 const char* orc_last_error(void) { return orc_err; }
 static int fail(const char* msg) {
@@ -889,6 +896,20 @@ static void force_calc(orc_sys* s) {
     for (int k = 0; k < 6; k++) s->S_pe[ia[k]][ja[k]] = s->S_pe[ja[k]][ia[k]] = vv[k + 1];
 }
 
+/* force_calc over the full list with nthreads threads (timing baseline);
+   the sign and volume conventions of ForceFieldMD::force_calc */
+double orc_sys_force_full(void* p, double* out7, int nthreads);
+static void force_calc_threads(orc_sys* s, int nthreads) {
+    double o[7];
+    orc_sys_force_full(s, o, nthreads);
+    static const int ia[6] = {0, 0, 0, 1, 1, 2}, ja[6] = {0, 1, 2, 1, 2, 2};
+    s->pe = o[0];
+    for (int k = 0; k < 6; k++) {
+        s->F_H[ia[k]][ja[k]] = s->F_H[ja[k]][ia[k]] = o[k + 1];
+        s->S_pe[ia[k]][ja[k]] = s->S_pe[ja[k]][ia[k]] = o[k + 1] / -s->vol;
+    }
+}
+
 /* returns pe; out7 = [pe, F_H voigt (xx,xy,xz,yy,yz,zz)] */
 double orc_sys_force(void* p, double* out7) {
     orc_sys* s = (orc_sys*)p;
@@ -1084,8 +1105,13 @@ static void dyadic_add(double m, const double* v, double* d) {
  * Returns the number of neighbour-list rebuilds, or -1.
  */
 int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int L, int niters,
-                   int nsteps, double* eta_io, double* thermo) {
+                   int nsteps, double* eta_io, double* thermo, int threads, double* loop_seconds) {
     orc_sys* s = (orc_sys*)p;
+    /* threads > 0: full-list force and integrator loops on that many
+       threads (the timed CPU baseline); otherwise the reference's serial
+       half-list algorithm */
+    if (threads > 0) s->pair_wise = 0;
+#define FORCE_CALC() (threads > 0 ? force_calc_threads(s, threads) : force_calc(s))
     if (isnan(kB)) return fail("boltzmann constant should be set prior to MD");
     if (L < 1 || L > 16 || niters < 1) return fail("invalid thermostat parameters");
     nhc_t th;
@@ -1102,7 +1128,7 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
     /* DynamicMD::init */
     if (orc_sys_init_dynamic(s)) return -1;
     /* run  md_nvt.cpp:383-480 */
-    force_calc(s);
+    FORCE_CALC();
     int row = 0;
 #define THERMO_ROW()                                                         \
     if (thermo) {                                                            \
@@ -1116,6 +1142,7 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
     row++;
     THERMO_ROW();
     double fac, fac_x_d = 1.0;
+    double t0 = now_seconds();
     for (int istep = 0; istep < nsteps; istep++) {
         fac_x_d *= fac = nhc_step(&th, T_part / T, ndof_part);
         fac *= fac;
@@ -1123,15 +1150,38 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
         T_part *= fac;
         /* update_x_d__x  md_nvt.cpp:70-102 */
         double dxl[3] = {0, 0, 0};
-        for (int i = 0; i < n; i++) {
-            double mi = s->masses[s->elem[i]];
-            double* xd = s->v + 3 * i;
-            double* xx = s->x + 3 * i;
-            double* ff = s->f + 3 * i;
-            for (int j = 0; j < 3; j++) {
-                xd[j] = xd[j] * fac_x_d + ff[j] * dt2 / mi;
-                dxl[j] += xd[j] * dt;
-                xx[j] += xd[j] * dt;
+        if (threads > 0) {
+            double d0 = 0, d1 = 0, d2 = 0;
+#pragma omp parallel for schedule(static) num_threads(threads) reduction(+ : d0, d1, d2)
+            for (int i = 0; i < n; i++) {
+                double mi = s->masses[s->elem[i]];
+                double* xd = s->v + 3 * i;
+                double* xx = s->x + 3 * i;
+                double* ff = s->f + 3 * i;
+                double dd[3];
+                for (int j = 0; j < 3; j++) {
+                    xd[j] = xd[j] * fac_x_d + ff[j] * dt2 / mi;
+                    dd[j] = xd[j] * dt;
+                    xx[j] += dd[j];
+                }
+                d0 += dd[0];
+                d1 += dd[1];
+                d2 += dd[2];
+            }
+            dxl[0] = d0;
+            dxl[1] = d1;
+            dxl[2] = d2;
+        } else {
+            for (int i = 0; i < n; i++) {
+                double mi = s->masses[s->elem[i]];
+                double* xd = s->v + 3 * i;
+                double* xx = s->x + 3 * i;
+                double* ff = s->f + 3 * i;
+                for (int j = 0; j < 3; j++) {
+                    xd[j] = xd[j] * fac_x_d + ff[j] * dt2 / mi;
+                    dxl[j] += xd[j] * dt;
+                    xx[j] += xd[j] * dt;
+                }
             }
         }
         double natms = (double)n;
@@ -1139,7 +1189,7 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
         for (int i = 0; i < n; i++)
             for (int j = 0; j < 3; j++) s->x[3 * i + j] -= dxl[j];
         if (dynamic_update(s)) return -1;
-        force_calc(s);
+        FORCE_CALC();
         /* update_x_d  md_nvt.cpp:106-128 */
         for (int k = 0; k < 6; k++) mvv[k] = 0.0;
         for (int i = 0; i < n; i++) {
@@ -1156,11 +1206,13 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
         T_part *= fac;
         THERMO_ROW();
     }
+    if (loop_seconds) *loop_seconds = now_seconds() - t0;
     /* update_x_d_final  md_nvt.cpp:51-56 */
     for (int i = 0; i < 3 * n; i++) s->v[i] *= fac_x_d;
     if (eta_io)
         for (int i = 0; i < L; i++) eta_io[i] = th.eta_d[i];
 #undef THERMO_ROW
+#undef FORCE_CALC
     return s->nrebuild;
 }
 

@@ -60,7 +60,7 @@ def lib():
         L.orc_sys_energy.argtypes = [C.c_void_p]
         L.orc_sys_get_rho.argtypes = [C.c_void_p, _D, _D]
         L.orc_md_nvt_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
-                                     C.c_int, C.c_int, C.c_int, _D, _D]
+                                     C.c_int, C.c_int, C.c_int, _D, _D, C.c_int, _D]
         L.orc_lbfgs_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_double, C.c_int, _D]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
@@ -202,15 +202,20 @@ class System:
         lib().orc_sys_neighbors(self.h, cnt.ctypes.data_as(_I), ent.ctypes.data_as(_I))
         return cnt, ent
 
-    def nvt_run(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None):
+    def nvt_run(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, threads=0):
+        """MDNVT::run.  threads > 0 switches to the full-list multi-threaded
+        restatement (timing baseline); the loop time is in self.loop_seconds."""
         if t_relax is None:
             t_relax = 100.0 * dt
         eta_a = np.zeros(max(L, 1)) if eta is None else np.ascontiguousarray(eta, dtype=np.float64)
         thermo = np.zeros((nsteps + 1, 14))
-        r = lib().orc_md_nvt_run(self.h, T, dt, kB, t_relax, L, niters, nsteps, _dp(eta_a), _dp(thermo))
+        secs = np.zeros(1)
+        r = lib().orc_md_nvt_run(self.h, T, dt, kB, t_relax, L, niters, nsteps, _dp(eta_a), _dp(thermo),
+                                 int(threads), _dp(secs))
         if r < 0:
             raise RuntimeError("oracle: " + _err())
         self.initialized = True
+        self.loop_seconds = float(secs[0])
         return thermo, eta_a, r
 
     def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=10000):

@@ -1,0 +1,113 @@
+"""Host-side checks that need no GPU: the product's potential readers and
+spline tables against the oracle, file errors, create_temp, and that the
+C-ABI library exports every entry point its header declares."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import ROOT
+from mapp4py_gb300 import _lib, synth
+
+
+@pytest.fixture(scope="module")
+def built():
+    from mapp4py_gb300 import build
+
+    build.build()
+    return _lib.load()
+
+
+@pytest.mark.parametrize("elems", [("A",), ("A", "B")])
+def test_setfl_tables_bitwise_equal_oracle(built, potentials, elems):
+    path, _ = potentials[elems]
+    ff = _lib.ForceField.setfl(path)
+    ref = O.Eam.setfl(path).tables()
+    for a, b in zip(ff.tables(), ref):
+        assert np.array_equal(a, b)
+    F, rho, rphi, cut = ff.tables()
+    # cutoff = last knot where any table is nonzero (5.5 A switch, dr = 5.5/5000)
+    assert np.allclose(cut, 4999 * 5.5 / 5000, rtol=0, atol=1e-15)
+
+
+def test_knot_tables_match_setfl(built, potentials):
+    path, _ = potentials[("A", "B")]
+    dr, drho, F, rho, rphi = synth.analytic_knots(("A", "B"))
+    rho2 = np.stack([rho, rho], axis=1)  # setfl: rho[i][j] = rho_i for every j
+    ff = _lib.ForceField.knots(5000, 5000, dr, drho, F, rho2, rphi)
+    ref = _lib.ForceField.setfl(path).tables()
+    for a, b in zip(ff.tables(), ref):
+        assert np.allclose(a, b, rtol=1e-13, atol=1e-15)
+
+
+def test_element_selection_and_order(built, potentials):
+    path, _ = potentials[("A", "B")]
+    ff = _lib.ForceField.setfl(path, ["B", "A"])
+    assert ff.names == ["B", "A"]
+    F, rho, rphi, cut = ff.tables()
+    F0, rho0, rphi0, cut0 = _lib.ForceField.setfl(path).tables()
+    assert np.array_equal(F[0], F0[1]) and np.array_equal(rphi[0, 0], rphi0[1, 1])
+    assert np.array_equal(rphi[0, 1], rphi0[1, 0])
+    with pytest.raises(_lib.MappgError) as ei:
+        _lib.ForceField.setfl(path, ["C"])
+    assert "element C" in str(ei.value)
+
+
+def test_malformed_setfl_is_rejected(built, potentials, tmp_path):
+    path, _ = potentials[("A",)]
+    lines = open(path).read().splitlines(True)
+    bad = tmp_path / "trunc.setfl"
+    bad.write_text("".join(lines[: len(lines) // 2]))
+    with pytest.raises(_lib.MappgError) as ei:
+        _lib.ForceField.setfl(str(bad))
+    assert ei.value.code == -3 and "immaturely" in str(ei.value)
+    extra = tmp_path / "extra.setfl"
+    k = 7
+    extra.write_text("".join(lines[:k]) + lines[k].rstrip("\n") + " 1.0\n" + "".join(lines[k + 1:]))
+    with pytest.raises(_lib.MappgError) as ei:
+        _lib.ForceField.setfl(str(extra))
+    assert "extra arguments" in str(ei.value)
+    with pytest.raises(_lib.MappgError):
+        _lib.ForceField.setfl(str(tmp_path / "missing.setfl"))
+
+
+def test_create_temp_matches_oracle(built):
+    elem = (np.arange(1000) % 2).astype(np.uint8)
+    masses = [63.5, 40.0]
+    v = _lib.create_temp(elem, masses, 300.0, synth.KB, 846244)
+    vo = O.create_temp(elem, masses, 300.0, synth.KB, 846244)
+    assert np.array_equal(v, vo)
+    with pytest.raises(_lib.MappgError):
+        _lib.create_temp(elem, masses, 300.0, synth.KB, 0)
+
+
+def test_library_exports_every_declared_symbol(built):
+    hdr = open(os.path.join(ROOT, "include", "mappg.h")).read()
+    declared = set(re.findall(r"\b(mappg_[a-z0-9_]+)\s*\(", hdr))
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if " T mappg_" in l)
+    assert declared and declared <= exported, sorted(declared - exported)
+    assert declared == set(_lib.SIGNATURES), sorted(declared ^ set(_lib.SIGNATURES))
+    L = _lib.load()
+    for name in declared:
+        assert hasattr(L, name)
+
+
+def test_api_surface_mirrors_reference(built):
+    from mapp4py_gb300 import md, ls_bt
+
+    n = md.nvt(300.0, 0.1)
+    assert (n.t_relax, n.L, n.niters, n.ntally) == (10.0, 3, 1, 10000)
+    m = md.min_lbfgs()
+    assert m.m == 2 and m.max_dx == 1.0 and abs(m.e_tol - 2 ** -26) < 1e-20
+    ls = ls_bt()
+    assert (ls.c, ls.rho, ls.min_alpha) == (0.4, 0.5, 0.0)
+    with pytest.raises(TypeError):
+        md.nvt(-1.0, 0.1)
+    H, x = synth.fcc((4, 4, 4))
+    a = md.atoms(H, x, np.zeros(len(x), np.uint8))
+    with pytest.raises(TypeError):
+        a.create_temp(300.0, 1)  # kB not set
