@@ -43,6 +43,12 @@ struct Prec<true> {
     using R4 = float4;
 };
 
+// r/dr with 1/dr split as hi + lo so the FP32 index carries no systematic
+// scale error (a plain FP32 1/dr is off by up to 3e-8 relative, which biases
+// every pair the same way)
+__device__ __forceinline__ float r_over_dr(float r, float hi, float lo) { return fmaf(r, hi, r * lo); }
+__device__ __forceinline__ double r_over_dr(double r, double hi, double) { return r * hi; }
+
 template <typename R, typename R4>
 __device__ __forceinline__ R spl_val(const R4& c, R p) {
     return ((c.w * p + c.z) * p + c.y) * p + c.x;
@@ -148,13 +154,16 @@ template <>
 struct Pos<true> {
     float4 p;
     __device__ __forceinline__ void load(const EamArgs& a, int i) { p = a.p32[i]; }
-    __device__ __forceinline__ void delta(const EamArgs& a, const float4* off, int j, int c, float& dx, float& dy,
-                                          float& dz, int& ej) const {
+    // dx = ((p_i - p_j) + offset head) + offset tail: the tail removes the
+    // rounding of the per-code offset, which is shared by every pair that
+    // crosses that bin face and would otherwise bias those distances alike
+    __device__ __forceinline__ void delta(const EamArgs& a, const float4* off, const float4* offlo, int j, int c,
+                                          float& dx, float& dy, float& dz, int& ej) const {
         float4 q = __ldg(a.p32 + j);
-        float4 o = off[c];
-        dx = (p.x - q.x) + o.x;
-        dy = (p.y - q.y) + o.y;
-        dz = (p.z - q.z) + o.z;
+        float4 o = off[c], l = offlo[c];
+        dx = ((p.x - q.x) + o.x) + l.x;
+        dy = ((p.y - q.y) + o.y) + l.y;
+        dz = ((p.z - q.z) + o.z) + l.z;
         ej = __float_as_int(q.w);
     }
 };
@@ -177,6 +186,7 @@ template <bool MIX>
 struct Smem {
     double sh[27][3];
     float4 off[27];
+    float4 offlo[27];
     typename Prec<MIX>::R cut_sq[kMaxElem * kMaxElem];
     __device__ void fill(const EamArgs& a) {
         for (int t = threadIdx.x; t < 27; t += blockDim.x) {
@@ -184,6 +194,7 @@ struct Smem {
             sh[t][1] = a.shift[t][1];
             sh[t][2] = a.shift[t][2];
             off[t] = make_float4(a.off32[t][0], a.off32[t][1], a.off32[t][2], 0.f);
+            offlo[t] = make_float4(a.off32lo[t][0], a.off32lo[t][1], a.off32lo[t][2], 0.f);
         }
         for (int t = threadIdx.x; t < a.ne * a.ne; t += blockDim.x) cut_sq[t] = (typename Prec<MIX>::R)a.cut_sq[t];
         __syncthreads();
@@ -195,7 +206,7 @@ __device__ __forceinline__ void geom(const Pos<MIX>& P, const EamArgs& a, const 
                                      R& dz, int& ej) {
     int j = e >> kCodeBits, c = e & 31;
     if constexpr (MIX)
-        P.delta(a, S.off, j, c, dx, dy, dz, ej);
+        P.delta(a, S.off, S.offlo, j, c, dx, dy, dz, ej);
     else
         P.delta(a, S.sh, j, c, dx, dy, dz, ej);
 }
@@ -233,6 +244,7 @@ __global__ void __launch_bounds__(256) k_density(EamArgs a) {
     __shared__ Smem<MIX> S;
     S.fill(a);
     const R dr_inv = (R)a.dr_inv;
+    const R dr_lo = (R)(a.dr_inv - (double)dr_inv);
     const int lane = threadIdx.x % TPA;
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
@@ -257,7 +269,7 @@ __global__ void __launch_bounds__(256) k_density(EamArgs a) {
                 R rsq = dx * dx + dy * dy + dz * dz;
                 if (rsq < S.cut_sq[ei * a.ne + ej]) {
                     R r = my_sqrt(rsq);
-                    R p = r * dr_inv;
+                    R p = r_over_dr(r, dr_inv, dr_lo);
                     int m = min((int)p, a.nr - 2);
                     p -= (R)m;
                     p = p < R(1) ? p : R(1);
@@ -270,9 +282,13 @@ __global__ void __launch_bounds__(256) k_density(EamArgs a) {
         if (active && lane == 0) {
             double Fv, dFv;
             if constexpr (MIX) {
+                // F' in FP32 feeds the FP32 force pass; the energy value is
+                // taken in FP64 (one spline per atom) so that rounding of the
+                // FP32 table does not bias the total
                 float F32v, dF32v;
                 embed32(a, ei, acc, F32v, dF32v);
-                Fv = F32v;
+                double dF64;
+                embed64(a, ei, (double)acc, Fv, dF64);
                 dFv = dF32v;
                 a.dF32[i] = dF32v;
             } else {
@@ -296,6 +312,7 @@ __global__ void __launch_bounds__(256) k_force(EamArgs a) {
     __shared__ Smem<MIX> S;
     S.fill(a);
     const R dr_inv = (R)a.dr_inv;
+    const R dr_lo = (R)(a.dr_inv - (double)dr_inv);
     const int lane = threadIdx.x % TPA;
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
@@ -328,7 +345,7 @@ __global__ void __launch_bounds__(256) k_force(EamArgs a) {
                     const int j = e >> kCodeBits;
                     R r = my_sqrt(rsq);
                     R rinv = R(1) / r;
-                    R p = r * dr_inv;
+                    R p = r_over_dr(r, dr_inv, dr_lo);
                     int m = min((int)p, a.nr - 2);
                     p -= (R)m;
                     p = p < R(1) ? p : R(1);
@@ -396,6 +413,7 @@ __global__ void __launch_bounds__(256) k_energy(EamArgs a) {
     __shared__ Smem<MIX> S;
     S.fill(a);
     const R dr_inv = (R)a.dr_inv;
+    const R dr_lo = (R)(a.dr_inv - (double)dr_inv);
     const int lane = threadIdx.x % TPA;
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
@@ -422,7 +440,7 @@ __global__ void __launch_bounds__(256) k_energy(EamArgs a) {
                 R rsq = dx * dx + dy * dy + dz * dz;
                 if (rsq < S.cut_sq[ei * a.ne + ej]) {
                     R r = my_sqrt(rsq);
-                    R p = r * dr_inv;
+                    R p = r_over_dr(r, dr_inv, dr_lo);
                     int m = min((int)p, a.nr - 2);
                     p -= (R)m;
                     p = p < R(1) ? p : R(1);
@@ -435,13 +453,7 @@ __global__ void __launch_bounds__(256) k_energy(EamArgs a) {
         for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
         if (active && lane == 0) {
             double Fv, dFv;
-            if constexpr (MIX) {
-                float F32v, dF32v;
-                embed32(a, ei, acc, F32v, dF32v);
-                Fv = F32v;
-            } else {
-                embed64(a, ei, acc, Fv, dFv);
-            }
+            embed64(a, ei, (double)acc, Fv, dFv);
             eacc += Fv;
         }
     }

@@ -73,9 +73,11 @@ void sys_set_box(mappg_sys* s, const double* H) {
                 sh += d[q] * s->box.H[q][k];
             }
             s->off32[c][k] = (float)o;
+            s->off32lo[c][k] = (float)(o - (double)s->off32[c][k]);
             s->shift[c][k] = sh;  // indexed by image code n instead of d
         }
         s->off32[c][3] = 0.f;
+        s->off32lo[c][3] = 0.f;
     }
     double pmax = s->skin;
     for (int q = 0; q < 3; q++) {
@@ -489,6 +491,7 @@ EamArgs eam_args(mappg_sys* s) {
     for (int p = 0; p < s->ne * s->ne; p++) a.cut_sq[p] = s->cut_sq[p];
     memcpy(a.shift, s->shift, sizeof(a.shift));
     memcpy(a.off32, s->off32, sizeof(a.off32));
+    memcpy(a.off32lo, s->off32lo, sizeof(a.off32lo));
     for (int d = 0; d < 3; d++) a.nb[d] = s->nb[d];
     a.rho = s->rho;
     a.dF = s->dF;

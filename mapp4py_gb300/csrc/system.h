@@ -76,7 +76,8 @@ struct EamArgs {
     double dr_inv, drho_inv, rho_max;
     double cut_sq[kMaxElem * kMaxElem];
     double shift[27][3];   // image shift n*H for image code (n0+1)+3(n1+1)+9(n2+1)
-    float off32[27][4];    // bin-step offset for neighbour code
+    float off32[27][4];    // bin-step offset for neighbour code (FP32 head)
+    float off32lo[27][4];  // its FP32 tail: off = head + tail to ~1e-15
     int nb[3];
     double* rho;
     double* dF;
@@ -105,6 +106,7 @@ struct mappg_sys {
     int nb[3] = {1, 1, 1};
     int nbins = 1;
     float off32[27][4];
+    float off32lo[27][4];
     double shift[27][3];
     double band = 0.0;  // half-width of the exact-arithmetic band of the list filter
     cudaStream_t stream = nullptr;

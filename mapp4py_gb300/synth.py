@@ -21,6 +21,24 @@ ALPHA = 1.4  # 1/A, Morse stiffness of the pair term
 R_SW0, R_SW1 = 5.0, 5.5  # cubic switch applied to phi and rho
 
 
+_LN2_HI = 0.693147180369123816490  # ln 2 split so that k*_LN2_HI is exact for |k| < 2^11
+_LN2_LO = 1.90821492927058770002e-10
+
+
+def pexp(x):
+    """exp(x) from IEEE +,-,*,/ only (range reduction by ln 2, then the
+    Taylor series of exp(r) for |r| <= ln2/2 to 20 terms, then an exact
+    scaling by 2^k), so generated tables are bit-identical on every host
+    whatever its libm.  Accurate to about one unit in the last place."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x / 0.6931471805599453)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    t = np.ones_like(r)
+    for n in range(20, 0, -1):
+        t = 1.0 + t * r / float(n)
+    return np.ldexp(t, k.astype(np.int64))
+
+
 def switch(r):
     """1 below 5.0 A, 1-3t^2+2t^3 on [5.0,5.5) with t=(r-5)/0.5, 0 beyond."""
     r = np.asarray(r, dtype=np.float64)
@@ -29,12 +47,12 @@ def switch(r):
 
 
 def phi(r, D, r0):
-    e = np.exp(-ALPHA * (r - r0))
+    e = pexp(-ALPHA * (r - r0))
     return D * (e * e - 2.0 * e) * switch(r)
 
 
 def rho_fn(r, r0):
-    return np.exp(-3.0 * (r / r0 - 1.0)) * switch(r)
+    return pexp(-3.0 * (r / r0 - 1.0)) * switch(r)
 
 
 def analytic_knots(elems=("A",), nr=5000, nrho=5000, rc=5.5, drho=0.01):
