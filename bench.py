@@ -113,10 +113,10 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_cell():
+def make_cell(cells=80):
     from mapp4py_gb300 import synth
 
-    return synth.alloy(N_CELLS, xB=0.5, sigma=0.05, T=T_K, seed=1)
+    return synth.alloy((cells, cells, cells), xB=0.5, sigma=0.05, T=T_K, seed=1)
 
 
 def write_potential(d):
@@ -191,7 +191,7 @@ def run_gpu(args, rank, world, local_rank):
     K, W = args.steps, args.warmup
     tmp = tempfile.TemporaryDirectory()
     path = write_potential(tmp.name)
-    cell = make_cell()
+    cell = make_cell(args.cells)
     N = cell.natoms
     ff = _lib.ForceField.setfl(path)
     prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
@@ -297,7 +297,7 @@ def run_gpu(args, rank, world, local_rank):
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "data": "synthetic",
-                "config": {"workload": "EAM NVT MD, 2,048,000-atom A/B alloy (FCC 80^3, seed 1)",
+                "config": {"workload": "EAM NVT MD, %d-atom A/B alloy (FCC %d^3, seed 1)" % (N, args.cells),
                            "natoms": N, "precision": args.precision, "dt_fs": 1.0, "T_K": T_K,
                            "l2": "inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6),
                            "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None},
@@ -323,6 +323,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cells", type=int, default=N_CELLS[0],
+                    help="FCC repeats per side (80 = the 2,048,000-atom workload; smaller for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

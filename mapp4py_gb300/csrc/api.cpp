@@ -88,11 +88,15 @@ void upload_tables(mappg_ff* ff) {
     up32(&d.rho32, t.rho, nrt);
     up32(&d.rphi32, t.rphi, nrt);
     up32(&d.F32, t.F, nFt);
+    std::vector<float> lo(nrt);
+    for (size_t k = 0; k < nrt; k++) lo[k] = (float)(t.rphi[4 * k] - (double)(float)t.rphi[4 * k]);
+    MAPPG_CUDA(cudaMalloc(&d.rphi32_lo, sizeof(float) * nrt));
+    MAPPG_CUDA(cudaMemcpy(d.rphi32_lo, lo.data(), sizeof(float) * nrt, cudaMemcpyHostToDevice));
 }
 
 void free_tables(mappg_ff* ff) {
     DevTables& d = ff->dev;
-    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.rphi32, d.F32};
+    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.rphi32, d.F32, d.rphi32_lo};
     for (void* q : p)
         if (q) cudaFree(q);
 }

@@ -53,6 +53,18 @@ template <typename R, typename R4>
 __device__ __forceinline__ R spl_val(const R4& c, R p) {
     return ((c.w * p + c.z) * p + c.y) * p + c.x;
 }
+// r*phi value with the FP32 table's constant term carried as head + tail:
+// the head's rounding is shared by every pair that lands on the knot and
+// would otherwise bias the pair energy
+template <bool MIX>
+__device__ __forceinline__ typename Prec<MIX>::R z_val(const EamArgs& a, size_t k, const typename Prec<MIX>::R4& c,
+                                                       typename Prec<MIX>::R p) {
+    if constexpr (MIX)
+        return c.x + (__ldg(a.rphi32_lo + k) + ((c.w * p + c.z) * p + c.y) * p);
+    else
+        return ((c.w * p + c.z) * p + c.y) * p + c.x;
+}
+
 template <typename R, typename R4>
 __device__ __forceinline__ R spl_der(const R4& c, R p) {
     return (R(3) * c.w * p + R(2) * c.z) * p + c.y;
@@ -353,8 +365,9 @@ __global__ void __launch_bounds__(256) k_force(EamArgs a) {
                     const R der_i = spl_der<R, R4>(ci, p) * dr_inv;
                     R der_j = der_i;
                     if (ej != ei) der_j = spl_der<R, R4>(ldg4(rt + (size_t)(ei * a.ne + ej) * a.nr + m), p) * dr_inv;
-                    const R4 cz = ldg4(zt + (size_t)(ei * a.ne + ej) * a.nr + m);
-                    const R z = spl_val<R, R4>(cz, p);
+                    const size_t kz = (size_t)(ei * a.ne + ej) * a.nr + m;
+                    const R4 cz = ldg4(zt + kz);
+                    const R z = z_val<MIX>(a, kz, cz, p);
                     const R zp = spl_der<R, R4>(cz, p) * dr_inv;
                     const R phi = z * rinv;
                     const R dphi = zp * rinv - phi * rinv;
@@ -445,7 +458,8 @@ __global__ void __launch_bounds__(256) k_energy(EamArgs a) {
                     p -= (R)m;
                     p = p < R(1) ? p : R(1);
                     acc += spl_val<R, R4>(ldg4(rt + (size_t)(ej * a.ne + ei) * a.nr + m), p);
-                    ep += spl_val<R, R4>(ldg4(zt + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
+                    const size_t kz = (size_t)(ei * a.ne + ej) * a.nr + m;
+                    ep += z_val<MIX>(a, kz, ldg4(zt + kz), p) / r;
                 }
             }
         }

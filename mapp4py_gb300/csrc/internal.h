@@ -63,6 +63,7 @@ struct DevTables {
     float4* rho32 = nullptr;
     float4* rphi32 = nullptr;
     float4* F32 = nullptr;
+    float* rphi32_lo = nullptr;  // c0 - (float)c0 of the r*phi table
 };
 
 }  // namespace mappg

@@ -296,8 +296,9 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
     // NewDynamicMD::init then the opening force call
     sys_build(s);
     long long n_en = 0, n_fc = 1;
-    double e_curr;
-    lb_force(s, &e_curr);
+    double e_curr, pe_force;
+    lb_force(s, &pe_force);
+    e_curr = pe_force;
     double e_prev, alpha_m = 0.0;
     int k = 0;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
@@ -396,7 +397,9 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             istep--;
             continue;
         }
-        lb_force(s, &e_curr);
+        // handler.force_calc(): forces and atoms->pe; e_curr stays the line
+        // search's energy, as in min_l-bfgs.h:181-188
+        lb_force(s, &pe_force);
         n_fc++;
         if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
         if (f_tol > 0.0) {
@@ -448,7 +451,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
     if (hs.bad) throw Error{MAPPG_ERR_NAN, "non-finite value during minimization"};
     if (stats) {
         stats[0] = istep;
-        stats[1] = e_curr;
+        stats[1] = pe_force;
         stats[2] = fmaxv;
         stats[3] = err;
         stats[4] = (double)n_en;

@@ -485,6 +485,7 @@ EamArgs eam_args(mappg_sys* s) {
     a.rho32 = ff->dev.rho32;
     a.rphi32 = ff->dev.rphi32;
     a.F32 = ff->dev.F32;
+    a.rphi32_lo = ff->dev.rphi32_lo;
     a.dr_inv = ff->dev.dr_inv;
     a.drho_inv = ff->dev.drho_inv;
     a.rho_max = ff->dev.rho_max;

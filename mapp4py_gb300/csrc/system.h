@@ -73,6 +73,7 @@ struct EamArgs {
     const float4* rho32;
     const float4* rphi32;
     const float4* F32;
+    const float* rphi32_lo;
     double dr_inv, drho_inv, rho_max;
     double cut_sq[kMaxElem * kMaxElem];
     double shift[27][3];   // image shift n*H for image code (n0+1)+3(n1+1)+9(n2+1)
