@@ -72,9 +72,9 @@ void upload_tables(mappg_ff* ff) {
     }
     MAPPG_CUDA(cudaGetDevice(&ff->device));
     size_t nrt = (size_t)ne * ne * t.nr, nFt = (size_t)ne * t.nrho;
-    auto up64 = [](double4** dst, const std::vector<double>& src, size_t n) {
-        MAPPG_CUDA(cudaMalloc(dst, sizeof(double4) * n));
-        MAPPG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(double4) * n, cudaMemcpyHostToDevice));
+    auto up64 = [](Dbl4** dst, const std::vector<double>& src, size_t n) {
+        MAPPG_CUDA(cudaMalloc(dst, sizeof(Dbl4) * n));
+        MAPPG_CUDA(cudaMemcpy(*dst, src.data(), sizeof(Dbl4) * n, cudaMemcpyHostToDevice));
     };
     auto up32 = [](float4** dst, const std::vector<double>& src, size_t n) {
         std::vector<float> f(4 * n);
@@ -86,17 +86,41 @@ void upload_tables(mappg_ff* ff) {
     up64(&d.rphi64, t.rphi, nrt);
     up64(&d.F64, t.F, nFt);
     up32(&d.rho32, t.rho, nrt);
-    up32(&d.rphi32, t.rphi, nrt);
     up32(&d.F32, t.F, nFt);
-    std::vector<float> lo(nrt);
-    for (size_t k = 0; k < nrt; k++) lo[k] = (float)(t.rphi[4 * k] - (double)(float)t.rphi[4 * k]);
-    MAPPG_CUDA(cudaMalloc(&d.rphi32_lo, sizeof(float) * nrt));
-    MAPPG_CUDA(cudaMemcpy(d.rphi32_lo, lo.data(), sizeof(float) * nrt, cudaMemcpyHostToDevice));
+    std::vector<float> lo(nFt);
+    for (size_t k = 0; k < nFt; k++) lo[k] = (float)(t.F[4 * k] - (double)(float)t.F[4 * k]);
+    MAPPG_CUDA(cudaMalloc(&d.F32lo, sizeof(float) * nFt));
+    MAPPG_CUDA(cudaMemcpy(d.F32lo, lo.data(), sizeof(float) * nFt, cudaMemcpyHostToDevice));
+    // packed force records of the mixed force kernel
+    const double dri = 1.0 / t.dr;
+    std::vector<float> rec((size_t)12 * nrt);
+    for (int ei = 0; ei < ne; ei++)
+        for (int ej = 0; ej < ne; ej++)
+            for (int m = 0; m < t.nr; m++) {
+                const double* ci = t.rho_at(ej, ei) + 4 * (size_t)m;  // density at i from j
+                const double* cj = t.rho_at(ei, ej) + 4 * (size_t)m;  // density at j from i
+                const double* cz = t.rphi_at(ei, ej) + 4 * (size_t)m;
+                float* r = rec.data() + 12 * ((size_t)(ei * ne + ej) * t.nr + m);
+                r[0] = (float)(ci[1] * dri);
+                r[1] = (float)(2.0 * ci[2] * dri);
+                r[2] = (float)(3.0 * ci[3] * dri);
+                r[3] = (float)(cj[1] * dri);
+                r[4] = (float)(2.0 * cj[2] * dri);
+                r[5] = (float)(3.0 * cj[3] * dri);
+                r[6] = (float)cz[0];
+                r[7] = (float)(cz[0] - (double)r[6]);
+                r[8] = (float)cz[1];
+                r[9] = (float)cz[2];
+                r[10] = (float)cz[3];
+                r[11] = 0.f;
+            }
+    MAPPG_CUDA(cudaMalloc(&d.ftab, sizeof(float) * rec.size()));
+    MAPPG_CUDA(cudaMemcpy(d.ftab, rec.data(), sizeof(float) * rec.size(), cudaMemcpyHostToDevice));
 }
 
 void free_tables(mappg_ff* ff) {
     DevTables& d = ff->dev;
-    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.rphi32, d.F32, d.rphi32_lo};
+    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.ftab, d.F32, d.F32lo};
     for (void* q : p)
         if (q) cudaFree(q);
 }
@@ -251,7 +275,8 @@ int mappg_sys_create(const mappg_ff* ff, int natoms, const double* H, const doub
                      const double* masses, double skin, int precision, mappg_sys** out) {
     return guard([&] {
         if (!ff || !H || !x || !elem || !masses || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
-        if (natoms < 1 || natoms >= (1 << (31 - kCodeBits))) throw Error{MAPPG_ERR_ARG, "natoms out of range"};
+        if (natoms < 1 || natoms > kMaxAtoms)
+            throw Error{MAPPG_ERR_ARG, "natoms out of range (1.." + std::to_string(kMaxAtoms) + " per system)"};
         if (precision != MAPPG_FP64 && precision != MAPPG_MIXED) throw Error{MAPPG_ERR_ARG, "unknown precision mode"};
         if (!(skin >= 0.0)) throw Error{MAPPG_ERR_ARG, "skin must be >= 0"};
         const int ne = ff->host.nelem;
@@ -321,7 +346,6 @@ int mappg_sys_set_x(mappg_sys* s, const double* x) {
         if (!s || !x) throw Error{MAPPG_ERR_ARG, "null argument"};
         sys_upload(s, x, s->x);
         s->built = false;
-        s->forces_valid = false;
     });
 }
 
@@ -350,6 +374,7 @@ int mappg_sys_get_v(mappg_sys* s, double* v) {
 int mappg_sys_get_f(mappg_sys* s, double* f) {
     return guard([&] {
         if (!s || !f) throw Error{MAPPG_ERR_ARG, "null argument"};
+        sync_forces64(s);
         sys_download(s, s->f, f);
     });
 }
@@ -401,7 +426,6 @@ int mappg_sys_force(mappg_sys* s, double* pe, double* virial6) {
         if (pe) *pe = h.energy;
         if (virial6)
             for (int k = 0; k < 6; k++) virial6[k] = h.virial[k];
-        s->forces_valid = true;
         if (!std::isfinite(h.energy)) throw Error{MAPPG_ERR_NAN, "non-finite energy"};
     });
 }
@@ -422,9 +446,21 @@ int mappg_sys_get_rho(mappg_sys* s, double* rho, double* dF) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         std::vector<double> a(s->n), b(s->n);
-        MAPPG_CUDA(cudaMemcpyAsync(a.data(), s->rho, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
-        MAPPG_CUDA(cudaMemcpyAsync(b.data(), s->dF, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
-        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (s->precision == MAPPG_MIXED) {
+            std::vector<float> r32(s->n);
+            std::vector<float4> q(s->n);
+            MAPPG_CUDA(cudaMemcpyAsync(r32.data(), s->rho32, sizeof(float) * s->n, cudaMemcpyDeviceToHost, s->stream));
+            MAPPG_CUDA(cudaMemcpyAsync(q.data(), s->q32, sizeof(float4) * s->n, cudaMemcpyDeviceToHost, s->stream));
+            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+            for (int i = 0; i < s->n; i++) {
+                a[i] = r32[i];
+                b[i] = q[i].w;
+            }
+        } else {
+            MAPPG_CUDA(cudaMemcpyAsync(a.data(), s->rho, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+            MAPPG_CUDA(cudaMemcpyAsync(b.data(), s->dF, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        }
         for (int i = 0; i < s->n; i++) {
             int u = s->host_id[i];
             if (rho) rho[u] = a[i];

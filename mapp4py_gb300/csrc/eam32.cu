@@ -1,0 +1,395 @@
+// Mixed-precision EAM kernels: FP32 pair geometry and spline arithmetic in
+// the scaled bin frame (system.h), FP64 state, FP64 totals.
+//
+//   k_density32  rho_i in FP32, then F'(rho_i) and F(rho_i) from the FP32
+//                embedding table with its constant term carried as head +
+//                tail; writes q32[i] = (p'_i, F'_i) for the force pass
+//   k_force32    forces, pair energy and virial from one 48-byte record per
+//                (pair type, knot); F'_j rides in q32[j].w, so a neighbour
+//                costs one 16-byte gather plus the record; optional MD tail:
+//                kinetic tensor of v + f dt/2m and the closing half of the
+//                Nose-Hoover chain in the last block
+//   k_energy32   energy only (line-search trials)
+//
+// Precision: every per-pair term is FP32; per-atom sums are FP32 within a
+// lane group; energies are accumulated per lane with compensated FP32 sums
+// and reduced in FP64 across lanes and blocks.  Constants shared by many
+// pairs (1/dr, the frame-to-Cartesian scale, the spline constant terms) are
+// carried as head + tail so their rounding does not bias the totals.
+//
+// Table index: p = r/dr, m = floor(p) via an add with round-toward-zero
+// against 2^23, then the reference's clamps m <= nr-2, p - m <= 1
+// (ff_eam.cpp:122-128).
+#include <math.h>
+
+#include "eam_common.cuh"
+#include "nhc.cuh"
+
+namespace mappg {
+
+struct Smem32 {
+    float4 off[27];
+    float cut_sq[kMaxElem * kMaxElem];
+    __device__ void fill(const EamArgs& a) {
+        for (int t = threadIdx.x; t < 27; t += blockDim.x)
+            off[t] = make_float4(a.fr.off[t][0], a.fr.off[t][1], a.fr.off[t][2], 0.f);
+        for (int t = threadIdx.x; t < a.ne * a.ne; t += blockDim.x) cut_sq[t] = (float)a.cut_sq[t];
+        __syncthreads();
+    }
+};
+
+// frame displacement (a,b,c) to Cartesian with the head + tail scale
+template <bool ORTHO>
+__device__ __forceinline__ void cart(const Frame& fr, float a, float b, float c, float& x, float& y, float& z) {
+    if (ORTHO) {
+        x = fmaf(a, fr.G[0][0], a * fr.Glo[0][0]);
+        y = fmaf(b, fr.G[1][1], b * fr.Glo[1][1]);
+        z = fmaf(c, fr.G[2][2], c * fr.Glo[2][2]);
+    } else {
+        x = fmaf(a, fr.G[0][0], fmaf(b, fr.G[1][0], fmaf(c, fr.G[2][0], a * fr.Glo[0][0] + b * fr.Glo[1][0] +
+                                                                        c * fr.Glo[2][0])));
+        y = fmaf(b, fr.G[1][1], fmaf(c, fr.G[2][1], b * fr.Glo[1][1] + c * fr.Glo[2][1]));
+        z = fmaf(c, fr.G[2][2], c * fr.Glo[2][2]);
+    }
+}
+
+// 1/r from the hardware reciprocal square root and one Newton step
+__device__ __forceinline__ float inv_sqrt(float x) {
+    float y = rsqrtf(x);
+    return y * fmaf(-0.5f * x * y, y, 1.5f);
+}
+
+// knot index and fraction: m = min(floor(p), nmax), p - m clamped to 1
+__device__ __forceinline__ int knot32(float p, int nmax, float& fr) {
+    const float t = __fadd_rz(p, 8388608.0f);
+    int m = __float_as_int(t) - 0x4B000000;
+    fr = p - (t - 8388608.0f);
+    if (m > nmax) {
+        m = nmax;
+        fr = 1.0f;
+    }
+    return m;
+}
+
+// compensated FP32 accumulation (s, c) += v
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+struct Consts32 {
+    float dri, dri_lo, drhoi, drhoi_lo, rho_max;
+    __device__ Consts32(const EamArgs& a) {
+        dri = (float)a.dr_inv;
+        dri_lo = (float)(a.dr_inv - (double)dri);
+        drhoi = (float)a.drho_inv;
+        drhoi_lo = (float)(a.drho_inv - (double)drhoi);
+        rho_max = (float)a.rho_max;
+    }
+};
+
+// embedding F and F' from the FP32 table, constant term as head + tail;
+// linear extrapolation above rho_max as ff_eam.cpp:180-191
+__device__ __forceinline__ void embed32(const EamArgs& a, const Consts32& K, int ei, float rho, float& Fv,
+                                        float& dFv) {
+    float fr;
+    const int m = knot32(fmaf(rho, K.drhoi, rho * K.drhoi_lo), a.nrho - 2, fr);
+    const size_t k = (size_t)ei * a.nrho + m;
+    const float4 c = __ldg(a.F32 + k);
+    dFv = fmaf(fmaf(3.0f * c.w, fr, 2.0f * c.z), fr, c.y) * K.drhoi;
+    Fv = c.x + (__ldg(a.F32lo + k) + fr * fmaf(fmaf(c.w, fr, c.z), fr, c.y));
+    if (rho > K.rho_max) Fv += dFv * (rho - K.rho_max);
+}
+
+// per-kernel persistent grid: as many blocks as fit on the GPU at once
+template <class Kern>
+static int occupancy_grid(mappg_sys* s, Kern k, int block) {
+    int per_sm = 0;
+    MAPPG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, 0));
+    if (per_sm < 1) per_sm = 1;
+    long long g = (long long)per_sm * s->sm_count;
+    if (g > kMaxBlocks) g = kMaxBlocks;
+    return (int)g;
+}
+
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_density32(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    float es = 0.f, ec = 0.f;
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        float acc = 0.f;
+        int ei = 0;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (active) {
+            pi = __ldg(a.p32 + i);
+            ei = a.elem[i];
+            const int nn = __ldg(a.nnbr + i);
+            const int* row = a.nbr + (size_t)i * a.maxnbr;
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                const int ej = entry_elem(e);
+                const float4 q = __ldg(a.p32 + entry_j(e));
+                const float4 o = S.off[entry_code(e)];
+                float dx, dy, dz;
+                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (rsq < S.cut_sq[ei * a.ne + ej]) {
+                    const float r = rsq * inv_sqrt(rsq);
+                    float fr;
+                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                    const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                    acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+        if (active && lane == 0) {
+            float Fv, dFv;
+            embed32(a, K, ei, acc, Fv, dFv);
+            a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
+            a.rho32out[i] = acc;
+            kahan_add(es, ec, Fv);
+        }
+    }
+    double v[1] = {(double)es - (double)ec};
+    if (block_partials<1>(v, a.partials, 0, &a.sc->counter[1]) && threadIdx.x < 32) {
+        double tot[1];
+        final_sums<1>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            a.sc->e_embed = tot[0];
+            a.sc->counter[1] = 0;
+        }
+    }
+}
+
+template <int TPA, bool ORTHO, bool TAIL>
+__global__ void __launch_bounds__(256) k_force32(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    float es = 0.f, ec = 0.f;  // pair energy, compensated
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+    float k0 = 0.f, k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f, k5 = 0.f;  // kinetic tensor (TAIL)
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
+        int ei = 0;
+        if (active) {
+            const float4 pi = __ldg(a.q32 + i);
+            const float dFi = pi.w;
+            ei = a.elem[i];
+            const int nn = __ldg(a.nnbr + i);
+            const int* row = a.nbr + (size_t)i * a.maxnbr;
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                const int t = ei * a.ne + entry_elem(e);
+                const float4 q = __ldg(a.q32 + entry_j(e));
+                const float4 o = S.off[entry_code(e)];
+                float dx, dy, dz;
+                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (rsq < S.cut_sq[t]) {
+                    const float rinv = inv_sqrt(rsq);
+                    const float r = rsq * rinv;
+                    float fr;
+                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                    const float4* rec = a.ftab + 3 * ((size_t)t * a.nr + m);
+                    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+                    const float der_i = fmaf(fmaf(r0.z, fr, r0.y), fr, r0.x);
+                    const float der_j = fmaf(fmaf(r1.y, fr, r1.x), fr, r0.w);
+                    const float zpoly = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
+                    const float z = r1.z + fmaf(fr, zpoly, r1.w);
+                    const float zp = fmaf(fmaf(3.0f * r2.z, fr, 2.0f * r2.y), fr, r2.x) * K.dri;
+                    const float phi = z * rinv;
+                    const float dphi = (zp - phi) * rinv;
+                    const float fp = -fmaf(dFi, der_i, fmaf(q.w, der_j, dphi)) * rinv;
+                    const float fdx = fp * dx, fdy = fp * dy, fdz = fp * dz;
+                    fx += fdx;
+                    fy += fdy;
+                    fz += fdz;
+                    ep += phi;
+                    w0 = fmaf(fdx, dx, w0);
+                    w1 = fmaf(fdx, dy, w1);
+                    w2 = fmaf(fdx, dz, w2);
+                    w3 = fmaf(fdy, dy, w3);
+                    w4 = fmaf(fdy, dz, w4);
+                    w5 = fmaf(fdz, dz, w5);
+                }
+            }
+            kahan_add(es, ec, ep);
+        }
+#pragma unroll
+        for (int o = TPA / 2; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o, TPA);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o, TPA);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o, TPA);
+        }
+        if (active && lane == 0) {
+            a.f32[i] = fx;
+            a.f32[a.n + i] = fy;
+            a.f32[2 * a.n + i] = fz;
+            if (TAIL) {
+                // kinetic tensor of the half-kicked velocity v + f dt/2m
+                const float dtm = a.dtm32[ei], m = a.mass32[ei];
+                const float vx = fmaf(fx, dtm, __ldg(a.v32 + i));
+                const float vy = fmaf(fy, dtm, __ldg(a.v32 + a.n + i));
+                const float vz = fmaf(fz, dtm, __ldg(a.v32 + 2 * a.n + i));
+                const float mx = m * vx, my = m * vy, mz = m * vz;
+                k0 = fmaf(mx, vx, k0);
+                k1 = fmaf(mx, vy, k1);
+                k2 = fmaf(mx, vz, k2);
+                k3 = fmaf(my, vy, k3);
+                k4 = fmaf(my, vz, k4);
+                k5 = fmaf(mz, vz, k5);
+            }
+        }
+    }
+    double v[13] = {0.5 * ((double)es - (double)ec), 0.5 * (double)w0, 0.5 * (double)w1, 0.5 * (double)w2,
+                    0.5 * (double)w3, 0.5 * (double)w4, 0.5 * (double)w5, (double)k0, (double)k1, (double)k2,
+                    (double)k3, (double)k4, (double)k5};
+    if (block_partials<13>(v, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
+        double tot[13];
+        final_sums<13>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            DevScalars* sc = a.sc;
+            sc->energy = tot[0] + sc->e_embed;
+            for (int k = 0; k < 6; k++) sc->virial[k] = tot[k + 1];
+            if (TAIL) {
+                // update_x_d (md_nvt.cpp:106-128) then the closing half of the
+                // thermostat (md_nvt.cpp:427-432)
+                for (int k = 0; k < 6; k++) sc->mvv[k] = tot[7 + k];
+                sc->T_part = (tot[7] + (tot[10] + tot[12])) / a.nhc.ndof_kB;
+                sc->fac_close = thermo_half(a.nhc, sc);
+                sc->pending_kick = 1;
+                long long st = ++sc->step;
+                if (st <= a.nsteps) write_thermo_row(a.thermo, sc, st);
+                if (!(isfinite(sc->energy) && isfinite(sc->T_part))) sc->bad = 1;
+            }
+            sc->counter[0] = 0;
+        }
+    }
+}
+
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_energy32(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    float es = 0.f, ec = 0.f;
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        float acc = 0.f, ep = 0.f;
+        int ei = 0;
+        if (active) {
+            const float4 pi = __ldg(a.p32 + i);
+            ei = a.elem[i];
+            const int nn = __ldg(a.nnbr + i);
+            const int* row = a.nbr + (size_t)i * a.maxnbr;
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                const int ej = entry_elem(e);
+                const int t = ei * a.ne + ej;
+                const float4 q = __ldg(a.p32 + entry_j(e));
+                const float4 o = S.off[entry_code(e)];
+                float dx, dy, dz;
+                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (rsq < S.cut_sq[t]) {
+                    const float rinv = inv_sqrt(rsq);
+                    const float r = rsq * rinv;
+                    float fr;
+                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                    const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                    acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+                    const float4* rec = a.ftab + 3 * ((size_t)t * a.nr + m);
+                    const float4 r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+                    const float z = r1.z + fmaf(fr, fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x), r1.w);
+                    ep += 0.5f * z * rinv;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+        if (active) kahan_add(es, ec, ep);
+        if (active && lane == 0) {
+            float Fv, dFv;
+            embed32(a, K, ei, acc, Fv, dFv);
+            kahan_add(es, ec, Fv);
+        }
+    }
+    double v[1] = {(double)es - (double)ec};
+    if (block_partials<1>(v, a.partials, 0, &a.sc->counter[2]) && threadIdx.x < 32) {
+        double tot[1];
+        final_sums<1>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            a.sc->energy = tot[0];
+            a.sc->counter[2] = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+template <int TPA, bool ORTHO>
+static void density_t(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_density32<TPA, ORTHO>, 256);
+    k_density32<TPA, ORTHO><<<grid, 256, 0, s->stream>>>(a);
+}
+
+template <int TPA, bool ORTHO>
+static void force_t(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0, grid_tail = 0;
+    if (a.md_tail) {
+        if (!grid_tail) grid_tail = occupancy_grid(s, k_force32<TPA, ORTHO, true>, 256);
+        k_force32<TPA, ORTHO, true><<<grid_tail, 256, 0, s->stream>>>(a);
+    } else {
+        if (!grid) grid = occupancy_grid(s, k_force32<TPA, ORTHO, false>, 256);
+        k_force32<TPA, ORTHO, false><<<grid, 256, 0, s->stream>>>(a);
+    }
+}
+
+template <int TPA, bool ORTHO>
+static void energy_t(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_energy32<TPA, ORTHO>, 256);
+    k_energy32<TPA, ORTHO><<<grid, 256, 0, s->stream>>>(a);
+}
+
+#define MAPPG_TPA32(FN)                                  \
+    do {                                                 \
+        const bool o = a.fr.ortho != 0;                  \
+        switch (s->tpa) {                                \
+            case 4: o ? FN<4, true>(s, a) : FN<4, false>(s, a); break;    \
+            case 16: o ? FN<16, true>(s, a) : FN<16, false>(s, a); break; \
+            case 32: o ? FN<32, true>(s, a) : FN<32, false>(s, a); break; \
+            default: o ? FN<8, true>(s, a) : FN<8, false>(s, a); break;   \
+        }                                                \
+        MAPPG_CUDA(cudaGetLastError());                  \
+    } while (0)
+
+void launch_density32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(density_t); }
+void launch_force32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(force_t); }
+void launch_energy32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(energy_t); }
+
+}  // namespace mappg

@@ -1,0 +1,56 @@
+// Reduction helpers shared by the EAM kernels: block partials written to a
+// per-block slot row, and a fixed-order final sum by the last block to
+// finish (deterministic, no floating-point atomics).
+#pragma once
+
+#include "system.h"
+
+namespace mappg {
+
+// block-wide sum of K doubles into partials[blockIdx.x*kRedSlots + slot0 + k];
+// returns true in the block that finished last (its threads then see all
+// partials)
+template <int K>
+__device__ bool block_partials(double (&v)[K], double* partials, int slot0, unsigned* counter) {
+    __shared__ double red[32][K];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[w][k] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int q = 0; q < nw; q++) t += red[q][threadIdx.x];
+        partials[blockIdx.x * kRedSlots + slot0 + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
+// sums of the first K partial slots over nblk blocks by one warp, in a fixed
+// order (lane-strided, then a shuffle tree): every lane gets the totals
+template <int K>
+__device__ void final_sums(const double* partials, int nblk, double (&tot)[K]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double t = 0.0;
+        for (int b = lane; b < nblk; b += 32) t += partials[b * kRedSlots + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        tot[k] = t;
+    }
+}
+
+}  // namespace mappg

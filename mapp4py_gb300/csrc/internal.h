@@ -11,8 +11,12 @@
 
 namespace mappg {
 
+// one cubic-spline interval of an FP64 table (c0, c1, c2, c3)
+struct alignas(32) Dbl4 {
+    double x, y, z, w;
+};
+
 constexpr int kMaxElem = 8;   // elements supported by the device kernels
-constexpr int kCodeBits = 5;  // low bits of a neighbour entry: image code
 
 // thread-local error message behind mappg_last_error()
 void set_error(const std::string& msg);
@@ -57,13 +61,15 @@ struct DevTables {
     int nelem = 0, nr = 0, nrho = 0;
     double dr_inv = 0, drho_inv = 0, rho_max = 0, max_cut = 0;
     double cut[kMaxElem * kMaxElem];
-    double4* rho64 = nullptr;   // [ne*ne][nr]
-    double4* rphi64 = nullptr;  // [ne*ne][nr]
-    double4* F64 = nullptr;     // [ne][nrho]
-    float4* rho32 = nullptr;
-    float4* rphi32 = nullptr;
-    float4* F32 = nullptr;
-    float* rphi32_lo = nullptr;  // c0 - (float)c0 of the r*phi table
+    Dbl4* rho64 = nullptr;   // [ne*ne][nr]
+    Dbl4* rphi64 = nullptr;  // [ne*ne][nr]
+    Dbl4* F64 = nullptr;     // [ne][nrho]
+    float4* rho32 = nullptr;    // rho value coefficients, [ne*ne][nr]
+    float4* ftab = nullptr;     // force records, 3 float4 per (ei*ne+ej, knot):
+                                // (d1i,d2i,d3i,d1j) (d2j,d3j,z0,z0lo) (z1,z2,z3,0)
+                                // d = (c1, 2c2, 3c3)/dr of rho_{j->i} and rho_{i->j}
+    float4* F32 = nullptr;      // embedding coefficients, [ne][nrho]
+    float* F32lo = nullptr;     // c0 - (float)c0 of the embedding table
 };
 
 }  // namespace mappg

@@ -245,11 +245,14 @@ void lb_update(mappg_sys* s) {
     k_clear_rebuild<<<1, 1, 0, s->stream>>>(s->sc);
     launch_skin_test(s);
     launch_rebuild_chain(s);
+    // positions moved without a rebuild: refresh the mixed kernels' frame
+    if (s->precision == MAPPG_MIXED) launch_shadow(s, false);
     MAPPG_CUDA(cudaGetLastError());
 }
 
 static void lb_force(mappg_sys* s, double* pe) {
     launch_force(s);
+    sync_forces64(s);
     MAPPG_CUDA(cudaMemcpyAsync(pe, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
 }
@@ -457,7 +460,6 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
         stats[4] = (double)n_en;
         stats[5] = (double)n_fc;
     }
-    s->forces_valid = true;
 }
 
 }  // namespace mappg

@@ -1,35 +1,44 @@
 // NVT molecular dynamics on the device: md.nvt(T,dt).run(atoms,nsteps).
 //
-// One step (MDNVT::run, md_nvt.cpp:409-438) is a fixed kernel sequence that
-// is captured once into a CUDA graph and replayed:
-//   k_step_open    fac_x_d *= chain(T/T0)  (first half of the thermostat)
-//   k_kick_drift   v = v*fac_x_d + f*dt2/m; x += v*dt; sum of v*dt
-//                  (update_x_d__x, md_nvt.cpp:70-102); the last block forms
-//                  the mean displacement and clears the rebuild gate
-//   k_com_skin     x -= mean displacement; skin test (DynamicMD::decide,
-//                  dynamic_md.cpp:90-105) opens the rebuild gate; mixed
-//                  precision also refreshes the FP32 bin-relative positions
-//   rebuild chain  (system.cu) runs only when the gate is open
-//   k_density, k_force (eam.cu)
-//   k_kick2        v += f*dt2/m and the kinetic tensor (update_x_d,
-//                  md_nvt.cpp:106-128); the last block runs the closing half
-//                  of the Nose-Hoover chain (ThermostatNHC::operator(),
-//                  thermostat.cpp:47-143) and writes the thermo row
-// A one-thread kernel opens each step with the chain's first half.
-// Velocity scaling stays lazy as in the reference: the chain's factor is
-// folded into the next kick and applied once more at the end of the run
-// (update_x_d_final, md_nvt.cpp:51-56).
+// One step of MDNVT::run (md_nvt.cpp:409-438) is a fixed kernel sequence,
+// captured once into a CUDA graph and replayed.
 //
-// FP64 mode keeps the reference's operation order (f*dt2/m with a division,
-// no fused multiply-adds) so the trajectory matches the oracle to rounding;
-// mixed mode multiplies by a per-element dt2/m and lets the compiler fuse.
+// FP64 path (the reference's operation order, f*dt2/m with a division and no
+// fused multiply-adds, so the trajectory follows the oracle to rounding):
+//   k_step_open      fac_x_d *= chain(T/T0), the opening thermostat half
+//   k_kick_drift64   v = v*fac_x_d + f*dt2/m; x += v*dt; sum of v*dt
+//                    (update_x_d__x, md_nvt.cpp:70-102)
+//   k_com_skin64     x -= mean displacement; skin test (DynamicMD::decide,
+//                    dynamic_md.cpp:90-105) opens the rebuild gate
+//   rebuild chain    (system.cu) only when the gate is open
+//   density, force   (eam.cu)
+//   k_kick2_64       v += f*dt2/m, kinetic tensor (update_x_d,
+//                    md_nvt.cpp:106-128), closing thermostat half, thermo row
+//
+// Mixed path (FP64 state, fewer FP64 instructions; GB300 runs FP64 at a
+// small fraction of FP32):
+//   k_step_open32    opening half; the pending closing kick of the previous
+//                    step and this step's kick fold into v <- A v + B f dt/2m
+//                    (A = fc*fo, B = 1 + fc*fo; A = fo, B = 1 on the first)
+//   k_integrate32    that kick, x += v dt (FP64), v32 = (float)v, the frame
+//                    position p32 from x, the FP32 skin test and the
+//                    displacement sum; the mean displacement is accumulated
+//                    in sc->drift and removed from x at the next rebuild and
+//                    at the end of the run (a uniform shift leaves forces and
+//                    energies unchanged)
+//   rebuild chain, k_density32, k_force32 with the MD tail (kinetic tensor of
+//   v + f dt/2m, closing half, thermo row)
+// Velocity scaling stays lazy as in the reference: the chain's factor is
+// folded into the next kick and applied at the end of the run
+// (update_x_d_final, md_nvt.cpp:51-56).
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
 #include <vector>
 
-#include "system.h"
+#include "eam_common.cuh"
+#include "nhc.cuh"
 
 namespace mappg {
 
@@ -38,121 +47,30 @@ struct MdArgs {
     double* x;
     double* v;
     const double* f;
+    const float* f32;
+    float* v32;
     const double* x0;
     const uint8_t* elem;
     const int* binc;
     float4* p32;
+    const float4* p0;
     double masses[kMaxElem];
     double dtm[kMaxElem];  // dt2/m
+    float dtm32[kMaxElem];
     double dt, dt2, skin_sq;
-    double bv[3][3];
+    float dt32, skin_sq32;
+    double bs[6];          // x -> scaled frame
+    Frame fr;
     double* partials;
     double* thermo;  // rows of 14 or null
-    int nsteps;
-    int mixed;
+    long long nsteps;
     NhcParams nhc;
     DevScalars* sc;
 };
 
-__device__ __forceinline__ double nhc_f(double x) {
-    if (fabs(x) < 0.015625) return 1.0 + x / 2.0 + x * x / 6.0 + x * x * x / 24.0;
-    return (exp(x) - 1.0) / x;
-}
-
-// ThermostatNHC::operator()(T_r, ndof)  thermostat.cpp:47-143
-__device__ double nhc_step(const NhcParams& P, double* eta, double T_r) {
-    double rescale = 1.0, prev_fac, tmp;
-    const int L = P.L;
-    if (L == 1) {
-        for (int it = 0; it < P.niters; it++) {
-            eta[0] += P.ddt2 * P.freq_sq * (T_r - 1.0);
-            prev_fac = exp(-P.ddt * eta[0]);
-            rescale *= prev_fac;
-            T_r *= prev_fac * prev_fac;
-            eta[0] += P.ddt2 * P.freq_sq * (T_r - 1.0);
-        }
-        return rescale;
-    }
-    for (int it = 0; it < P.niters; it++) {
-        eta[L - 1] += P.ddt2 * (eta[L - 2] * eta[L - 2] - P.freq_sq);
-        prev_fac = -eta[L - 1];
-        for (int ich = L - 2; ich > 0; ich--) {
-            eta[ich] += P.ddt2 * nhc_f(prev_fac * P.ddt2) * (prev_fac * eta[ich] + eta[ich - 1] * eta[ich - 1] - P.freq_sq);
-            prev_fac = -eta[ich];
-        }
-        eta[0] += P.ddt2 * nhc_f(prev_fac * P.ddt2) * (prev_fac * eta[0] + P.freq_sq * (T_r - 1.0));
-        prev_fac = -eta[0];
-        tmp = exp(P.ddt * prev_fac);
-        rescale *= tmp;
-        T_r *= tmp * tmp;
-        prev_fac = (T_r - 1.0) * P.freq_sq;
-        eta[0] += P.ddt2 * nhc_f(-eta[1] * P.ddt2) * (-eta[1] * eta[0] + prev_fac);
-        prev_fac = P.ndof * eta[0] * eta[0] - P.freq_sq;
-        for (int ich = 1; ich < L - 1; ich++) {
-            eta[ich] += P.ddt2 * nhc_f(-eta[ich + 1] * P.ddt2) * (-eta[ich + 1] * eta[ich] + prev_fac);
-            prev_fac = eta[ich] * eta[ich] - P.freq_sq;
-        }
-        eta[L - 1] += P.ddt2 * prev_fac;
-    }
-    return rescale;
-}
-
-// one half of the particle thermostat as MDNVT::run applies it:
-// fac = chain(T/T0); mvv *= fac^2; T *= fac^2
-__device__ double thermo_half(const NhcParams& P, DevScalars* sc) {
-    double fac = nhc_step(P, sc->eta, sc->T_part / P.T);
-    double f2 = fac * fac;
-    for (int k = 0; k < 6; k++) sc->mvv[k] *= f2;
-    sc->T_part *= f2;
-    return fac;
-}
-
-__device__ void write_thermo(const MdArgs& a, long long row) {
-    if (!a.thermo) return;
-    double* r = a.thermo + 14 * row;
-    DevScalars* sc = a.sc;
-    r[0] = sc->energy;
-    r[1] = sc->T_part;
-    for (int k = 0; k < 6; k++) r[2 + k] = sc->mvv[k];
-    for (int k = 0; k < 6; k++) r[8 + k] = sc->virial[k];
-}
-
 template <int K>
 __device__ bool md_block_partials(double (&v)[K], double* partials, unsigned* counter) {
-    __shared__ double red[32][K];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        double t = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) red[w][k] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x < K) {
-        double t = 0.0;
-        for (int q = 0; q < nw; q++) t += red[q][threadIdx.x];
-        partials[blockIdx.x * kRedSlots + threadIdx.x] = t;
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    return last;
-}
-
-template <int K>
-__device__ void md_final_sums(const double* partials, int nblk, double (&tot)[K]) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        double t = 0.0;
-        for (int b = lane; b < nblk; b += 32) t += partials[b * kRedSlots + k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        tot[k] = t;
-    }
+    return block_partials<K>(v, partials, 0, counter);
 }
 
 // pre_init (md_nvt.cpp:256-340): kinetic tensor and temperature of the
@@ -172,7 +90,7 @@ __global__ void k_mvv_init(MdArgs a) {
     }
     if (md_block_partials<6>(d, a.partials, &a.sc->counter[3]) && threadIdx.x < 32) {
         double t[6];
-        md_final_sums<6>(a.partials, gridDim.x, t);
+        final_sums<6>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
             for (int k = 0; k < 6; k++) a.sc->mvv[k] = t[k];
             a.sc->T_part = (t[0] + (t[3] + t[5])) / a.nhc.ndof_kB;
@@ -182,17 +100,17 @@ __global__ void k_mvv_init(MdArgs a) {
     }
 }
 
-// run start: thermo row 0, no pending velocity scale
+// run start: thermo row 0, no pending velocity scale or kick
 __global__ void k_run_begin(MdArgs a) {
-    write_thermo(a, 0);
+    write_thermo_row(a.thermo, a.sc, 0);
     a.sc->fac_x_d = 1.0;
+    a.sc->pending_kick = 0;
 }
 
-// opening thermostat half of a step: fac_x_d *= chain(T/T0)
+// ------------------------------------------------------------------ FP64 path
 __global__ void k_step_open(MdArgs a) { a.sc->fac_x_d *= thermo_half(a.nhc, a.sc); }
 
-template <bool MIX>
-__global__ void __launch_bounds__(256) k_kick_drift(MdArgs a) {
+__global__ void __launch_bounds__(256) k_kick_drift64(MdArgs a) {
     const int n = a.n;
     const double fac = a.sc->fac_x_d;
     double dsum[3] = {0, 0, 0};
@@ -201,24 +119,17 @@ __global__ void __launch_bounds__(256) k_kick_drift(MdArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             double vv = a.v[c * n + i], ff = a.f[c * n + i], xx = a.x[c * n + i];
-            if (MIX) {
-                vv = vv * fac + ff * a.dtm[e];
-                double dx = vv * a.dt;
-                dsum[c] += dx;
-                xx += dx;
-            } else {
-                vv = __dadd_rn(__dmul_rn(vv, fac), __ddiv_rn(__dmul_rn(ff, a.dt2), a.masses[e]));
-                double dx = __dmul_rn(vv, a.dt);
-                dsum[c] = __dadd_rn(dsum[c], dx);
-                xx = __dadd_rn(xx, dx);
-            }
+            vv = __dadd_rn(__dmul_rn(vv, fac), __ddiv_rn(__dmul_rn(ff, a.dt2), a.masses[e]));
+            double dx = __dmul_rn(vv, a.dt);
+            dsum[c] = __dadd_rn(dsum[c], dx);
+            xx = __dadd_rn(xx, dx);
             a.v[c * n + i] = vv;
             a.x[c * n + i] = xx;
         }
     }
     if (md_block_partials<3>(dsum, a.partials, &a.sc->counter[4]) && threadIdx.x < 32) {
         double t[3];
-        md_final_sums<3>(a.partials, gridDim.x, t);
+        final_sums<3>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
             double natms = (double)n;
             for (int c = 0; c < 3; c++) a.sc->com[c] = t[c] / natms;
@@ -228,8 +139,7 @@ __global__ void __launch_bounds__(256) k_kick_drift(MdArgs a) {
     }
 }
 
-template <bool MIX>
-__global__ void __launch_bounds__(256) k_com_skin(MdArgs a) {
+__global__ void __launch_bounds__(256) k_com_skin64(MdArgs a) {
     const int n = a.n;
     const double c0 = a.sc->com[0], c1 = a.sc->com[1], c2 = a.sc->com[2];
     int moved = 0;
@@ -241,24 +151,11 @@ __global__ void __launch_bounds__(256) k_com_skin(MdArgs a) {
         double d0 = __dsub_rn(a.x0[i], x0), d1 = __dsub_rn(a.x0[n + i], x1), d2 = __dsub_rn(a.x0[2 * n + i], x2);
         double r = __dadd_rn(__dmul_rn(d0, d0), __dadd_rn(__dmul_rn(d1, d1), __dmul_rn(d2, d2)));
         moved |= r > a.skin_sq;
-        if (MIX) {
-            int bc = a.binc[i];
-            double b0 = bc & 1023, b1 = (bc >> 10) & 1023, b2 = (bc >> 20) & 1023;
-            double o0 = b0 * a.bv[0][0] + b1 * a.bv[1][0] + b2 * a.bv[2][0];
-            double o1 = b1 * a.bv[1][1] + b2 * a.bv[2][1];
-            double o2 = b2 * a.bv[2][2];
-            float4 p = a.p32[i];
-            p.x = (float)(x0 - o0);
-            p.y = (float)(x1 - o1);
-            p.z = (float)(x2 - o2);
-            a.p32[i] = p;
-        }
     }
     if (__syncthreads_or(moved) && threadIdx.x == 0) a.sc->rebuild = 1;
 }
 
-template <bool MIX>
-__global__ void __launch_bounds__(256) k_kick2(MdArgs a) {
+__global__ void __launch_bounds__(256) k_kick2_64(MdArgs a) {
     const int n = a.n;
     double d[6] = {0, 0, 0, 0, 0, 0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -268,10 +165,7 @@ __global__ void __launch_bounds__(256) k_kick2(MdArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             double v0 = a.v[c * n + i], ff = a.f[c * n + i];
-            if (MIX)
-                v0 += ff * a.dtm[e];
-            else
-                v0 = __dadd_rn(v0, __ddiv_rn(__dmul_rn(ff, a.dt2), m));
+            v0 = __dadd_rn(v0, __ddiv_rn(__dmul_rn(ff, a.dt2), m));
             a.v[c * n + i] = v0;
             vv[c] = v0;
         }
@@ -284,26 +178,126 @@ __global__ void __launch_bounds__(256) k_kick2(MdArgs a) {
     }
     if (md_block_partials<6>(d, a.partials, &a.sc->counter[5]) && threadIdx.x < 32) {
         double t[6];
-        md_final_sums<6>(a.partials, gridDim.x, t);
+        final_sums<6>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
             DevScalars* sc = a.sc;
             for (int k = 0; k < 6; k++) sc->mvv[k] = t[k];
             sc->T_part = (t[0] + (t[3] + t[5])) / a.nhc.ndof_kB;
-            // closing half of this step
             sc->fac_x_d = thermo_half(a.nhc, sc);
             long long st = ++sc->step;
-            if (st <= a.nsteps) write_thermo(a, st);
+            if (st <= a.nsteps) write_thermo_row(a.thermo, sc, st);
             if (!(isfinite(sc->energy) && isfinite(sc->T_part))) sc->bad = 1;
             sc->counter[5] = 0;
         }
     }
 }
 
-__global__ void k_run_end(MdArgs a) {
+__global__ void k_run_end64(MdArgs a) {
     const int n = a.n;
     const double fac = a.sc->fac_x_d;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n; i += gridDim.x * blockDim.x)
         a.v[i] = __dmul_rn(a.v[i], fac);
+}
+
+// ------------------------------------------------------------------ mixed path
+__global__ void k_step_open32(MdArgs a) {
+    DevScalars* sc = a.sc;
+    const double fo = thermo_half(a.nhc, sc);
+    if (sc->pending_kick) {
+        const double F = sc->fac_close * fo;
+        sc->kickA = F;
+        sc->kickB = 1.0 + F;
+    } else {
+        sc->kickA = fo;
+        sc->kickB = 1.0;
+    }
+    sc->rebuild = 0;
+}
+
+__global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
+    const int n = a.n;
+    const double A = a.sc->kickA;
+    const float B = (float)a.sc->kickB;
+    float dsum0 = 0.f, dsum1 = 0.f, dsum2 = 0.f;
+    int moved = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int e = a.elem[i];
+        const float kf = a.dtm32[e] * B;
+        double xv[3];
+        float vf[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            double v = fma(a.v[c * n + i], A, (double)(a.f32[c * n + i] * kf));
+            double x = fma(v, a.dt, a.x[c * n + i]);
+            a.v[c * n + i] = v;
+            a.x[c * n + i] = x;
+            xv[c] = x;
+            vf[c] = (float)v;
+            a.v32[c * n + i] = vf[c];
+        }
+        dsum0 = fmaf(vf[0], a.dt32, dsum0);
+        dsum1 = fmaf(vf[1], a.dt32, dsum1);
+        dsum2 = fmaf(vf[2], a.dt32, dsum2);
+        // frame position and the skin test against the position at the build
+        const int bc = a.binc[i];
+        const double u0 = a.bs[0] * xv[0] + (a.bs[1] * xv[1] + a.bs[2] * xv[2]);
+        const double u1 = a.bs[3] * xv[1] + a.bs[4] * xv[2];
+        const double u2 = a.bs[5] * xv[2];
+        float4 p;
+        p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
+        p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
+        p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+        p.w = 0.f;
+        a.p32[i] = p;
+        const float4 q = a.p0[i];
+        const float da = p.x - q.x, db = p.y - q.y, dc = p.z - q.z;
+        float cx, cy, cz;
+        if (a.fr.ortho) {
+            cx = da * a.fr.G[0][0];
+            cy = db * a.fr.G[1][1];
+            cz = dc * a.fr.G[2][2];
+        } else {
+            cx = da * a.fr.G[0][0] + db * a.fr.G[1][0] + dc * a.fr.G[2][0];
+            cy = db * a.fr.G[1][1] + dc * a.fr.G[2][1];
+            cz = dc * a.fr.G[2][2];
+        }
+        moved |= fmaf(cx, cx, fmaf(cy, cy, cz * cz)) > a.skin_sq32;
+    }
+    if (__syncthreads_or(moved) && threadIdx.x == 0) a.sc->rebuild = 1;
+    double dv[3] = {(double)dsum0, (double)dsum1, (double)dsum2};
+    if (md_block_partials<3>(dv, a.partials, &a.sc->counter[4]) && threadIdx.x < 32) {
+        double t[3];
+        final_sums<3>(a.partials, gridDim.x, t);
+        if (threadIdx.x == 0) {
+            const double natms = (double)n;
+            for (int c = 0; c < 3; c++) {
+                a.sc->com[c] = t[c] / natms;
+                a.sc->drift[c] += a.sc->com[c];
+            }
+            a.sc->pending_kick = 0;
+            a.sc->counter[4] = 0;
+        }
+    }
+}
+
+// end of a mixed run: the pending closing kick and scale, v = (v + f dt/2m) fc,
+// and the accumulated mean displacement removed from x
+__global__ void k_run_end32(MdArgs a) {
+    const int n = a.n;
+    const bool pend = a.sc->pending_kick != 0;
+    const double fc = pend ? a.sc->fac_close : a.sc->fac_x_d;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+        const int i = q % n, c = q / n;
+        double v = a.v[q];
+        if (pend) v += (double)a.f32[q] * a.dtm[a.elem[i]];
+        a.v[q] = v * fc;
+        a.x[q] -= a.sc->drift[c];
+    }
+}
+
+__global__ void k_clear_drift(DevScalars* sc) {
+    sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
+    sc->pending_kick = 0;
 }
 
 }  // namespace mappg
@@ -313,31 +307,44 @@ using namespace mappg;
 namespace mappg {
 void sys_build(mappg_sys* s);
 
-static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps,
-                      double* thermo_dev) {
+static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters,
+                      long long nsteps, double* thermo_dev) {
     MdArgs a;
     memset(&a, 0, sizeof(a));
     a.n = s->n;
     a.x = s->x;
     a.v = s->v;
     a.f = s->f;
+    a.f32 = s->f32;
+    a.v32 = s->v32;
     a.x0 = s->x0;
     a.elem = s->elem;
     a.binc = s->binc;
     a.p32 = s->p32;
+    a.p0 = s->p0;
     a.dt = dt;
     a.dt2 = dt / 2.0;
+    a.dt32 = (float)dt;
     for (int e = 0; e < s->ne; e++) {
         a.masses[e] = s->masses[e];
         a.dtm[e] = a.dt2 / s->masses[e];
+        a.dtm32[e] = (float)a.dtm[e];
     }
     a.skin_sq = 0.25 * s->skin * s->skin;
-    for (int d = 0; d < 3; d++)
-        for (int k = 0; k < 3; k++) a.bv[d][k] = s->box.H[d][k] / s->nb[d];
+    // the FP32 skin test triggers a little early rather than late
+    a.skin_sq32 = (float)(a.skin_sq * (1.0 - 1e-4));
+    const double S[3] = {8.0 * s->nb[0], 8.0 * s->nb[1], 8.0 * s->nb[2]};
+    const double* b6 = s->box.b6;
+    a.bs[0] = b6[0] * S[0];
+    a.bs[1] = b6[1] * S[0];
+    a.bs[2] = b6[2] * S[0];
+    a.bs[3] = b6[3] * S[1];
+    a.bs[4] = b6[4] * S[1];
+    a.bs[5] = b6[5] * S[2];
+    a.fr = s->frame;
     a.partials = s->partials;
     a.thermo = thermo_dev;
     a.nsteps = nsteps;
-    a.mixed = s->precision == MAPPG_MIXED;
     // ThermostatNHC(dt/2, t_relax, L, niters)  md_nvt.cpp:19, thermostat.cpp:20-36
     const double tdt = dt / 2.0;
     a.nhc.T = T;
@@ -353,15 +360,29 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
     return a;
 }
 
-template <bool MIX>
-static void launch_step(mappg_sys* s, const MdArgs& a) {
+static void launch_step64(mappg_sys* s, const MdArgs& a) {
     int g = grid_for(s, s->n, 256);
     k_step_open<<<1, 1, 0, s->stream>>>(a);
-    k_kick_drift<MIX><<<g, 256, 0, s->stream>>>(a);
-    k_com_skin<MIX><<<g, 256, 0, s->stream>>>(a);
+    k_kick_drift64<<<g, 256, 0, s->stream>>>(a);
+    k_com_skin64<<<g, 256, 0, s->stream>>>(a);
     launch_rebuild_chain(s);
     launch_force(s);
-    k_kick2<MIX><<<g, 256, 0, s->stream>>>(a);
+    k_kick2_64<<<g, 256, 0, s->stream>>>(a);
+}
+
+static void launch_step32(mappg_sys* s, const MdArgs& a) {
+    int g = grid_for(s, s->n, 256);
+    k_step_open32<<<1, 1, 0, s->stream>>>(a);
+    k_integrate32<<<g, 256, 0, s->stream>>>(a);
+    launch_rebuild_chain(s);
+    EamArgs e = eam_args(s);
+    launch_density32(s, e);
+    e.md_tail = 1;
+    e.thermo = a.thermo;
+    e.nsteps = a.nsteps;
+    e.nhc = a.nhc;
+    for (int k = 0; k < s->ne; k++) e.dtm32[k] = a.dtm32[k];
+    launch_force32(s, e);
 }
 
 struct NvtRun {
@@ -411,7 +432,7 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     }
     NvtRun* r = new NvtRun();
     s->run = r;
-    r->a = md_args(s, T, dt, kB, t_relax, L, niters, (int)std::min<long long>(nsteps, 1LL << 30), tdev);
+    r->a = md_args(s, T, dt, kB, t_relax, L, niters, nsteps, tdev);
     r->L = L;
     r->planned = nsteps;
     r->thermo = thermo;
@@ -421,6 +442,7 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
         for (int k = 0; k < L; k++) eta_h[k] = eta[k];
     MAPPG_CUDA(cudaMemcpyAsync(s->sc->eta, eta_h, sizeof(double) * kMaxChain, cudaMemcpyHostToDevice, s->stream));
     int g = grid_for(s, s->n, 256);
+    k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
     k_mvv_init<<<g, 256, 0, s->stream>>>(a);
     sys_build(s);
     launch_force(s);
@@ -429,11 +451,11 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     MAPPG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     try {
         if (s->precision == MAPPG_MIXED)
-            launch_step<true>(s, a);
+            launch_step32(s, a);
         else
-            launch_step<false>(s, a);
+            launch_step64(s, a);
     } catch (...) {
-        cudaGraph_t g2;
+        cudaGraph_t g2 = nullptr;
         cudaStreamEndCapture(s->stream, &g2);
         if (g2) cudaGraphDestroy(g2);
         throw;
@@ -455,8 +477,13 @@ void nvt_steps(mappg_sys* s, long long nsteps) {
 void nvt_end(mappg_sys* s, double* eta, double* thermo) {
     NvtRun* r = (NvtRun*)s->run;
     if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
-    int g = grid_for(s, s->n, 256);
-    k_run_end<<<g, 256, 0, s->stream>>>(r->a);
+    int g = grid_for(s, 3LL * s->n, 256);
+    if (s->precision == MAPPG_MIXED) {
+        k_run_end32<<<g, 256, 0, s->stream>>>(r->a);
+        k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
+    } else {
+        k_run_end64<<<g, 256, 0, s->stream>>>(r->a);
+    }
     MAPPG_CUDA(cudaGetLastError());
     DevScalars h;
     MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
@@ -467,7 +494,6 @@ void nvt_end(mappg_sys* s, double* eta, double* thermo) {
     if (eta)
         for (int k = 0; k < r->L; k++) eta[k] = h.eta[k];
     run_clear(s);
-    s->forces_valid = true;
     if (h.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during the run"};
     if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite position, energy or temperature during the run"};
 }

@@ -63,21 +63,27 @@ void sys_set_box(mappg_sys* s, const double* H) {
         nbv[d] = 1.0 / nb;
     }
     s->nbins = s->nb[0] * s->nb[1] * s->nb[2];
-    // neighbour code c = (d0+1)+3(d1+1)+9(d2+1): the image's bin is atom i's bin + d
+    // scaled bin frame: s'_d = s_d * 8 nb_d; Cartesian dx = dx' G with
+    // G_dk = H_dk / (8 nb_d), kept as head + tail
+    Frame& fr = s->frame;
+    fr.ortho = (H[3] == 0.0 && H[6] == 0.0 && H[7] == 0.0) ? 1 : 0;
+    for (int d = 0; d < 3; d++)
+        for (int k = 0; k < 3; k++) {
+            double g = s->box.H[d][k] / (8.0 * s->nb[d]);
+            fr.G[d][k] = (float)g;
+            fr.Glo[d][k] = (float)(g - (double)fr.G[d][k]);
+        }
+    // neighbour code c = (d0+1)+3(d1+1)+9(d2+1): the image's bin is atom i's
+    // bin + d; its frame offset is exactly -8 d
     for (int c = 0; c < 27; c++) {
         int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
         for (int k = 0; k < 3; k++) {
-            double o = 0.0, sh = 0.0;
-            for (int q = 0; q < 3; q++) {
-                o -= d[q] * nbv[q] * s->box.H[q][k];
-                sh += d[q] * s->box.H[q][k];
-            }
-            s->off32[c][k] = (float)o;
-            s->off32lo[c][k] = (float)(o - (double)s->off32[c][k]);
+            double sh = 0.0;
+            for (int q = 0; q < 3; q++) sh += d[q] * s->box.H[q][k];
+            fr.off[c][k] = -kBinW * d[k];
             s->shift[c][k] = sh;  // indexed by image code n instead of d
         }
-        s->off32[c][3] = 0.f;
-        s->off32lo[c][3] = 0.f;
+        fr.off[c][3] = 0.f;
     }
     double pmax = s->skin;
     for (int q = 0; q < 3; q++) {
@@ -107,7 +113,7 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 
 struct Geo {
     double h6[6], b6[6];
-    double bv[3][3];  // bin vectors H[d]/nb[d]
+    double bs[6];  // b6 with each column scaled by 8 nb_d: x -> s' directly
     int nb[3];
 };
 
@@ -115,10 +121,14 @@ static Geo make_geo(mappg_sys* s) {
     Geo g;
     memcpy(g.h6, s->box.h6, sizeof(g.h6));
     memcpy(g.b6, s->box.b6, sizeof(g.b6));
-    for (int d = 0; d < 3; d++) {
-        g.nb[d] = s->nb[d];
-        for (int k = 0; k < 3; k++) g.bv[d][k] = s->box.H[d][k] / s->nb[d];
-    }
+    for (int d = 0; d < 3; d++) g.nb[d] = s->nb[d];
+    const double S0 = 8.0 * s->nb[0], S1 = 8.0 * s->nb[1], S2 = 8.0 * s->nb[2];
+    g.bs[0] = g.b6[0] * S0;
+    g.bs[1] = g.b6[1] * S0;
+    g.bs[2] = g.b6[2] * S0;
+    g.bs[3] = g.b6[3] * S1;
+    g.bs[4] = g.b6[4] * S1;
+    g.bs[5] = g.b6[5] * S2;
     return g;
 }
 
@@ -152,8 +162,10 @@ __global__ void k_wrap_bin(int n, double* __restrict__ x, double* __restrict__ s
                            int* __restrict__ binid, int* __restrict__ bin_count, DevScalars* sc) {
     if (!sc->rebuild) return;
     int bad = 0;
+    const double drift0 = sc->drift[0], drift1 = sc->drift[1], drift2 = sc->drift[2];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double x0 = x[i], x1 = x[n + i], x2 = x[2 * n + i];
+        // the mixed MD path defers its mean-displacement removal to here
+        double x0 = dsub(x[i], drift0), x1 = dsub(x[n + i], drift1), x2 = dsub(x[2 * n + i], drift2);
         double s0 = dadd(dmul(g.b6[0], x0), dadd(dmul(g.b6[1], x1), dmul(g.b6[2], x2)));
         s0 = wrap01(s0, &bad);
         double s1 = dadd(dmul(g.b6[3], x1), dmul(g.b6[4], x2));
@@ -240,24 +252,28 @@ __global__ void k_sort_bins(int nbins, const int* __restrict__ bin_start, const 
     }
 }
 
-// FP32 bin-relative positions (the shadow the mixed kernels gather);
-// gated == true only runs inside a rebuild
-__global__ void k_shadow(int n, const double* __restrict__ x, const int* __restrict__ binc,
-                         const uint8_t* __restrict__ elem, float4* __restrict__ p32, Geo g, int gated,
-                         DevScalars* sc) {
+// FP32 positions in the scaled bin frame, relative to the atom's bin corner:
+// p'_d = (x B)_d * 8 nb_d - 8 b_d (x not wrapped between builds, so p' may
+// leave [0,8) by the drift since the build); gated == true only in a rebuild
+__device__ __forceinline__ float4 frame_pos(const Geo& g, double x0, double x1, double x2, int bc) {
+    double u0 = g.bs[0] * x0 + (g.bs[1] * x1 + g.bs[2] * x2);
+    double u1 = g.bs[3] * x1 + g.bs[4] * x2;
+    double u2 = g.bs[5] * x2;
+    float4 p;
+    p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
+    p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
+    p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+    p.w = 0.f;
+    return p;
+}
+
+__global__ void k_shadow(int n, const double* __restrict__ x, const int* __restrict__ binc, float4* __restrict__ p32,
+                         float4* __restrict__ p0, Geo g, int gated, DevScalars* sc) {
     if (gated && !sc->rebuild) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int bc = binc[i];
-        double b0 = bc & 1023, b1 = (bc >> 10) & 1023, b2 = (bc >> 20) & 1023;
-        double o0 = b0 * g.bv[0][0] + b1 * g.bv[1][0] + b2 * g.bv[2][0];
-        double o1 = b1 * g.bv[1][1] + b2 * g.bv[2][1];
-        double o2 = b2 * g.bv[2][2];
-        float4 p;
-        p.x = (float)(x[i] - o0);
-        p.y = (float)(x[n + i] - o1);
-        p.z = (float)(x[2 * n + i] - o2);
-        p.w = __int_as_float((int)elem[i]);
+        float4 p = frame_pos(g, x[i], x[n + i], x[2 * n + i], binc[i]);
         p32[i] = p;
+        if (gated) p0[i] = p;
     }
 }
 
@@ -267,16 +283,32 @@ struct BuildArgs {
     const double* s;
     const float4* p32;
     const int* binc;
+    const uint8_t* elem;
     const int* bin_start;
     const int* bin_atoms;
     int* nbr;
     int* nnbr;
     double* x0;
     Geo g;
+    Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
     double cut_sk_sq[kMaxElem * kMaxElem];
-    float off32[27][4];
 };
+
+// frame displacement to Cartesian: dx' G with G as head + tail
+__device__ __forceinline__ void frame_to_cart(const Frame& fr, float a, float b, float c, float& x, float& y,
+                                              float& z) {
+    if (fr.ortho) {
+        x = fmaf(a, fr.G[0][0], a * fr.Glo[0][0]);
+        y = fmaf(b, fr.G[1][1], b * fr.Glo[1][1]);
+        z = fmaf(c, fr.G[2][2], c * fr.Glo[2][2]);
+    } else {
+        x = fmaf(a, fr.G[0][0], fmaf(b, fr.G[1][0], fmaf(c, fr.G[2][0], a * fr.Glo[0][0] + b * fr.Glo[1][0] +
+                                                                        c * fr.Glo[2][0])));
+        y = fmaf(b, fr.G[1][1], fmaf(c, fr.G[2][1], b * fr.Glo[1][1] + c * fr.Glo[2][1]));
+        z = fmaf(c, fr.G[2][2], c * fr.Glo[2][2]);
+    }
+}
 
 // rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
 // candidates, ballots keep the row in (bin, index) order; x0 <- x
@@ -284,7 +316,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
     if (!sc->rebuild) return;
     __shared__ float4 off[27];
     if (threadIdx.x < 27)
-        off[threadIdx.x] = make_float4(a.off32[threadIdx.x][0], a.off32[threadIdx.x][1], a.off32[threadIdx.x][2], 0.f);
+        off[threadIdx.x] = make_float4(a.fr.off[threadIdx.x][0], a.fr.off[threadIdx.x][1], a.fr.off[threadIdx.x][2], 0.f);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -295,7 +327,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
     int overflow = 0;
     for (int i = warp; i < n; i += nw) {
         float4 pi = a.p32[i];
-        int ei = __float_as_int(pi.w);
+        int ei = a.elem[i];
         int bc = a.binc[i];
         int bi[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
         double xi0 = a.x[i], xi1 = a.x[n + i], xi2 = a.x[2 * n + i];
@@ -315,13 +347,15 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
             for (int k0 = lo; k0 < hi; k0 += 32) {
                 int k = k0 + lane;
                 bool keep = false;
-                int j = 0;
+                int j = 0, ej = 0;
                 if (k < hi) {
                     j = a.bin_atoms[k];
                     if (!(self_img && j == i)) {
                         float4 pj = a.p32[j];
-                        int ej = __float_as_int(pj.w);
-                        float dx = (pi.x - pj.x) + o.x, dy = (pi.y - pj.y) + o.y, dz = (pi.z - pj.z) + o.z;
+                        ej = a.elem[j];
+                        float dx, dy, dz;
+                        frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
+                                      dz);
                         float r2 = dx * dx + (dy * dy + dz * dz);
                         int pe = ei * a.ne + ej;
                         if (r2 < a.lo2[pe]) {
@@ -346,7 +380,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
                 unsigned m = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
                     int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    if (pos < a.maxnbr) row[pos] = (j << kCodeBits) | c;
+                    if (pos < a.maxnbr) row[pos] = (j << kEntryShift) | (ej << 5) | c;
                 }
                 cnt += __popc(m);
             }
@@ -369,6 +403,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
 __global__ void k_rebuild_done(DevScalars* sc) {
     if (!sc->rebuild) return;
     sc->nrebuild++;
+    sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
 }
 
 // skin test of DynamicMD::decide (dynamic_md.cpp:90-105): rebuild when any
@@ -409,7 +444,18 @@ __global__ void k_scatter_aos(int n, const int* __restrict__ id, const double* _
     }
 }
 
+__global__ void k_f32_to_f64(int n3, const float* __restrict__ a, double* __restrict__ b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+
 // ------------------------------------------------------------------ launchers
+void sync_forces64(mappg_sys* s) {
+    if (!s->f_is_f32) return;
+    k_f32_to_f64<<<grid_for(s, 3LL * s->n, 256), 256, 0, s->stream>>>(3 * s->n, s->f32, s->f);
+    MAPPG_CUDA(cudaGetLastError());
+    s->f_is_f32 = false;
+}
+
 void request_rebuild(mappg_sys* s) {
     k_set_rebuild<<<1, 1, 0, s->stream>>>(s->sc, 1);
     MAPPG_CUDA(cudaGetLastError());
@@ -417,7 +463,7 @@ void request_rebuild(mappg_sys* s) {
 
 void launch_shadow(mappg_sys* s, bool gated) {
     Geo g = make_geo(s);
-    k_shadow<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->elem, s->p32, g, gated ? 1 : 0,
+    k_shadow<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, gated ? 1 : 0,
                                                             s->sc);
     MAPPG_CUDA(cudaGetLastError());
 }
@@ -432,7 +478,7 @@ void launch_rebuild_chain(mappg_sys* s) {
     k_scatter_bins<<<gb, B, 0, s->stream>>>(s->n, s->binid, s->bin_start, s->bin_count, bin_tmp, s->sc);
     k_sort_bins<<<grid_for(s, (long long)s->nbins * 32, B), B, 0, s->stream>>>(s->nbins, s->bin_start, bin_tmp,
                                                                                s->bin_atoms, s->bin_count, s->sc);
-    k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->elem, s->p32, g, 1, s->sc);
+    k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, 1, s->sc);
     BuildArgs a;
     a.n = s->n;
     a.maxnbr = s->maxnbr;
@@ -441,6 +487,7 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.s = s->s;
     a.p32 = s->p32;
     a.binc = s->binc;
+    a.elem = s->elem;
     a.bin_start = s->bin_start;
     a.bin_atoms = s->bin_atoms;
     a.nbr = s->nbr;
@@ -452,7 +499,7 @@ void launch_rebuild_chain(mappg_sys* s) {
         a.lo2[p] = (float)(s->cut_sk_sq[p] - s->band);
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
     }
-    memcpy(a.off32, s->off32, sizeof(a.off32));
+    a.fr = s->frame;
     k_build_list<<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
     k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
     MAPPG_CUDA(cudaGetLastError());
@@ -483,21 +530,24 @@ EamArgs eam_args(mappg_sys* s) {
     a.rphi64 = ff->dev.rphi64;
     a.F64 = ff->dev.F64;
     a.rho32 = ff->dev.rho32;
-    a.rphi32 = ff->dev.rphi32;
+    a.ftab = ff->dev.ftab;
     a.F32 = ff->dev.F32;
-    a.rphi32_lo = ff->dev.rphi32_lo;
+    a.F32lo = ff->dev.F32lo;
     a.dr_inv = ff->dev.dr_inv;
     a.drho_inv = ff->dev.drho_inv;
     a.rho_max = ff->dev.rho_max;
     for (int p = 0; p < s->ne * s->ne; p++) a.cut_sq[p] = s->cut_sq[p];
     memcpy(a.shift, s->shift, sizeof(a.shift));
-    memcpy(a.off32, s->off32, sizeof(a.off32));
-    memcpy(a.off32lo, s->off32lo, sizeof(a.off32lo));
+    a.fr = s->frame;
     for (int d = 0; d < 3; d++) a.nb[d] = s->nb[d];
+    a.q32 = s->q32;
     a.rho = s->rho;
     a.dF = s->dF;
-    a.dF32 = s->dF32;
+    a.rho32out = s->rho32;
     a.f = s->f;
+    a.f32 = s->f32;
+    a.v32 = s->v32;
+    for (int e = 0; e < s->ne; e++) a.mass32[e] = (float)s->masses[e];
     a.partials = s->partials;
     a.sc = s->sc;
     return a;
@@ -522,9 +572,9 @@ namespace mappg {
 static void dev_alloc(void** p, size_t bytes) { MAPPG_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 16)); }
 
 void sys_free(mappg_sys* s) {
-    void* ptrs[] = {s->x, s->v, s->f, s->x0, s->s, s->elem, s->id, s->inv, s->p32, s->binc, s->binid,
-                    s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr, s->rho, s->dF, s->dF32,
-                    s->partials, s->sc, s->stage, s->thermo_dev};
+    void* ptrs[] = {s->x, s->v, s->f, s->x0, s->s, s->elem, s->id, s->inv, s->p32, s->q32, s->p0, s->f32, s->v32,
+                    s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
+                    s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -577,13 +627,17 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
     dev_alloc((void**)&s->id, sizeof(int) * n);
     dev_alloc((void**)&s->inv, sizeof(int) * n);
     dev_alloc((void**)&s->p32, sizeof(float4) * n);
+    dev_alloc((void**)&s->q32, sizeof(float4) * n);
+    dev_alloc((void**)&s->p0, sizeof(float4) * n);
+    dev_alloc((void**)&s->f32, sizeof(float) * 3 * (size_t)n);
+    dev_alloc((void**)&s->v32, sizeof(float) * 3 * (size_t)n);
+    dev_alloc((void**)&s->rho32, sizeof(float) * n);
     dev_alloc((void**)&s->binc, sizeof(int) * n);
     dev_alloc((void**)&s->binid, sizeof(int) * n);
     dev_alloc((void**)&s->bin_atoms, sizeof(int) * 2 * (size_t)n);
     dev_alloc((void**)&s->nnbr, sizeof(int) * n);
     dev_alloc((void**)&s->rho, sizeof(double) * n);
     dev_alloc((void**)&s->dF, sizeof(double) * n);
-    dev_alloc((void**)&s->dF32, sizeof(float) * n);
     dev_alloc((void**)&s->partials, sizeof(double) * kRedSlots * kMaxBlocks);
     dev_alloc((void**)&s->sc, sizeof(DevScalars));
     MAPPG_CUDA(cudaMemsetAsync(s->sc, 0, sizeof(DevScalars), s->stream));
@@ -678,7 +732,7 @@ void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
         int* out = entries + 4 * uoff[u];
         for (int k = 0; k < nn[i]; k++) {
             int e = rows[(size_t)i * s->maxnbr + k];
-            int j = e >> kCodeBits, c = e & 31;
+            int j = entry_j(e), c = entry_code(e);
             int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
             out[4 * k] = s->host_id[j];
             for (int q = 0; q < 3; q++) {

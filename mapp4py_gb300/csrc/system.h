@@ -4,14 +4,24 @@
 // maps it back to the caller's order):
 //   x, v, f, x0, s   FP64 structure-of-arrays, 3 planes of n doubles each
 //   elem             uint8 per atom
-//   p32              float4 per atom: position relative to its bin corner
-//                    (FP32) and the element in .w; what the mixed-precision
-//                    kernels gather per neighbour
 //   binc             packed bin coordinates per atom (10 bits each)
+//   p32              float4 per atom: the position in the scaled bin frame
+//                    (below), relative to the atom's bin corner
+//   q32              float4 per atom: p32.xyz and F'(rho) in .w, written by
+//                    the mixed density kernel and gathered by the force kernel
 //   nbr              full neighbour list, row i holds nnbr[i] entries
-//                    (j << 5 | code), code = bin step (dx+1)+3(dy+1)+9(dz+1)
-//                    from atom i's bin to the neighbour image's bin
-//   rho, dF, dF32    per-atom host density and F'(rho)
+//                    (j << 8 | e_j << 5 | code), code = (d0+1)+3(d1+1)+9(d2+1)
+//                    the bin step from atom i's bin to the neighbour image's bin
+//   f32, v32         FP32 copies for the mixed path (forces out of the force
+//                    kernel; velocities for its kinetic-energy epilogue)
+//
+// Scaled bin frame: with nb_d bins along fractional axis d, the scaled
+// coordinate is s'_d = s_d * 8 nb_d, so every bin is exactly 8 wide, bin
+// steps are exact (+-8) and the periodic seam is exact (8 nb_d).  A pair's
+// displacement in the frame, dx' = (p'_i - p'_j) - 8 d, is therefore free of
+// rounded constants; it becomes Cartesian through G = diag(1/(8 nb)) H,
+// applied as a head + tail pair so that its rounding is not shared by all
+// pairs either.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,9 +31,16 @@
 
 namespace mappg {
 
-constexpr int kRedSlots = 8;     // doubles per block partial
+constexpr int kRedSlots = 16;    // doubles per block partial
 constexpr int kMaxBlocks = 4096; // partial slots
 constexpr int kMaxChain = 16;    // NHC chain length
+constexpr int kEntryShift = 8;   // j << 8 | element << 5 | code
+constexpr int kMaxAtoms = 1 << 23;
+constexpr float kBinW = 8.0f;    // bin width in the scaled frame
+
+__host__ __device__ inline int entry_j(int e) { return e >> kEntryShift; }
+__host__ __device__ inline int entry_elem(int e) { return (e >> 5) & 7; }
+__host__ __device__ inline int entry_code(int e) { return e & 31; }
 
 struct Box {
     double H[3][3], B[3][3], h6[6], b6[6], vol, depth_inv[3];
@@ -34,11 +51,13 @@ struct DevScalars {
     int rebuild;       // set: the rebuild kernels of this step do their work
     int overflow;      // a neighbour row ran out of capacity
     int bad;           // non-finite value seen
-    int pad0;
+    int pending_kick;  // mixed MD: v still lacks the closing half kick
     unsigned counter[8];  // last-block-done counters, one per reduction site
     double energy;     // last force/energy call
+    double e_embed;    // embedding energy of the last mixed density pass
     double virial[6];  // F_H voigt
-    double com[3];     // mean displacement of the step (removed from x)
+    double com[3];     // mean displacement of the step
+    double drift[3];   // mixed MD: displacement not yet removed from x
     int maxrow;        // longest neighbour row of the last build
     int pad1;
     unsigned long long sumrow;  // total entries of the last build
@@ -46,6 +65,9 @@ struct DevScalars {
     double mvv[6];
     double T_part;
     double fac_x_d;    // pending velocity scale applied in the next kick
+    double fac_close;  // mixed MD: closing factor of the last step
+    double kickA;      // mixed MD: v <- A v + B f dt/2m
+    double kickB;
     double eta[kMaxChain];
     long long step;    // steps done in this run
     long long nrebuild;
@@ -56,7 +78,13 @@ struct NhcParams {
     int L, niters, ndof;
 };
 
-struct Sys;
+// geometry of the scaled bin frame
+struct Frame {
+    float G[3][3];     // Cartesian = dx' G (row vector), head
+    float Glo[3][3];   // tail
+    float off[27][4];  // -8 d for code c (exact)
+    int ortho;         // H has no off-diagonal terms
+};
 
 // arguments of the EAM kernels (passed by value)
 struct EamArgs {
@@ -66,26 +94,35 @@ struct EamArgs {
     const uint8_t* elem;
     const double* x;   // SoA 3n
     const float4* p32;
+    float4* q32;
     const int* binc;
-    const double4* rho64;
-    const double4* rphi64;
-    const double4* F64;
+    const Dbl4* rho64;
+    const Dbl4* rphi64;
+    const Dbl4* F64;
     const float4* rho32;
-    const float4* rphi32;
+    const float4* ftab;     // mixed force records, 3 float4 per (pair type, knot)
     const float4* F32;
-    const float* rphi32_lo;
+    const float* F32lo;
     double dr_inv, drho_inv, rho_max;
     double cut_sq[kMaxElem * kMaxElem];
     double shift[27][3];   // image shift n*H for image code (n0+1)+3(n1+1)+9(n2+1)
-    float off32[27][4];    // bin-step offset for neighbour code (FP32 head)
-    float off32lo[27][4];  // its FP32 tail: off = head + tail to ~1e-15
+    Frame fr;
     int nb[3];
     double* rho;
     double* dF;
-    float* dF32;
-    double* f;             // SoA 3n
+    float* rho32out;
+    double* f;             // SoA 3n (FP64 kernels)
+    float* f32;            // SoA 3n (mixed kernels)
     double* partials;
     DevScalars* sc;
+    // mixed MD tail of the force kernel (kinetic energy and thermostat)
+    const float* v32;      // SoA 3n
+    float dtm32[kMaxElem]; // dt/2/m
+    float mass32[kMaxElem];
+    double* thermo;
+    int md_tail;
+    long long nsteps;
+    NhcParams nhc;
 };
 
 }  // namespace mappg
@@ -106,8 +143,7 @@ struct mappg_sys {
     mappg::Box box;
     int nb[3] = {1, 1, 1};
     int nbins = 1;
-    float off32[27][4];
-    float off32lo[27][4];
+    mappg::Frame frame;
     double shift[27][3];
     double band = 0.0;  // half-width of the exact-arithmetic band of the list filter
     cudaStream_t stream = nullptr;
@@ -118,6 +154,11 @@ struct mappg_sys {
     int* id = nullptr;   // sorted -> caller index
     int* inv = nullptr;  // caller -> sorted index
     float4* p32 = nullptr;
+    float4* q32 = nullptr;
+    float4* p0 = nullptr;  // p32 at the last build (mixed skin test)
+    float* f32 = nullptr;
+    float* v32 = nullptr;
+    float* rho32 = nullptr;
     int* binc = nullptr;
     int* binid = nullptr;
     int* bin_count = nullptr;
@@ -127,7 +168,6 @@ struct mappg_sys {
     int* nbr = nullptr;
     int* nnbr = nullptr;
     double *rho = nullptr, *dF = nullptr;
-    float* dF32 = nullptr;
     double* partials = nullptr;
     mappg::DevScalars* sc = nullptr;
     double* stage = nullptr;      // device staging, 3n doubles (caller order)
@@ -137,7 +177,7 @@ struct mappg_sys {
     void* run = nullptr;  // an NVT run in progress (md.cu)
     bool built = false;
     bool have_v = false;
-    bool forces_valid = false;
+    bool f_is_f32 = false;  // the newest forces are in f32 (mixed kernels)
     std::vector<int> host_id;  // sorted -> caller (host copy)
 };
 
@@ -150,13 +190,19 @@ void request_rebuild(mappg_sys* s);        // host sets the gate
 void launch_shadow(mappg_sys* s, bool gated);
 void check_build(mappg_sys* s);            // host: overflow / capacity
 void launch_skin_test(mappg_sys* s);       // sets sc->rebuild if needed
+void sync_forces64(mappg_sys* s);          // f (FP64) from f32 when needed
 EamArgs eam_args(mappg_sys* s);
 int grid_for(mappg_sys* s, long long threads, int block);
 
-// eam.cu
+// eam.cu (FP64 kernels; dispatches to eam32.cu in mixed mode)
 void launch_force(mappg_sys* s);           // density+embed, force; totals in sc
 void launch_energy(mappg_sys* s);          // energy only; total in sc->energy
-void launch_density_only(mappg_sys* s);    // k_density alone (timing)
-void launch_force_only(mappg_sys* s);      // k_force alone (timing; needs dF)
+void launch_density_only(mappg_sys* s);    // the density kernel alone (timing)
+void launch_force_only(mappg_sys* s);      // the force kernel alone (timing; needs dF)
+
+// eam32.cu (mixed kernels)
+void launch_density32(mappg_sys* s, const EamArgs& a);
+void launch_force32(mappg_sys* s, const EamArgs& a);
+void launch_energy32(mappg_sys* s, const EamArgs& a);
 
 }  // namespace mappg
