@@ -1,0 +1,154 @@
+"""The CPU oracle against its committed golden fixtures and against physics
+it must satisfy: finite-difference forces, perfect-lattice symmetry,
+Newton's third law, half-list vs full-list agreement, NVE energy
+conservation, the thermostat reaching its temperature, and (when the
+reference tree is present) the published cohesive energy of the Cu setfl
+file shipped with the reference."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden, golden_potential
+from mapp4py_gb300 import synth
+
+STATIC = ["fcc_a_256", "alloy_ab_475", "thin_a_32", "tric_ab_240"]
+
+
+def keys(cnt, ent):
+    atom = np.repeat(np.arange(cnt.shape[0]), cnt)
+    rows = np.column_stack([atom, ent]).astype(np.int64)
+    return rows[np.lexsort(rows.T[::-1])]
+
+
+@pytest.mark.parametrize("name", STATIC)
+def test_oracle_reproduces_golden(potentials, name):
+    g = golden(name)
+    path = golden_potential(potentials, g)
+    e = O.Eam.setfl(path)
+    s = O.System(e, g["H"], g["x"], g["elem"], g["masses"])
+    pe, vir = s.force()
+    assert pe == float(g["pe"]) and np.array_equal(vir, g["virial"])
+    assert np.array_equal(s.f, g["f"])
+    full = O.System(e, g["H"], g["x"], g["elem"], g["masses"], pair_wise=False)
+    full.init_dynamic()
+    assert np.array_equal(keys(*full.neighbors()), g["nbr"])
+
+
+@pytest.mark.parametrize("name", ["alloy_ab_475", "tric_ab_240"])
+def test_full_list_restatement_matches_half_list(potentials, name):
+    g = golden(name)
+    e = O.Eam.setfl(golden_potential(potentials, g))
+    full = O.System(e, g["H"], g["x"], g["elem"], g["masses"], pair_wise=False)
+    pe, vir = full.force_full(nthreads=2)
+    assert abs(pe - g["pe"]) <= 1e-12 * abs(g["pe"])
+    assert np.max(np.abs(vir - g["virial"])) <= 1e-11 * np.max(np.abs(g["virial"]))
+    assert np.max(np.abs(full.f - g["f"])) <= 1e-11 * np.max(np.abs(g["f"]))
+
+
+def test_finite_difference_forces(potentials):
+    """Central differences of the energy (h = 1e-5 A) against the forces:
+    the check MinCGOld::ff_test (min_cg_old.cpp:168-240) makes."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((3, 3, 3), xB=0.5, sigma=0.1, seed=4)
+    e = O.Eam.setfl(path)
+    s = O.System(e, c.H, c.x, c.elem, c.masses)
+    s.force()
+    f = s.f
+    rng = np.random.default_rng(0)
+    h = 1e-5
+    for a in rng.choice(c.natoms, 6, replace=False):
+        for k in range(3):
+            xp = c.x.copy()
+            xp[a, k] += h
+            xm = c.x.copy()
+            xm[a, k] -= h
+            ep = O.System(e, c.H, xp, c.elem, c.masses).energy()
+            em = O.System(e, c.H, xm, c.elem, c.masses).energy()
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - f[a, k]) < 2e-6 * max(1.0, abs(f[a, k])), (a, k, fd, f[a, k])
+
+
+def test_perfect_lattice_symmetry(potentials):
+    path, _ = potentials[("A",)]
+    H, x = synth.fcc((5, 5, 5))
+    e = O.Eam.setfl(path)
+    s = O.System(e, H, x, np.zeros(len(x), np.uint8), [synth.MASS])
+    pe, vir = s.force()
+    assert np.max(np.abs(s.f)) < 1e-12
+    assert abs(vir[1]) + abs(vir[2]) + abs(vir[4]) < 1e-9 * abs(vir[0])
+    assert abs(vir[0] - vir[3]) < 1e-9 * abs(vir[0]) and abs(vir[0] - vir[5]) < 1e-9 * abs(vir[0])
+    # energy per atom from the analytic functions on the FCC shells
+    shells = [(12, 2.5561), (6, 3.615), (24, 4.4275), (12, 5.1124)]
+    a = 3.615
+    shells = [(12, a / np.sqrt(2)), (6, a), (24, a * np.sqrt(1.5)), (12, a * np.sqrt(2)), (24, a * np.sqrt(2.5))]
+    D, r0, pref = synth.ELEMENTS["A"]
+    rho = sum(n * synth.rho_fn(np.array([r]), r0)[0] for n, r in shells)
+    ep = 0.5 * sum(n * synth.phi(np.array([r]), D, r0)[0] for n, r in shells)
+    assert abs(pe / len(x) - (-pref * np.sqrt(rho) + ep)) < 1e-6
+
+
+def test_newton_third_law_and_translation(potentials):
+    g = golden("alloy_ab_475")
+    e = O.Eam.setfl(golden_potential(potentials, g))
+    s = O.System(e, g["H"], g["x"], g["elem"], g["masses"])
+    s.force()
+    assert np.max(np.abs(s.f.sum(axis=0))) < 1e-10
+    t = O.System(e, g["H"], g["x"] + np.array([1.3, -0.4, 2.2]), g["elem"], g["masses"])
+    t.force()
+    assert np.max(np.abs(t.f - s.f)) < 1e-10
+
+
+def test_nve_conservation_and_nhc_temperature(potentials):
+    path, _ = potentials[("A",)]
+    e = O.Eam.setfl(path)
+    c = synth.md_single((4, 4, 4), T=300.0, seed=3)
+    dev = []
+    for dt_fs, n in ((1.0, 200), (0.5, 400)):
+        s = O.System(e, c.H, c.x, c.elem, c.masses)
+        s.v = c.v
+        th, _, _ = s.nvt_run(300.0, dt_fs * synth.FS, synth.KB, n, t_relax=float("inf"))
+        etot = th[:, 0] + 0.5 * (th[:, 2] + th[:, 5] + th[:, 7])
+        dev.append(np.max(np.abs(etot - etot[0])) / c.natoms)
+    # velocity Verlet: the total-energy offset is O(dt^2) and small
+    assert dev[0] < 2e-5 and dev[1] < 0.35 * dev[0]
+    # the chain drives a cold start towards its set temperature
+    s = O.System(e, c.H, c.x, c.elem, c.masses)
+    s.v = 0.2 * c.v
+    th, eta, _ = s.nvt_run(600.0, 2 * synth.FS, synth.KB, 1500, t_relax=20 * synth.FS)
+    assert abs(np.mean(th[-500:, 1]) - 600.0) < 60.0
+    assert np.all(np.isfinite(eta))
+
+
+def test_create_temp_statistics():
+    elem = np.zeros(30000, np.uint8)
+    v = O.create_temp(elem, [63.5], 300.0, synth.KB, 12345)
+    assert abs(np.std(v) - np.sqrt(synth.KB * 300.0 / 63.5)) < 0.01 * np.sqrt(synth.KB * 300.0 / 63.5)
+    with pytest.raises(ValueError):
+        O.create_temp(elem[:4], [63.5], 300.0, synth.KB, 0)
+
+
+def test_lbfgs_reaches_force_tolerance(potentials):
+    g = golden("lbfgs_ab_475")
+    path = golden_potential(potentials, dict(g, elems=np.array(["A", "B"])))
+    s = O.System(O.Eam.setfl(path), g["H"], g["x"], g["elem"], g["masses"])
+    r = s.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert r["err"] == 100 and r["fmax"] < 1e-4
+    assert r["pe"] == float(g["pe"]) and r["niter"] == int(g["niter"])
+
+
+REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_CU), reason="reference tree not present")
+def test_cu_mishin_cohesive_energy():
+    """Mishin et al. (2001) Cu: FCC a0 = 3.615 A, E_coh = -3.54 eV/atom; the
+    setfl file shipped with the reference, read by the oracle."""
+    e = O.Eam.setfl(REF_CU)
+    H, x = synth.fcc((5, 5, 5), a=3.615)
+    s = O.System(e, H, x, np.zeros(len(x), np.uint8), [63.546])
+    pe, vir = s.force()
+    assert abs(pe / len(x) - (-3.54)) < 0.005
+    # a0 is the energy minimum: the pressure (virial) nearly vanishes
+    assert abs(vir[0]) / len(x) < 0.01
