@@ -113,6 +113,28 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, dist=None, device=None):
+    """The largest value of x over all ranks (x itself without a process group)."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def throughput(natoms, steps, world, ms):
+    """Whole-job atom-steps/s: every rank advances its own replica of natoms."""
+    return natoms * steps * world / (ms / 1000.0)
+
+
+def workload_config(natoms, cells, precision, world):
+    return {"workload": "EAM NVT MD, %d-atom A/B alloy (FCC %d^3, seed 1)" % (natoms, cells),
+            "natoms": natoms, "precision": precision, "dt_fs": 1.0, "T_K": T_K,
+            "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None}
+
+
 def make_cell(cells=80):
     from mapp4py_gb300 import synth
 
@@ -163,14 +185,14 @@ def run_reference(args, rank, world):
         o.nvt_run(T_K, synth.FS, synth.KB, args.steps, threads=threads)
         secs = o.loop_seconds
     value = c.natoms * args.steps / secs
-    sample = ("each step: one NVT step of a 256,000-atom (FCC 40^3) block of the 2,048,000-atom alloy; "
+    sample = ("each step: one NVT step of a 256,000-atom (FCC 40^3) block of the %d-atom alloy; "
               "the reference does not build here (MPI and Python<=3.10 C-API), so this is the oracle's "
-              "OpenMP restatement")
+              "OpenMP restatement" % (args.cells ** 3 * 4))
+    config = workload_config(args.cells ** 3 * 4, args.cells, args.precision, world)
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "EAM NVT MD, A/B alloy FCC 40^3 sample of 80^3",
-                                            "natoms": int(c.natoms), "seq_len": None, "global_batch": None},
+            "data": "synthetic", "config": config,
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -217,11 +239,8 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     sysm.nvt_end(K + W)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = N * K * world / (ms / 1000.0)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = throughput(N, K, world, ms)
     st = sysm.stats()
     kbar = st["mean_row_x1000"] / 1000.0
 
@@ -284,11 +303,8 @@ def run_gpu(args, rank, world, local_rank):
         nv.run(at, 1)
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([te], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te = float(t.item())
-    e2e = {"value": N * E * world / te, "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * N,
+    te = max_over_ranks(te, dist, "cuda")
+    e2e = {"value": throughput(N, E, world, 1000.0 * te), "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * N,
            "d2h_bytes_per_step": 72 * N, "steps": E,
            "call": "mapp4py_gb300.md.nvt(600,1fs).run(atoms,1): x,v in; x,v,f out; neighbour build + "
                    "opening force call + one step per call, as MDNVT::run"}
@@ -297,10 +313,8 @@ def run_gpu(args, rank, world, local_rank):
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "data": "synthetic",
-                "config": {"workload": "EAM NVT MD, %d-atom A/B alloy (FCC %d^3, seed 1)" % (N, args.cells),
-                           "natoms": N, "precision": args.precision, "dt_fs": 1.0, "T_K": T_K,
-                           "l2": "inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6),
-                           "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None},
+                "config": dict(workload_config(N, args.cells, args.precision, world),
+                               l2="inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6)),
                 "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * K,
                 "neighbor": {"rebuilds_in_run": st["rebuilds"], "max_row": st["max_row"], "capacity": st["capacity"]}}
         if not args.no_cpu and world == 1:

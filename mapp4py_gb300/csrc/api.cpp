@@ -91,36 +91,43 @@ void upload_tables(mappg_ff* ff) {
     for (size_t k = 0; k < nFt; k++) lo[k] = (float)(t.F[4 * k] - (double)(float)t.F[4 * k]);
     MAPPG_CUDA(cudaMalloc(&d.F32lo, sizeof(float) * nFt));
     MAPPG_CUDA(cudaMemcpy(d.F32lo, lo.data(), sizeof(float) * nFt, cudaMemcpyHostToDevice));
-    // packed force records of the mixed force kernel
+    // force records of the mixed force kernel: one 32-byte sector per
+    // (pair type, knot) holds rho'_{j->i} and r*phi; rho'_{i->j} sits in a
+    // second table that only pairs of unlike elements read (for like
+    // elements the two derivatives are the same function)
     const double dri = 1.0 / t.dr;
-    std::vector<float> rec((size_t)12 * nrt);
+    std::vector<float> rec((size_t)8 * nrt), recj((size_t)4 * nrt);
     for (int ei = 0; ei < ne; ei++)
         for (int ej = 0; ej < ne; ej++)
             for (int m = 0; m < t.nr; m++) {
                 const double* ci = t.rho_at(ej, ei) + 4 * (size_t)m;  // density at i from j
                 const double* cj = t.rho_at(ei, ej) + 4 * (size_t)m;  // density at j from i
                 const double* cz = t.rphi_at(ei, ej) + 4 * (size_t)m;
-                float* r = rec.data() + 12 * ((size_t)(ei * ne + ej) * t.nr + m);
+                const size_t k = (size_t)(ei * ne + ej) * t.nr + m;
+                float* r = rec.data() + 8 * k;
                 r[0] = (float)(ci[1] * dri);
                 r[1] = (float)(2.0 * ci[2] * dri);
                 r[2] = (float)(3.0 * ci[3] * dri);
-                r[3] = (float)(cj[1] * dri);
-                r[4] = (float)(2.0 * cj[2] * dri);
-                r[5] = (float)(3.0 * cj[3] * dri);
-                r[6] = (float)cz[0];
-                r[7] = (float)(cz[0] - (double)r[6]);
-                r[8] = (float)cz[1];
-                r[9] = (float)cz[2];
-                r[10] = (float)cz[3];
-                r[11] = 0.f;
+                r[3] = (float)cz[0];
+                r[4] = (float)cz[1];
+                r[5] = (float)cz[2];
+                r[6] = (float)cz[3];
+                r[7] = (float)(cz[0] - (double)r[3]);
+                float* q = recj.data() + 4 * k;
+                q[0] = (float)(cj[1] * dri);
+                q[1] = (float)(2.0 * cj[2] * dri);
+                q[2] = (float)(3.0 * cj[3] * dri);
+                q[3] = 0.f;
             }
     MAPPG_CUDA(cudaMalloc(&d.ftab, sizeof(float) * rec.size()));
     MAPPG_CUDA(cudaMemcpy(d.ftab, rec.data(), sizeof(float) * rec.size(), cudaMemcpyHostToDevice));
+    MAPPG_CUDA(cudaMalloc(&d.fjtab, sizeof(float) * recj.size()));
+    MAPPG_CUDA(cudaMemcpy(d.fjtab, recj.data(), sizeof(float) * recj.size(), cudaMemcpyHostToDevice));
 }
 
 void free_tables(mappg_ff* ff) {
     DevTables& d = ff->dev;
-    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.ftab, d.F32, d.F32lo};
+    void* p[] = {d.rho64, d.rphi64, d.F64, d.rho32, d.ftab, d.fjtab, d.F32, d.F32lo};
     for (void* q : p)
         if (q) cudaFree(q);
 }

@@ -28,12 +28,6 @@
 
 namespace mappg {
 
-__device__ __forceinline__ Dbl4 ldg4(const Dbl4* p) {
-    const double2* q = reinterpret_cast<const double2*>(p);
-    double2 a = __ldg(q), b = __ldg(q + 1);
-    return Dbl4{a.x, a.y, b.x, b.y};
-}
-
 __device__ __forceinline__ double spl_val(const Dbl4& c, double p) { return ((c.w * p + c.z) * p + c.y) * p + c.x; }
 __device__ __forceinline__ double spl_der(const Dbl4& c, double p) { return (3.0 * c.w * p + 2.0 * c.z) * p + c.y; }
 

@@ -55,8 +55,12 @@ __device__ __forceinline__ void cart(const Frame& fr, float a, float b, float c,
 
 // 1/r from the hardware reciprocal square root and one Newton step
 __device__ __forceinline__ float inv_sqrt(float x) {
-    float y = rsqrtf(x);
-    return y * fmaf(-0.5f * x * y, y, 1.5f);
+    // one Newton step written as y + y * (1/2 - x y^2 / 2): the correction is
+    // small and added with a single rounding, so the result carries no
+    // systematic bias (the form y * (3/2 - x y^2 / 2) rounds a factor next to
+    // 1.0, where the spacing of floats changes, and comes out low by ~1e-8)
+    const float y = rsqrtf(x);
+    return fmaf(y, fmaf(-0.5f * x * y, y, 0.5f), y);
 }
 
 // knot index and fraction: m = min(floor(p), nmax), p - m clamped to 1
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
 }
 
 template <int TPA, bool ORTHO, bool TAIL>
-__global__ void __launch_bounds__(256) k_force32(EamArgs a) {
+__global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -183,7 +187,13 @@ __global__ void __launch_bounds__(256) k_force32(EamArgs a) {
     const int stride = (gridDim.x * blockDim.x) / TPA;
     float es = 0.f, ec = 0.f;  // pair energy, compensated
     float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
-    float k0 = 0.f, k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f, k5 = 0.f;  // kinetic tensor (TAIL)
+    // kinetic tensor (TAIL): one private shared-memory slot per thread keeps
+    // these six sums out of registers, so the MD variant runs at the same
+    // occupancy as the plain one
+    __shared__ float ke[TAIL ? 6 : 1][256];
+    if (TAIL)
+#pragma unroll
+        for (int c = 0; c < 6; c++) ke[c][threadIdx.x] = 0.f;
     for (int base = 0;; base += stride) {
         const int i = gid + base;
         const bool active = i < a.n;
@@ -209,13 +219,18 @@ __global__ void __launch_bounds__(256) k_force32(EamArgs a) {
                     const float r = rsq * rinv;
                     float fr;
                     const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                    const float4* rec = a.ftab + 3 * ((size_t)t * a.nr + m);
-                    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+                    const size_t kt = (size_t)t * a.nr + m;
+                    float4 r0, r1;
+                    ldg8(a.ftab + 2 * kt, r0, r1);
                     const float der_i = fmaf(fmaf(r0.z, fr, r0.y), fr, r0.x);
-                    const float der_j = fmaf(fmaf(r1.y, fr, r1.x), fr, r0.w);
-                    const float zpoly = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
-                    const float z = r1.z + fmaf(fr, zpoly, r1.w);
-                    const float zp = fmaf(fmaf(3.0f * r2.z, fr, 2.0f * r2.y), fr, r2.x) * K.dri;
+                    float der_j = der_i;
+                    if (entry_elem(e) != ei) {
+                        const float4 r2 = __ldg(a.fjtab + kt);
+                        der_j = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
+                    }
+                    const float zpoly = fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x);
+                    const float z = r0.w + fmaf(fr, zpoly, r1.w);
+                    const float zp = fmaf(fmaf(3.0f * r1.z, fr, 2.0f * r1.y), fr, r1.x) * K.dri;
                     const float phi = z * rinv;
                     const float dphi = (zp - phi) * rinv;
                     const float fp = -fmaf(dFi, der_i, fmaf(q.w, der_j, dphi)) * rinv;
@@ -251,21 +266,32 @@ __global__ void __launch_bounds__(256) k_force32(EamArgs a) {
                 const float vy = fmaf(fy, dtm, __ldg(a.v32 + a.n + i));
                 const float vz = fmaf(fz, dtm, __ldg(a.v32 + 2 * a.n + i));
                 const float mx = m * vx, my = m * vy, mz = m * vz;
-                k0 = fmaf(mx, vx, k0);
-                k1 = fmaf(mx, vy, k1);
-                k2 = fmaf(mx, vz, k2);
-                k3 = fmaf(my, vy, k3);
-                k4 = fmaf(my, vz, k4);
-                k5 = fmaf(mz, vz, k5);
+                float* k = &ke[0][threadIdx.x];
+                k[0] = fmaf(mx, vx, k[0]);
+                k[256] = fmaf(mx, vy, k[256]);
+                k[512] = fmaf(mx, vz, k[512]);
+                k[768] = fmaf(my, vy, k[768]);
+                k[1024] = fmaf(my, vz, k[1024]);
+                k[1280] = fmaf(mz, vz, k[1280]);
             }
         }
     }
-    double v[13] = {0.5 * ((double)es - (double)ec), 0.5 * (double)w0, 0.5 * (double)w1, 0.5 * (double)w2,
-                    0.5 * (double)w3, 0.5 * (double)w4, 0.5 * (double)w5, (double)k0, (double)k1, (double)k2,
-                    (double)k3, (double)k4, (double)k5};
-    if (block_partials<13>(v, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
-        double tot[13];
-        final_sums<13>(a.partials, gridDim.x, tot);
+    constexpr int NS = TAIL ? 13 : 7;  // energy, virial[6], kinetic tensor[6]
+    auto sum_k = [&](int k) -> double {
+        switch (k) {
+            case 0: return 0.5 * ((double)es - (double)ec);
+            case 1: return 0.5 * (double)w0;
+            case 2: return 0.5 * (double)w1;
+            case 3: return 0.5 * (double)w2;
+            case 4: return 0.5 * (double)w3;
+            case 5: return 0.5 * (double)w4;
+            case 6: return 0.5 * (double)w5;
+            default: return (double)ke[TAIL ? k - 7 : 0][threadIdx.x];
+        }
+    };
+    __shared__ double tot[NS];
+    if (block_partials_fn<NS>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
+        final_sums_smem<NS>(a.partials, gridDim.x, tot);
         if (threadIdx.x == 0) {
             DevScalars* sc = a.sc;
             sc->energy = tot[0] + sc->e_embed;
@@ -322,9 +348,10 @@ __global__ void __launch_bounds__(256) k_energy32(EamArgs a) {
                     const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
                     const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
                     acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
-                    const float4* rec = a.ftab + 3 * ((size_t)t * a.nr + m);
-                    const float4 r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
-                    const float z = r1.z + fmaf(fr, fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x), r1.w);
+                    const float4* rec = a.ftab + 2 * ((size_t)t * a.nr + m);
+                    float4 r0, r1;
+                    ldg8(rec, r0, r1);
+                    const float z = r0.w + fmaf(fr, fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x), r1.w);
                     ep += 0.5f * z * rinv;
                 }
             }

@@ -65,9 +65,10 @@ struct DevTables {
     Dbl4* rphi64 = nullptr;  // [ne*ne][nr]
     Dbl4* F64 = nullptr;     // [ne][nrho]
     float4* rho32 = nullptr;    // rho value coefficients, [ne*ne][nr]
-    float4* ftab = nullptr;     // force records, 3 float4 per (ei*ne+ej, knot):
-                                // (d1i,d2i,d3i,d1j) (d2j,d3j,z0,z0lo) (z1,z2,z3,0)
-                                // d = (c1, 2c2, 3c3)/dr of rho_{j->i} and rho_{i->j}
+    float4* ftab = nullptr;     // force records, 2 float4 per (ei*ne+ej, knot):
+                                // (d1i,d2i,d3i,z0) (z1,z2,z3,z0lo)
+    float4* fjtab = nullptr;    // (d1j,d2j,d3j,0) per (ei*ne+ej, knot)
+                                // d = (c1, 2c2, 3c3)/dr of rho_{j->i} / rho_{i->j}
     float4* F32 = nullptr;      // embedding coefficients, [ne][nrho]
     float* F32lo = nullptr;     // c0 - (float)c0 of the embedding table
 };

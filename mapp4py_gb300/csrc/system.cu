@@ -531,6 +531,7 @@ EamArgs eam_args(mappg_sys* s) {
     a.F64 = ff->dev.F64;
     a.rho32 = ff->dev.rho32;
     a.ftab = ff->dev.ftab;
+    a.fjtab = ff->dev.fjtab;
     a.F32 = ff->dev.F32;
     a.F32lo = ff->dev.F32lo;
     a.dr_inv = ff->dev.dr_inv;

@@ -100,7 +100,8 @@ struct EamArgs {
     const Dbl4* rphi64;
     const Dbl4* F64;
     const float4* rho32;
-    const float4* ftab;     // mixed force records, 3 float4 per (pair type, knot)
+    const float4* ftab;     // mixed force records, 2 float4 per (pair type, knot)
+    const float4* fjtab;    // rho_{i->j} derivative per (pair type, knot)
     const float4* F32;
     const float* F32lo;
     double dr_inv, drho_inv, rho_max;
