@@ -127,6 +127,23 @@ int mappg_sys_force(mappg_sys* sys, double* pe, double* virial6);
  * ForceFieldEAM::__energy_calc, ff_eam.cpp:244-318). */
 int mappg_sys_energy(mappg_sys* sys, double* pe);
 
+/* Forces, energy and virial of an FP64 system, computed without allocating
+ * any device memory: for callers whose memory pool owns the device, or that
+ * must not let a library call cudaMalloc/cudaFree (which synchronise the
+ * device) once they are running.  No counterpart in the reference.
+ * f_dev: 3*natoms doubles of device memory, written as x, y, z per atom in
+ * the caller's order; ev_dev: NULL or 7 doubles of device memory, written as
+ * [pe, virial xx, xy, xz, yy, yz, zz].  The work is queued on the system's
+ * stream and the call returns without waiting (mappg_sys_sync waits).
+ * The system must be FP64, hold a neighbour list (mappg_sys_build or
+ * mappg_sys_update) and have at most 262144 atoms; other calls are refused
+ * with MAPPG_ERR_ARG.  Intermediate arrays live in one fixed device array of
+ * about 11 MB (10.5 MiB) that every GPU using this call holds until the process
+ * exits; the first call on each device looks up that array's address and
+ * loads the kernels, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised. */
+int mappg_sys_force_noalloc(mappg_sys* sys, double* f_dev, double* ev_dev);
+
 /* Per-atom host density rho and F'(rho) from the last force call. */
 int mappg_sys_get_rho(mappg_sys* sys, double* rho, double* dF);
 

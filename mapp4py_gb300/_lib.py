@@ -45,6 +45,7 @@ SIGNATURES = {
     "mappg_sys_build": (C.c_int, [_VP]),
     "mappg_sys_update": (C.c_int, [_VP, _I]),
     "mappg_sys_force": (C.c_int, [_VP, _D, _D]),
+    "mappg_sys_force_noalloc": (C.c_int, [_VP, _VP, _VP]),
     "mappg_sys_energy": (C.c_int, [_VP, _D]),
     "mappg_sys_get_rho": (C.c_int, [_VP, _D, _D]),
     "mappg_sys_neighbors": (C.c_int, [_VP, _I, _I, _LL]),

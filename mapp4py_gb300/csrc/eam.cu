@@ -319,6 +319,29 @@ void launch_force(mappg_sys* s) {
     launch_force_only(s);
 }
 
+// FP64 density and force passes whose outputs, partial sums and device
+// scalars are the ones in `a` (mappg_sys_force_noalloc points them at its
+// scratch); launches only, no allocation
+void launch_force64_args(mappg_sys* s, const EamArgs& a) {
+    MAPPG_TPA64(k_density64)
+    MAPPG_TPA64(k_force64)
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+// loads every instantiation launch_force64_args can pick onto the current
+// device, so that later launches do no module loading of their own
+void preload_force64() {
+    cudaFuncAttributes fa;
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_density64<4>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_density64<8>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_density64<16>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_density64<32>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<4>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<8>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<16>));
+    MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<32>));
+}
+
 void launch_energy(mappg_sys* s) {
     EamArgs a = eam_args(s);
     if (s->precision == MAPPG_MIXED) {
