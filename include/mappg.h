@@ -192,6 +192,13 @@ int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
 int mappg_sys_stream(mappg_sys* sys, void** stream);
 int mappg_sys_sync(mappg_sys* sys);
 
+/* Choose the lanes per atom (4, 8 or 16; 256/lanes atoms per block) of the
+ * density and force kernels by timing them on this system's atoms and
+ * neighbour list; the choice is kept for the system.  tpa (may be NULL)
+ * receives it, ms (3 doubles, may be NULL) the density+force time of each
+ * candidate.  No counterpart in the reference. */
+int mappg_sys_autotune(mappg_sys* sys, int* tpa, double* ms);
+
 /* Enqueue one kernel launch on the system's stream without waiting, for
  * timing: 0 density + embedding, 1 force/virial (uses the last F'(rho)),
  * 2 energy only, 3 neighbour rebuild. */
@@ -205,6 +212,99 @@ int mappg_sys_enqueue(mappg_sys* sys, int what);
  * iterations) plus 100 = force tolerance. */
 int mappg_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f_tol, double c,
                     double rho, double min_alpha, int nsteps, double* stats);
+
+/* ------------------------------------------------------- batches of cells */
+
+/* Several independent periodic cells (ncell >= 2) in one system, for runs
+ * over many small cells: every kernel of a step covers all cells at once.
+ * The reference runs one cell per process (its drivers take one Atoms); a
+ * batch is the same per-cell computation as mappg_sys_create's, cell by
+ * cell.  natoms[c] atoms per cell, H is ncell boxes of 9 doubles, x and
+ * elem hold the cells' atoms one cell after the other.  Mixed precision
+ * only.  The per-atom calls (set/get x, v, f, build, update, neighbours)
+ * work on the concatenated atoms; energies and MD state are per cell. */
+int mappg_batch_create(const mappg_ff* ff, int ncell, const int* natoms, const double* H, const double* x,
+                       const unsigned char* elem, const double* masses, double skin, int precision,
+                       mappg_sys** out);
+int mappg_batch_ncell(const mappg_sys* sys);
+
+/* Per-cell energy (pe[ncell]) and virial (virial[ncell][6], may be NULL)
+ * after a force pass over all cells; forces via mappg_sys_get_f. */
+int mappg_batch_force(mappg_sys* sys, double* pe, double* virial);
+int mappg_batch_energy(mappg_sys* sys, double* pe);
+
+/* md.nvt run of every cell at its own temperature T[c] (MDNVT::run,
+ * md_nvt.cpp:383-480, one chain per cell), one CUDA graph per step over all
+ * cells.  eta: ncell x L doubles in/out (may be NULL); thermo: NULL or
+ * (nsteps+1) x ncell x 2 doubles (pe, T per cell per step).  begin/end as
+ * mappg_nvt_begin/end; mappg_nvt_steps enqueues steps of either. */
+int mappg_batch_nvt_begin(mappg_sys* sys, const double* T, double dt, double kB, double t_relax, int L, int niters,
+                          long long nsteps, const double* eta, int record_thermo);
+int mappg_batch_nvt_end(mappg_sys* sys, double* eta, double* thermo);
+int mappg_batch_nvt_run(mappg_sys* sys, const double* T, double dt, double kB, double t_relax, int L, int niters,
+                        int nsteps, double* eta, double* thermo);
+
+/* ------------------------------------------- learned L-BFGS preconditioner */
+
+/* A small network predicts each atom's three diagonal Hessian elements from
+ * 33 local features; their inverses replace the scalar initial inverse
+ * Hessian of the L-BFGS two-loop recursion.  No counterpart in the
+ * reference (MinLBFGS uses gamma*I, min_l-bfgs.h:148-170).
+ * Network: 33 -> 64 -> 64 -> 3, tanh hidden units, softplus outputs, BF16
+ * tensor-core forward/backward with FP32 accumulation, AdamW on FP32
+ * master weights.  Parameters: W1 [64][64] | W2 [64][80] | W3 [16][80]
+ * row-major [unit][input] (input 33 of W1 and input 64 of W2/W3 are the
+ * biases); norm: 33 feature means then 33 standard deviations. */
+typedef struct mappg_mlp mappg_mlp;
+int mappg_mlp_nparams(void);
+int mappg_mlp_create(int seed, mappg_mlp** out);
+void mappg_mlp_destroy(mappg_mlp* net);
+/* training rows: feat [n][33], target [n][3] (Hessian diagonals, eV/A^2);
+ * sets the feature standardisation from these rows and shuffles them */
+int mappg_mlp_set_data(mappg_mlp* net, const float* feat, const float* target, int n, int seed);
+/* minibatch AdamW; losses[epochs] (may be NULL) = mean squared log error */
+int mappg_mlp_train(mappg_mlp* net, int epochs, int batch, double lr, double wd, double* losses);
+/* loss and gradient over the given rows (grad: nparams floats) */
+int mappg_mlp_grad(mappg_mlp* net, const float* feat, const float* target, int n, float* grad, double* loss);
+int mappg_mlp_predict(mappg_mlp* net, const float* feat, int n, float* out);
+int mappg_mlp_get_params(mappg_mlp* net, float* w, float* norm);
+int mappg_mlp_set_params(mappg_mlp* net, const float* w, const float* norm);
+
+/* Features of a system's atoms, [natoms][33] in caller order: 16 Gaussian
+ * radial functions (centres 2.0..5.5 A, width 0.3 A, cosine cutoff 5.5 A)
+ * per neighbour species (A, B), then the host density rho_i. */
+int mappg_sys_descriptors(mappg_sys* sys, float* feat);
+
+/* Diagonal Hessian elements [natoms][3] by central differences of the
+ * forces with step h; atoms of one colour (color[natoms], caller order)
+ * move together, so same-coloured atoms must be further apart than twice
+ * the cutoff.  FP64 systems. */
+int mappg_sys_hessian_diag(mappg_sys* sys, const int* color, double h, double* out);
+
+/* mappg_lbfgs_run with H0 = diag(1/y), y the network's prediction for the
+ * starting configuration; a non-descent direction falls back to plain
+ * L-BFGS (gamma*I) for that iteration.  stats: 7 doubles, the six of
+ * mappg_lbfgs_run then the number of fallbacks. */
+int mappg_lbfgs_run_precond(mappg_sys* sys, mappg_mlp* net, int m, double e_tol, double max_dx, double f_tol,
+                            double c, double rho, double min_alpha, int nsteps, double* stats);
+
+/* L-BFGS over a batch of cells: every cell runs mappg_lbfgs_run's
+ * iteration with its own history, line search and stopping state; the
+ * kernels of each phase cover all cells.  m in 1..32.  stats: ncell x 7
+ * doubles (iterations, pe, max|F|, stop code, energy calls, force calls,
+ * learned-direction fallbacks). */
+int mappg_batch_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f_tol, double c, double rho,
+                          double min_alpha, int nsteps, double* stats);
+int mappg_batch_lbfgs_run_precond(mappg_sys* sys, mappg_mlp* net, int m, double e_tol, double max_dx,
+                                  double f_tol, double c, double rho, double min_alpha, int nsteps, double* stats);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* D[128][64] = A[128][64] * Bt[64][64]^T through the tensor-core path the
+ * learned preconditioner uses (tcgen05 MMA, BF16 operands as raw 16-bit
+ * patterns, FP32 result), for checking it against plain arithmetic.  No
+ * counterpart in the reference. */
+int mappg_tc_gemm_check(const unsigned short* A, const unsigned short* Bt, float* D);
 
 #ifdef __cplusplus
 }

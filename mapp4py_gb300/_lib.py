@@ -15,6 +15,7 @@ FP64 = 0
 MIXED = 1
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int)
 _U8 = C.POINTER(C.c_ubyte)
 _LL = C.POINTER(C.c_longlong)
@@ -62,6 +63,34 @@ SIGNATURES = {
     "mappg_sys_enqueue": (C.c_int, [_VP, C.c_int]),
     "mappg_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_int, _D]),
+    "mappg_sys_autotune": (C.c_int, [_VP, _I, _D]),
+    "mappg_batch_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, _D]),
+    "mappg_batch_lbfgs_run_precond": (C.c_int, [_VP, _VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                C.c_double, C.c_double, C.c_int, _D]),
+    "mappg_tc_gemm_check": (C.c_int, [_VP, _VP, _VP]),
+    "mappg_mlp_nparams": (C.c_int, []),
+    "mappg_mlp_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "mappg_mlp_destroy": (None, [_VP]),
+    "mappg_mlp_set_data": (C.c_int, [_VP, _F, _F, C.c_int, C.c_int]),
+    "mappg_mlp_train": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_double, _D]),
+    "mappg_mlp_grad": (C.c_int, [_VP, _F, _F, C.c_int, _F, _D]),
+    "mappg_mlp_predict": (C.c_int, [_VP, _F, C.c_int, _F]),
+    "mappg_mlp_get_params": (C.c_int, [_VP, _F, _F]),
+    "mappg_mlp_set_params": (C.c_int, [_VP, _F, _F]),
+    "mappg_sys_descriptors": (C.c_int, [_VP, _F]),
+    "mappg_sys_hessian_diag": (C.c_int, [_VP, _I, C.c_double, _D]),
+    "mappg_lbfgs_run_precond": (C.c_int, [_VP, _VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_int, _D]),
+    "mappg_batch_create": (C.c_int, [_VP, C.c_int, _I, _D, _D, _U8, _D, C.c_double, C.c_int, C.POINTER(_VP)]),
+    "mappg_batch_ncell": (C.c_int, [_VP]),
+    "mappg_batch_force": (C.c_int, [_VP, _D, _D]),
+    "mappg_batch_energy": (C.c_int, [_VP, _D]),
+    "mappg_batch_nvt_begin": (C.c_int, [_VP, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                        C.c_longlong, _D, C.c_int]),
+    "mappg_batch_nvt_end": (C.c_int, [_VP, _D, _D]),
+    "mappg_batch_nvt_run": (C.c_int, [_VP, _D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                      _D, _D]),
 }
 
 _lib = None
@@ -297,6 +326,12 @@ class System:
     def sync(self):
         check(load().mappg_sys_sync(self.h))
 
+    def autotune(self):
+        tpa = C.c_int()
+        ms = np.zeros(3)
+        check(load().mappg_sys_autotune(self.h, C.byref(tpa), dptr(ms)))
+        return tpa.value, dict(zip((4, 8, 16), ms))
+
     def enqueue(self, what):
         check(load().mappg_sys_enqueue(self.h, int(what)))
 
@@ -306,6 +341,169 @@ class System:
                                      float(rho), float(min_alpha), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+
+class Batch(System):
+    """Independent periodic cells in one device system (one mappg_sys handle
+    made by mappg_batch_create); per-atom arrays are the cells' atoms one cell
+    after the other, energies and MD state are per cell."""
+
+    def __init__(self, ff, cells, masses, skin=0.5, precision=MIXED):
+        """cells: sequence of (H, x, elem)."""
+        self.ff = ff
+        Hs = np.ascontiguousarray(np.stack([f64(c[0], (3, 3)) for c in cells]))
+        xs = [f64(c[1], (-1, 3)) for c in cells]
+        self.natoms = np.array([x.shape[0] for x in xs], dtype=np.int32)
+        x = np.ascontiguousarray(np.concatenate(xs))
+        self.elem = np.ascontiguousarray(np.concatenate([np.asarray(c[2], dtype=np.uint8) for c in cells]))
+        self.n = x.shape[0]
+        self.ncell = len(cells)
+        self.offsets = np.concatenate([[0], np.cumsum(self.natoms)])
+        masses = f64(masses)
+        out = _VP()
+        check(load().mappg_batch_create(ff.h, self.ncell, self.natoms.ctypes.data_as(_I), dptr(Hs), dptr(x),
+                                        self.elem.ctypes.data_as(_U8), dptr(masses), float(skin), int(precision),
+                                        C.byref(out)))
+        self.h = out
+        self.precision = precision
+
+    def split(self, a):
+        """Per-cell views of a concatenated per-atom array."""
+        return [a[self.offsets[c]:self.offsets[c + 1]] for c in range(self.ncell)]
+
+    def force(self):
+        pe = np.zeros(self.ncell)
+        vir = np.zeros((self.ncell, 6))
+        check(load().mappg_batch_force(self.h, dptr(pe), dptr(vir)))
+        return pe, vir
+
+    def energy(self):
+        pe = np.zeros(self.ncell)
+        check(load().mappg_batch_energy(self.h, dptr(pe)))
+        return pe
+
+    def nvt_run(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False):
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        Tc = f64(np.broadcast_to(np.asarray(T, dtype=np.float64), (self.ncell,)).copy())
+        eta_a = np.zeros((self.ncell, max(L, 1))) if eta is None else f64(eta).copy()
+        th = np.zeros((nsteps + 1, self.ncell, 2)) if thermo else None
+        check(load().mappg_batch_nvt_run(self.h, dptr(Tc), float(dt), float(kB), float(t_relax), int(L),
+                                         int(niters), int(nsteps), dptr(eta_a), dptr(th) if th is not None else None))
+        return th, eta_a
+
+    def nvt_begin(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False):
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        Tc = f64(np.broadcast_to(np.asarray(T, dtype=np.float64), (self.ncell,)).copy())
+        eta_a = np.zeros((self.ncell, max(L, 1))) if eta is None else f64(eta).copy()
+        self._run = (L, nsteps, thermo)
+        check(load().mappg_batch_nvt_begin(self.h, dptr(Tc), float(dt), float(kB), float(t_relax), int(L),
+                                           int(niters), int(nsteps), dptr(eta_a), 1 if thermo else 0))
+
+    def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000,
+                  net=None):
+        st = np.zeros((self.ncell, 7))
+        args = (int(m), float(e_tol), float(max_dx), float(f_tol), float(c), float(rho), float(min_alpha),
+                int(nsteps), dptr(st))
+        if net is None:
+            check(load().mappg_batch_lbfgs_run(self.h, *args))
+        else:
+            check(load().mappg_batch_lbfgs_run_precond(self.h, net.h, *args))
+        keys = ("niter", "pe", "fmax", "err", "n_energy", "n_force", "fallbacks")
+        return [{k: (st[c][i] if k in ("pe", "fmax") else int(st[c][i])) for i, k in enumerate(keys)}
+                for c in range(self.ncell)]
+
+    def nvt_end(self, steps_done=None):
+        L, nsteps, thermo = self._run
+        n = nsteps if steps_done is None else steps_done
+        eta = np.zeros((self.ncell, max(L, 1)))
+        th = np.zeros((n + 1, self.ncell, 2)) if thermo else None
+        check(load().mappg_batch_nvt_end(self.h, dptr(eta), dptr(th) if th is not None else None))
+        return th, eta
+
+
+def fptr(a):
+    return a.ctypes.data_as(_F)
+
+
+def f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(shape) if shape is not None else a
+
+
+class Mlp:
+    """The learned L-BFGS preconditioner network (one mappg_mlp handle)."""
+
+    def __init__(self, seed=0):
+        out = _VP()
+        check(load().mappg_mlp_create(int(seed), C.byref(out)))
+        self.h = out
+        self.nparams = load().mappg_mlp_nparams()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.mappg_mlp_destroy(self.h)
+            self.h = None
+
+    def set_data(self, feat, target, seed=0):
+        feat = f32(feat, (-1, 33))
+        target = f32(target, (-1, 3))
+        check(load().mappg_mlp_set_data(self.h, fptr(feat), fptr(target), feat.shape[0], int(seed)))
+
+    def train(self, epochs, batch=4096, lr=2e-3, wd=1e-4):
+        losses = np.zeros(max(epochs, 1))
+        check(load().mappg_mlp_train(self.h, int(epochs), int(batch), float(lr), float(wd), dptr(losses)))
+        return losses[:epochs]
+
+    def grad(self, feat, target):
+        feat = f32(feat, (-1, 33))
+        target = f32(target, (-1, 3))
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = C.c_double()
+        check(load().mappg_mlp_grad(self.h, fptr(feat), fptr(target), feat.shape[0], fptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def predict(self, feat):
+        feat = f32(feat, (-1, 33))
+        out = np.zeros((feat.shape[0], 3), dtype=np.float32)
+        check(load().mappg_mlp_predict(self.h, fptr(feat), feat.shape[0], fptr(out)))
+        return out
+
+    def params(self):
+        w = np.zeros(self.nparams, dtype=np.float32)
+        norm = np.zeros(66, dtype=np.float32)
+        check(load().mappg_mlp_get_params(self.h, fptr(w), fptr(norm)))
+        return w, norm[:33].copy(), norm[33:].copy()
+
+    def set_params(self, w=None, mean=None, sdev=None):
+        wp = fptr(f32(w)) if w is not None else None
+        norm = None
+        if mean is not None:
+            norm = f32(np.concatenate([mean, sdev]))
+        check(load().mappg_mlp_set_params(self.h, wp, fptr(norm) if norm is not None else None))
+
+
+def descriptors(system):
+    out = np.zeros((system.n, 33), dtype=np.float32)
+    check(load().mappg_sys_descriptors(system.h, fptr(out)))
+    return out
+
+
+def hessian_diag(system, color, h=1e-4):
+    color = np.ascontiguousarray(color, dtype=np.int32)
+    out = np.zeros((system.n, 3))
+    check(load().mappg_sys_hessian_diag(system.h, color.ctypes.data_as(_I), float(h), dptr(out)))
+    return out
+
+
+def lbfgs_run_precond(system, net, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0,
+                      nsteps=100000):
+    st = np.zeros(7)
+    check(load().mappg_lbfgs_run_precond(system.h, net.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
+                                         float(rho), float(min_alpha), int(nsteps), dptr(st)))
+    return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]), "n_energy": int(st[4]),
+            "n_force": int(st[5]), "fallbacks": int(st[6])}
 
 
 def create_temp(elem, masses, T, kB, seed):

@@ -25,15 +25,19 @@ void sys_download(mappg_sys* s, const double* dev, double* host);
 void sys_build(mappg_sys* s);
 void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total);
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
-             double* thermo);
+             double* thermo, const double* Tcell);
 void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
-               double min_alpha, int nsteps, double* stats);
+               double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback);
 void lb_update(mappg_sys* s);
 void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
-               const double* eta, bool thermo);
+               const double* eta, bool thermo, const double* Tcell);
 void nvt_steps(mappg_sys* s, long long nsteps);
 void nvt_end(mappg_sys* s, double* eta, double* thermo);
 void nvt_free(mappg_sys* s);
+void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
+                     double min_alpha, int nsteps, const double* P, double* stats);
+void launch_density_only(mappg_sys* s);
+void launch_force_only(mappg_sys* s);
 
 template <class F>
 static int guard(F&& f) {
@@ -389,6 +393,7 @@ int mappg_sys_get_f(mappg_sys* s, double* f) {
 int mappg_sys_set_box(mappg_sys* s, const double* H) {
     return guard([&] {
         if (!s || !H) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "the boxes of a batch are fixed at creation"};
         int nb_old = s->nbins;
         sys_set_box(s, H);
         if (s->nbins != nb_old) sys_alloc_bins(s);
@@ -425,6 +430,7 @@ int mappg_sys_update(mappg_sys* s, int* rebuilt) {
 int mappg_sys_force(mappg_sys* s, double* pe, double* virial6) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells reports per cell: mappg_batch_force"};
         if (!s->built) sys_build(s);
         launch_force(s);
         DevScalars h;
@@ -440,6 +446,7 @@ int mappg_sys_force(mappg_sys* s, double* pe, double* virial6) {
 int mappg_sys_energy(mappg_sys* s, double* pe) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells reports per cell: mappg_batch_energy"};
         if (!s->built) sys_build(s);
         launch_energy(s);
         double e;
@@ -499,6 +506,53 @@ int mappg_sys_stats(mappg_sys* s, long long* out6) {
     });
 }
 
+// atoms-per-block / lanes-per-atom choice: the density and force passes on
+// the system's own atoms and neighbour list, timed with CUDA events for
+// each lane count; the fastest is kept for the system's later launches
+int mappg_sys_autotune(mappg_sys* s, int* tpa_out, double* ms_out) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->run) throw Error{MAPPG_ERR_ARG, "an NVT run is in progress"};
+        if (!s->built) sys_build(s);
+        const int cand[3] = {4, 8, 16};
+        cudaEvent_t e0, e1;
+        MAPPG_CUDA(cudaEventCreate(&e0));
+        MAPPG_CUDA(cudaEventCreate(&e1));
+        double best = 1e30;
+        int best_tpa = s->tpa;
+        try {
+            for (int c = 0; c < 3; c++) {
+                s->tpa = cand[c];
+                launch_density_only(s);  // warm-up (and first-use set-up)
+                launch_force_only(s);
+                MAPPG_CUDA(cudaEventRecord(e0, s->stream));
+                for (int r = 0; r < 3; r++) {
+                    launch_density_only(s);
+                    launch_force_only(s);
+                }
+                MAPPG_CUDA(cudaEventRecord(e1, s->stream));
+                MAPPG_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms_out) ms_out[c] = ms / 3.0;
+                if (ms < best) {
+                    best = ms;
+                    best_tpa = cand[c];
+                }
+            }
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            s->tpa = best_tpa;
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        s->tpa = best_tpa;
+        if (tpa_out) *tpa_out = best_tpa;
+    });
+}
+
 int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
                       double* v) {
     return guard([&] {
@@ -544,7 +598,8 @@ int mappg_nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, 
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
-        nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo);
+        if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells runs with mappg_batch_nvt_run"};
+        nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, nullptr);
     });
 }
 
@@ -552,7 +607,8 @@ int mappg_nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax
                     long long nsteps, const double* eta, int record_thermo) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
-        nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, record_thermo != 0);
+        if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells runs with mappg_batch_nvt_begin"};
+        nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, record_thermo != 0, nullptr);
     });
 }
 
@@ -568,6 +624,144 @@ int mappg_nvt_end(mappg_sys* s, double* eta, double* thermo) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         nvt_end(s, eta, thermo);
+    });
+}
+
+// ------------------------------------------------------------------ batches of cells
+int mappg_batch_create(const mappg_ff* ff, int ncell, const int* natoms, const double* H, const double* x,
+                       const unsigned char* elem, const double* masses, double skin, int precision, mappg_sys** out) {
+    return guard([&] {
+        if (!ff || !natoms || !H || !x || !elem || !masses || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (ncell < 2 || ncell > kMaxCells)
+            throw Error{MAPPG_ERR_ARG, "a batch holds 2.." + std::to_string(kMaxCells) + " cells"};
+        if (precision != MAPPG_MIXED) throw Error{MAPPG_ERR_UNSUPP, "batches run in mixed precision"};
+        if (!(skin >= 0.0)) throw Error{MAPPG_ERR_ARG, "skin must be >= 0"};
+        long long total = 0;
+        for (int c = 0; c < ncell; c++) {
+            if (natoms[c] < 1) throw Error{MAPPG_ERR_ARG, "every cell needs at least one atom"};
+            total += natoms[c];
+        }
+        if (total > kMaxAtoms) throw Error{MAPPG_ERR_ARG, "too many atoms in the batch"};
+        const int n = (int)total;
+        const int ne = ff->host.nelem;
+        for (int i = 0; i < n; i++)
+            if (elem[i] >= ne) throw Error{MAPPG_ERR_ARG, "element index beyond the force field's elements"};
+        for (int e = 0; e < ne; e++)
+            if (!(masses[e] > 0.0)) throw Error{MAPPG_ERR_ARG, "masses must be positive"};
+        for (long long i = 0; i < 3 * total; i++)
+            if (!std::isfinite(x[i])) throw Error{MAPPG_ERR_NAN, "non-finite position"};
+        ensure_uploaded(ff);
+        mappg_sys* s = new mappg_sys();
+        try {
+            s->ff = ff;
+            s->n = n;
+            s->precision = precision;
+            s->ne = ne;
+            s->skin = skin;
+            for (int e = 0; e < ne; e++) s->masses[e] = masses[e];
+            double mc = 0.0;
+            for (int i = 0; i < ne; i++)
+                for (int j = 0; j < ne; j++) {
+                    double c = ff->host.cut[i * ne + j];
+                    mc = std::max(mc, c);
+                    s->cut_sq[i * ne + j] = c * c;
+                    double ck = c + skin;
+                    s->cut_sk_sq[i * ne + j] = ck * ck;
+                }
+            s->max_cut = mc + skin;
+            MAPPG_CUDA(cudaGetDevice(&s->device));
+            cudaDeviceProp p;
+            MAPPG_CUDA(cudaGetDeviceProperties(&p, s->device));
+            s->sm_count = p.multiProcessorCount;
+            sys_set_cells(s, ncell, natoms, H);
+            sys_alloc(s, x);
+            sys_alloc_bins(s);
+            double vol = 0.0;
+            for (const CellGeo& g : s->cells) vol += g.h6[0] * g.h6[3] * g.h6[5];
+            double est = (n / vol) * 4.18879 * s->max_cut * s->max_cut * s->max_cut;
+            int cap = ((int)(est * 1.35) + 32 + 31) / 32 * 32;
+            sys_alloc_nbr(s, std::min(cap, 4096));
+            sys_upload(s, x, s->x);
+            std::vector<uint8_t> es(n);
+            for (int i = 0; i < n; i++) es[i] = elem[s->host_id[i]];
+            MAPPG_CUDA(cudaMemcpyAsync(s->elem, es.data(), n, cudaMemcpyHostToDevice, s->stream));
+            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        } catch (...) {
+            sys_free(s);
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+int mappg_batch_ncell(const mappg_sys* s) { return s ? s->ncell : 0; }
+
+static void batch_cells_out(mappg_sys* s, double* pe, double* virial) {
+    std::vector<CellMd> cm(s->ncell);
+    MAPPG_CUDA(cudaMemcpyAsync(cm.data(), s->cmd, sizeof(CellMd) * s->ncell, cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int c = 0; c < s->ncell; c++) {
+        if (!std::isfinite(cm[c].energy)) throw Error{MAPPG_ERR_NAN, "non-finite energy"};
+        if (pe) pe[c] = cm[c].energy;
+        if (virial)
+            for (int k = 0; k < 6; k++) virial[6 * (size_t)c + k] = cm[c].virial[k];
+    }
+}
+
+int mappg_batch_force(mappg_sys* s, double* pe, double* virial) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        if (!s->built) sys_build(s);
+        launch_force(s);
+        batch_cells_out(s, pe, virial);
+    });
+}
+
+int mappg_batch_energy(mappg_sys* s, double* pe) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        if (!s->built) sys_build(s);
+        launch_energy(s);
+        batch_cells_out(s, pe, nullptr);
+    });
+}
+
+int mappg_batch_nvt_begin(mappg_sys* s, const double* T, double dt, double kB, double t_relax, int L, int niters,
+                          long long nsteps, const double* eta, int record_thermo) {
+    return guard([&] {
+        if (!s || !T) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        nvt_begin(s, 1.0, dt, kB, t_relax, L, niters, nsteps, eta, record_thermo != 0, T);
+    });
+}
+
+int mappg_batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c, double rho,
+                          double min_alpha, int nsteps, double* stats) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        batch_lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, nullptr, stats);
+    });
+}
+
+int mappg_batch_nvt_end(mappg_sys* s, double* eta, double* thermo) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        nvt_end(s, eta, thermo);
+    });
+}
+
+int mappg_batch_nvt_run(mappg_sys* s, const double* T, double dt, double kB, double t_relax, int L, int niters,
+                        int nsteps, double* eta, double* thermo) {
+    return guard([&] {
+        if (!s || !T) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell < 2) throw Error{MAPPG_ERR_ARG, "not a batch of cells"};
+        if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
+        nvt_run(s, 1.0, dt, kB, t_relax, L, niters, nsteps, eta, thermo, T);
     });
 }
 
@@ -606,7 +800,8 @@ int mappg_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_t
                     double min_alpha, int nsteps, double* stats) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
-        lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats);
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "L-BFGS on a batch of cells runs with mappg_batch_lbfgs_run"};
+        lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats, nullptr, nullptr);
     });
 }
 

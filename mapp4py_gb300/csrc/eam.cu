@@ -24,6 +24,8 @@
 // as x_j + n*H with n from the entry's bin step and atom i's bin.
 #include <math.h>
 
+#include <algorithm>
+
 #include "eam_common.cuh"
 
 namespace mappg {
@@ -225,6 +227,120 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
     }
 }
 
+// input features of the learned preconditioner, per atom: 16 Gaussian radial
+// functions exp(-(r - mu_k)^2 / (2 w^2)) fc(r), mu_k = 2.0 + 3.5 k/15 A,
+// w = 0.3 A, fc(r) = (1 + cos(pi r / 5.5))/2 for r < 5.5 A, summed over the
+// neighbours of each species (A in 0..15, B in 16..31), and the host
+// density rho_i (32); FP64 positions, FP32 sums
+constexpr int kDescR = 16;
+constexpr float kDescRc = 5.5f, kDescW = 0.3f;
+
+// batch: atom i's position and image flags from its cell's bins; image
+// shifts n*H from the cell's box
+struct PosCell {
+    double x, y, z;
+    int lo[3], hi[3];
+    double h6[6];
+    __device__ __forceinline__ void load(const EamArgs& a, const int* cell_of, int i) {
+        const CellGeo& g = a.cells[cell_of[i]];
+        x = a.x[i];
+        y = a.x[a.n + i];
+        z = a.x[2 * a.n + i];
+        const int bc = a.binc[i];
+        const int b[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
+        for (int d = 0; d < 3; d++) {
+            lo[d] = b[d] == 0;
+            hi[d] = b[d] == g.nb[d] - 1;
+        }
+        for (int k = 0; k < 6; k++) h6[k] = g.h6[k];
+    }
+    __device__ __forceinline__ void delta(const EamArgs& a, int e, double& dx, double& dy, double& dz) const {
+        const int j = entry_j(e), c = entry_code(e);
+        const int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
+        const int n0 = (d0 < 0 && lo[0]) ? -1 : ((d0 > 0 && hi[0]) ? 1 : 0);
+        const int n1 = (d1 < 0 && lo[1]) ? -1 : ((d1 > 0 && hi[1]) ? 1 : 0);
+        const int n2 = (d2 < 0 && lo[2]) ? -1 : ((d2 > 0 && hi[2]) ? 1 : 0);
+        // rows of H: (h0,0,0), (h1,h3,0), (h2,h4,h5)
+        const double s0 = n0 * h6[0] + n1 * h6[1] + n2 * h6[2];
+        const double s1 = n1 * h6[3] + n2 * h6[4];
+        const double s2 = n2 * h6[5];
+        dx = x - (__ldg(a.x + j) + s0);
+        dy = y - (__ldg(a.x + a.n + j) + s1);
+        dz = z - (__ldg(a.x + 2 * a.n + j) + s2);
+    }
+};
+
+template <int TPA, bool BATCH>
+__global__ void __launch_bounds__(256) k_descriptors(EamArgs a, const int* __restrict__ cell_of,
+                                                     float* __restrict__ out) {
+    __shared__ Smem64 S;
+    S.fill(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    const float inv2w2 = 1.f / (2.f * kDescW * kDescW);
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        float g[2 * kDescR];
+#pragma unroll
+        for (int q = 0; q < 2 * kDescR; q++) g[q] = 0.f;
+        double rho = 0.0;
+        if (active) {
+            Pos64 P;
+            PosCell PC;
+            if (BATCH)
+                PC.load(a, cell_of, i);
+            else
+                P.load(a, i);
+            const int ei = a.elem[i];
+            const int nn = __ldg(a.nnbr + i);
+            const int* row = a.nbr + (size_t)i * a.maxnbr;
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                const int ej = entry_elem(e);
+                double dx, dy, dz;
+                if (BATCH)
+                    PC.delta(a, e, dx, dy, dz);
+                else
+                    P.delta(a, S.sh, e, dx, dy, dz);
+                const double rsq = dx * dx + dy * dy + dz * dz;
+                if (rsq < S.cut_sq[ei * a.ne + ej]) {
+                    double p;
+                    const int m = knot64(sqrt(rsq), a, p);
+                    rho += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+                }
+                const float r = (float)sqrt(rsq);
+                if (r < kDescRc && ej < 2) {
+                    const float fc = 0.5f * (1.f + cosf(3.14159265f * r / kDescRc));
+#pragma unroll
+                    for (int q = 0; q < kDescR; q++) {
+                        const float d = r - (2.0f + 3.5f * (float)q / 15.f);
+                        const float v = expf(-d * d * inv2w2) * fc;
+                        if (ej == 0)
+                            g[q] += v;
+                        else
+                            g[kDescR + q] += v;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int o = TPA / 2; o > 0; o >>= 1) {
+#pragma unroll
+            for (int q = 0; q < 2 * kDescR; q++) g[q] += __shfl_xor_sync(0xffffffffu, g[q], o, TPA);
+            rho += __shfl_xor_sync(0xffffffffu, rho, o, TPA);
+        }
+        if (active && lane == 0) {
+            float* o = out + (size_t)i * (2 * kDescR + 1);
+#pragma unroll
+            for (int q = 0; q < 2 * kDescR; q++) o[q] = g[q];
+            o[2 * kDescR] = (float)rho;
+        }
+    }
+}
+
 template <int TPA>
 __global__ void __launch_bounds__(256) k_energy64(EamArgs a) {
     __shared__ Smem64 S;
@@ -279,6 +395,55 @@ __global__ void __launch_bounds__(256) k_energy64(EamArgs a) {
     }
 }
 
+// batch: FP64 energy of every cell (the line-search energies of mixed
+// batches), chunk sums into slot 0 of the chunk partials
+template <int TPA>
+__global__ void __launch_bounds__(256) k_energy64b(EamArgs a, const int* __restrict__ cell_of) {
+    __shared__ Smem64 S;
+    S.fill(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        double ep = 0.0, eacc = 0.0;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            const bool active = i < hi;
+            double acc = 0.0;
+            int ei = 0;
+            if (active) {
+                PosCell P;
+                P.load(a, cell_of, i);
+                ei = a.elem[i];
+                const int nn = __ldg(a.nnbr + i);
+                const int* row = a.nbr + (size_t)i * a.maxnbr;
+                for (int k = lane; k < nn; k += TPA) {
+                    const int e = __ldg(row + k);
+                    const int ej = entry_elem(e);
+                    double dx, dy, dz;
+                    P.delta(a, e, dx, dy, dz);
+                    const double rsq = dx * dx + dy * dy + dz * dz;
+                    if (rsq < S.cut_sq[ei * a.ne + ej]) {
+                        const double r = sqrt(rsq);
+                        double p;
+                        const int m = knot64(r, a, p);
+                        acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+                        ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+            if (active && lane == 0) {
+                double Fv, dFv;
+                embed64(a, ei, acc, Fv, dFv);
+                eacc += Fv;
+            }
+        }
+        chunk_store<1>([&](int) { return eacc + 0.5 * ep; }, a.chunk_part + (size_t)ch * kChunkSlots);
+    }
+}
+
 template <int TPA>
 static int grid64(mappg_sys* s) {
     return grid_for(s, (long long)s->n * TPA, 256);
@@ -322,6 +487,16 @@ void launch_force(mappg_sys* s) {
 // FP64 density and force passes whose outputs, partial sums and device
 // scalars are the ones in `a` (mappg_sys_force_noalloc points them at its
 // scratch); launches only, no allocation
+// preconditioner features of every atom (bin order), n x 33 floats
+void launch_descriptors(mappg_sys* s, float* out) {
+    EamArgs a = eam_args(s);
+    if (s->ncell > 1)
+        k_descriptors<8, true><<<grid64<8>(s), 256, 0, s->stream>>>(a, s->cell_of, out);
+    else
+        k_descriptors<8, false><<<grid64<8>(s), 256, 0, s->stream>>>(a, nullptr, out);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
 void launch_force64_args(mappg_sys* s, const EamArgs& a) {
     MAPPG_TPA64(k_density64)
     MAPPG_TPA64(k_force64)
@@ -340,6 +515,22 @@ void preload_force64() {
     MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<8>));
     MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<16>));
     MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<32>));
+}
+
+void launch_cells_done(mappg_sys* s, const EamArgs& a, int what);  // eam32.cu
+
+// FP64 energy in either precision (line searches of mixed systems compare
+// FP64 energies): sc->energy for one cell, CellMd::energy per cell of a batch
+void launch_energy64(mappg_sys* s) {
+    EamArgs a = eam_args(s);
+    if (s->ncell > 1) {
+        k_energy64b<8><<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a, s->cell_of);
+        MAPPG_CUDA(cudaGetLastError());
+        launch_cells_done(s, a, 1);
+        return;
+    }
+    MAPPG_TPA64(k_energy64)
+    MAPPG_CUDA(cudaGetLastError());
 }
 
 void launch_energy(mappg_sys* s) {

@@ -22,6 +22,8 @@
 // (ff_eam.cpp:122-128).
 #include <math.h>
 
+#include <algorithm>
+
 #include "eam_common.cuh"
 #include "nhc.cuh"
 
@@ -39,8 +41,8 @@ struct Smem32 {
 };
 
 // frame displacement (a,b,c) to Cartesian with the head + tail scale
-template <bool ORTHO>
-__device__ __forceinline__ void cart(const Frame& fr, float a, float b, float c, float& x, float& y, float& z) {
+template <bool ORTHO, class FR>
+__device__ __forceinline__ void cart(const FR& fr, float a, float b, float c, float& x, float& y, float& z) {
     if (ORTHO) {
         x = fmaf(a, fr.G[0][0], a * fr.Glo[0][0]);
         y = fmaf(b, fr.G[1][1], b * fr.Glo[1][1]);
@@ -118,6 +120,65 @@ static int occupancy_grid(mappg_sys* s, Kern k, int block) {
     return (int)g;
 }
 
+// frame of a batch cell (the G head/tail of CellGeo), read once per chunk
+struct CellFrame {
+    float G[3][3], Glo[3][3];
+};
+
+template <bool ORTHO>
+__device__ __forceinline__ CellFrame cell_frame(const CellGeo* g) {
+    CellFrame f;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const bool used = ORTHO ? d == k : k <= d;
+            f.G[d][k] = used ? g->G[d][k] : 0.f;
+            f.Glo[d][k] = used ? g->Glo[d][k] : 0.f;
+        }
+    return f;
+}
+
+// one atom's density row (TPA lanes), its embedding terms and q32 record
+template <int TPA, bool ORTHO, class FR>
+__device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
+                                             int i, int lane, bool active, float& es, float& ec) {
+    float acc = 0.f;
+    int ei = 0;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+        pi = __ldg(a.p32 + i);
+        ei = a.elem[i];
+        const int nn = __ldg(a.nnbr + i);
+        const int* row = a.nbr + (size_t)i * a.maxnbr;
+        for (int k = lane; k < nn; k += TPA) {
+            const int e = __ldg(row + k);
+            const int ej = entry_elem(e);
+            const float4 q = __ldg(a.p32 + entry_j(e));
+            const float4 o = S.off[entry_code(e)];
+            float dx, dy, dz;
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (rsq < S.cut_sq[ei * a.ne + ej]) {
+                const float r = rsq * inv_sqrt(rsq);
+                float fr;
+                const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+    if (active && lane == 0) {
+        float Fv, dFv;
+        embed32(a, K, ei, acc, Fv, dFv);
+        a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
+        a.rho32out[i] = acc;
+        kahan_add(es, ec, Fv);
+    }
+}
+
 template <int TPA, bool ORTHO>
 __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
     __shared__ Smem32 S;
@@ -131,40 +192,7 @@ __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        float acc = 0.f;
-        int ei = 0;
-        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (active) {
-            pi = __ldg(a.p32 + i);
-            ei = a.elem[i];
-            const int nn = __ldg(a.nnbr + i);
-            const int* row = a.nbr + (size_t)i * a.maxnbr;
-            for (int k = lane; k < nn; k += TPA) {
-                const int e = __ldg(row + k);
-                const int ej = entry_elem(e);
-                const float4 q = __ldg(a.p32 + entry_j(e));
-                const float4 o = S.off[entry_code(e)];
-                float dx, dy, dz;
-                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
-                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (rsq < S.cut_sq[ei * a.ne + ej]) {
-                    const float r = rsq * inv_sqrt(rsq);
-                    float fr;
-                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                    const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
-                    acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
-                }
-            }
-        }
-#pragma unroll
-        for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
-        if (active && lane == 0) {
-            float Fv, dFv;
-            embed32(a, K, ei, acc, Fv, dFv);
-            a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
-            a.rho32out[i] = acc;
-            kahan_add(es, ec, Fv);
-        }
+        density_atom<TPA, ORTHO>(a, S, K, a.fr, i, lane, active, es, ec);
     }
     double v[1] = {(double)es - (double)ec};
     if (block_partials<1>(v, a.partials, 0, &a.sc->counter[1]) && threadIdx.x < 32) {
@@ -173,6 +201,110 @@ __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
         if (threadIdx.x == 0) {
             a.sc->e_embed = tot[0];
             a.sc->counter[1] = 0;
+        }
+    }
+}
+
+// batch: blocks walk chunks; the chunk's embedding energy goes to slot 13
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
+        float es = 0.f, ec = 0.f;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            density_atom<TPA, ORTHO>(a, S, K, fr, i, lane, i < hi, es, ec);
+        }
+        chunk_store<1>([&](int) { return (double)es - (double)ec; }, a.chunk_part + (size_t)ch * kChunkSlots + 13);
+    }
+}
+
+// one atom's force row (TPA lanes): force, pair energy, virial and (TAIL) the
+// kinetic tensor of v + f dt/2m into the thread's shared slots ke[c*256]
+template <int TPA, bool ORTHO, bool TAIL, class FR>
+__device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
+                                           int i, int lane, bool active, float& es, float& ec, float (&w)[6],
+                                           float* ke) {
+    float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
+    int ei = 0;
+    if (active) {
+        const float4 pi = __ldg(a.q32 + i);
+        const float dFi = pi.w;
+        ei = a.elem[i];
+        const int nn = __ldg(a.nnbr + i);
+        const int* row = a.nbr + (size_t)i * a.maxnbr;
+        for (int k = lane; k < nn; k += TPA) {
+            const int e = __ldg(row + k);
+            const int t = ei * a.ne + entry_elem(e);
+            const float4 q = __ldg(a.q32 + entry_j(e));
+            const float4 o = S.off[entry_code(e)];
+            float dx, dy, dz;
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (rsq < S.cut_sq[t]) {
+                const float rinv = inv_sqrt(rsq);
+                const float r = rsq * rinv;
+                float fr;
+                const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                const size_t kt = (size_t)t * a.nr + m;
+                float4 r0, r1;
+                ldg8(a.ftab + 2 * kt, r0, r1);
+                const float der_i = fmaf(fmaf(r0.z, fr, r0.y), fr, r0.x);
+                float der_j = der_i;
+                if (entry_elem(e) != ei) {
+                    const float4 r2 = __ldg(a.fjtab + kt);
+                    der_j = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
+                }
+                const float zpoly = fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x);
+                const float z = r0.w + fmaf(fr, zpoly, r1.w);
+                const float zp = fmaf(fmaf(3.0f * r1.z, fr, 2.0f * r1.y), fr, r1.x) * K.dri;
+                const float phi = z * rinv;
+                const float dphi = (zp - phi) * rinv;
+                const float fp = -fmaf(dFi, der_i, fmaf(q.w, der_j, dphi)) * rinv;
+                const float fdx = fp * dx, fdy = fp * dy, fdz = fp * dz;
+                fx += fdx;
+                fy += fdy;
+                fz += fdz;
+                ep += phi;
+                w[0] = fmaf(fdx, dx, w[0]);
+                w[1] = fmaf(fdx, dy, w[1]);
+                w[2] = fmaf(fdx, dz, w[2]);
+                w[3] = fmaf(fdy, dy, w[3]);
+                w[4] = fmaf(fdy, dz, w[4]);
+                w[5] = fmaf(fdz, dz, w[5]);
+            }
+        }
+        kahan_add(es, ec, ep);
+    }
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o, TPA);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o, TPA);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o, TPA);
+    }
+    if (active && lane == 0) {
+        a.f32[i] = fx;
+        a.f32[a.n + i] = fy;
+        a.f32[2 * a.n + i] = fz;
+        if (TAIL) {
+            // kinetic tensor of the half-kicked velocity v + f dt/2m
+            const float dtm = a.dtm32[ei], m = a.mass32[ei];
+            const float vx = fmaf(fx, dtm, __ldg(a.v32 + i));
+            const float vy = fmaf(fy, dtm, __ldg(a.v32 + a.n + i));
+            const float vz = fmaf(fz, dtm, __ldg(a.v32 + 2 * a.n + i));
+            const float mx = m * vx, my = m * vy, mz = m * vz;
+            ke[0] = fmaf(mx, vx, ke[0]);
+            ke[256] = fmaf(mx, vy, ke[256]);
+            ke[512] = fmaf(mx, vz, ke[512]);
+            ke[768] = fmaf(my, vy, ke[768]);
+            ke[1024] = fmaf(my, vz, ke[1024]);
+            ke[1280] = fmaf(mz, vz, ke[1280]);
         }
     }
 }
@@ -186,7 +318,7 @@ __global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
     float es = 0.f, ec = 0.f;  // pair energy, compensated
-    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     // kinetic tensor (TAIL): one private shared-memory slot per thread keeps
     // these six sums out of registers, so the MD variant runs at the same
     // occupancy as the plain one
@@ -198,94 +330,18 @@ __global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
-        int ei = 0;
-        if (active) {
-            const float4 pi = __ldg(a.q32 + i);
-            const float dFi = pi.w;
-            ei = a.elem[i];
-            const int nn = __ldg(a.nnbr + i);
-            const int* row = a.nbr + (size_t)i * a.maxnbr;
-            for (int k = lane; k < nn; k += TPA) {
-                const int e = __ldg(row + k);
-                const int t = ei * a.ne + entry_elem(e);
-                const float4 q = __ldg(a.q32 + entry_j(e));
-                const float4 o = S.off[entry_code(e)];
-                float dx, dy, dz;
-                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
-                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (rsq < S.cut_sq[t]) {
-                    const float rinv = inv_sqrt(rsq);
-                    const float r = rsq * rinv;
-                    float fr;
-                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                    const size_t kt = (size_t)t * a.nr + m;
-                    float4 r0, r1;
-                    ldg8(a.ftab + 2 * kt, r0, r1);
-                    const float der_i = fmaf(fmaf(r0.z, fr, r0.y), fr, r0.x);
-                    float der_j = der_i;
-                    if (entry_elem(e) != ei) {
-                        const float4 r2 = __ldg(a.fjtab + kt);
-                        der_j = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
-                    }
-                    const float zpoly = fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x);
-                    const float z = r0.w + fmaf(fr, zpoly, r1.w);
-                    const float zp = fmaf(fmaf(3.0f * r1.z, fr, 2.0f * r1.y), fr, r1.x) * K.dri;
-                    const float phi = z * rinv;
-                    const float dphi = (zp - phi) * rinv;
-                    const float fp = -fmaf(dFi, der_i, fmaf(q.w, der_j, dphi)) * rinv;
-                    const float fdx = fp * dx, fdy = fp * dy, fdz = fp * dz;
-                    fx += fdx;
-                    fy += fdy;
-                    fz += fdz;
-                    ep += phi;
-                    w0 = fmaf(fdx, dx, w0);
-                    w1 = fmaf(fdx, dy, w1);
-                    w2 = fmaf(fdx, dz, w2);
-                    w3 = fmaf(fdy, dy, w3);
-                    w4 = fmaf(fdy, dz, w4);
-                    w5 = fmaf(fdz, dz, w5);
-                }
-            }
-            kahan_add(es, ec, ep);
-        }
-#pragma unroll
-        for (int o = TPA / 2; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o, TPA);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o, TPA);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o, TPA);
-        }
-        if (active && lane == 0) {
-            a.f32[i] = fx;
-            a.f32[a.n + i] = fy;
-            a.f32[2 * a.n + i] = fz;
-            if (TAIL) {
-                // kinetic tensor of the half-kicked velocity v + f dt/2m
-                const float dtm = a.dtm32[ei], m = a.mass32[ei];
-                const float vx = fmaf(fx, dtm, __ldg(a.v32 + i));
-                const float vy = fmaf(fy, dtm, __ldg(a.v32 + a.n + i));
-                const float vz = fmaf(fz, dtm, __ldg(a.v32 + 2 * a.n + i));
-                const float mx = m * vx, my = m * vy, mz = m * vz;
-                float* k = &ke[0][threadIdx.x];
-                k[0] = fmaf(mx, vx, k[0]);
-                k[256] = fmaf(mx, vy, k[256]);
-                k[512] = fmaf(mx, vz, k[512]);
-                k[768] = fmaf(my, vy, k[768]);
-                k[1024] = fmaf(my, vz, k[1024]);
-                k[1280] = fmaf(mz, vz, k[1280]);
-            }
-        }
+        force_atom<TPA, ORTHO, TAIL>(a, S, K, a.fr, i, lane, active, es, ec, w, &ke[0][threadIdx.x]);
     }
     constexpr int NS = TAIL ? 13 : 7;  // energy, virial[6], kinetic tensor[6]
     auto sum_k = [&](int k) -> double {
         switch (k) {
             case 0: return 0.5 * ((double)es - (double)ec);
-            case 1: return 0.5 * (double)w0;
-            case 2: return 0.5 * (double)w1;
-            case 3: return 0.5 * (double)w2;
-            case 4: return 0.5 * (double)w3;
-            case 5: return 0.5 * (double)w4;
-            case 6: return 0.5 * (double)w5;
+            case 1: return 0.5 * (double)w[0];
+            case 2: return 0.5 * (double)w[1];
+            case 3: return 0.5 * (double)w[2];
+            case 4: return 0.5 * (double)w[3];
+            case 5: return 0.5 * (double)w[4];
+            case 6: return 0.5 * (double)w[5];
             default: return (double)ke[TAIL ? k - 7 : 0][threadIdx.x];
         }
     };
@@ -312,6 +368,90 @@ __global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
     }
 }
 
+// batch: chunk slots 0 pair energy, 1-6 virial, 7-12 kinetic tensor (TAIL)
+template <int TPA, bool ORTHO, bool TAIL>
+__global__ void __launch_bounds__(256, 5) k_force32b(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    __shared__ float ke[TAIL ? 6 : 1][256];
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
+        float es = 0.f, ec = 0.f;
+        float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (TAIL)
+#pragma unroll
+            for (int c = 0; c < 6; c++) ke[c][threadIdx.x] = 0.f;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            force_atom<TPA, ORTHO, TAIL>(a, S, K, fr, i, lane, i < hi, es, ec, w, &ke[0][threadIdx.x]);
+        }
+        constexpr int NS = TAIL ? 13 : 7;
+        chunk_store<NS>(
+            [&](int k) -> double {
+                switch (k) {
+                    case 0: return 0.5 * ((double)es - (double)ec);
+                    case 1: return 0.5 * (double)w[0];
+                    case 2: return 0.5 * (double)w[1];
+                    case 3: return 0.5 * (double)w[2];
+                    case 4: return 0.5 * (double)w[3];
+                    case 5: return 0.5 * (double)w[4];
+                    case 6: return 0.5 * (double)w[5];
+                    default: return (double)ke[TAIL ? k - 7 : 0][threadIdx.x];
+                }
+            },
+            a.chunk_part + (size_t)ch * kChunkSlots);
+    }
+}
+
+// one atom's energy: density and pair terms in one pass, then F(rho_i)
+template <int TPA, bool ORTHO, class FR>
+__device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
+                                            int i, int lane, bool active, float& es, float& ec) {
+    float acc = 0.f, ep = 0.f;
+    int ei = 0;
+    if (active) {
+        const float4 pi = __ldg(a.p32 + i);
+        ei = a.elem[i];
+        const int nn = __ldg(a.nnbr + i);
+        const int* row = a.nbr + (size_t)i * a.maxnbr;
+        for (int k = lane; k < nn; k += TPA) {
+            const int e = __ldg(row + k);
+            const int ej = entry_elem(e);
+            const int t = ei * a.ne + ej;
+            const float4 q = __ldg(a.p32 + entry_j(e));
+            const float4 o = S.off[entry_code(e)];
+            float dx, dy, dz;
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            if (rsq < S.cut_sq[t]) {
+                const float rinv = inv_sqrt(rsq);
+                const float r = rsq * rinv;
+                float fr;
+                const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
+                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+                const float4* rec = a.ftab + 2 * ((size_t)t * a.nr + m);
+                float4 r0, r1;
+                ldg8(rec, r0, r1);
+                const float z = r0.w + fmaf(fr, fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x), r1.w);
+                ep += 0.5f * z * rinv;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+    if (active) kahan_add(es, ec, ep);
+    if (active && lane == 0) {
+        float Fv, dFv;
+        embed32(a, K, ei, acc, Fv, dFv);
+        kahan_add(es, ec, Fv);
+    }
+}
+
 template <int TPA, bool ORTHO>
 __global__ void __launch_bounds__(256) k_energy32(EamArgs a) {
     __shared__ Smem32 S;
@@ -325,45 +465,7 @@ __global__ void __launch_bounds__(256) k_energy32(EamArgs a) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        float acc = 0.f, ep = 0.f;
-        int ei = 0;
-        if (active) {
-            const float4 pi = __ldg(a.p32 + i);
-            ei = a.elem[i];
-            const int nn = __ldg(a.nnbr + i);
-            const int* row = a.nbr + (size_t)i * a.maxnbr;
-            for (int k = lane; k < nn; k += TPA) {
-                const int e = __ldg(row + k);
-                const int ej = entry_elem(e);
-                const int t = ei * a.ne + ej;
-                const float4 q = __ldg(a.p32 + entry_j(e));
-                const float4 o = S.off[entry_code(e)];
-                float dx, dy, dz;
-                cart<ORTHO>(a.fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
-                const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (rsq < S.cut_sq[t]) {
-                    const float rinv = inv_sqrt(rsq);
-                    const float r = rsq * rinv;
-                    float fr;
-                    const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                    const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
-                    acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
-                    const float4* rec = a.ftab + 2 * ((size_t)t * a.nr + m);
-                    float4 r0, r1;
-                    ldg8(rec, r0, r1);
-                    const float z = r0.w + fmaf(fr, fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x), r1.w);
-                    ep += 0.5f * z * rinv;
-                }
-            }
-        }
-#pragma unroll
-        for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
-        if (active) kahan_add(es, ec, ep);
-        if (active && lane == 0) {
-            float Fv, dFv;
-            embed32(a, K, ei, acc, Fv, dFv);
-            kahan_add(es, ec, Fv);
-        }
+        energy_atom<TPA, ORTHO>(a, S, K, a.fr, i, lane, active, es, ec);
     }
     double v[1] = {(double)es - (double)ec};
     if (block_partials<1>(v, a.partials, 0, &a.sc->counter[2]) && threadIdx.x < 32) {
@@ -373,6 +475,75 @@ __global__ void __launch_bounds__(256) k_energy32(EamArgs a) {
             a.sc->energy = tot[0];
             a.sc->counter[2] = 0;
         }
+    }
+}
+
+// batch: the chunk's energy goes to slot 0
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_energy32b(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
+        float es = 0.f, ec = 0.f;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            energy_atom<TPA, ORTHO>(a, S, K, fr, i, lane, i < hi, es, ec);
+        }
+        chunk_store<1>([&](int) { return (double)es - (double)ec; }, a.chunk_part + (size_t)ch * kChunkSlots);
+    }
+}
+
+// per-cell totals of a batch from the chunk slots, one warp per cell in a
+// fixed order: what = 0 after a force pass (energy = pair + embedding,
+// virial), 1 after an energy pass, 2 after a force pass with the MD tail
+// (kinetic tensor and the closing half of each cell's chain, thermo rows of
+// pe and T per cell)
+__global__ void k_cells_done(EamArgs a, const int* __restrict__ cell_chunk, CellMd* __restrict__ cmd, int what) {
+    const int lane = threadIdx.x & 31;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.ncell) return;
+    const int lo = cell_chunk[c], hi = cell_chunk[c + 1];
+    double t[14];
+#pragma unroll 1
+    for (int k = 0; k < 14; k++) {
+        double v = 0.0;
+        const bool need = what == 1 ? k == 0 : (what == 0 ? (k <= 6 || k == 13) : true);
+        if (need)
+            for (int ch = lo + lane; ch < hi; ch += 32) v += a.chunk_part[(size_t)ch * kChunkSlots + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        t[k] = v;
+    }
+    if (lane != 0) return;
+    CellMd* m = cmd + c;
+    if (what == 1) {
+        m->energy = t[0];
+        return;
+    }
+    m->e_embed = t[13];
+    m->energy = t[0] + t[13];
+    for (int k = 0; k < 6; k++) m->virial[k] = t[1 + k];
+    if (what == 2) {
+        NhcParams P = a.nhc;
+        P.T = m->T;
+        P.ndof = (int)m->ndof;
+        P.ndof_kB = m->ndof_kB;
+        for (int k = 0; k < 6; k++) m->mvv[k] = t[7 + k];
+        m->T_part = (t[7] + (t[10] + t[12])) / m->ndof_kB;
+        m->fac_close = thermo_half(P, m);
+        m->pending_kick = 1;
+        const long long st = ++m->step;
+        if (a.thermo && st <= a.nsteps) {
+            double* r = a.thermo + 2 * ((size_t)st * a.ncell + c);
+            r[0] = m->energy;
+            r[1] = m->T_part;
+        }
+        if (!(isfinite(m->energy) && isfinite(m->T_part))) a.sc->bad = 1;
     }
 }
 
@@ -415,8 +586,79 @@ static void energy_t(mappg_sys* s, const EamArgs& a) {
         MAPPG_CUDA(cudaGetLastError());                  \
     } while (0)
 
-void launch_density32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(density_t); }
-void launch_force32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(force_t); }
-void launch_energy32(mappg_sys* s, const EamArgs& a) { MAPPG_TPA32(energy_t); }
+template <int TPA, bool ORTHO>
+static void density_b(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_density32b<TPA, ORTHO>, 256);
+    k_density32b<TPA, ORTHO><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
+}
+
+template <int TPA, bool ORTHO>
+static void force_b(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0, grid_tail = 0;
+    if (a.md_tail) {
+        if (!grid_tail) grid_tail = occupancy_grid(s, k_force32b<TPA, ORTHO, true>, 256);
+        k_force32b<TPA, ORTHO, true><<<std::min(grid_tail, a.nchunk), 256, 0, s->stream>>>(a);
+    } else {
+        if (!grid) grid = occupancy_grid(s, k_force32b<TPA, ORTHO, false>, 256);
+        k_force32b<TPA, ORTHO, false><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
+    }
+}
+
+template <int TPA, bool ORTHO>
+static void energy_b(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_energy32b<TPA, ORTHO>, 256);
+    k_energy32b<TPA, ORTHO><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
+}
+
+// a batch takes the orthorhombic kernels only when every cell is orthorhombic
+static bool all_ortho(const mappg_sys* s) {
+    for (const CellGeo& g : s->cells)
+        if (!g.ortho) return false;
+    return true;
+}
+
+#define MAPPG_TPA32B(FN)                                 \
+    do {                                                 \
+        const bool o = all_ortho(s);                     \
+        switch (s->tpa) {                                \
+            case 4: o ? FN<4, true>(s, a) : FN<4, false>(s, a); break;    \
+            case 16: o ? FN<16, true>(s, a) : FN<16, false>(s, a); break; \
+            case 32: o ? FN<32, true>(s, a) : FN<32, false>(s, a); break; \
+            default: o ? FN<8, true>(s, a) : FN<8, false>(s, a); break;   \
+        }                                                \
+        MAPPG_CUDA(cudaGetLastError());                  \
+    } while (0)
+
+static void cells_done(mappg_sys* s, const EamArgs& a, int what) {
+    k_cells_done<<<(s->ncell * 32 + 255) / 256, 256, 0, s->stream>>>(a, s->cell_chunk, s->cmd, what);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
+void launch_cells_done(mappg_sys* s, const EamArgs& a, int what) { cells_done(s, a, what); }
+
+void launch_density32(mappg_sys* s, const EamArgs& a) {
+    if (s->ncell > 1)
+        MAPPG_TPA32B(density_b);
+    else
+        MAPPG_TPA32(density_t);
+}
+void launch_force32(mappg_sys* s, const EamArgs& a) {
+    if (s->ncell > 1) {
+        MAPPG_TPA32B(force_b);
+        cells_done(s, a, a.md_tail ? 2 : 0);
+    } else {
+        MAPPG_TPA32(force_t);
+    }
+}
+void launch_energy32(mappg_sys* s, const EamArgs& a) {
+    if (s->ncell > 1) {
+        MAPPG_TPA32B(energy_b);
+        cells_done(s, a, 1);
+    } else {
+        MAPPG_TPA32(energy_t);
+    }
+}
 
 }  // namespace mappg

@@ -100,6 +100,27 @@ __device__ void final_sums_smem(const double* partials, int nblk, double* out) {
     __syncwarp();
 }
 
+// block sums of K values from get(k) into out[0..K-1] (one batch chunk)
+template <int K, class Get>
+__device__ __forceinline__ void chunk_store(Get get, double* out) {
+    __shared__ double red[8][K];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll 1
+    for (int k = 0; k < K; k++) {
+        double t = get(k);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[w][k] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int q = 0; q < nw; q++) t += red[q][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
 // sums of the first K partial slots over nblk blocks by one warp, in a fixed
 // order (lane-strided, then a shuffle tree): every lane gets the totals
 template <int K>

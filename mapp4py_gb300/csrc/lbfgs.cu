@@ -87,7 +87,8 @@ __device__ void lb_final(const double* partials, int nblk, double (&tot)[K], boo
 // h <- h + coef*y, then dot = s.h (s may be null: no dot).  coef is read
 // from the device: mode 0: coef = 0 (plain dot); mode 1: alpha_i =
 // -rho_i*dot_in, stored; mode 2: beta = -alpha_i - rho_i*dot_in; mode 3:
-// coef applies as a scale: h <- gamma*h
+// coef applies as a scale: h <- gamma*h; mode 4: h <- P*h elementwise with
+// P (passed as y) the learned diagonal initial inverse Hessian
 __global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__ h, const double* __restrict__ y,
                                                      const double* __restrict__ s, LbScal* L, int mode, int idx,
                                                      int dot_in, int dot_out, double* partials, unsigned* counter) {
@@ -107,6 +108,8 @@ __global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__
             hv = hv + coef * y[q];
         else if (mode == 3)
             hv = hv * coef;
+        else if (mode == 4)
+            hv = hv * y[q];
         if (mode) h[q] = hv;
         if (s) acc += s[q] * hv;
     }
@@ -229,10 +232,17 @@ struct LbState {
     unsigned* counter;
 };
 
+void launch_energy64(mappg_sys* s);  // eam.cu
+
 static double lb_energy(mappg_sys* s) {
-    // skin test and (gated) rebuild, then the energy kernel
+    // skin test and (gated) rebuild, then the energy kernel; mixed systems
+    // compare FP64 line-search energies, so FP32 rounding of the pair terms
+    // does not decide the Armijo test near convergence
     lb_update(s);
-    launch_energy(s);
+    if (s->precision == MAPPG_MIXED)
+        launch_energy64(s);
+    else
+        launch_energy(s);
     double e;
     MAPPG_CUDA(cudaMemcpyAsync(&e, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
@@ -258,7 +268,7 @@ static void lb_force(mappg_sys* s, double* pe) {
 }
 
 void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
-               double min_alpha, int nsteps, double* stats) {
+               double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback) {
     enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
     if (m < 0 || m > 64) throw Error{MAPPG_ERR_ARG, "m must be in 0..64"};
     if (!(max_dx > 0.0)) throw Error{MAPPG_ERR_ARG, "max_dx must be positive"};
@@ -301,7 +311,8 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
     long long n_en = 0, n_fc = 1;
     double e_curr, pe_force;
     lb_force(s, &pe_force);
-    e_curr = pe_force;
+    // the line search's reference energy is an FP64 energy in both modes
+    e_curr = s->precision == MAPPG_MIXED ? lb_energy(s) : pe_force;
     double e_prev, alpha_m = 0.0;
     int k = 0;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
@@ -322,10 +333,9 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
         read_prep(&fh, &hh, &hmax, &fmaxv);
         if (fmaxv < f_tol) err = MIN_S_FTOL;
     }
-    int istep = 0;
-    for (; err == LS_S; istep++) {
-        MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-        MAPPG_CUDA(cudaMemcpyAsync(f0, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    // the two-loop recursion (min_l-bfgs.h:148-170) with the initial inverse
+    // Hessian gamma*I, or diag(P) when a learned preconditioner is given
+    auto two_loop = [&](bool diag) {
         MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         // first loop: alpha_i = -rho_i (s_i.h); h += alpha_i y_i
         if (k > 0) k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, nullptr, sv[0], L, 0, 0, 0, 0, part, counter);
@@ -333,17 +343,29 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             const double* nxt = (i + 1 < k) ? sv[i + 1] : nullptr;
             k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, yv[i], nxt, L, 1, i, i, i + 1, part, counter);
         }
-        // h *= gamma, and the first dot of the second loop y_{k-1}.h
-        k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, nullptr, k > 0 ? yv[k - 1] : nullptr, L, 3, 0, 0, 64, part,
-                                            counter);
+        // h *= H0, and the first dot of the second loop y_{k-1}.h
+        k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, diag ? P : nullptr, k > 0 ? yv[k - 1] : nullptr, L, diag ? 4 : 3,
+                                            0, 0, 64, part, counter);
         for (int i = k - 1; i > -1; i--) {
             const double* nxt = i > 0 ? yv[i - 1] : nullptr;
             k_lb_axpy_dot<<<grid, 256, 0, st>>>(N, h, sv[i], nxt, L, 2, i, 64 + (k - 1 - i), 64 + (k - i), part,
                                                 counter);
         }
         MAPPG_CUDA(cudaGetLastError());
+    };
+    int istep = 0;
+    for (; err == LS_S; istep++) {
+        MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        MAPPG_CUDA(cudaMemcpyAsync(f0, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        two_loop(P != nullptr);
         e_prev = e_curr;
         read_prep(&fh, &hh, &hmax, &fmaxv);
+        if (P && fh < 0.0) {
+            // a non-descent preconditioned direction: plain L-BFGS instead
+            if (n_fallback) (*n_fallback)++;
+            two_loop(false);
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+        }
         if (fh < 0.0) {
             MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
             k = 0;

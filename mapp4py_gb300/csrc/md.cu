@@ -62,11 +62,30 @@ struct MdArgs {
     double bs[6];          // x -> scaled frame
     Frame fr;
     double* partials;
-    double* thermo;  // rows of 14 or null
+    double* thermo;  // rows of 14 or null (a batch: rows of ncell x (pe, T))
     long long nsteps;
     NhcParams nhc;
     DevScalars* sc;
+    // batch of cells
+    int ncell, nchunk;
+    const CellGeo* cells;
+    const int* cell_of;
+    const int* chunk_begin;
+    const int* chunk_cell;
+    const int* cell_chunk;
+    double* chunk_part;
+    double* chunk_disp;
+    CellMd* cmd;
 };
+
+// NHC parameters of one cell of a batch: its own target and dof
+__device__ __forceinline__ NhcParams cell_nhc(const NhcParams& P0, const CellMd* m) {
+    NhcParams P = P0;
+    P.T = m->T;
+    P.ndof = (int)m->ndof;
+    P.ndof_kB = m->ndof_kB;
+    return P;
+}
 
 template <int K>
 __device__ bool md_block_partials(double (&v)[K], double* partials, unsigned* counter) {
@@ -300,6 +319,172 @@ __global__ void k_clear_drift(DevScalars* sc) {
     sc->pending_kick = 0;
 }
 
+// ------------------------------------------------------------------ batch of cells (mixed path)
+// per-cell sums of chunk slots lo..lo+K-1 by one warp per cell, fixed order
+template <int K>
+__device__ __forceinline__ void cell_sums(const MdArgs& a, const double* part, int stride, int c, double (&t)[K]) {
+    const int lane = threadIdx.x & 31;
+    const int lo = a.cell_chunk[c], hi = a.cell_chunk[c + 1];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double v = 0.0;
+        for (int ch = lo + lane; ch < hi; ch += 32) v += part[(size_t)ch * stride + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        t[k] = v;
+    }
+}
+
+// kinetic tensor of the incoming velocities per chunk (slots 7-12)
+__global__ void __launch_bounds__(256) k_mvv_init_b(MdArgs a) {
+    const int n = a.n;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        double d[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            double m = a.masses[a.elem[i]];
+            double v0 = a.v[i], v1 = a.v[n + i], v2 = a.v[2 * n + i];
+            d[0] += __dmul_rn(__dmul_rn(v0, v0), m);
+            d[1] += __dmul_rn(__dmul_rn(v0, v1), m);
+            d[2] += __dmul_rn(__dmul_rn(v0, v2), m);
+            d[3] += __dmul_rn(__dmul_rn(v1, v1), m);
+            d[4] += __dmul_rn(__dmul_rn(v1, v2), m);
+            d[5] += __dmul_rn(__dmul_rn(v2, v2), m);
+        }
+        chunk_store<6>([&](int k) { return d[k]; }, a.chunk_part + (size_t)ch * kChunkSlots + 7);
+    }
+}
+
+// run start per cell: kinetic tensor, T, thermo row 0, no pending scale/kick
+__global__ void k_cells_begin(MdArgs a) {
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.ncell) return;
+    double t[6];
+    cell_sums<6>(a, a.chunk_part + 7, kChunkSlots, c, t);
+    if ((threadIdx.x & 31) != 0) return;
+    CellMd* m = a.cmd + c;
+    for (int k = 0; k < 6; k++) m->mvv[k] = t[k];
+    m->T_part = (t[0] + (t[3] + t[5])) / m->ndof_kB;
+    m->step = 0;
+    m->fac_x_d = 1.0;
+    m->pending_kick = 0;
+    if (a.thermo) {
+        a.thermo[2 * c] = m->energy;
+        a.thermo[2 * c + 1] = m->T_part;
+    }
+}
+
+// opening half of every cell's chain and its kick factors (k_step_open32)
+__global__ void k_cells_open(MdArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c == 0) a.sc->rebuild = 0;
+    if (c >= a.ncell) return;
+    CellMd* m = a.cmd + c;
+    const NhcParams P = cell_nhc(a.nhc, m);
+    const double fo = thermo_half(P, m);
+    if (m->pending_kick) {
+        const double F = m->fac_close * fo;
+        m->kickA = F;
+        m->kickB = 1.0 + F;
+    } else {
+        m->kickA = fo;
+        m->kickB = 1.0;
+    }
+}
+
+// k_integrate32 per chunk: the cell's kick factors and frame, displacement
+// sums per chunk
+__global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
+    const int n = a.n;
+    int moved = 0;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        const int c = a.chunk_cell[ch];
+        const CellGeo& g = a.cells[c];
+        const double A = a.cmd[c].kickA;
+        const float B = (float)a.cmd[c].kickB;
+        float dsum0 = 0.f, dsum1 = 0.f, dsum2 = 0.f;
+        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const int e = a.elem[i];
+            const float kf = a.dtm32[e] * B;
+            double xv[3];
+            float vf[3];
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                double v = fma(a.v[q * n + i], A, (double)(a.f32[q * n + i] * kf));
+                double x = fma(v, a.dt, a.x[q * n + i]);
+                a.v[q * n + i] = v;
+                a.x[q * n + i] = x;
+                xv[q] = x;
+                vf[q] = (float)v;
+                a.v32[q * n + i] = vf[q];
+            }
+            dsum0 = fmaf(vf[0], a.dt32, dsum0);
+            dsum1 = fmaf(vf[1], a.dt32, dsum1);
+            dsum2 = fmaf(vf[2], a.dt32, dsum2);
+            const int bc = a.binc[i];
+            const double u0 = g.bs[0] * xv[0] + (g.bs[1] * xv[1] + g.bs[2] * xv[2]);
+            const double u1 = g.bs[3] * xv[1] + g.bs[4] * xv[2];
+            const double u2 = g.bs[5] * xv[2];
+            float4 p;
+            p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
+            p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
+            p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+            p.w = 0.f;
+            a.p32[i] = p;
+            const float4 q = a.p0[i];
+            const float da = p.x - q.x, db = p.y - q.y, dc = p.z - q.z;
+            const float cx = da * g.G[0][0] + db * g.G[1][0] + dc * g.G[2][0];
+            const float cy = db * g.G[1][1] + dc * g.G[2][1];
+            const float cz = dc * g.G[2][2];
+            moved |= fmaf(cx, cx, fmaf(cy, cy, cz * cz)) > a.skin_sq32;
+        }
+        chunk_store<3>(
+            [&](int k) -> double { return k == 0 ? (double)dsum0 : (k == 1 ? (double)dsum1 : (double)dsum2); },
+            a.chunk_disp + (size_t)ch * 4);
+    }
+    if (__syncthreads_or(moved) && threadIdx.x == 0) a.sc->rebuild = 1;
+}
+
+// per-cell mean displacement of the step, added to the cell's drift
+__global__ void k_cells_com(MdArgs a) {
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.ncell) return;
+    double t[3];
+    cell_sums<3>(a, a.chunk_disp, 4, c, t);
+    if ((threadIdx.x & 31) != 0) return;
+    CellMd* m = a.cmd + c;
+    const double natms = (double)(a.cells[c].end - a.cells[c].begin);
+    for (int k = 0; k < 3; k++) {
+        m->com[k] = t[k] / natms;
+        m->drift[k] += m->com[k];
+    }
+    m->pending_kick = 0;
+}
+
+// end of a batch run: pending closing kick and scale, drift removed, per cell
+__global__ void k_run_end32b(MdArgs a) {
+    const int n = a.n;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+        const int i = q % n, k = q / n;
+        const CellMd* m = a.cmd + a.cell_of[i];
+        const bool pend = m->pending_kick != 0;
+        const double fc = pend ? m->fac_close : m->fac_x_d;
+        double v = a.v[q];
+        if (pend) v += (double)a.f32[q] * a.dtm[a.elem[i]];
+        a.v[q] = v * fc;
+        a.x[q] -= m->drift[k];
+    }
+}
+
+__global__ void k_cells_clear(MdArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    CellMd* m = a.cmd + c;
+    m->drift[0] = m->drift[1] = m->drift[2] = 0.0;
+    m->pending_kick = 0;
+}
+
 }  // namespace mappg
 
 using namespace mappg;
@@ -357,6 +542,16 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
     a.nhc.L = L;
     a.nhc.niters = niters;
     a.sc = s->sc;
+    a.ncell = s->ncell;
+    a.nchunk = s->nchunk;
+    a.cells = s->cells_dev;
+    a.cell_of = s->cell_of;
+    a.chunk_begin = s->chunk_begin;
+    a.chunk_cell = s->chunk_cell;
+    a.cell_chunk = s->cell_chunk;
+    a.chunk_part = s->chunk_part;
+    a.chunk_disp = s->chunk_disp;
+    a.cmd = s->cmd;
     return a;
 }
 
@@ -385,6 +580,22 @@ static void launch_step32(mappg_sys* s, const MdArgs& a) {
     launch_force32(s, e);
 }
 
+static void launch_step32b(mappg_sys* s, const MdArgs& a) {
+    const int nc = s->ncell;
+    k_cells_open<<<(nc + 255) / 256, 256, 0, s->stream>>>(a);
+    k_integrate32b<<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a);
+    k_cells_com<<<(nc * 32 + 255) / 256, 256, 0, s->stream>>>(a);
+    launch_rebuild_chain(s);
+    EamArgs e = eam_args(s);
+    launch_density32(s, e);
+    e.md_tail = 1;
+    e.thermo = a.thermo;
+    e.nsteps = a.nsteps;
+    e.nhc = a.nhc;
+    for (int k = 0; k < s->ne; k++) e.dtm32[k] = a.dtm32[k];
+    launch_force32(s, e);  // with the per-cell closing half (k_cells_done)
+}
+
 struct NvtRun {
     MdArgs a;
     cudaGraphExec_t exec = nullptr;
@@ -408,7 +619,16 @@ void nvt_free(mappg_sys* s) { run_clear(s); }
 
 // MDNVT::init + the opening force call of MDNVT::run, then the step graph
 void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
-               const double* eta, bool thermo) {
+               const double* eta, bool thermo, const double* Tcell) {
+    const bool batch = s->ncell > 1;
+    if (batch && s->precision != MAPPG_MIXED) throw Error{MAPPG_ERR_UNSUPP, "batched MD runs in mixed precision"};
+    if (batch && !Tcell) throw Error{MAPPG_ERR_ARG, "a batch needs one temperature per cell"};
+    if (!batch && Tcell) throw Error{MAPPG_ERR_ARG, "per-cell temperatures need a batch of cells"};
+    if (batch) {
+        T = 1.0;
+        for (int c = 0; c < s->ncell; c++)
+            if (!(Tcell[c] > 0.0)) throw Error{MAPPG_ERR_ARG, "T must be positive"};
+    }
     if (!(kB == kB)) throw Error{MAPPG_ERR_ARG, "boltzmann constant should be set prior to MD"};
     if (L < 1 || L > kMaxChain) throw Error{MAPPG_ERR_ARG, "L must be in 1..16"};
     if (niters < 1) throw Error{MAPPG_ERR_ARG, "niters must be positive"};
@@ -420,7 +640,7 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     run_clear(s);
     double* tdev = nullptr;
     if (thermo) {
-        long long need = 14LL * (nsteps + 1);
+        long long need = (batch ? 2LL * s->ncell : 14LL) * (nsteps + 1);
         if (need > s->thermo_cap) {
             if (s->thermo_dev) cudaFree(s->thermo_dev);
             s->thermo_dev = nullptr;
@@ -437,11 +657,46 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     r->planned = nsteps;
     r->thermo = thermo;
     MdArgs& a = r->a;
+    int g = grid_for(s, s->n, 256);
+    if (batch) {
+        // per-cell targets, degrees of freedom and chain state
+        std::vector<CellMd> cm(s->ncell);
+        MAPPG_CUDA(cudaMemcpyAsync(cm.data(), s->cmd, sizeof(CellMd) * s->ncell, cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        for (int c = 0; c < s->ncell; c++) {
+            CellMd& m = cm[c];
+            m.T = Tcell[c];
+            m.ndof = 3.0 * (s->cell_begin[c + 1] - s->cell_begin[c]);
+            m.ndof_kB = m.ndof * kB;
+            for (int k = 0; k < kMaxChain; k++) m.eta[k] = (eta && k < L) ? eta[(size_t)c * L + k] : 0.0;
+            m.drift[0] = m.drift[1] = m.drift[2] = 0.0;
+            m.pending_kick = 0;
+            m.step = 0;
+        }
+        MAPPG_CUDA(cudaMemcpyAsync(s->cmd, cm.data(), sizeof(CellMd) * s->ncell, cudaMemcpyHostToDevice, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        sys_build(s);
+        launch_force(s);
+        k_mvv_init_b<<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a);
+        k_cells_begin<<<(s->ncell * 32 + 255) / 256, 256, 0, s->stream>>>(a);
+        MAPPG_CUDA(cudaGetLastError());
+        MAPPG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            launch_step32b(s, a);
+        } catch (...) {
+            cudaGraph_t g2 = nullptr;
+            cudaStreamEndCapture(s->stream, &g2);
+            if (g2) cudaGraphDestroy(g2);
+            throw;
+        }
+        MAPPG_CUDA(cudaStreamEndCapture(s->stream, &r->graph));
+        MAPPG_CUDA(cudaGraphInstantiate(&r->exec, r->graph, 0));
+        return;
+    }
     double eta_h[kMaxChain] = {0};
     if (eta)
         for (int k = 0; k < L; k++) eta_h[k] = eta[k];
     MAPPG_CUDA(cudaMemcpyAsync(s->sc->eta, eta_h, sizeof(double) * kMaxChain, cudaMemcpyHostToDevice, s->stream));
-    int g = grid_for(s, s->n, 256);
     k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
     k_mvv_init<<<g, 256, 0, s->stream>>>(a);
     sys_build(s);
@@ -478,6 +733,26 @@ void nvt_end(mappg_sys* s, double* eta, double* thermo) {
     NvtRun* r = (NvtRun*)s->run;
     if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
     int g = grid_for(s, 3LL * s->n, 256);
+    if (s->ncell > 1) {
+        k_run_end32b<<<g, 256, 0, s->stream>>>(r->a);
+        k_cells_clear<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(r->a);
+        MAPPG_CUDA(cudaGetLastError());
+        DevScalars h;
+        std::vector<CellMd> cm(s->ncell);
+        MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(cm.data(), s->cmd, sizeof(CellMd) * s->ncell, cudaMemcpyDeviceToHost, s->stream));
+        if (thermo && r->thermo)
+            MAPPG_CUDA(cudaMemcpyAsync(thermo, r->a.thermo, sizeof(double) * 2 * s->ncell * (r->done + 1),
+                                       cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (eta)
+            for (int c = 0; c < s->ncell; c++)
+                for (int k = 0; k < r->L; k++) eta[(size_t)c * r->L + k] = cm[c].eta[k];
+        run_clear(s);
+        if (h.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during the run"};
+        if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite position, energy or temperature during the run"};
+        return;
+    }
     if (s->precision == MAPPG_MIXED) {
         k_run_end32<<<g, 256, 0, s->stream>>>(r->a);
         k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
@@ -499,8 +774,8 @@ void nvt_end(mappg_sys* s, double* eta, double* thermo) {
 }
 
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
-             double* thermo) {
-    nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo != nullptr);
+             double* thermo, const double* Tcell) {
+    nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo != nullptr, Tcell);
     nvt_steps(s, nsteps);
     nvt_end(s, eta, thermo);
 }

@@ -50,7 +50,8 @@ __device__ inline double nhc_step(const NhcParams& P, double* eta, double T_r) {
     return rescale;
 }
 
-__device__ inline double thermo_half(const NhcParams& P, DevScalars* sc) {
+template <class State>
+__device__ inline double thermo_half(const NhcParams& P, State* sc) {
     double fac = nhc_step(P, sc->eta, sc->T_part / P.T);
     double f2 = fac * fac;
     for (int k = 0; k < 6; k++) sc->mvv[k] *= f2;

@@ -97,6 +97,56 @@ void sys_set_box(mappg_sys* s, const double* H) {
     s->built = false;
 }
 
+// a batch: every cell gets its own box, bins (a block of global bin ids) and
+// frame; the system-level box fields keep cell 0's for code that reads them
+void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) {
+    s->ncell = ncell;
+    s->cells.assign(ncell, CellGeo());
+    s->cell_begin.assign(ncell + 1, 0);
+    double band = 0.0;
+    int bins = 0;
+    for (int c = 0; c < ncell; c++) {
+        sys_set_box(s, H + 9 * (size_t)c);
+        CellGeo& g = s->cells[c];
+        memcpy(g.h6, s->box.h6, sizeof(g.h6));
+        memcpy(g.b6, s->box.b6, sizeof(g.b6));
+        const double S[3] = {8.0 * s->nb[0], 8.0 * s->nb[1], 8.0 * s->nb[2]};
+        g.bs[0] = g.b6[0] * S[0];
+        g.bs[1] = g.b6[1] * S[0];
+        g.bs[2] = g.b6[2] * S[0];
+        g.bs[3] = g.b6[3] * S[1];
+        g.bs[4] = g.b6[4] * S[1];
+        g.bs[5] = g.b6[5] * S[2];
+        memcpy(g.G, s->frame.G, sizeof(g.G));
+        memcpy(g.Glo, s->frame.Glo, sizeof(g.Glo));
+        for (int d = 0; d < 3; d++) g.nb[d] = s->nb[d];
+        g.bin_base = bins;
+        g.ortho = s->frame.ortho;
+        bins += s->nbins;
+        band = std::max(band, s->band);
+        s->cell_begin[c + 1] = s->cell_begin[c] + natoms[c];
+        g.begin = s->cell_begin[c];
+        g.end = s->cell_begin[c + 1];
+    }
+    sys_set_box(s, H);  // cell 0
+    s->nbins = bins;
+    s->band = band;
+    // chunks of at most kChunk atoms, never across cells
+    s->chunk_begin_h.clear();
+    s->cell_chunk_h.assign(ncell + 1, 0);
+    std::vector<int> chunk_cell;
+    for (int c = 0; c < ncell; c++) {
+        for (int a = s->cell_begin[c]; a < s->cell_begin[c + 1]; a += kChunk) {
+            s->chunk_begin_h.push_back(a);
+            chunk_cell.push_back(c);
+        }
+        s->cell_chunk_h[c + 1] = (int)s->chunk_begin_h.size();
+    }
+    s->nchunk = (int)s->chunk_begin_h.size();
+    s->chunk_begin_h.push_back(s->cell_begin[ncell]);
+    s->cells_chunk_cell_h = chunk_cell;
+}
+
 int grid_for(mappg_sys* s, long long threads, int block) {
     long long g = (threads + block - 1) / block;
     long long cap = (long long)s->sm_count * 8;
@@ -190,6 +240,41 @@ __global__ void k_wrap_bin(int n, double* __restrict__ x, double* __restrict__ s
     if (bad) sc->bad = 1;
 }
 
+// batch variant of step 1: each atom uses its cell's box, bins and drift
+__global__ void k_wrap_bin_b(int n, double* __restrict__ x, double* __restrict__ s, const CellGeo* __restrict__ cells,
+                             const int* __restrict__ cell_of, const CellMd* __restrict__ cmd, int* __restrict__ binc,
+                             int* __restrict__ binid, int* __restrict__ bin_count, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int c = cell_of[i];
+        const CellGeo& g = cells[c];
+        const double* dr = cmd[c].drift;
+        double x0 = dsub(x[i], dr[0]), x1 = dsub(x[n + i], dr[1]), x2 = dsub(x[2 * n + i], dr[2]);
+        double s0 = dadd(dmul(g.b6[0], x0), dadd(dmul(g.b6[1], x1), dmul(g.b6[2], x2)));
+        s0 = wrap01(s0, &bad);
+        double s1 = dadd(dmul(g.b6[3], x1), dmul(g.b6[4], x2));
+        s1 = wrap01(s1, &bad);
+        double s2 = dmul(x2, g.b6[5]);
+        s2 = wrap01(s2, &bad);
+        s2x(g.h6, s0, s1, s2, x0, x1, x2);
+        x[i] = x0;
+        x[n + i] = x1;
+        x[2 * n + i] = x2;
+        s[i] = s0;
+        s[n + i] = s1;
+        s[2 * n + i] = s2;
+        int b0 = min((int)(s0 * g.nb[0]), g.nb[0] - 1);
+        int b1 = min((int)(s1 * g.nb[1]), g.nb[1] - 1);
+        int b2 = min((int)(s2 * g.nb[2]), g.nb[2] - 1);
+        binc[i] = b0 | (b1 << 10) | (b2 << 20);
+        int b = g.bin_base + b0 + g.nb[0] * (b1 + g.nb[1] * b2);
+        binid[i] = b;
+        atomicAdd(&bin_count[b], 1);
+    }
+    if (bad) sc->bad = 1;
+}
+
 // rebuild step 2: exclusive scan of bin counts (one block), counts zeroed
 __global__ void k_scan_bins(int nbins, int* __restrict__ bin_count, int* __restrict__ bin_start, DevScalars* sc) {
     if (!sc->rebuild) return;
@@ -277,6 +362,20 @@ __global__ void k_shadow(int n, const double* __restrict__ x, const int* __restr
     }
 }
 
+__global__ void k_shadow_b(int n, const double* __restrict__ x, const int* __restrict__ binc,
+                           const CellGeo* __restrict__ cells, const int* __restrict__ cell_of,
+                           float4* __restrict__ p32, float4* __restrict__ p0, int gated, DevScalars* sc) {
+    if (gated && !sc->rebuild) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const CellGeo& cg = cells[cell_of[i]];
+        Geo g;
+        for (int k = 0; k < 6; k++) g.bs[k] = cg.bs[k];
+        float4 p = frame_pos(g, x[i], x[n + i], x[2 * n + i], binc[i]);
+        p32[i] = p;
+        if (gated) p0[i] = p;
+    }
+}
+
 struct BuildArgs {
     int n, maxnbr, ne;
     const double* x;
@@ -293,10 +392,13 @@ struct BuildArgs {
     Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
     double cut_sk_sq[kMaxElem * kMaxElem];
+    const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
+    const int* cell_of;
 };
 
 // frame displacement to Cartesian: dx' G with G as head + tail
-__device__ __forceinline__ void frame_to_cart(const Frame& fr, float a, float b, float c, float& x, float& y,
+template <class FR>
+__device__ __forceinline__ void frame_to_cart(const FR& fr, float a, float b, float c, float& x, float& y,
                                               float& z) {
     if (fr.ortho) {
         x = fmaf(a, fr.G[0][0], a * fr.Glo[0][0]);
@@ -312,6 +414,7 @@ __device__ __forceinline__ void frame_to_cart(const Frame& fr, float a, float b,
 
 // rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
 // candidates, ballots keep the row in (bin, index) order; x0 <- x
+template <bool BATCH>
 __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc) {
     if (!sc->rebuild) return;
     __shared__ float4 off[27];
@@ -326,6 +429,12 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
     long long sumrow = 0;
     int overflow = 0;
     for (int i = warp; i < n; i += nw) {
+        // the atom's cell: its bins, frame and box (the system's for one cell)
+        const CellGeo* cg = BATCH ? a.cells + a.cell_of[i] : nullptr;
+        const int nbx = BATCH ? cg->nb[0] : a.g.nb[0], nby = BATCH ? cg->nb[1] : a.g.nb[1],
+                  nbz = BATCH ? cg->nb[2] : a.g.nb[2];
+        const int bin_base = BATCH ? cg->bin_base : 0;
+        const double* h6 = BATCH ? cg->h6 : a.g.h6;
         float4 pi = a.p32[i];
         int ei = a.elem[i];
         int bc = a.binc[i];
@@ -336,11 +445,11 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         for (int c = 0; c < 27; c++) {
             int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
             int u0 = bi[0] + d0, u1 = bi[1] + d1, u2 = bi[2] + d2;
-            int n0 = u0 < 0 ? -1 : (u0 >= a.g.nb[0] ? 1 : 0);
-            int n1 = u1 < 0 ? -1 : (u1 >= a.g.nb[1] ? 1 : 0);
-            int n2 = u2 < 0 ? -1 : (u2 >= a.g.nb[2] ? 1 : 0);
-            int w0 = u0 - n0 * a.g.nb[0], w1 = u1 - n1 * a.g.nb[1], w2 = u2 - n2 * a.g.nb[2];
-            int b = w0 + a.g.nb[0] * (w1 + a.g.nb[1] * w2);
+            int n0 = u0 < 0 ? -1 : (u0 >= nbx ? 1 : 0);
+            int n1 = u1 < 0 ? -1 : (u1 >= nby ? 1 : 0);
+            int n2 = u2 < 0 ? -1 : (u2 >= nbz ? 1 : 0);
+            int w0 = u0 - n0 * nbx, w1 = u1 - n1 * nby, w2 = u2 - n2 * nbz;
+            int b = bin_base + w0 + nbx * (w1 + nby * w2);
             int lo = a.bin_start[b], hi = a.bin_start[b + 1];
             float4 o = off[c];
             bool self_img = (n0 | n1 | n2) == 0;
@@ -354,8 +463,12 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
                         float4 pj = a.p32[j];
                         ej = a.elem[j];
                         float dx, dy, dz;
-                        frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
-                                      dz);
+                        if (BATCH)
+                            frame_to_cart(*cg, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx,
+                                          dy, dz);
+                        else
+                            frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx,
+                                          dy, dz);
                         float r2 = dx * dx + (dy * dy + dz * dz);
                         int pe = ei * a.ne + ej;
                         if (r2 < a.lo2[pe]) {
@@ -370,7 +483,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
                             if (n2 > 0) s2 = dadd(s2, 1.0);
                             if (n2 < 0) s2 = dsub(s2, 1.0);
                             double xj0, xj1, xj2;
-                            s2x(a.g.h6, s0, s1, s2, xj0, xj1, xj2);
+                            s2x(h6, s0, s1, s2, xj0, xj1, xj2);
                             double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
                             double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
                             keep = rsq < a.cut_sk_sq[pe];
@@ -404,6 +517,16 @@ __global__ void k_rebuild_done(DevScalars* sc) {
     if (!sc->rebuild) return;
     sc->nrebuild++;
     sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
+}
+
+__global__ void k_rebuild_done_b(DevScalars* sc, CellMd* cmd, int ncell) {
+    if (!sc->rebuild) return;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x)
+        cmd[c].drift[0] = cmd[c].drift[1] = cmd[c].drift[2] = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->nrebuild++;
+        sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
+    }
 }
 
 // skin test of DynamicMD::decide (dynamic_md.cpp:90-105): rebuild when any
@@ -462,6 +585,12 @@ void request_rebuild(mappg_sys* s) {
 }
 
 void launch_shadow(mappg_sys* s, bool gated) {
+    if (s->ncell > 1) {
+        k_shadow_b<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->cells_dev, s->cell_of,
+                                                                   s->p32, s->p0, gated ? 1 : 0, s->sc);
+        MAPPG_CUDA(cudaGetLastError());
+        return;
+    }
     Geo g = make_geo(s);
     k_shadow<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, gated ? 1 : 0,
                                                             s->sc);
@@ -472,13 +601,21 @@ void launch_rebuild_chain(mappg_sys* s) {
     Geo g = make_geo(s);
     const int B = 256;
     int gb = grid_for(s, s->n, B);
-    k_wrap_bin<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, g, s->binc, s->binid, s->bin_count, s->sc);
+    const bool batch = s->ncell > 1;
+    if (batch)
+        k_wrap_bin_b<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, s->cells_dev, s->cell_of, s->cmd, s->binc, s->binid,
+                                              s->bin_count, s->sc);
+    else
+        k_wrap_bin<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, g, s->binc, s->binid, s->bin_count, s->sc);
     k_scan_bins<<<1, 1024, 0, s->stream>>>(s->nbins, s->bin_count, s->bin_start, s->sc);
     int* bin_tmp = s->bin_atoms + s->n;
     k_scatter_bins<<<gb, B, 0, s->stream>>>(s->n, s->binid, s->bin_start, s->bin_count, bin_tmp, s->sc);
     k_sort_bins<<<grid_for(s, (long long)s->nbins * 32, B), B, 0, s->stream>>>(s->nbins, s->bin_start, bin_tmp,
                                                                                s->bin_atoms, s->bin_count, s->sc);
-    k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, 1, s->sc);
+    if (batch)
+        k_shadow_b<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->cells_dev, s->cell_of, s->p32, s->p0, 1, s->sc);
+    else
+        k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, 1, s->sc);
     BuildArgs a;
     a.n = s->n;
     a.maxnbr = s->maxnbr;
@@ -500,8 +637,15 @@ void launch_rebuild_chain(mappg_sys* s) {
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
     }
     a.fr = s->frame;
-    k_build_list<<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
-    k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
+    a.cells = s->cells_dev;
+    a.cell_of = s->cell_of;
+    if (batch) {
+        k_build_list<true><<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
+        k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->ncell);
+    } else {
+        k_build_list<false><<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
+        k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
+    }
     MAPPG_CUDA(cudaGetLastError());
 }
 
@@ -551,6 +695,12 @@ EamArgs eam_args(mappg_sys* s) {
     for (int e = 0; e < s->ne; e++) a.mass32[e] = (float)s->masses[e];
     a.partials = s->partials;
     a.sc = s->sc;
+    a.ncell = s->ncell;
+    a.nchunk = s->nchunk;
+    a.cells = s->cells_dev;
+    a.chunk_begin = s->chunk_begin;
+    a.chunk_cell = s->chunk_cell;
+    a.chunk_part = s->chunk_part;
     return a;
 }
 
@@ -575,7 +725,9 @@ static void dev_alloc(void** p, size_t bytes) { MAPPG_CUDA(cudaMalloc(p, bytes >
 void sys_free(mappg_sys* s) {
     void* ptrs[] = {s->x, s->v, s->f, s->x0, s->s, s->elem, s->id, s->inv, s->p32, s->q32, s->p0, s->f32, s->v32,
                     s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
-                    s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev};
+                    s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev, s->cells_dev, s->cell_of,
+                    s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp, s->cmd,
+                    s->cell_out};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -598,18 +750,25 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
     const int n = s->n;
     MAPPG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     // fixed atom order: Morton order of the initial bins, then caller index
+    // (a batch: cell by cell, Morton order within each cell)
     std::vector<unsigned long long> key(n);
-    const double* b6 = s->box.b6;
-    for (int u = 0; u < n; u++) {
-        const double* xu = x_host + 3 * (size_t)u;
-        double sv[3] = {b6[0] * xu[0] + (b6[1] * xu[1] + b6[2] * xu[2]), b6[3] * xu[1] + b6[4] * xu[2], xu[2] * b6[5]};
-        unsigned b[3];
-        for (int d = 0; d < 3; d++) {
-            double w = sv[d] - floor(sv[d]);
-            if (!(w >= 0.0 && w < 1.0)) w = 0.0;
-            b[d] = (unsigned)std::min((int)(w * s->nb[d] * 2), 2 * s->nb[d] - 1);
+    for (int c = 0; c < s->ncell; c++) {
+        const bool batch = s->ncell > 1;
+        const double* b6 = batch ? s->cells[c].b6 : s->box.b6;
+        const int* nb = batch ? s->cells[c].nb : s->nb;
+        const int u0 = batch ? s->cell_begin[c] : 0, u1 = batch ? s->cell_begin[c + 1] : n;
+        for (int u = u0; u < u1; u++) {
+            const double* xu = x_host + 3 * (size_t)u;
+            double sv[3] = {b6[0] * xu[0] + (b6[1] * xu[1] + b6[2] * xu[2]), b6[3] * xu[1] + b6[4] * xu[2],
+                            xu[2] * b6[5]};
+            unsigned b[3];
+            for (int d = 0; d < 3; d++) {
+                double w = sv[d] - floor(sv[d]);
+                if (!(w >= 0.0 && w < 1.0)) w = 0.0;
+                b[d] = (unsigned)std::min((int)(w * nb[d] * 2), 2 * nb[d] - 1);
+            }
+            key[u] = ((unsigned long long)c << 40) | morton3(b[0], b[1], b[2]);
         }
-        key[u] = morton3(b[0], b[1], b[2]);
     }
     s->host_id.resize(n);
     std::iota(s->host_id.begin(), s->host_id.end(), 0);
@@ -646,6 +805,32 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
     MAPPG_CUDA(cudaMemsetAsync(s->f, 0, nd, s->stream));
     MAPPG_CUDA(cudaMemcpyAsync(s->id, s->host_id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
     MAPPG_CUDA(cudaMemcpyAsync(s->inv, inv.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    if (s->ncell > 1) {
+        const int nc = s->ncell, nk = s->nchunk;
+        std::vector<int> cell_of(n);
+        for (int c = 0; c < nc; c++)
+            for (int i = s->cell_begin[c]; i < s->cell_begin[c + 1]; i++) cell_of[i] = c;
+        dev_alloc((void**)&s->cells_dev, sizeof(CellGeo) * nc);
+        dev_alloc((void**)&s->cell_of, sizeof(int) * n);
+        dev_alloc((void**)&s->chunk_begin, sizeof(int) * (nk + 1));
+        dev_alloc((void**)&s->chunk_cell, sizeof(int) * nk);
+        dev_alloc((void**)&s->cell_chunk, sizeof(int) * (nc + 1));
+        dev_alloc((void**)&s->chunk_part, sizeof(double) * kChunkSlots * (size_t)nk);
+        dev_alloc((void**)&s->chunk_disp, sizeof(double) * 4 * (size_t)nk);
+        dev_alloc((void**)&s->cmd, sizeof(CellMd) * nc);
+        dev_alloc((void**)&s->cell_out, sizeof(double) * 8 * nc);
+        MAPPG_CUDA(cudaMemsetAsync(s->cmd, 0, sizeof(CellMd) * nc, s->stream));
+        MAPPG_CUDA(cudaMemsetAsync(s->chunk_part, 0, sizeof(double) * kChunkSlots * (size_t)nk, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(s->cells_dev, s->cells.data(), sizeof(CellGeo) * nc, cudaMemcpyHostToDevice,
+                                   s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(s->cell_of, cell_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(s->chunk_begin, s->chunk_begin_h.data(), sizeof(int) * (nk + 1),
+                                   cudaMemcpyHostToDevice, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(s->chunk_cell, s->cells_chunk_cell_h.data(), sizeof(int) * nk,
+                                   cudaMemcpyHostToDevice, s->stream));
+        MAPPG_CUDA(cudaMemcpyAsync(s->cell_chunk, s->cell_chunk_h.data(), sizeof(int) * (nc + 1),
+                                   cudaMemcpyHostToDevice, s->stream));
+    }
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
 }
 
@@ -702,6 +887,11 @@ void sys_build(mappg_sys* s) {
     throw Error{MAPPG_ERR_NBR, "neighbour list capacity could not be sized"};
 }
 
+// the cell of atom i (bin-sorted order) of a batch
+static int cell_of_host(const mappg_sys* s, int i) {
+    return (int)(std::upper_bound(s->cell_begin.begin(), s->cell_begin.end(), i) - s->cell_begin.begin()) - 1;
+}
+
 void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
     const int n = s->n;
     std::vector<int> nn(n), bc(n);
@@ -736,9 +926,10 @@ void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
             int j = entry_j(e), c = entry_code(e);
             int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
             out[4 * k] = s->host_id[j];
+            const int* nbq = s->ncell > 1 ? s->cells[cell_of_host(s, i)].nb : s->nb;
             for (int q = 0; q < 3; q++) {
                 int uq = b[q] + d[q];
-                out[4 * k + 1 + q] = uq < 0 ? -1 : (uq >= s->nb[q] ? 1 : 0);
+                out[4 * k + 1 + q] = uq < 0 ? -1 : (uq >= nbq[q] ? 1 : 0);
             }
         }
     }

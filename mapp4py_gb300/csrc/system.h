@@ -86,6 +86,40 @@ struct Frame {
     int ortho;         // H has no off-diagonal terms
 };
 
+// one cell of a batch (several independent periodic cells in one system):
+// its box, bins and scaled frame, read per atom by the batch kernels
+struct CellGeo {
+    double h6[6], b6[6];   // H and its inverse, lower-triangular packed
+    double bs[6];          // b6 with column d scaled by 8 nb_d: x -> s'
+    float G[3][3];         // scaled frame to Cartesian, head
+    float Glo[3][3];       // tail
+    int nb[3];             // bins per axis
+    int bin_base;          // first global bin index of the cell
+    int begin, end;        // atom range (bin-sorted order)
+    int ortho;
+    int pad;
+};
+
+// per-cell dynamic state of a batch (the DevScalars fields that are per cell)
+struct CellMd {
+    double T, ndof, ndof_kB;  // thermostat target and degrees of freedom
+    double eta[kMaxChain];
+    double mvv[6];
+    double T_part;
+    double fac_x_d, fac_close, kickA, kickB;
+    double energy, e_embed, virial[6];
+    double com[3], drift[3];
+    long long step;           // steps done in this run
+    int pending_kick, pad;
+};
+
+// a batch kernel walks chunks of at most kChunk atoms of one cell; each chunk
+// leaves kChunkSlots block sums (energy, virial, kinetic tensor, embedding
+// energy) that a per-cell kernel adds up in a fixed order
+constexpr int kChunk = 256;
+constexpr int kChunkSlots = 16;
+constexpr int kMaxCells = 1 << 16;
+
 // arguments of the EAM kernels (passed by value)
 struct EamArgs {
     int n, maxnbr, ne, nr, nrho;
@@ -124,6 +158,12 @@ struct EamArgs {
     int md_tail;
     long long nsteps;
     NhcParams nhc;
+    // batch of cells (ncell > 1): per-atom cell, chunks, per-chunk sums
+    int ncell, nchunk;
+    const CellGeo* cells;
+    const int* chunk_begin;   // nchunk + 1 atom offsets
+    const int* chunk_cell;
+    double* chunk_part;       // nchunk x kChunkSlots
 };
 
 }  // namespace mappg
@@ -175,6 +215,24 @@ struct mappg_sys {
     double* thermo_dev = nullptr; // per-step thermo rows of an NVT run
     long long thermo_cap = 0;
 
+    // batch of independent cells (ncell > 1); a single cell leaves these empty
+    int ncell = 1;
+    std::vector<mappg::CellGeo> cells;   // host copy
+    std::vector<int> cell_begin;         // ncell + 1 atom offsets
+    std::vector<int> chunk_begin_h;      // nchunk + 1
+    std::vector<int> cell_chunk_h;       // ncell + 1 chunk offsets
+    std::vector<int> cells_chunk_cell_h; // cell of each chunk
+    int nchunk = 0;
+    mappg::CellGeo* cells_dev = nullptr;
+    int* cell_of = nullptr;              // per atom
+    int* chunk_begin = nullptr;
+    int* chunk_cell = nullptr;
+    int* cell_chunk = nullptr;           // ncell + 1
+    double* chunk_part = nullptr;
+    double* chunk_disp = nullptr;        // nchunk x 4 (integrator displacement sums)
+    mappg::CellMd* cmd = nullptr;        // per-cell MD state
+    double* cell_out = nullptr;          // ncell x 8 (pe, virial6, spare) staging
+
     void* run = nullptr;  // an NVT run in progress (md.cu)
     bool built = false;
     bool have_v = false;
@@ -186,6 +244,7 @@ namespace mappg {
 
 // system.cu
 void sys_set_box(mappg_sys* s, const double* H);
+void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H);  // a batch
 void launch_rebuild_chain(mappg_sys* s);   // kernels gated by sc->rebuild
 void request_rebuild(mappg_sys* s);        // host sets the gate
 void launch_shadow(mappg_sys* s, bool gated);

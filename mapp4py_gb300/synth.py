@@ -179,3 +179,40 @@ def alloy(n, a=3.615, xB=0.5, sigma=0.0, T=0.0, vac=0.0, strain=None, seed=1):
     masses = np.array([MASS, MASS])
     v = maxwell(rng, masses[elem], T) if T > 0 else np.zeros_like(x)
     return Cell(H, x, elem, v, ("A", "B"), masses)
+
+
+def fcc_repeats(natoms, rng, min_side=4):
+    """FCC repeats (n0, n1, n2), each >= min_side, with a random aspect ratio
+    and 4*n0*n1*n2 close to natoms."""
+    cells = max(natoms / 4.0, float(min_side ** 3))
+    logs = rng.normal(0.0, 0.25, 3)
+    logs -= logs.mean()
+    side = cells ** (1.0 / 3.0) * np.exp(logs)
+    n = np.maximum(np.rint(side).astype(int), min_side)
+    return tuple(int(v) for v in n)
+
+
+def batch_cells(ncell, seed=7, nmin=500, nmax=32000, T=(100.0, 1200.0), vac=(0.0, 0.02), sigma=(0.05, 0.05),
+                strain=0.0, min_side=4):
+    """Independent A/B alloy cells: atom counts log-uniform in [nmin, nmax]
+    rounded to whole FCC repeats (every side at least min_side repeats, 14.5 A
+    for min_side 4), x_B ~ U(0,1), vacancy fraction ~ U(vac), temperature ~
+    U(T) with Maxwell-Boltzmann velocities, position noise ~ U(sigma), and a
+    random homogeneous strain up to +-strain per component (lower-triangular
+    so the box stays in MAPP's form).  Returns (cells, temperatures)."""
+    rng = np.random.default_rng(seed)
+    out, temps = [], []
+    for c in range(ncell):
+        target = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        n = fcc_repeats(target, rng, min_side)
+        xb = rng.uniform(0.0, 1.0)
+        vf = rng.uniform(*vac)
+        tc = rng.uniform(*T)
+        sg = rng.uniform(*sigma)
+        st = None
+        if strain > 0.0:
+            st = np.tril(rng.uniform(-strain, strain, (3, 3)))
+        cell = alloy(n, xB=xb, sigma=sg, T=tc, vac=vf, strain=st, seed=int(rng.integers(1 << 30)))
+        out.append(cell)
+        temps.append(tc)
+    return out, np.array(temps)

@@ -1,0 +1,124 @@
+"""Batches of independent cells (mappg_batch_*) against the same cells run
+one at a time: neighbour sets, forces, energies, virials and NVT
+trajectories, plus the mixed-precision error budget against the oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+from mapp4py_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _cells():
+    # orthorhombic cells of uneven size and composition, and strained
+    # (triclinic) ones, some small enough for 1-2 bins per axis
+    a, Ta = synth.batch_cells(4, seed=5, nmin=300, nmax=4000)
+    b, Tb = synth.batch_cells(3, seed=6, nmin=300, nmax=2500, strain=0.02)
+    return a + b, np.concatenate([Ta, Tb])
+
+
+def _keys(cnt, ent):
+    atom = np.repeat(np.arange(cnt.shape[0]), cnt)
+    rows = np.column_stack([atom, ent]).astype(np.int64)
+    return rows[np.lexsort(rows.T[::-1])]
+
+
+@pytest.fixture(scope="module")
+def ff(potentials):
+    return _lib.ForceField.setfl(potentials[("A", "B")][0])
+
+
+def test_batch_forces_match_single_cells(ff):
+    cells, _ = _cells()
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    pe, vir = b.force()
+    f = b.split(b.get_f())
+    cnt, ent = b.neighbors()
+    off = b.offsets
+    for k, c in enumerate(cells):
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+        pe1, vir1 = s.force()
+        # same rows, same order, same arithmetic: forces agree bit for bit
+        assert np.array_equal(f[k], s.get_f())
+        # energies and virials are FP32 sums per thread over other sets of
+        # atoms (chunks instead of a grid stride): equal well inside the
+        # mixed-precision budget, not bit for bit
+        assert abs(pe[k] - pe1) / c.natoms < 1e-8
+        assert np.max(np.abs(vir[k] - vir1)) <= 1e-6 * np.max(np.abs(vir1))
+        # the cell's neighbour set, in its own atom numbering
+        sel = slice(off[k], off[k + 1])
+        first = int(cnt[:off[k]].sum())
+        ek = ent[first:first + int(cnt[sel].sum())].copy()
+        ek[:, 0] -= off[k]
+        assert np.array_equal(_keys(cnt[sel], ek), _keys(*s.neighbors()))
+
+
+def test_batch_mixed_error_against_oracle(ff, potentials):
+    cells, _ = _cells()
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    pe, _ = b.force()
+    f = b.split(b.get_f())
+    e = O.Eam.setfl(potentials[("A", "B")][0])
+    for k, c in enumerate(cells):
+        o = O.System(e, c.H, c.x, c.elem, c.masses)
+        pe_o, _ = o.force()
+        rms = np.sqrt(np.mean(np.sum((f[k] - o.f) ** 2, axis=1)))
+        assert rms < 1e-5, rms
+        assert abs(pe[k] - pe_o) / c.natoms < 1e-7
+
+
+def test_batch_nvt_follows_single_cell_runs(ff):
+    cells, T = _cells()
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    b.set_v(np.concatenate([c.v for c in cells]))
+    dt = synth.FS
+    th, eta = b.nvt_run(T, dt, synth.KB, 20, thermo=True)
+    xb = b.split(b.get_x())
+    vb = b.split(b.get_v())
+    assert th.shape == (21, len(cells), 2) and np.all(np.isfinite(th))
+    for k, c in enumerate(cells):
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+        s.set_v(c.v)
+        th1, eta1 = s.nvt_run(T[k], dt, synth.KB, 20, thermo=True)
+        # the per-cell totals are summed in another order than the single
+        # cell's, and FP32 forces carry the last-bit differences along: the
+        # runs agree within the mixed-precision budget, not bit for bit
+        assert np.max(np.abs(th[:, k, 0] - th1[:, 0])) / c.natoms < 1e-7
+        assert np.max(np.abs(th[:, k, 1] - th1[:, 1])) <= 1e-5 * np.max(th1[:, 1])
+        assert np.max(np.abs(eta[k] - eta1)) <= 1e-6 * max(1.0, np.max(np.abs(eta1)))
+        d = xb[k] - s.get_x()
+        d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
+        assert np.max(np.abs(d)) < 1e-5
+        v1 = s.get_v()
+        assert np.max(np.abs(vb[k] - v1)) < 1e-5 * np.max(np.abs(v1))
+
+
+def test_batch_refuses_single_cell_calls(ff):
+    cells, _ = _cells()
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells[:2]], cells[0].masses)
+    with pytest.raises(_lib.MappgError):
+        _lib.System.force(b)
+    with pytest.raises(_lib.MappgError):
+        _lib.System.nvt_run(b, 300.0, synth.FS, synth.KB, 1)
+    with pytest.raises(_lib.MappgError):
+        _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells[:2]], cells[0].masses, precision=_lib.FP64)
+
+
+def test_batch_lbfgs_follows_single_cells(ff):
+    """Each cell of a batched relaxation runs the single-cell iteration: the
+    first iterations agree with mappg_lbfgs_run on the cell alone to
+    rounding, and well-conditioned cells all reach the force tolerance."""
+    cells = [synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2 + k, vac=0.01) for k in range(3)]
+    cells += [synth.alloy((3, 4, 5), xB=0.6, sigma=0.08, seed=9, vac=0.0)]
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    r5 = b.lbfgs_run(m=10, f_tol=1e-4, nsteps=5)
+    for k, c in enumerate(cells):
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+        s5 = s.lbfgs_run(m=10, f_tol=1e-4, nsteps=5)
+        assert r5[k]["niter"] == s5["niter"] and r5[k]["n_energy"] == s5["n_energy"]
+        assert abs(r5[k]["pe"] - s5["pe"]) / c.natoms < 1e-7
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    r = b.lbfgs_run(m=10, f_tol=1e-4, nsteps=3000)
+    for k, c in enumerate(cells):
+        assert r[k]["err"] == 100 and r[k]["fmax"] < 1e-4, r[k]

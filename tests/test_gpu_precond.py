@@ -1,0 +1,84 @@
+"""The learned L-BFGS preconditioner: the tensor-core network's loss and
+gradient against the CPU restatement (oracle/mlp_ref.py), the
+finite-difference Hessian diagonals against the oracle's forces, training,
+and what the trained network gains over plain L-BFGS."""
+import numpy as np
+import pytest
+
+import mlp_ref as R
+import oracle as O
+from mapp4py_gb300 import _lib, precond, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ff(potentials):
+    return _lib.ForceField.setfl(potentials[("A", "B")][0])
+
+
+def test_network_gradient_matches_oracle():
+    rng = np.random.default_rng(1)
+    net = _lib.Mlp(seed=3)
+    n = 300  # two full tiles of 128 atoms and a partial one
+    feat = rng.normal(size=(n, 33)).astype(np.float32) * 2.0 + 1.0
+    target = np.exp(rng.normal(1.5, 0.5, size=(n, 3))).astype(np.float32)
+    mean = feat.mean(axis=0).astype(np.float32)
+    sdev = feat.std(axis=0).astype(np.float32)
+    w, _, _ = net.params()
+    w = w + rng.normal(0.0, 0.05, w.shape).astype(np.float32)  # not the initial zeros of the biases
+    net.set_params(w, mean, sdev)
+    loss, g = net.grad(feat, target)
+    X = R.inputs(feat, mean, sdev)
+    loss_ref, g_ref = R.loss_grad(w, X, target.astype(np.float64))
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    scale = np.max(np.abs(g_ref))
+    assert np.max(np.abs(g - g_ref)) <= 2e-2 * scale, np.max(np.abs(g - g_ref)) / scale
+    assert np.corrcoef(g, g_ref)[0, 1] > 0.9999
+    y = net.predict(feat)
+    _, _, Z3 = R.forward(w, X)
+    y_ref = R.softplus(Z3[:, :3])
+    assert np.max(np.abs(y - y_ref) / y_ref) < 1e-2
+
+
+def test_hessian_diagonal_matches_oracle_differences(ff, potentials):
+    rng = np.random.default_rng(2)
+    H, x, elem, col = precond.alloy_cell((4, 4, 4), rng, 0.5, 0.02, 0.05)
+    s = _lib.System(ff, H, x, elem, [synth.MASS, synth.MASS])
+    hd = _lib.hessian_diag(s, col, 1e-4)
+    # the system is left where it was
+    d = s.get_x() - x
+    d -= np.round(d @ np.linalg.inv(H)) @ H
+    assert np.max(np.abs(d)) < 1e-12
+    e = O.Eam.setfl(potentials[("A", "B")][0])
+    h = 1e-4
+    for a in rng.choice(len(x), 5, replace=False):
+        for ax in range(3):
+            fs = []
+            for sg in (1, -1):
+                xp = x.copy()
+                xp[a, ax] += sg * h
+                o = O.System(e, H, xp, elem, [synth.MASS, synth.MASS])
+                o.force()
+                fs.append(o.f[a, ax])
+            ref = -(fs[0] - fs[1]) / (2 * h)
+            assert abs(hd[a, ax] - ref) <= 1e-6 * max(1.0, abs(ref)), (a, ax, hd[a, ax], ref)
+
+
+def test_training_and_preconditioned_lbfgs(ff):
+    net, losses = precond.train(ff, count=16, epochs=30, seed=5, batch=2048, n=(4, 4, 4))
+    assert np.all(np.isfinite(losses)) and losses[-1] < 0.5 * losses[0]
+    # held-out cells: the preconditioned run converges, and over several
+    # cells it needs fewer force evaluations than plain L-BFGS
+    plain, learned = 0, 0
+    for seed in range(4):
+        c = synth.alloy((5, 5, 5), xB=0.4, sigma=0.1, vac=0.01, seed=100 + seed)
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+        r0 = s.lbfgs_run(m=10, f_tol=1e-4, nsteps=5000)
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+        r1 = _lib.lbfgs_run_precond(s, net, m=10, f_tol=1e-4, nsteps=5000)
+        assert r1["err"] == 100 and r1["fmax"] < 1e-4
+        plain += r0["n_force"] + r0["n_energy"]
+        learned += r1["n_force"] + r1["n_energy"]
+    print("force+energy evaluations, plain %d, learned %d" % (plain, learned))
+    assert learned < plain
