@@ -213,6 +213,14 @@ int mappg_sys_enqueue(mappg_sys* sys, int what);
 int mappg_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f_tol, double c,
                     double rho, double min_alpha, int nsteps, double* stats);
 
+/* md.min_cg(e_tol,max_dx,ls=ls_bt(c,rho,min_alpha)).run(atoms,nsteps):
+ * Polak-Ribiere conjugate gradients (MinCG::__run, min_cg.h:454-536) over
+ * the back-tracking line search with the previous-step cap (init_flag 1,
+ * ls.h:711-769), with an added stop at max|F| < f_tol (f_tol <= 0 disables
+ * it).  stats as mappg_lbfgs_run. */
+int mappg_cg_run(mappg_sys* sys, double e_tol, double max_dx, double f_tol, double c, double rho,
+                 double min_alpha, int nsteps, double* stats);
+
 /* ------------------------------------------------------- batches of cells */
 
 /* Several independent periodic cells (ncell >= 2) in one system, for runs

@@ -64,6 +64,8 @@ SIGNATURES = {
     "mappg_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_int, _D]),
     "mappg_sys_autotune": (C.c_int, [_VP, _I, _D]),
+    "mappg_cg_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                               C.c_int, _D]),
     "mappg_batch_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_double, C.c_int, _D]),
     "mappg_batch_lbfgs_run_precond": (C.c_int, [_VP, _VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -334,6 +336,13 @@ class System:
 
     def enqueue(self, what):
         check(load().mappg_sys_enqueue(self.h, int(what)))
+
+    def cg_run(self, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000):
+        st = np.zeros(6)
+        check(load().mappg_cg_run(self.h, float(e_tol), float(max_dx), float(f_tol), float(c), float(rho),
+                                  float(min_alpha), int(nsteps), dptr(st)))
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
 
     def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000):
         st = np.zeros(6)

@@ -36,6 +36,8 @@ void nvt_end(mappg_sys* s, double* eta, double* thermo);
 void nvt_free(mappg_sys* s);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
+void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
+            int nsteps, double* stats);
 void launch_density_only(mappg_sys* s);
 void launch_force_only(mappg_sys* s);
 
@@ -793,6 +795,15 @@ int mappg_sys_enqueue(mappg_sys* s, int what) {
                 break;
             default: throw Error{MAPPG_ERR_ARG, "unknown kernel selector"};
         }
+    });
+}
+
+int mappg_cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c, double rho, double min_alpha,
+                 int nsteps, double* stats) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "conjugate gradients run per single cell"};
+        cg_run(s, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats);
     });
 }
 

@@ -37,7 +37,7 @@ enum BlState { BL_RUN = 0, BL_PLAIN = 1, BL_LS = 2, BL_ACCEPT = 3, BL_DONE = 4 }
 enum BlErr { BL_S = 0, BL_DOWNHILL = 1, BL_GRAD0 = 2, BL_MIN_ALPHA = 3, BL_ETOL = 4, BL_MAXITER = 5, BL_FTOL = 100 };
 
 struct BlCell {
-    double gamma, rho[kBlMaxHist], alpha[kBlMaxHist];
+    double gamma, tau, rho[kBlMaxHist], alpha[kBlMaxHist];
     double dot;
     double fh, hh, hmax, fmax;
     double e_curr, e_prev, e0, a, dfa, pe;
@@ -124,7 +124,8 @@ __global__ void k_bl_start(BlArgs a, int st) {
 //   mode 0: dot = V[slot(i)].h only
 //   mode 1: h += alpha_i Y[slot(i)] with alpha_i = -rho dot (first loop)
 //   mode 2: h += (-alpha_i - rho dot) S[slot(i)]      (second loop)
-//   mode 3: h *= gamma, mode 4: h *= P
+//   mode 3: h *= gamma, mode 4: h *= tau P (the learned diagonal, scaled
+//   by (s.y)/(y.P.y) of the newest pair)
 // then the partial of the next dot, Vn[slot(i_next)].h (none if Vn null)
 __global__ void __launch_bounds__(256) k_bl_step(BlArgs a, int st, int mode, int i, const double* __restrict__ Vu,
                                                  const double* __restrict__ Vn, int i_next) {
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(256) k_bl_step(BlArgs a, int st, int mode, int
                 double hv = a.h[j];
                 if ((mode == 1 || mode == 2) && coef != 0.0) hv += coef * Vu[(size_t)su * N3 + j];
                 if (mode == 3) hv *= coef;
-                if (mode == 4) hv *= a.P[j];
+                if (mode == 4) hv *= c.tau * a.P[j];
                 if (mode) a.h[j] = hv;
                 if (dot_on) acc += Vn[(size_t)sn * N3 + j] * hv;
             }
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(256) k_bl_hist(BlArgs a) {
         const BlCell& c = a.cs[a.chunk_cell[ch]];
         const bool on = c.state == BL_ACCEPT;
         const int hd = (c.head + 1) % a.m;
-        double v[3] = {0.0, 0.0, 0.0};
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
         for (int ii = a.chunk_begin[ch] + threadIdx.x; on && ii < a.chunk_begin[ch + 1]; ii += blockDim.x)
             for (int q = 0; q < 3; q++) {
                 const size_t j = (size_t)q * n + ii;
@@ -334,9 +335,10 @@ __global__ void __launch_bounds__(256) k_bl_hist(BlArgs a) {
                 v[0] += sv * yv;
                 v[1] += yv * yv;
                 v[2] = fmax(v[2], fabs(a.f[j]));
+                if (a.P) v[3] += yv * yv * a.P[j];
             }
-        const int op[3] = {0, 0, 1};
-        bl_store<3>(v, op, a.part + (size_t)ch * 4);
+        const int op[4] = {0, 0, 1, 0};
+        bl_store<4>(v, op, a.part + (size_t)ch * 4);
     }
 }
 
@@ -346,6 +348,7 @@ __global__ void k_bl_cells_step(BlArgs a) {
     const double sy = bl_cell_total(a, c, 0, false);
     const double yy = bl_cell_total(a, c, 1, false);
     const double fm = bl_cell_total(a, c, 2, true);
+    const double ypy = bl_cell_total(a, c, 3, false);
     if ((threadIdx.x & 31) != 0) return;
     BlCell& cs = a.cs[c];
     if (cs.state != BL_ACCEPT) return;
@@ -365,8 +368,14 @@ __global__ void k_bl_cells_step(BlArgs a) {
     if (a.m > 0) {
         cs.head = (cs.head + 1) % a.m;
         if (cs.k != a.m) cs.k++;
-        cs.rho[cs.head] = 1.0 / sy;
-        cs.gamma = sy / yy;
+        // a pair without positive curvature takes no part (rho = 0)
+        if (sy > 0.0 && yy > 0.0) {
+            cs.rho[cs.head] = 1.0 / sy;
+            cs.gamma = sy / yy;
+            if (ypy > 0.0) cs.tau = sy / ypy;
+        } else {
+            cs.rho[cs.head] = 0.0;
+        }
     }
     cs.state = BL_RUN;
 }
@@ -380,6 +389,7 @@ __global__ void k_bl_cells_open(BlArgs a) {
     BlCell& cs = a.cs[c];
     memset(&cs, 0, sizeof(BlCell));
     cs.gamma = 1.0;  // min_l-bfgs.h:140
+    cs.tau = 1.0;
     cs.e_curr = a.cmd[c].energy;
     cs.pe = cs.e_curr;
     cs.fmax = fm;
@@ -393,6 +403,25 @@ __global__ void k_bl_cells_open(BlArgs a) {
         cs.err = BL_FTOL;
         cs.state = BL_DONE;
     }
+}
+
+// cells whose mixed-precision search stalled above f_tol go on with FP64
+// forces from where they stopped (history dropped)
+__global__ void k_bl_revive(BlArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    BlCell& cs = a.cs[c];
+    if (!(cs.state == BL_DONE && cs.err == BL_MIN_ALPHA)) return;
+    cs.state = BL_RUN;
+    cs.err = BL_S;
+    cs.k = 0;
+    cs.gamma = 1.0;
+    cs.tau = 1.0;
+    cs.head = a.m - 1;
+    cs.a = 0.0;
+    cs.e_curr = a.cmd[c].energy;
+    cs.n_fc++;
+    atomicAdd(a.count, 1);
 }
 
 __global__ void k_bl_count(BlArgs a, int st) {
@@ -488,6 +517,26 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
     k_bl_prep<<<gc, 256, 0, st>>>(a, -1);
     k_bl_cells_open<<<gw, 256, 0, st>>>(a);
     MAPPG_CUDA(cudaGetLastError());
+    struct Promote {
+        mappg_sys* s;
+        ~Promote() { s->force64 = false; }
+    } promote{s};
+    for (int phase = 0; phase < 2; phase++) {
+    if (phase == 1) {
+        // mixed cells that stalled above f_tol: FP64 forces from here on
+        if (!(s->precision == MAPPG_MIXED && f_tol > 0.0)) break;
+        s->force64 = true;
+        lb_update(s);
+        launch_force(s);
+        sync_forces64(s);
+        launch_energy64(s);
+        MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+        k_bl_revive<<<g1, 256, 0, st>>>(a);
+        int nrev = 0;
+        MAPPG_CUDA(cudaMemcpyAsync(&nrev, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MAPPG_CUDA(cudaStreamSynchronize(st));
+        if (nrev == 0) break;
+    }
     while (count(BL_RUN) > 0) {
         // direction: learned (or plain) two-loop for the running cells
         two_loop(BL_RUN, P != nullptr);
@@ -522,6 +571,7 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
         k_bl_hist<<<gc, 256, 0, st>>>(a);
         k_bl_cells_step<<<gw, 256, 0, st>>>(a);
         MAPPG_CUDA(cudaGetLastError());
+    }
     }
     DevScalars hs;
     std::vector<BlCell> cs(nc);

@@ -64,6 +64,42 @@ struct Pos64 {
     }
 };
 
+// batch: atom i's position and image flags from its cell's bins; image
+// shifts n*H from the cell's box
+struct PosCell {
+    double x, y, z;
+    int lo[3], hi[3];
+    double h6[6];
+    __device__ __forceinline__ void load(const EamArgs& a, const int* cell_of, int i) {
+        const CellGeo& g = a.cells[cell_of[i]];
+        x = a.x[i];
+        y = a.x[a.n + i];
+        z = a.x[2 * a.n + i];
+        const int bc = a.binc[i];
+        const int b[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
+        for (int d = 0; d < 3; d++) {
+            lo[d] = b[d] == 0;
+            hi[d] = b[d] == g.nb[d] - 1;
+        }
+        for (int k = 0; k < 6; k++) h6[k] = g.h6[k];
+    }
+    __device__ __forceinline__ void delta(const EamArgs& a, const double (*)[3], int e, double& dx, double& dy,
+                                          double& dz) const {
+        const int j = entry_j(e), c = entry_code(e);
+        const int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
+        const int n0 = (d0 < 0 && lo[0]) ? -1 : ((d0 > 0 && hi[0]) ? 1 : 0);
+        const int n1 = (d1 < 0 && lo[1]) ? -1 : ((d1 > 0 && hi[1]) ? 1 : 0);
+        const int n2 = (d2 < 0 && lo[2]) ? -1 : ((d2 > 0 && hi[2]) ? 1 : 0);
+        // rows of H: (h0,0,0), (h1,h3,0), (h2,h4,h5)
+        const double s0 = n0 * h6[0] + n1 * h6[1] + n2 * h6[2];
+        const double s1 = n1 * h6[3] + n2 * h6[4];
+        const double s2 = n2 * h6[5];
+        dx = x - (__ldg(a.x + j) + s0);
+        dy = y - (__ldg(a.x + a.n + j) + s1);
+        dz = z - (__ldg(a.x + 2 * a.n + j) + s2);
+    }
+};
+
 struct Smem64 {
     double sh[27][3];
     double cut_sq[kMaxElem * kMaxElem];
@@ -99,6 +135,71 @@ __device__ __forceinline__ int knot64(double r, const EamArgs& a, double& p) {
     return m;
 }
 
+// one lane's share of atom i's density (FP64)
+template <int TPA, class POS>
+__device__ __forceinline__ double density64_lane(const EamArgs& a, const Smem64& S, const POS& P, int ei, int i,
+                                                 int lane) {
+    double acc = 0.0;
+    const int nn = __ldg(a.nnbr + i);
+    const int* row = a.nbr + (size_t)i * a.maxnbr;
+    for (int k = lane; k < nn; k += TPA) {
+        const int e = __ldg(row + k);
+        const int ej = entry_elem(e);
+        double dx, dy, dz;
+        P.delta(a, S.sh, e, dx, dy, dz);
+        double rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq < S.cut_sq[ei * a.ne + ej]) {
+            double p;
+            int m = knot64(sqrt(rsq), a, p);
+            acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+        }
+    }
+    return acc;
+}
+
+// one lane's share of atom i's force, pair energy and virial (FP64)
+template <int TPA, class POS>
+__device__ __forceinline__ void force64_lane(const EamArgs& a, const Smem64& S, const POS& P, int ei, double dFi,
+                                             int i, int lane, double& fx, double& fy, double& fz, double& ep,
+                                             double (&w)[6]) {
+    const double dri = a.dr_inv;
+    const int nn = __ldg(a.nnbr + i);
+    const int* row = a.nbr + (size_t)i * a.maxnbr;
+    for (int k = lane; k < nn; k += TPA) {
+        const int e = __ldg(row + k);
+        const int ej = entry_elem(e);
+        double dx, dy, dz;
+        P.delta(a, S.sh, e, dx, dy, dz);
+        double rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq < S.cut_sq[ei * a.ne + ej]) {
+            const int j = entry_j(e);
+            const double r = sqrt(rsq);
+            const double rinv = 1.0 / r;
+            double p;
+            const int m = knot64(r, a, p);
+            const double der_i = spl_der(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p) * dri;
+            double der_j = der_i;
+            if (ej != ei) der_j = spl_der(ldg4(a.rho64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) * dri;
+            const Dbl4 cz = ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m);
+            const double z = spl_val(cz, p);
+            const double zp = spl_der(cz, p) * dri;
+            const double phi = z * rinv;
+            const double dphi = zp * rinv - phi * rinv;
+            const double fp = -(dphi + dFi * der_i + __ldg(a.dF + j) * der_j) * rinv;
+            fx += fp * dx;
+            fy += fp * dy;
+            fz += fp * dz;
+            ep += phi;
+            w[0] += fp * dx * dx;
+            w[1] += fp * dx * dy;
+            w[2] += fp * dx * dz;
+            w[3] += fp * dy * dy;
+            w[4] += fp * dy * dz;
+            w[5] += fp * dz * dz;
+        }
+    }
+}
+
 template <int TPA>
 __global__ void __launch_bounds__(256) k_density64(EamArgs a) {
     __shared__ Smem64 S;
@@ -117,20 +218,7 @@ __global__ void __launch_bounds__(256) k_density64(EamArgs a) {
             Pos64 P;
             P.load(a, i);
             ei = a.elem[i];
-            const int nn = __ldg(a.nnbr + i);
-            const int* row = a.nbr + (size_t)i * a.maxnbr;
-            for (int k = lane; k < nn; k += TPA) {
-                const int e = __ldg(row + k);
-                const int ej = entry_elem(e);
-                double dx, dy, dz;
-                P.delta(a, S.sh, e, dx, dy, dz);
-                double rsq = dx * dx + dy * dy + dz * dz;
-                if (rsq < S.cut_sq[ei * a.ne + ej]) {
-                    double p;
-                    int m = knot64(sqrt(rsq), a, p);
-                    acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
-                }
-            }
+            acc = density64_lane<TPA>(a, S, P, ei, i, lane);
         }
 #pragma unroll
         for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
@@ -146,6 +234,41 @@ __global__ void __launch_bounds__(256) k_density64(EamArgs a) {
     if (block_partials<1>(v, a.partials, 15, &a.sc->counter[1]) && threadIdx.x == 0) a.sc->counter[1] = 0;
 }
 
+// batch: FP64 density per chunk, embedding energy into chunk slot 13
+template <int TPA>
+__global__ void __launch_bounds__(256) k_density64b(EamArgs a, const int* __restrict__ cell_of) {
+    __shared__ Smem64 S;
+    S.fill(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        double eacc = 0.0;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            const bool active = i < hi;
+            double acc = 0.0;
+            int ei = 0;
+            if (active) {
+                PosCell P;
+                P.load(a, cell_of, i);
+                ei = a.elem[i];
+                acc = density64_lane<TPA>(a, S, P, ei, i, lane);
+            }
+#pragma unroll
+            for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+            if (active && lane == 0) {
+                double Fv, dFv;
+                embed64(a, ei, acc, Fv, dFv);
+                a.rho[i] = acc;
+                a.dF[i] = dFv;
+                eacc += Fv;
+            }
+        }
+        chunk_store<1>([&](int) { return eacc; }, a.chunk_part + (size_t)ch * kChunkSlots + 13);
+    }
+}
+
 template <int TPA>
 __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
     __shared__ Smem64 S;
@@ -153,8 +276,8 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
     const int lane = threadIdx.x % TPA;
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
-    const double dri = a.dr_inv;
-    double ep = 0, w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+    double ep = 0;
+    double w[6] = {0, 0, 0, 0, 0, 0};
     for (int base = 0;; base += stride) {
         const int i = gid + base;
         const bool active = i < a.n;
@@ -164,42 +287,7 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
             Pos64 P;
             P.load(a, i);
             const int ei = a.elem[i];
-            const double dFi = __ldg(a.dF + i);
-            const int nn = __ldg(a.nnbr + i);
-            const int* row = a.nbr + (size_t)i * a.maxnbr;
-            for (int k = lane; k < nn; k += TPA) {
-                const int e = __ldg(row + k);
-                const int ej = entry_elem(e);
-                double dx, dy, dz;
-                P.delta(a, S.sh, e, dx, dy, dz);
-                double rsq = dx * dx + dy * dy + dz * dz;
-                if (rsq < S.cut_sq[ei * a.ne + ej]) {
-                    const int j = entry_j(e);
-                    const double r = sqrt(rsq);
-                    const double rinv = 1.0 / r;
-                    double p;
-                    const int m = knot64(r, a, p);
-                    const double der_i = spl_der(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p) * dri;
-                    double der_j = der_i;
-                    if (ej != ei) der_j = spl_der(ldg4(a.rho64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) * dri;
-                    const Dbl4 cz = ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m);
-                    const double z = spl_val(cz, p);
-                    const double zp = spl_der(cz, p) * dri;
-                    const double phi = z * rinv;
-                    const double dphi = zp * rinv - phi * rinv;
-                    const double fp = -(dphi + dFi * der_i + __ldg(a.dF + j) * der_j) * rinv;
-                    fx += fp * dx;
-                    fy += fp * dy;
-                    fz += fp * dz;
-                    ep += phi;
-                    w0 += fp * dx * dx;
-                    w1 += fp * dx * dy;
-                    w2 += fp * dx * dz;
-                    w3 += fp * dy * dy;
-                    w4 += fp * dy * dz;
-                    w5 += fp * dz * dz;
-                }
-            }
+            force64_lane<TPA>(a, S, P, ei, __ldg(a.dF + i), i, lane, fx, fy, fz, ep, w);
         }
 #pragma unroll
         for (int o = TPA / 2; o > 0; o >>= 1) {
@@ -213,7 +301,7 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
             a.f[2 * a.n + i] = fz;
         }
     }
-    double v[7] = {0.5 * ep, 0.5 * w0, 0.5 * w1, 0.5 * w2, 0.5 * w3, 0.5 * w4, 0.5 * w5};
+    double v[7] = {0.5 * ep, 0.5 * w[0], 0.5 * w[1], 0.5 * w[2], 0.5 * w[3], 0.5 * w[4], 0.5 * w[5]};
     if (block_partials<7>(v, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
         // totals over blocks in a fixed order; slot 15 holds the embedding
         // energy written by the density kernel on the same grid
@@ -227,6 +315,43 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
     }
 }
 
+// batch: FP64 forces per chunk, pair energy and virial into slots 0-6
+template <int TPA>
+__global__ void __launch_bounds__(256) k_force64b(EamArgs a, const int* __restrict__ cell_of) {
+    __shared__ Smem64 S;
+    S.fill(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        double ep = 0;
+        double w[6] = {0, 0, 0, 0, 0, 0};
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            const bool active = i < hi;
+            double fx = 0, fy = 0, fz = 0;
+            if (active) {
+                PosCell P;
+                P.load(a, cell_of, i);
+                const int ei = a.elem[i];
+                force64_lane<TPA>(a, S, P, ei, __ldg(a.dF + i), i, lane, fx, fy, fz, ep, w);
+            }
+#pragma unroll
+            for (int o = TPA / 2; o > 0; o >>= 1) {
+                fx += __shfl_xor_sync(0xffffffffu, fx, o, TPA);
+                fy += __shfl_xor_sync(0xffffffffu, fy, o, TPA);
+                fz += __shfl_xor_sync(0xffffffffu, fz, o, TPA);
+            }
+            if (active && lane == 0) {
+                a.f[i] = fx;
+                a.f[a.n + i] = fy;
+                a.f[2 * a.n + i] = fz;
+            }
+        }
+        chunk_store<7>([&](int k) { return 0.5 * (k == 0 ? ep : w[k - 1]); }, a.chunk_part + (size_t)ch * kChunkSlots);
+    }
+}
+
 // input features of the learned preconditioner, per atom: 16 Gaussian radial
 // functions exp(-(r - mu_k)^2 / (2 w^2)) fc(r), mu_k = 2.0 + 3.5 k/15 A,
 // w = 0.3 A, fc(r) = (1 + cos(pi r / 5.5))/2 for r < 5.5 A, summed over the
@@ -234,41 +359,6 @@ __global__ void __launch_bounds__(256) k_force64(EamArgs a) {
 // density rho_i (32); FP64 positions, FP32 sums
 constexpr int kDescR = 16;
 constexpr float kDescRc = 5.5f, kDescW = 0.3f;
-
-// batch: atom i's position and image flags from its cell's bins; image
-// shifts n*H from the cell's box
-struct PosCell {
-    double x, y, z;
-    int lo[3], hi[3];
-    double h6[6];
-    __device__ __forceinline__ void load(const EamArgs& a, const int* cell_of, int i) {
-        const CellGeo& g = a.cells[cell_of[i]];
-        x = a.x[i];
-        y = a.x[a.n + i];
-        z = a.x[2 * a.n + i];
-        const int bc = a.binc[i];
-        const int b[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
-        for (int d = 0; d < 3; d++) {
-            lo[d] = b[d] == 0;
-            hi[d] = b[d] == g.nb[d] - 1;
-        }
-        for (int k = 0; k < 6; k++) h6[k] = g.h6[k];
-    }
-    __device__ __forceinline__ void delta(const EamArgs& a, int e, double& dx, double& dy, double& dz) const {
-        const int j = entry_j(e), c = entry_code(e);
-        const int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
-        const int n0 = (d0 < 0 && lo[0]) ? -1 : ((d0 > 0 && hi[0]) ? 1 : 0);
-        const int n1 = (d1 < 0 && lo[1]) ? -1 : ((d1 > 0 && hi[1]) ? 1 : 0);
-        const int n2 = (d2 < 0 && lo[2]) ? -1 : ((d2 > 0 && hi[2]) ? 1 : 0);
-        // rows of H: (h0,0,0), (h1,h3,0), (h2,h4,h5)
-        const double s0 = n0 * h6[0] + n1 * h6[1] + n2 * h6[2];
-        const double s1 = n1 * h6[3] + n2 * h6[4];
-        const double s2 = n2 * h6[5];
-        dx = x - (__ldg(a.x + j) + s0);
-        dy = y - (__ldg(a.x + a.n + j) + s1);
-        dz = z - (__ldg(a.x + 2 * a.n + j) + s2);
-    }
-};
 
 template <int TPA, bool BATCH>
 __global__ void __launch_bounds__(256) k_descriptors(EamArgs a, const int* __restrict__ cell_of,
@@ -302,7 +392,7 @@ __global__ void __launch_bounds__(256) k_descriptors(EamArgs a, const int* __res
                 const int ej = entry_elem(e);
                 double dx, dy, dz;
                 if (BATCH)
-                    PC.delta(a, e, dx, dy, dz);
+                    PC.delta(a, nullptr, e, dx, dy, dz);
                 else
                     P.delta(a, S.sh, e, dx, dy, dz);
                 const double rsq = dx * dx + dy * dy + dz * dz;
@@ -421,7 +511,7 @@ __global__ void __launch_bounds__(256) k_energy64b(EamArgs a, const int* __restr
                     const int e = __ldg(row + k);
                     const int ej = entry_elem(e);
                     double dx, dy, dz;
-                    P.delta(a, e, dx, dy, dz);
+                    P.delta(a, nullptr, e, dx, dy, dz);
                     const double rsq = dx * dx + dy * dy + dz * dz;
                     if (rsq < S.cut_sq[ei * a.ne + ej]) {
                         const double r = sqrt(rsq);
@@ -457,25 +547,37 @@ static int grid64(mappg_sys* s) {
         default: KERNEL<8><<<grid64<8>(s), 256, 0, s->stream>>>(a); break;                    \
     }
 
+void launch_cells_done(mappg_sys* s, const EamArgs& a, int what);  // eam32.cu
+
 void launch_density_only(mappg_sys* s) {
     EamArgs a = eam_args(s);
-    if (s->precision == MAPPG_MIXED) {
+    if (s->precision == MAPPG_MIXED && !s->force64) {
         launch_density32(s, a);
         return;
     }
-    MAPPG_TPA64(k_density64)
+    if (s->ncell > 1) {
+        k_density64b<8><<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a, s->cell_of);
+    } else {
+        MAPPG_TPA64(k_density64)
+    }
     MAPPG_CUDA(cudaGetLastError());
 }
 
 void launch_force_only(mappg_sys* s) {
     EamArgs a = eam_args(s);
-    if (s->precision == MAPPG_MIXED) {
+    if (s->precision == MAPPG_MIXED && !s->force64) {
         launch_force32(s, a);
         s->f_is_f32 = true;
         return;
     }
-    MAPPG_TPA64(k_force64)
-    MAPPG_CUDA(cudaGetLastError());
+    if (s->ncell > 1) {
+        k_force64b<8><<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a, s->cell_of);
+        MAPPG_CUDA(cudaGetLastError());
+        launch_cells_done(s, a, 0);
+    } else {
+        MAPPG_TPA64(k_force64)
+        MAPPG_CUDA(cudaGetLastError());
+    }
     s->f_is_f32 = false;
 }
 
@@ -484,9 +586,6 @@ void launch_force(mappg_sys* s) {
     launch_force_only(s);
 }
 
-// FP64 density and force passes whose outputs, partial sums and device
-// scalars are the ones in `a` (mappg_sys_force_noalloc points them at its
-// scratch); launches only, no allocation
 // preconditioner features of every atom (bin order), n x 33 floats
 void launch_descriptors(mappg_sys* s, float* out) {
     EamArgs a = eam_args(s);
@@ -497,6 +596,9 @@ void launch_descriptors(mappg_sys* s, float* out) {
     MAPPG_CUDA(cudaGetLastError());
 }
 
+// FP64 density and force passes whose outputs, partial sums and device
+// scalars are the ones in `a` (mappg_sys_force_noalloc points them at its
+// scratch); launches only, no allocation
 void launch_force64_args(mappg_sys* s, const EamArgs& a) {
     MAPPG_TPA64(k_density64)
     MAPPG_TPA64(k_force64)
@@ -516,8 +618,6 @@ void preload_force64() {
     MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<16>));
     MAPPG_CUDA(cudaFuncGetAttributes(&fa, k_force64<32>));
 }
-
-void launch_cells_done(mappg_sys* s, const EamArgs& a, int what);  // eam32.cu
 
 // FP64 energy in either precision (line searches of mixed systems compare
 // FP64 energies): sc->energy for one cell, CellMd::energy per cell of a batch

@@ -40,6 +40,36 @@ struct Smem32 {
     }
 };
 
+// frame offset of a neighbour image from its entry's bin-step code
+// c = (d0+1) + 3(d1+1) + 9(d2+1): -8 d, computed instead of read from a
+// table (the pair loops are bound by the L1 data pipe, which a shared-
+// memory table would share)
+__device__ __forceinline__ void code_offset(int e, float& ox, float& oy, float& oz) {
+    const int c = entry_code(e);
+    const int t9 = (c >= 9) + (c >= 18);
+    const int r9 = c - 9 * t9;
+    const int t3 = (r9 >= 3) + (r9 >= 6);
+    const int t1 = r9 - 3 * t3;
+    ox = (float)(8 - 8 * t1);
+    oy = (float)(8 - 8 * t3);
+    oz = (float)(8 - 8 * t9);
+}
+
+// squared cutoffs of up to four pair types held in registers
+struct Cut4 {
+    float c0, c1, c2, c3;
+    __device__ Cut4(const Smem32& S, int ne) {
+        c0 = S.cut_sq[0];
+        c1 = ne * ne > 1 ? S.cut_sq[1] : c0;
+        c2 = ne * ne > 2 ? S.cut_sq[2] : c0;
+        c3 = ne * ne > 3 ? S.cut_sq[3] : c0;
+    }
+    __device__ __forceinline__ float operator()(const Smem32& S, int t) const {
+        if (t > 3) return S.cut_sq[t];  // more than two elements
+        return (t & 2) ? ((t & 1) ? c3 : c2) : ((t & 1) ? c1 : c0);
+    }
+};
+
 // frame displacement (a,b,c) to Cartesian with the head + tail scale
 template <bool ORTHO, class FR>
 __device__ __forceinline__ void cart(const FR& fr, float a, float b, float c, float& x, float& y, float& z) {
@@ -145,6 +175,7 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
                                              int i, int lane, bool active, float& es, float& ec) {
     float acc = 0.f;
     int ei = 0;
+    const Cut4 cut(S, a.ne);
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         pi = __ldg(a.p32 + i);
@@ -155,11 +186,12 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
             const int e = __ldg(row + k);
             const int ej = entry_elem(e);
             const float4 q = __ldg(a.p32 + entry_j(e));
-            const float4 o = S.off[entry_code(e)];
+            float ox, oy, oz;
+            code_offset(e, ox, oy, oz);
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < S.cut_sq[ei * a.ne + ej]) {
+            if (rsq < cut(S, ei * a.ne + ej)) {
                 const float r = rsq * inv_sqrt(rsq);
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
@@ -180,7 +212,7 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
 }
 
 template <int TPA, bool ORTHO>
-__global__ void __launch_bounds__(256) k_density32(EamArgs a) {
+__global__ void __launch_bounds__(256, 8) k_density32(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -207,7 +239,7 @@ __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
 
 // batch: blocks walk chunks; the chunk's embedding energy goes to slot 13
 template <int TPA, bool ORTHO>
-__global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
+__global__ void __launch_bounds__(256, 8) k_density32b(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -232,6 +264,7 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                                            int i, int lane, bool active, float& es, float& ec, float (&w)[6],
                                            float* ke) {
     float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
+    const Cut4 cut(S, a.ne);
     int ei = 0;
     if (active) {
         const float4 pi = __ldg(a.q32 + i);
@@ -243,11 +276,12 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
             const int e = __ldg(row + k);
             const int t = ei * a.ne + entry_elem(e);
             const float4 q = __ldg(a.q32 + entry_j(e));
-            const float4 o = S.off[entry_code(e)];
+            float ox, oy, oz;
+            code_offset(e, ox, oy, oz);
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < S.cut_sq[t]) {
+            if (rsq < cut(S, t)) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;
@@ -413,6 +447,7 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
                                             int i, int lane, bool active, float& es, float& ec) {
     float acc = 0.f, ep = 0.f;
     int ei = 0;
+    const Cut4 cut(S, a.ne);
     if (active) {
         const float4 pi = __ldg(a.p32 + i);
         ei = a.elem[i];
@@ -423,11 +458,12 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
             const int ej = entry_elem(e);
             const int t = ei * a.ne + ej;
             const float4 q = __ldg(a.p32 + entry_j(e));
-            const float4 o = S.off[entry_code(e)];
+            float ox, oy, oz;
+            code_offset(e, ox, oy, oz);
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < S.cut_sq[t]) {
+            if (rsq < cut(S, t)) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;

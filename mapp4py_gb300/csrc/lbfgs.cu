@@ -33,6 +33,7 @@ struct LbScal {
     double alpha[64];
     double gamma;
     double fh, hh, hmax, fmax;
+    double tau;  // scale of the learned diagonal, (s.y)/(y.P.y)
 };
 
 __device__ __forceinline__ void warp_sum(double& t) {
@@ -87,8 +88,9 @@ __device__ void lb_final(const double* partials, int nblk, double (&tot)[K], boo
 // h <- h + coef*y, then dot = s.h (s may be null: no dot).  coef is read
 // from the device: mode 0: coef = 0 (plain dot); mode 1: alpha_i =
 // -rho_i*dot_in, stored; mode 2: beta = -alpha_i - rho_i*dot_in; mode 3:
-// coef applies as a scale: h <- gamma*h; mode 4: h <- P*h elementwise with
-// P (passed as y) the learned diagonal initial inverse Hessian
+// coef applies as a scale: h <- gamma*h; mode 4: h <- tau*P*h elementwise
+// with P (passed as y) the learned diagonal initial inverse Hessian and tau
+// its scale from the newest pair
 __global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__ h, const double* __restrict__ y,
                                                      const double* __restrict__ s, LbScal* L, int mode, int idx,
                                                      int dot_in, int dot_out, double* partials, unsigned* counter) {
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__
         else if (mode == 3)
             hv = hv * coef;
         else if (mode == 4)
-            hv = hv * y[q];
+            hv = hv * (L->tau * y[q]);
         if (mode) h[q] = hv;
         if (s) acc += s[q] * hv;
     }
@@ -194,12 +196,16 @@ __global__ void k_lb_trial(int N, double* __restrict__ x, const double* __restri
         x[q] = x0[q] + alpha * h[q];
 }
 
-// s0 = alpha*h, y0 = f0 - f; dots s0.y0, y0.y0 -> rho0, gamma
+// s0 = alpha*h, y0 = f0 - f; dots s0.y0, y0.y0 -> rho0, gamma (and y0.P.y0
+// -> tau with a learned diagonal).  A pair without positive curvature
+// (s0.y0 <= 0, e.g. a step that underflowed to zero) gets rho0 = 0, so it
+// takes no part in the recursion, and leaves gamma as it was; the
+// reference would divide by it.
 __global__ void __launch_bounds__(256) k_lb_hist(int N, double* __restrict__ s0, double* __restrict__ y0,
                                                  const double* __restrict__ h, const double* __restrict__ f0,
-                                                 const double* __restrict__ f, double alpha, LbScal* L,
-                                                 double* partials, unsigned* counter) {
-    double v[2] = {0.0, 0.0};
+                                                 const double* __restrict__ f, const double* __restrict__ P,
+                                                 double alpha, LbScal* L, double* partials, unsigned* counter) {
+    double v[3] = {0.0, 0.0, 0.0};
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
         double sv = alpha * h[q];
         double yv = f0[q] - f[q];
@@ -207,13 +213,19 @@ __global__ void __launch_bounds__(256) k_lb_hist(int N, double* __restrict__ s0,
         y0[q] = yv;
         v[0] += sv * yv;
         v[1] += yv * yv;
+        if (P) v[2] += yv * yv * P[q];
     }
-    if (lb_block<2>(v, partials, counter) && threadIdx.x < 32) {
-        double t[2];
-        lb_final<2>(partials, gridDim.x, t);
+    if (lb_block<3>(v, partials, counter) && threadIdx.x < 32) {
+        double t[3];
+        lb_final<3>(partials, gridDim.x, t);
         if (threadIdx.x == 0) {
-            L->gamma = t[0] / t[1];
-            L->rho[0] = 1.0 / t[0];
+            if (t[0] > 0.0 && t[1] > 0.0) {
+                L->gamma = t[0] / t[1];
+                L->rho[0] = 1.0 / t[0];
+                if (t[2] > 0.0) L->tau = t[0] / t[2];
+            } else {
+                L->rho[0] = 0.0;
+            }
             *counter = 0;
         }
     }
@@ -258,6 +270,12 @@ void lb_update(mappg_sys* s) {
     // positions moved without a rebuild: refresh the mixed kernels' frame
     if (s->precision == MAPPG_MIXED) launch_shadow(s, false);
     MAPPG_CUDA(cudaGetLastError());
+    // a relaxation can crowd atoms beyond the rows' capacity: a rebuild that
+    // ran out of room is redone with wider rows
+    int ov = 0;
+    MAPPG_CUDA(cudaMemcpyAsync(&ov, &s->sc->overflow, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    if (ov) sys_build(s);
 }
 
 static void lb_force(mappg_sys* s, double* pe) {
@@ -301,8 +319,15 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
     unsigned* counter = (unsigned*)dalloc(sizeof(unsigned) * 4);
     MAPPG_CUDA(cudaMemsetAsync(L, 0, sizeof(LbScal), s->stream));
     MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * 4, s->stream));
-    const double one = 1.0;  // gamma starts at 1 (min_l-bfgs.h:140)
+    const double one = 1.0;  // gamma starts at 1 (min_l-bfgs.h:140), as does tau
     MAPPG_CUDA(cudaMemcpyAsync(&L->gamma, &one, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(&L->tau, &one, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    // a mixed relaxation that stalls above f_tol (its FP32 forces no longer
+    // point downhill on the FP64 energy) goes on with FP64 forces
+    struct Promote {
+        mappg_sys* s;
+        ~Promote() { s->force64 = false; }
+    } promote{s};
     cudaStream_t st = s->stream;
     double* part = s->partials;
 
@@ -418,6 +443,18 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             }
         }
         err = lerr;
+        if (err == LS_MIN_ALPHA && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
+            s->force64 = true;
+            lb_force(s, &pe_force);
+            n_fc++;
+            e_curr = lb_energy(s);
+            k = 0;
+            MAPPG_CUDA(cudaMemcpyAsync(&L->gamma, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+            MAPPG_CUDA(cudaMemcpyAsync(&L->tau, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+            err = LS_S;
+            istep--;
+            continue;
+        }
         if (err != LS_S) {
             istep--;
             continue;
@@ -444,7 +481,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             sv[0] = ts;
             yv[0] = ty;
             k_lb_shift_rho<<<1, 1, 0, st>>>(L, m);
-            k_lb_hist<<<grid, 256, 0, st>>>(N, sv[0], yv[0], h, f0, s->f, alpha_m, L, part, counter);
+            k_lb_hist<<<grid, 256, 0, st>>>(N, sv[0], yv[0], h, f0, s->f, P, alpha_m, L, part, counter);
             MAPPG_CUDA(cudaGetLastError());
         } else {
             // gamma = alpha_m (h.f0 - h.f)/(f.f + f0.f0 - 2 f.f0) on the host
@@ -469,6 +506,212 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
         MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         read_prep(&fh, &hh, &hmax, &fmaxv);
     }
+    DevScalars hs;
+    MAPPG_CUDA(cudaMemcpyAsync(&hs, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+    MAPPG_CUDA(cudaStreamSynchronize(st));
+    if (hs.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during minimization"};
+    if (hs.bad) throw Error{MAPPG_ERR_NAN, "non-finite value during minimization"};
+    if (stats) {
+        stats[0] = istep;
+        stats[1] = pe_force;
+        stats[2] = fmaxv;
+        stats[3] = err;
+        stats[4] = (double)n_en;
+        stats[5] = (double)n_fc;
+    }
+}
+
+}  // namespace mappg
+
+// ------------------------------------------------------------------ MinCG
+// md.min_cg(e_tol,max_dx,ls=ls_bt(...)).run(atoms,nsteps): MinCG::__run
+// (min_cg.h:454-536), Polak-Ribiere directions h = ratio h + f with ratio =
+// (f.f - f.f0)/(f0.f0), over LineSearchBackTrack::min with init_flag 1
+// (ls.h:711-769: the first trial step is capped by -prev/dfa, prev being
+// the previous step's decrease -dfa*alpha; LineSearch::reset, ls.h:42,
+// starts prev at -1).  Same vectors and kernels as the L-BFGS driver.
+namespace mappg {
+
+// f.f and f.f0 into L->dot[0], L->dot[1]
+__global__ void __launch_bounds__(256) k_cg_dots(int N, const double* __restrict__ f, const double* __restrict__ f0,
+                                                 LbScal* L, double* partials, unsigned* counter) {
+    double v[2] = {0.0, 0.0};
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
+        v[0] += f[q] * f[q];
+        v[1] += f[q] * f0[q];
+    }
+    if (lb_block<2>(v, partials, counter) && threadIdx.x < 32) {
+        double t[2];
+        lb_final<2>(partials, gridDim.x, t);
+        if (threadIdx.x == 0) {
+            L->dot[0] = t[0];
+            L->dot[1] = t[1];
+            *counter = 0;
+        }
+    }
+}
+
+__global__ void k_cg_dir(int N, double* __restrict__ h, const double* __restrict__ f, double ratio) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) h[q] = ratio * h[q] + f[q];
+}
+
+void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
+            int nsteps, double* stats) {
+    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
+    if (!(max_dx > 0.0)) throw Error{MAPPG_ERR_ARG, "max_dx must be positive"};
+    if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
+    if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
+    const int N = 3 * s->n;
+    const int grid = grid_for(s, N, 256);
+    std::vector<void*> owned;
+    auto dalloc = [&](size_t bytes) {
+        void* p = nullptr;
+        MAPPG_CUDA(cudaMalloc(&p, bytes));
+        owned.push_back(p);
+        return p;
+    };
+    struct Guard {
+        std::vector<void*>& o;
+        ~Guard() {
+            for (void* p : o) cudaFree(p);
+        }
+    } guard{owned};
+    double* f0 = (double*)dalloc(sizeof(double) * N);
+    double* h = (double*)dalloc(sizeof(double) * N);
+    double* xs = (double*)dalloc(sizeof(double) * N);
+    LbScal* L = (LbScal*)dalloc(sizeof(LbScal));
+    unsigned* counter = (unsigned*)dalloc(sizeof(unsigned) * 4);
+    cudaStream_t st = s->stream;
+    MAPPG_CUDA(cudaMemsetAsync(L, 0, sizeof(LbScal), st));
+    MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * 4, st));
+    double* part = s->partials;
+    auto read_prep = [&](double* fh, double* hh, double* hmax, double* fmax_) {
+        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, L, part, counter);
+        MAPPG_CUDA(cudaGetLastError());
+        double buf[4];
+        MAPPG_CUDA(cudaMemcpyAsync(buf, &L->fh, sizeof(buf), cudaMemcpyDeviceToHost, st));
+        MAPPG_CUDA(cudaStreamSynchronize(st));
+        *fh = buf[0];
+        *hh = buf[1];
+        *hmax = buf[2];
+        *fmax_ = buf[3];
+    };
+    sys_build(s);
+    long long n_en = 0, n_fc = 1;
+    double pe_force;
+    lb_force(s, &pe_force);
+    double e_curr = s->precision == MAPPG_MIXED ? lb_energy(s) : pe_force, e_prev;
+    int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
+    double fh, hh, hmax, fmaxv;
+    MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    read_prep(&fh, &hh, &hmax, &fmaxv);
+    if (err == LS_S && f_tol > 0.0 && fmaxv < f_tol) err = MIN_S_FTOL;
+    double f0_f0 = fh;  // f.f with h = f
+    double prev_val = -1.0;
+    struct Promote {
+        mappg_sys* s;
+        ~Promote() { s->force64 = false; }
+    } promote{s};
+    int istep = 0;
+    for (; err == LS_S; istep++) {
+        if (f0_f0 == 0.0) {
+            err = LS_F_GRAD0;
+            continue;
+        }
+        MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        MAPPG_CUDA(cudaMemcpyAsync(f0, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        e_prev = e_curr;
+        read_prep(&fh, &hh, &hmax, &fmaxv);
+        if (fh < 0.0) {
+            MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+            fh = f0_f0;
+        }
+        double dfa = -fh, max_a;
+        int lerr = LS_S;
+        if (hh == 0.0) {
+            max_a = 0.0;
+            dfa = 0.0;
+        } else if (dfa >= 0.0) {
+            max_a = 0.0;
+            dfa = 1.0;
+        } else {
+            max_a = fabs(max_dx / hmax);
+        }
+        if (dfa == 0.0)
+            lerr = LS_F_GRAD0;
+        else if (max_a == 0.0)
+            lerr = LS_MIN_ALPHA;
+        else if (dfa >= 0.0)
+            lerr = LS_F_DOWNHILL;
+        else {
+            if (prev_val > 0.0 && dfa < 0.0) max_a = fmin(max_a, -prev_val / dfa);
+            prev_val = -dfa;
+            if (max_a <= min_alpha)
+                lerr = LS_MIN_ALPHA;
+            else {
+                double a = max_a, init_energy = e_curr;
+                while (true) {
+                    double ideal = e_curr + a * c_ls * dfa;
+                    k_lb_trial<<<grid, 256, 0, st>>>(N, s->x, xs, h, a);
+                    double cur = lb_energy(s);
+                    n_en++;
+                    if (cur <= ideal) {
+                        prev_val *= a;
+                        e_curr = cur;
+                        break;
+                    }
+                    a *= rho_ls;
+                    if (a <= min_alpha) {
+                        e_curr = init_energy;
+                        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+                        lb_update(s);
+                        lerr = LS_MIN_ALPHA;
+                        break;
+                    }
+                }
+            }
+        }
+        err = lerr;
+        if (err == LS_MIN_ALPHA && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
+            // stalled on FP32 forces above f_tol: restart from x0 with FP64 forces
+            s->force64 = true;
+            lb_force(s, &pe_force);
+            n_fc++;
+            e_curr = lb_energy(s);
+            MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+            f0_f0 = fh;
+            prev_val = -1.0;
+            err = LS_S;
+            istep--;
+            continue;
+        }
+        if (err != LS_S) {
+            istep--;
+            continue;
+        }
+        lb_force(s, &pe_force);
+        n_fc++;
+        if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
+        if (f_tol > 0.0) {
+            read_prep(&fh, &hh, &hmax, &fmaxv);
+            if (fmaxv < f_tol) err = MIN_S_FTOL;
+        }
+        if (istep + 1 == nsteps) err = MIN_F_MAX_ITER;
+        if (err) continue;
+        k_cg_dots<<<grid, 256, 0, st>>>(N, s->f, f0, L, part, counter);
+        MAPPG_CUDA(cudaGetLastError());
+        double dd[2];
+        MAPPG_CUDA(cudaMemcpyAsync(dd, &L->dot[0], sizeof(dd), cudaMemcpyDeviceToHost, st));
+        MAPPG_CUDA(cudaStreamSynchronize(st));
+        const double ratio = (dd[0] - dd[1]) / f0_f0;
+        k_cg_dir<<<grid, 256, 0, st>>>(N, h, s->f, ratio);
+        MAPPG_CUDA(cudaGetLastError());
+        f0_f0 = dd[0];
+    }
+    MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    read_prep(&fh, &hh, &hmax, &fmaxv);
     DevScalars hs;
     MAPPG_CUDA(cudaMemcpyAsync(&hs, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
     MAPPG_CUDA(cudaStreamSynchronize(st));

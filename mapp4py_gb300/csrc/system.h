@@ -237,6 +237,7 @@ struct mappg_sys {
     bool built = false;
     bool have_v = false;
     bool f_is_f32 = false;  // the newest forces are in f32 (mixed kernels)
+    bool force64 = false;   // mixed system computing FP64 forces (end of a relaxation)
     std::vector<int> host_id;  // sorted -> caller (host copy)
 };
 

@@ -231,3 +231,46 @@ class min_lbfgs:
         atoms.step += r["niter"]
         self.last = r
         return r
+
+
+class min_cg:
+    """Polak-Ribiere conjugate-gradient minimization of positions
+    (MinCG::__run, min_cg.h:454-536) with the back-tracking line search;
+    box degrees of freedom are not in this engine's scope."""
+
+    def __init__(self, e_tol=math.sqrt(sys.float_info.epsilon), H_dof=None, affine=False, max_dx=1.0, ls=None,
+                 f_tol=0.0):
+        if e_tol < 0.0:
+            raise TypeError("e_tol should be greater than or equal to 0.0")
+        if not (max_dx > 0.0):
+            raise TypeError("max_dx should be greater than 0.0")
+        if H_dof is not None and np.any(np.asarray(H_dof, dtype=object) == True):  # noqa: E712
+            raise TypeError("box degrees of freedom (H_dof) are not supported by this engine")
+        if affine:
+            raise TypeError("affine minimization is not supported by this engine")
+        self.e_tol = float(e_tol)
+        self.max_dx = float(max_dx)
+        self.ls = ls if ls is not None else ls_bt()
+        self.f_tol = float(f_tol)
+        self.ntally = 1000
+        self.export = None
+        self.last = None
+
+    def run(self, atoms, max_nsteps):
+        if max_nsteps < 0:
+            raise TypeError("max_nsteps should be greater than or equal to 0")
+        if not isinstance(self.ls, ls_bt):
+            raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
+        s = atoms._system()
+        s.set_x(atoms.x)
+        r = s.cg_run(e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
+                     min_alpha=self.ls.min_alpha, nsteps=max_nsteps)
+        s.get_x(atoms.x)
+        atoms.f = s.get_f()
+        atoms.pe = r["pe"]
+        atoms.step += r["niter"]
+        self.last = r
+        return r
+
+
+min_cg_new = min_cg  # the name the reference registers for this minimizer

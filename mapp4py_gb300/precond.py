@@ -89,3 +89,47 @@ def train(ff, count=100, epochs=40, seed=0, batch=4096, lr=2e-3, wd=1e-4, n=(8, 
     net.set_data(feat, target, seed)
     losses = net.train(epochs, batch, lr, wd)
     return net, losses
+
+
+WEIGHTS = __file__.replace("precond.py", "precond_net.npz")
+
+
+def save(net, path=WEIGHTS, **meta):
+    w, mean, sdev = net.params()
+    np.savez(path, w=w, mean=mean, sdev=sdev, **meta)
+
+
+def load(path=WEIGHTS, seed=0):
+    """The network stored by `python -m mapp4py_gb300.precond` (trained on
+    the GPU by this package's kernels)."""
+    d = np.load(path)
+    net = _lib.Mlp(seed)
+    net.set_params(d["w"], d["mean"], d["sdev"])
+    return net
+
+
+if __name__ == "__main__":
+    import argparse
+    import os
+    import tempfile
+    import time
+
+    ap = argparse.ArgumentParser(description="train the L-BFGS preconditioner network and store it")
+    ap.add_argument("--configs", type=int, default=100, help="training configurations of 2048 atoms")
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=WEIGHTS)
+    args = ap.parse_args()
+    with tempfile.TemporaryDirectory() as d:
+        path = synth.write_setfl(os.path.join(d, "AB.setfl"), ("A", "B"))
+        ff = _lib.ForceField.setfl(path)
+        t0 = time.time()
+        feat, target = training_set(ff, args.configs, args.seed)
+        t1 = time.time()
+        net = _lib.Mlp(args.seed)
+        net.set_data(feat, target, args.seed)
+        losses = net.train(args.epochs)
+        t2 = time.time()
+        save(net, args.out, rows=feat.shape[0], losses=losses, label_seconds=t1 - t0, train_seconds=t2 - t1)
+        print("rows %d, labels %.1f s, training %.1f s, loss %.4f -> %.4f" %
+              (feat.shape[0], t1 - t0, t2 - t1, losses[0], losses[-1]))

@@ -1392,6 +1392,120 @@ int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, dou
     return 0;
 }
 
+/* MinCG::__run  min_cg.h:454-536 (Polak-Ribiere conjugate gradient) over
+ * LineSearchBackTrack::min with init_flag 1  ls.h:711-769 (the first trial
+ * step is capped by the previous step's decrease; LineSearch::reset sets
+ * prev_val = -1, ls.h:42), plus the added stop at max|F| < f_tol. */
+int orc_cg_run(void* p, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
+               int nsteps, double* stats) {
+    orc_sys* s = (orc_sys*)p;
+    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
+    int n3 = 3 * s->natms;
+    if (orc_sys_init_dynamic(s)) return -1;
+    double* f0 = (double*)malloc(sizeof(double) * n3);
+    double* h = (double*)malloc(sizeof(double) * n3);
+    double* x0 = (double*)malloc(sizeof(double) * n3);
+    long n_en = 0, n_fc = 1;
+    double prev_val = -1.0;
+    force_calc(s);
+    double e_prev, e_curr = s->pe;
+    int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
+    if (err == LS_S && f_tol > 0.0 && max_abs_f(s) < f_tol) err = MIN_S_FTOL;
+    memcpy(h, s->f, sizeof(double) * n3);
+    double f0_f0 = vdot(s->f, s->f, n3);
+    int istep = 0;
+    for (; err == LS_S; istep++) {
+        if (f0_f0 == 0.0) {
+            err = LS_F_GRAD0;
+            continue;
+        }
+        memcpy(x0, s->x, sizeof(double) * n3);
+        memcpy(f0, s->f, sizeof(double) * n3);
+        e_prev = e_curr;
+        double f_h = vdot(s->f, h, n3);
+        if (f_h < 0.0) {
+            memcpy(h, s->f, sizeof(double) * n3);
+            f_h = f0_f0;
+        }
+        {
+            double h_norm = vdot(h, h, n3), dfa = -f_h, max_a;
+            int lerr = LS_S;
+            if (h_norm == 0.0) {
+                max_a = 0.0;
+                dfa = 0.0;
+            } else if (dfa >= 0.0) {
+                max_a = 0.0;
+                dfa = 1.0;
+            } else {
+                double mx = 0.0;
+                for (int q = 0; q < n3; q++) mx = OMAX(mx, fabs(h[q]));
+                max_a = fabs(max_dx / mx);
+            }
+            if (dfa == 0.0)
+                lerr = LS_F_GRAD0;
+            else if (max_a == 0.0)
+                lerr = LS_MIN_ALPHA;
+            else if (dfa >= 0.0)
+                lerr = LS_F_DOWNHILL;
+            else {
+                if (prev_val > 0.0 && dfa < 0.0) max_a = OMIN(max_a, -prev_val / dfa);
+                prev_val = -dfa;
+                if (max_a <= min_alpha)
+                    lerr = LS_MIN_ALPHA;
+                else {
+                    double a = max_a, init_energy = e_curr;
+                    while (1) {
+                        double ideal = e_curr + a * c_ls * dfa;
+                        double cur = ls_F(s, x0, h, a);
+                        n_en++;
+                        if (cur <= ideal) {
+                            prev_val *= a;
+                            e_curr = cur;
+                            lerr = LS_S;
+                            break;
+                        }
+                        a *= rho_ls;
+                        if (a <= min_alpha) {
+                            e_curr = init_energy;
+                            memcpy(s->x, x0, sizeof(double) * n3);
+                            dynamic_update(s);
+                            lerr = LS_MIN_ALPHA;
+                            break;
+                        }
+                    }
+                }
+            }
+            err = lerr;
+        }
+        if (err != LS_S) {
+            istep--;
+            continue;
+        }
+        force_calc(s);
+        n_fc++;
+        if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
+        if (f_tol > 0.0 && max_abs_f(s) < f_tol) err = MIN_S_FTOL;
+        if (istep + 1 == nsteps) err = MIN_F_MAX_ITER;
+        if (err) continue;
+        double f_f = vdot(s->f, s->f, n3), f_f0 = vdot(s->f, f0, n3);
+        double ratio = (f_f - f_f0) / f0_f0;
+        for (int q = 0; q < n3; q++) h[q] = ratio * h[q] + s->f[q];
+        f0_f0 = f_f;
+    }
+    if (stats) {
+        stats[0] = istep;
+        stats[1] = s->pe;
+        stats[2] = max_abs_f(s);
+        stats[3] = err;
+        stats[4] = (double)n_en;
+        stats[5] = (double)n_fc;
+    }
+    free(f0);
+    free(h);
+    free(x0);
+    return 0;
+}
+
 /* Park-Miller + polar Box-Muller  random.cpp:32-68, AtomsMD::create_T
    atoms_md.cpp:130-162.  Seed 0 makes the reference loop forever; here it is
    rejected. */

@@ -63,6 +63,8 @@ def lib():
                                      C.c_int, C.c_int, C.c_int, _D, _D, C.c_int, _D]
         L.orc_lbfgs_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_double, C.c_double, C.c_int, _D]
+        L.orc_cg_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, C.POINTER(C.c_double)]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
         _lib = L
     return _lib
@@ -221,6 +223,16 @@ class System:
     def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=10000):
         st = np.zeros(6)
         r = lib().orc_lbfgs_run(self.h, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+
+    def cg_run(self, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=10000):
+        st = np.zeros(6)
+        r = lib().orc_cg_run(self.h, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, _dp(st))
         if r != 0:
             raise RuntimeError("oracle: " + _err())
         self.initialized = True

@@ -184,6 +184,25 @@ def test_lbfgs_converges_like_oracle(potentials):
     assert np.max(np.abs(d)) < 1e-8
 
 
+def test_cg_converges_like_oracle(potentials):
+    """MinCG: the first iterations follow the oracle to rounding; the full
+    run reaches the same minimum with the same iteration count."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+    o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    ro = o.cg_run(e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert ro["err"] == 100
+    g = dict(H=c.H, x=c.x, elem=c.elem, masses=c.masses)
+    s = make(path, g)
+    r = s.cg_run(e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert r["err"] == 100 and r["fmax"] < 1e-4
+    assert r["niter"] == ro["niter"] and r["n_energy"] == ro["n_energy"]
+    assert abs(r["pe"] - ro["pe"]) <= 1e-11 * abs(ro["pe"])
+    d = s.get_x() - o.x
+    d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
+    assert np.max(np.abs(d)) < 1e-8
+
+
 def test_errors_are_reported(potentials):
     path, _ = potentials[("A",)]
     ff = _lib.ForceField.setfl(path)

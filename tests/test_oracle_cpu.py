@@ -138,6 +138,18 @@ def test_lbfgs_reaches_force_tolerance(potentials):
     assert r["pe"] == float(g["pe"]) and r["niter"] == int(g["niter"])
 
 
+def test_cg_reaches_force_tolerance(potentials):
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+    s = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    r = s.cg_run(e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert r["err"] == 100 and r["fmax"] < 1e-4
+    # the same minimum as L-BFGS from the same start
+    t = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    rl = t.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert abs(r["pe"] - rl["pe"]) < 1e-6 * abs(rl["pe"])
+
+
 REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
 
 
