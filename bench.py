@@ -28,7 +28,9 @@ sys.path.insert(0, ROOT)
 METRIC = "EAM MD atom-steps/s"
 N_CELLS = (80, 80, 80)
 T_K = 600.0
-KERNELS_PER_STEP = 13  # step_open, kick_drift, com_skin, 7 rebuild-chain, density, force, kick2
+# kernels in one step's CUDA graph: FP64 step_open, kick_drift, com_skin, 7 rebuild-chain, density,
+# force, kick2; mixed step_open32, integrate32, 7 rebuild-chain, density32, force32, close32
+KERNELS_PER_STEP = {"fp64": 13, "mixed": 12}
 
 
 def env_int(k, d):
@@ -208,7 +210,7 @@ def run_batch(args, ff, torch):
     cells, temps = synth.batch_cells(args.batch_cells, seed=7)
     b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
     b.set_v(np.concatenate([c.v for c in cells]))
-    tpa, _ = b.autotune()
+    tpa, unroll, _ = b.autotune()
     K, W = args.batch_steps, 3
     b.nvt_begin(temps, synth.FS, synth.KB, W + K)
     stream = torch.cuda.ExternalStream(b.stream())
@@ -226,7 +228,41 @@ def run_batch(args, ff, torch):
     return {"workload": "%d independent cells, %d atoms (%d-%d per cell), NVT at 100-1200 K, mixed precision"
                         % (len(cells), b.n, int(b.natoms.min()), int(b.natoms.max())),
             "value": b.n * K / (ms / 1000.0), "unit": "atom-steps/s", "steps": K, "ms_per_step": ms / K,
-            "rebuilds_in_run": st["rebuilds"], "lanes_per_atom": tpa}
+            "rebuilds_in_run": st["rebuilds"], "lanes_per_atom": tpa, "entries_per_step": unroll}
+
+
+def run_lbfgs(args, ff):
+    """L-BFGS time to max|F| < 1e-4 eV/A, the learned diagonal initial inverse
+    Hessian against plain L-BFGS (scalar gamma), m = 10, back-tracking line
+    search, mixed precision (FP64 line-search energies, FP64 forces once FP32
+    forces stall).  Two cells of the same recipe (A/B alloy, 1 % vacancies,
+    0.15 A noise, seed 3): the 253,489-atom FCC 40^3 cell with an iteration
+    cap, and a 3,954-atom FCC 10^3 cell run to the tolerance."""
+    from mapp4py_gb300 import _lib, precond, synth
+
+    net = precond.load()
+
+    def one(cells, cap):
+        c = synth.alloy((cells,) * 3, xB=0.5, sigma=0.15, vac=0.01, seed=3)
+        res = {"natoms": c.natoms, "iteration_cap": cap}
+        for name in ("plain", "learned"):
+            s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+            s.build()
+            s.sync()
+            t0 = time.perf_counter()
+            if name == "plain":
+                r = s.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=cap)
+            else:
+                r = _lib.lbfgs_run_precond(s, net, m=10, e_tol=0.0, f_tol=1e-4, nsteps=cap)
+            dt = time.perf_counter() - t0
+            res[name] = {"seconds": dt, "converged": r["err"] == 100, "iterations": r["niter"],
+                         "fmax": r["fmax"], "energy_calls": r["n_energy"], "force_calls": r["n_force"]}
+        res["wall_ratio_plain_over_learned"] = res["plain"]["seconds"] / res["learned"]["seconds"]
+        return res
+
+    return {"metric": "L-BFGS time to max|F| < 1e-4 eV/A, learned vs plain", "unit": "s",
+            "network": "33-64-64-3 BF16 MLP trained on 201,814 FD Hessian diagonals (precond_net.npz)",
+            "cell_253k": one(40, args.lbfgs_cap), "cell_4k": one(10, 5 * args.lbfgs_cap)}
 
 
 def run_gpu(args, rank, world, local_rank):
@@ -249,7 +285,7 @@ def run_gpu(args, rank, world, local_rank):
     prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
     sysm = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, skin=0.5, precision=prec)
     sysm.set_v(cell.v)
-    tpa, tune_ms = sysm.autotune()  # lanes per atom of the density/force kernels
+    tpa, unroll, tune_ms = sysm.autotune()  # lanes per atom, entries per step of the density/force kernels
     dt = synth.FS
     sysm.nvt_begin(T_K, dt, synth.KB, W + K, t_relax=100.0 * dt, L=3, niters=1)
     stream = torch.cuda.ExternalStream(sysm.stream())
@@ -341,6 +377,7 @@ def run_gpu(args, rank, world, local_rank):
                    "opening force call + one step per call, as MDNVT::run"}
 
     batched = None if args.batch_steps <= 0 else run_batch(args, ff, torch)
+    lbfgs = None if args.lbfgs_cap <= 0 else run_lbfgs(args, ff)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -348,12 +385,14 @@ def run_gpu(args, rank, world, local_rank):
                 "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "data": "synthetic",
                 "config": dict(workload_config(N, args.cells, args.precision, world),
                                l2="inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6),
-                               lanes_per_atom=tpa,
-                               autotune_ms={str(k): round(v, 4) for k, v in tune_ms.items()}),
-                "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * K,
+                               lanes_per_atom=tpa, entries_per_step=unroll,
+                               autotune_ms={"%d,%d" % k: round(v, 4) for k, v in tune_ms.items()}),
+                "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP[args.precision] * K,
                 "neighbor": {"rebuilds_in_run": st["rebuilds"], "max_row": st["max_row"], "capacity": st["capacity"]}}
         if batched is not None:
             line["batched"] = batched
+        if lbfgs is not None:
+            line["lbfgs"] = lbfgs
         if not args.no_cpu and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline(path, cell, os.cpu_count() or 1)
@@ -377,6 +416,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=100,
                     help="steps of the 512-cell batch measurement (0 skips it)")
     ap.add_argument("--batch-cells", type=int, default=512)
+    ap.add_argument("--lbfgs-cap", type=int, default=1000,
+                    help="iteration cap of the 253k-atom L-BFGS comparison (0 skips the L-BFGS part)")
     ap.add_argument("--cells", type=int, default=N_CELLS[0],
                     help="FCC repeats per side (80 = the 2,048,000-atom workload; smaller for profiling)")
     args = ap.parse_args()

@@ -192,12 +192,13 @@ int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
 int mappg_sys_stream(mappg_sys* sys, void** stream);
 int mappg_sys_sync(mappg_sys* sys);
 
-/* Choose the lanes per atom (4, 8 or 16; 256/lanes atoms per block) of the
- * density and force kernels by timing them on this system's atoms and
- * neighbour list; the choice is kept for the system.  tpa (may be NULL)
- * receives it, ms (3 doubles, may be NULL) the density+force time of each
- * candidate.  No counterpart in the reference. */
-int mappg_sys_autotune(mappg_sys* sys, int* tpa, double* ms);
+/* Choose the lanes per atom (4, 8 or 16; 256/lanes atoms per block) and the
+ * neighbour entries per loop step (1 or 2, mixed kernels) of the density and
+ * force kernels by timing them on this system's atoms and neighbour list;
+ * the choice is kept for the system.  tpa, unroll (may be NULL) receive it,
+ * ms (6 doubles, may be NULL) the density+force time of each candidate
+ * (4,1) (8,1) (16,1) (4,2) (8,2) (16,2).  No counterpart in the reference. */
+int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
 
 /* Enqueue one kernel launch on the system's stream without waiting, for
  * timing: 0 density + embedding, 1 force/virial (uses the last F'(rho)),

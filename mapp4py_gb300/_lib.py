@@ -63,7 +63,7 @@ SIGNATURES = {
     "mappg_sys_enqueue": (C.c_int, [_VP, C.c_int]),
     "mappg_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_int, _D]),
-    "mappg_sys_autotune": (C.c_int, [_VP, _I, _D]),
+    "mappg_sys_autotune": (C.c_int, [_VP, _I, _I, _D]),
     "mappg_cg_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                C.c_int, _D]),
     "mappg_batch_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -329,10 +329,12 @@ class System:
         check(load().mappg_sys_sync(self.h))
 
     def autotune(self):
-        tpa = C.c_int()
-        ms = np.zeros(3)
-        check(load().mappg_sys_autotune(self.h, C.byref(tpa), dptr(ms)))
-        return tpa.value, dict(zip((4, 8, 16), ms))
+        """(lanes per atom, entries per step, {(lanes, entries): ms})"""
+        tpa, unroll = C.c_int(), C.c_int()
+        ms = np.zeros(6)
+        check(load().mappg_sys_autotune(self.h, C.byref(tpa), C.byref(unroll), dptr(ms)))
+        keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2))
+        return tpa.value, unroll.value, {k: v for k, v in zip(keys, ms) if v > 0}
 
     def enqueue(self, what):
         check(load().mappg_sys_enqueue(self.h, int(what)))

@@ -508,23 +508,26 @@ int mappg_sys_stats(mappg_sys* s, long long* out6) {
     });
 }
 
-// atoms-per-block / lanes-per-atom choice: the density and force passes on
-// the system's own atoms and neighbour list, timed with CUDA events for
-// each lane count; the fastest is kept for the system's later launches
-int mappg_sys_autotune(mappg_sys* s, int* tpa_out, double* ms_out) {
+// lanes per atom (atoms per block) and neighbour entries per loop step of
+// the density and force kernels: both passes on the system's own atoms and
+// neighbour list, timed with CUDA events for each candidate; the fastest is
+// kept for the system's later launches
+int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_out) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (s->run) throw Error{MAPPG_ERR_ARG, "an NVT run is in progress"};
         if (!s->built) sys_build(s);
-        const int cand[3] = {4, 8, 16};
+        const int cand[6][2] = {{4, 1}, {8, 1}, {16, 1}, {4, 2}, {8, 2}, {16, 2}};
+        const int ncand = s->precision == MAPPG_MIXED ? 6 : 3;  // the FP64 kernels have no unrolled form
         cudaEvent_t e0, e1;
         MAPPG_CUDA(cudaEventCreate(&e0));
         MAPPG_CUDA(cudaEventCreate(&e1));
         double best = 1e30;
-        int best_tpa = s->tpa;
+        int best_tpa = s->tpa, best_u = s->unroll;
         try {
-            for (int c = 0; c < 3; c++) {
-                s->tpa = cand[c];
+            for (int c = 0; c < ncand; c++) {
+                s->tpa = cand[c][0];
+                s->unroll = cand[c][1];
                 launch_density_only(s);  // warm-up (and first-use set-up)
                 launch_force_only(s);
                 MAPPG_CUDA(cudaEventRecord(e0, s->stream));
@@ -539,19 +542,23 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, double* ms_out) {
                 if (ms_out) ms_out[c] = ms / 3.0;
                 if (ms < best) {
                     best = ms;
-                    best_tpa = cand[c];
+                    best_tpa = cand[c][0];
+                    best_u = cand[c][1];
                 }
             }
         } catch (...) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             s->tpa = best_tpa;
+            s->unroll = best_u;
             throw;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         s->tpa = best_tpa;
+        s->unroll = best_u;
         if (tpa_out) *tpa_out = best_tpa;
+        if (unroll_out) *unroll_out = best_u;
     });
 }
 

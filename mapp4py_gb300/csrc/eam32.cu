@@ -4,11 +4,10 @@
 //   k_density32  rho_i in FP32, then F'(rho_i) and F(rho_i) from the FP32
 //                embedding table with its constant term carried as head +
 //                tail; writes q32[i] = (p'_i, F'_i) for the force pass
-//   k_force32    forces, pair energy and virial from one 48-byte record per
-//                (pair type, knot); F'_j rides in q32[j].w, so a neighbour
-//                costs one 16-byte gather plus the record; optional MD tail:
-//                kinetic tensor of v + f dt/2m and the closing half of the
-//                Nose-Hoover chain in the last block
+//   k_force32    forces, pair energy and virial from one 32-byte record per
+//                (pair type, knot) (plus a 16-byte one for unlike pairs);
+//                F'_j rides in q32[j].w, so a neighbour costs one 16-byte
+//                gather plus the record
 //   k_energy32   energy only (line-search trials)
 //
 // Precision: every per-pair term is FP32; per-atom sums are FP32 within a
@@ -23,6 +22,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "eam_common.cuh"
 #include "nhc.cuh"
@@ -37,36 +37,6 @@ struct Smem32 {
             off[t] = make_float4(a.fr.off[t][0], a.fr.off[t][1], a.fr.off[t][2], 0.f);
         for (int t = threadIdx.x; t < a.ne * a.ne; t += blockDim.x) cut_sq[t] = (float)a.cut_sq[t];
         __syncthreads();
-    }
-};
-
-// frame offset of a neighbour image from its entry's bin-step code
-// c = (d0+1) + 3(d1+1) + 9(d2+1): -8 d, computed instead of read from a
-// table (the pair loops are bound by the L1 data pipe, which a shared-
-// memory table would share)
-__device__ __forceinline__ void code_offset(int e, float& ox, float& oy, float& oz) {
-    const int c = entry_code(e);
-    const int t9 = (c >= 9) + (c >= 18);
-    const int r9 = c - 9 * t9;
-    const int t3 = (r9 >= 3) + (r9 >= 6);
-    const int t1 = r9 - 3 * t3;
-    ox = (float)(8 - 8 * t1);
-    oy = (float)(8 - 8 * t3);
-    oz = (float)(8 - 8 * t9);
-}
-
-// squared cutoffs of up to four pair types held in registers
-struct Cut4 {
-    float c0, c1, c2, c3;
-    __device__ Cut4(const Smem32& S, int ne) {
-        c0 = S.cut_sq[0];
-        c1 = ne * ne > 1 ? S.cut_sq[1] : c0;
-        c2 = ne * ne > 2 ? S.cut_sq[2] : c0;
-        c3 = ne * ne > 3 ? S.cut_sq[3] : c0;
-    }
-    __device__ __forceinline__ float operator()(const Smem32& S, int t) const {
-        if (t > 3) return S.cut_sq[t];  // more than two elements
-        return (t & 2) ? ((t & 1) ? c3 : c2) : ((t & 1) ? c1 : c0);
     }
 };
 
@@ -170,33 +140,47 @@ __device__ __forceinline__ CellFrame cell_frame(const CellGeo* g) {
 }
 
 // one atom's density row (TPA lanes), its embedding terms and q32 record
-template <int TPA, bool ORTHO, class FR>
+template <int TPA, bool ORTHO, int U, class FR>
 __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
                                              int i, int lane, bool active, float& es, float& ec) {
     float acc = 0.f;
     int ei = 0;
-    const Cut4 cut(S, a.ne);
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
         pi = __ldg(a.p32 + i);
         ei = a.elem[i];
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
-        for (int k = lane; k < nn; k += TPA) {
-            const int e = __ldg(row + k);
+        auto pair = [&](int e, const float4& q) {
             const int ej = entry_elem(e);
-            const float4 q = __ldg(a.p32 + entry_j(e));
-            float ox, oy, oz;
-            code_offset(e, ox, oy, oz);
+            const float4 o = S.off[entry_code(e)];
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < cut(S, ei * a.ne + ej)) {
+            if (rsq < S.cut_sq[ei * a.ne + ej]) {
                 const float r = rsq * inv_sqrt(rsq);
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
                 const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
                 acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+            }
+        };
+        if (U == 1) {
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                pair(e, __ldg(a.p32 + entry_j(e)));
+            }
+        } else {
+            // two entries per step: both gathers are in flight together;
+            // the additions keep the order of the one-entry loop
+            for (int k = lane; k < nn; k += 2 * TPA) {
+                const bool v1 = k + TPA < nn;
+                const int e0 = __ldg(row + k);
+                const int e1 = v1 ? __ldg(row + k + TPA) : e0;
+                const float4 q0 = __ldg(a.p32 + entry_j(e0));
+                const float4 q1 = __ldg(a.p32 + entry_j(e1));
+                pair(e0, q0);
+                if (v1) pair(e1, q1);
             }
         }
     }
@@ -211,8 +195,8 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
     }
 }
 
-template <int TPA, bool ORTHO>
-__global__ void __launch_bounds__(256, 8) k_density32(EamArgs a) {
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(256) k_density32(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -224,7 +208,7 @@ __global__ void __launch_bounds__(256, 8) k_density32(EamArgs a) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        density_atom<TPA, ORTHO>(a, S, K, a.fr, i, lane, active, es, ec);
+        density_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec);
     }
     double v[1] = {(double)es - (double)ec};
     if (block_partials<1>(v, a.partials, 0, &a.sc->counter[1]) && threadIdx.x < 32) {
@@ -238,8 +222,8 @@ __global__ void __launch_bounds__(256, 8) k_density32(EamArgs a) {
 }
 
 // batch: blocks walk chunks; the chunk's embedding energy goes to slot 13
-template <int TPA, bool ORTHO>
-__global__ void __launch_bounds__(256, 8) k_density32b(EamArgs a) {
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -251,20 +235,17 @@ __global__ void __launch_bounds__(256, 8) k_density32b(EamArgs a) {
         float es = 0.f, ec = 0.f;
         for (int i0 = lo; i0 < hi; i0 += apb) {
             const int i = i0 + (int)threadIdx.x / TPA;
-            density_atom<TPA, ORTHO>(a, S, K, fr, i, lane, i < hi, es, ec);
+            density_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec);
         }
         chunk_store<1>([&](int) { return (double)es - (double)ec; }, a.chunk_part + (size_t)ch * kChunkSlots + 13);
     }
 }
 
-// one atom's force row (TPA lanes): force, pair energy, virial and (TAIL) the
-// kinetic tensor of v + f dt/2m into the thread's shared slots ke[c*256]
-template <int TPA, bool ORTHO, bool TAIL, class FR>
+// one atom's force row (TPA lanes): force, pair energy and virial
+template <int TPA, bool ORTHO, int U, class FR>
 __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
-                                           int i, int lane, bool active, float& es, float& ec, float (&w)[6],
-                                           float* ke) {
+                                           int i, int lane, bool active, float& es, float& ec, float (&w)[6]) {
     float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
-    const Cut4 cut(S, a.ne);
     int ei = 0;
     if (active) {
         const float4 pi = __ldg(a.q32 + i);
@@ -272,16 +253,13 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         ei = a.elem[i];
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
-        for (int k = lane; k < nn; k += TPA) {
-            const int e = __ldg(row + k);
+        auto pair = [&](int e, const float4& q) {
             const int t = ei * a.ne + entry_elem(e);
-            const float4 q = __ldg(a.q32 + entry_j(e));
-            float ox, oy, oz;
-            code_offset(e, ox, oy, oz);
+            const float4 o = S.off[entry_code(e)];
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < cut(S, t)) {
+            if (rsq < S.cut_sq[t]) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;
@@ -313,6 +291,23 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 w[4] = fmaf(fdy, dz, w[4]);
                 w[5] = fmaf(fdz, dz, w[5]);
             }
+        };
+        if (U == 1) {
+            for (int k = lane; k < nn; k += TPA) {
+                const int e = __ldg(row + k);
+                pair(e, __ldg(a.q32 + entry_j(e)));
+            }
+        } else {
+            // two entries per step, sums in the order of the one-entry loop
+            for (int k = lane; k < nn; k += 2 * TPA) {
+                const bool v1 = k + TPA < nn;
+                const int e0 = __ldg(row + k);
+                const int e1 = v1 ? __ldg(row + k + TPA) : e0;
+                const float4 q0 = __ldg(a.q32 + entry_j(e0));
+                const float4 q1 = __ldg(a.q32 + entry_j(e1));
+                pair(e0, q0);
+                if (v1) pair(e1, q1);
+            }
         }
         kahan_add(es, ec, ep);
     }
@@ -326,25 +321,11 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         a.f32[i] = fx;
         a.f32[a.n + i] = fy;
         a.f32[2 * a.n + i] = fz;
-        if (TAIL) {
-            // kinetic tensor of the half-kicked velocity v + f dt/2m
-            const float dtm = a.dtm32[ei], m = a.mass32[ei];
-            const float vx = fmaf(fx, dtm, __ldg(a.v32 + i));
-            const float vy = fmaf(fy, dtm, __ldg(a.v32 + a.n + i));
-            const float vz = fmaf(fz, dtm, __ldg(a.v32 + 2 * a.n + i));
-            const float mx = m * vx, my = m * vy, mz = m * vz;
-            ke[0] = fmaf(mx, vx, ke[0]);
-            ke[256] = fmaf(mx, vy, ke[256]);
-            ke[512] = fmaf(mx, vz, ke[512]);
-            ke[768] = fmaf(my, vy, ke[768]);
-            ke[1024] = fmaf(my, vz, ke[1024]);
-            ke[1280] = fmaf(mz, vz, ke[1280]);
-        }
     }
 }
 
-template <int TPA, bool ORTHO, bool TAIL>
-__global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -353,90 +334,46 @@ __global__ void __launch_bounds__(256, 5) k_force32(EamArgs a) {
     const int stride = (gridDim.x * blockDim.x) / TPA;
     float es = 0.f, ec = 0.f;  // pair energy, compensated
     float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    // kinetic tensor (TAIL): one private shared-memory slot per thread keeps
-    // these six sums out of registers, so the MD variant runs at the same
-    // occupancy as the plain one
-    __shared__ float ke[TAIL ? 6 : 1][256];
-    if (TAIL)
-#pragma unroll
-        for (int c = 0; c < 6; c++) ke[c][threadIdx.x] = 0.f;
     for (int base = 0;; base += stride) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        force_atom<TPA, ORTHO, TAIL>(a, S, K, a.fr, i, lane, active, es, ec, w, &ke[0][threadIdx.x]);
+        force_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec, w);
     }
-    constexpr int NS = TAIL ? 13 : 7;  // energy, virial[6], kinetic tensor[6]
     auto sum_k = [&](int k) -> double {
-        switch (k) {
-            case 0: return 0.5 * ((double)es - (double)ec);
-            case 1: return 0.5 * (double)w[0];
-            case 2: return 0.5 * (double)w[1];
-            case 3: return 0.5 * (double)w[2];
-            case 4: return 0.5 * (double)w[3];
-            case 5: return 0.5 * (double)w[4];
-            case 6: return 0.5 * (double)w[5];
-            default: return (double)ke[TAIL ? k - 7 : 0][threadIdx.x];
-        }
+        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1];
     };
-    __shared__ double tot[NS];
-    if (block_partials_fn<NS>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
-        final_sums_smem<NS>(a.partials, gridDim.x, tot);
+    __shared__ double tot[7];
+    if (block_partials_fn<7>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
+        final_sums_smem<7>(a.partials, gridDim.x, tot);
         if (threadIdx.x == 0) {
             DevScalars* sc = a.sc;
             sc->energy = tot[0] + sc->e_embed;
             for (int k = 0; k < 6; k++) sc->virial[k] = tot[k + 1];
-            if (TAIL) {
-                // update_x_d (md_nvt.cpp:106-128) then the closing half of the
-                // thermostat (md_nvt.cpp:427-432)
-                for (int k = 0; k < 6; k++) sc->mvv[k] = tot[7 + k];
-                sc->T_part = (tot[7] + (tot[10] + tot[12])) / a.nhc.ndof_kB;
-                sc->fac_close = thermo_half(a.nhc, sc);
-                sc->pending_kick = 1;
-                long long st = ++sc->step;
-                if (st <= a.nsteps) write_thermo_row(a.thermo, sc, st);
-                if (!(isfinite(sc->energy) && isfinite(sc->T_part))) sc->bad = 1;
-            }
             sc->counter[0] = 0;
         }
     }
 }
 
-// batch: chunk slots 0 pair energy, 1-6 virial, 7-12 kinetic tensor (TAIL)
-template <int TPA, bool ORTHO, bool TAIL>
-__global__ void __launch_bounds__(256, 5) k_force32b(EamArgs a) {
+// batch: chunk slots 0 pair energy, 1-6 virial
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32b(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
-    __shared__ float ke[TAIL ? 6 : 1][256];
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
         float es = 0.f, ec = 0.f;
         float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (TAIL)
-#pragma unroll
-            for (int c = 0; c < 6; c++) ke[c][threadIdx.x] = 0.f;
         for (int i0 = lo; i0 < hi; i0 += apb) {
             const int i = i0 + (int)threadIdx.x / TPA;
-            force_atom<TPA, ORTHO, TAIL>(a, S, K, fr, i, lane, i < hi, es, ec, w, &ke[0][threadIdx.x]);
+            force_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec, w);
         }
-        constexpr int NS = TAIL ? 13 : 7;
-        chunk_store<NS>(
-            [&](int k) -> double {
-                switch (k) {
-                    case 0: return 0.5 * ((double)es - (double)ec);
-                    case 1: return 0.5 * (double)w[0];
-                    case 2: return 0.5 * (double)w[1];
-                    case 3: return 0.5 * (double)w[2];
-                    case 4: return 0.5 * (double)w[3];
-                    case 5: return 0.5 * (double)w[4];
-                    case 6: return 0.5 * (double)w[5];
-                    default: return (double)ke[TAIL ? k - 7 : 0][threadIdx.x];
-                }
-            },
+        chunk_store<7>(
+            [&](int k) -> double { return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1]; },
             a.chunk_part + (size_t)ch * kChunkSlots);
     }
 }
@@ -447,7 +384,6 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
                                             int i, int lane, bool active, float& es, float& ec) {
     float acc = 0.f, ep = 0.f;
     int ei = 0;
-    const Cut4 cut(S, a.ne);
     if (active) {
         const float4 pi = __ldg(a.p32 + i);
         ei = a.elem[i];
@@ -458,12 +394,11 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
             const int ej = entry_elem(e);
             const int t = ei * a.ne + ej;
             const float4 q = __ldg(a.p32 + entry_j(e));
-            float ox, oy, oz;
-            code_offset(e, ox, oy, oz);
+            const float4 o = S.off[entry_code(e)];
             float dx, dy, dz;
-            cart<ORTHO>(fr, (pi.x - q.x) + ox, (pi.y - q.y) + oy, (pi.z - q.z) + oz, dx, dy, dz);
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < cut(S, t)) {
+            if (rsq < S.cut_sq[t]) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;
@@ -584,64 +519,44 @@ __global__ void k_cells_done(EamArgs a, const int* __restrict__ cell_chunk, Cell
 }
 
 // ------------------------------------------------------------------ launchers
-template <int TPA, bool ORTHO>
+// kernels take (lanes per atom TPA, orthorhombic frame, neighbour entries per
+// loop step U); TPA and U come from the system (mappg_sys_autotune)
+template <int TPA, bool ORTHO, int U>
 static void density_t(mappg_sys* s, const EamArgs& a) {
     static int grid = 0;
-    if (!grid) grid = occupancy_grid(s, k_density32<TPA, ORTHO>, 256);
-    k_density32<TPA, ORTHO><<<grid, 256, 0, s->stream>>>(a);
+    if (!grid) grid = occupancy_grid(s, k_density32<TPA, ORTHO, U>, 256);
+    k_density32<TPA, ORTHO, U><<<grid, 256, 0, s->stream>>>(a);
 }
 
-template <int TPA, bool ORTHO>
+template <int TPA, bool ORTHO, int U>
 static void force_t(mappg_sys* s, const EamArgs& a) {
-    static int grid = 0, grid_tail = 0;
-    if (a.md_tail) {
-        if (!grid_tail) grid_tail = occupancy_grid(s, k_force32<TPA, ORTHO, true>, 256);
-        k_force32<TPA, ORTHO, true><<<grid_tail, 256, 0, s->stream>>>(a);
-    } else {
-        if (!grid) grid = occupancy_grid(s, k_force32<TPA, ORTHO, false>, 256);
-        k_force32<TPA, ORTHO, false><<<grid, 256, 0, s->stream>>>(a);
-    }
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_force32<TPA, ORTHO, U>, 256);
+    k_force32<TPA, ORTHO, U><<<grid, 256, 0, s->stream>>>(a);
 }
 
-template <int TPA, bool ORTHO>
+template <int TPA, bool ORTHO, int U>
 static void energy_t(mappg_sys* s, const EamArgs& a) {
     static int grid = 0;
     if (!grid) grid = occupancy_grid(s, k_energy32<TPA, ORTHO>, 256);
     k_energy32<TPA, ORTHO><<<grid, 256, 0, s->stream>>>(a);
 }
 
-#define MAPPG_TPA32(FN)                                  \
-    do {                                                 \
-        const bool o = a.fr.ortho != 0;                  \
-        switch (s->tpa) {                                \
-            case 4: o ? FN<4, true>(s, a) : FN<4, false>(s, a); break;    \
-            case 16: o ? FN<16, true>(s, a) : FN<16, false>(s, a); break; \
-            case 32: o ? FN<32, true>(s, a) : FN<32, false>(s, a); break; \
-            default: o ? FN<8, true>(s, a) : FN<8, false>(s, a); break;   \
-        }                                                \
-        MAPPG_CUDA(cudaGetLastError());                  \
-    } while (0)
-
-template <int TPA, bool ORTHO>
+template <int TPA, bool ORTHO, int U>
 static void density_b(mappg_sys* s, const EamArgs& a) {
     static int grid = 0;
-    if (!grid) grid = occupancy_grid(s, k_density32b<TPA, ORTHO>, 256);
-    k_density32b<TPA, ORTHO><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
+    if (!grid) grid = occupancy_grid(s, k_density32b<TPA, ORTHO, U>, 256);
+    k_density32b<TPA, ORTHO, U><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
 }
 
-template <int TPA, bool ORTHO>
+template <int TPA, bool ORTHO, int U>
 static void force_b(mappg_sys* s, const EamArgs& a) {
-    static int grid = 0, grid_tail = 0;
-    if (a.md_tail) {
-        if (!grid_tail) grid_tail = occupancy_grid(s, k_force32b<TPA, ORTHO, true>, 256);
-        k_force32b<TPA, ORTHO, true><<<std::min(grid_tail, a.nchunk), 256, 0, s->stream>>>(a);
-    } else {
-        if (!grid) grid = occupancy_grid(s, k_force32b<TPA, ORTHO, false>, 256);
-        k_force32b<TPA, ORTHO, false><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
-    }
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_force32b<TPA, ORTHO, U>, 256);
+    k_force32b<TPA, ORTHO, U><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
 }
 
-template <int TPA, bool ORTHO>
+template <int TPA, bool ORTHO, int U>
 static void energy_b(mappg_sys* s, const EamArgs& a) {
     static int grid = 0;
     if (!grid) grid = occupancy_grid(s, k_energy32b<TPA, ORTHO>, 256);
@@ -655,17 +570,31 @@ static bool all_ortho(const mappg_sys* s) {
     return true;
 }
 
-#define MAPPG_TPA32B(FN)                                 \
-    do {                                                 \
-        const bool o = all_ortho(s);                     \
-        switch (s->tpa) {                                \
-            case 4: o ? FN<4, true>(s, a) : FN<4, false>(s, a); break;    \
-            case 16: o ? FN<16, true>(s, a) : FN<16, false>(s, a); break; \
-            case 32: o ? FN<32, true>(s, a) : FN<32, false>(s, a); break; \
-            default: o ? FN<8, true>(s, a) : FN<8, false>(s, a); break;   \
-        }                                                \
-        MAPPG_CUDA(cudaGetLastError());                  \
+template <int TPA, int U, class F>
+static void pick_ortho(bool o, F&& fn) {
+    if (o)
+        fn(std::integral_constant<int, TPA>(), std::true_type(), std::integral_constant<int, U>());
+    else
+        fn(std::integral_constant<int, TPA>(), std::false_type(), std::integral_constant<int, U>());
+}
+
+// dispatch on the system's lanes per atom, unroll and frame shape
+#define MAPPG_DISPATCH32(FN, ORTHO_EXPR)                                                              \
+    do {                                                                                              \
+        const bool o = (ORTHO_EXPR);                                                                  \
+        auto call = [&](auto T, auto O, auto U) { FN<decltype(T)::value, decltype(O)::value, decltype(U)::value>(s, a); }; \
+        const bool u2 = s->unroll == 2;                                                               \
+        switch (s->tpa) {                                                                             \
+            case 4: u2 ? pick_ortho<4, 2>(o, call) : pick_ortho<4, 1>(o, call); break;                \
+            case 16: u2 ? pick_ortho<16, 2>(o, call) : pick_ortho<16, 1>(o, call); break;            \
+            case 32: pick_ortho<32, 1>(o, call); break;                                               \
+            default: u2 ? pick_ortho<8, 2>(o, call) : pick_ortho<8, 1>(o, call); break;               \
+        }                                                                                             \
+        MAPPG_CUDA(cudaGetLastError());                                                               \
     } while (0)
+
+#define MAPPG_TPA32(FN) MAPPG_DISPATCH32(FN, a.fr.ortho != 0)
+#define MAPPG_TPA32B(FN) MAPPG_DISPATCH32(FN, all_ortho(s))
 
 static void cells_done(mappg_sys* s, const EamArgs& a, int what) {
     k_cells_done<<<(s->ncell * 32 + 255) / 256, 256, 0, s->stream>>>(a, s->cell_chunk, s->cmd, what);
@@ -683,7 +612,7 @@ void launch_density32(mappg_sys* s, const EamArgs& a) {
 void launch_force32(mappg_sys* s, const EamArgs& a) {
     if (s->ncell > 1) {
         MAPPG_TPA32B(force_b);
-        cells_done(s, a, a.md_tail ? 2 : 0);
+        cells_done(s, a, 0);
     } else {
         MAPPG_TPA32(force_t);
     }

@@ -42,6 +42,8 @@
 
 namespace mappg {
 
+void launch_cells_done(mappg_sys* s, const EamArgs& a, int what);  // eam32.cu
+
 struct MdArgs {
     int n;
     double* x;
@@ -296,6 +298,70 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
             a.sc->pending_kick = 0;
             a.sc->counter[4] = 0;
         }
+    }
+}
+
+// update_x_d (md_nvt.cpp:106-128) and the closing half of the thermostat
+// (md_nvt.cpp:427-432) of a mixed step: kinetic tensor of the half-kicked
+// velocity v + f dt/2m (FP32 terms, FP64 sums), then in the last block the
+// chain, the pending kick and the thermo row
+__global__ void __launch_bounds__(256) k_close32(MdArgs a) {
+    const int n = a.n;
+    float k0 = 0.f, k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f, k5 = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int e = a.elem[i];
+        const float dtm = a.dtm32[e], m = (float)a.masses[e];
+        const float vx = fmaf(a.f32[i], dtm, a.v32[i]);
+        const float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
+        const float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
+        const float mx = m * vx, my = m * vy, mz = m * vz;
+        k0 = fmaf(mx, vx, k0);
+        k1 = fmaf(mx, vy, k1);
+        k2 = fmaf(mx, vz, k2);
+        k3 = fmaf(my, vy, k3);
+        k4 = fmaf(my, vz, k4);
+        k5 = fmaf(mz, vz, k5);
+    }
+    double d[6] = {k0, k1, k2, k3, k4, k5};
+    if (md_block_partials<6>(d, a.partials, &a.sc->counter[5]) && threadIdx.x < 32) {
+        double t[6];
+        final_sums<6>(a.partials, gridDim.x, t);
+        if (threadIdx.x == 0) {
+            DevScalars* sc = a.sc;
+            for (int k = 0; k < 6; k++) sc->mvv[k] = t[k];
+            sc->T_part = (t[0] + (t[3] + t[5])) / a.nhc.ndof_kB;
+            sc->fac_close = thermo_half(a.nhc, sc);
+            sc->pending_kick = 1;
+            long long st = ++sc->step;
+            if (st <= a.nsteps) write_thermo_row(a.thermo, sc, st);
+            if (!(isfinite(sc->energy) && isfinite(sc->T_part))) sc->bad = 1;
+            sc->counter[5] = 0;
+        }
+    }
+}
+
+// the same kinetic tensor per chunk of a batch (slots 7-12), for the
+// per-cell closing half in k_cells_done
+__global__ void __launch_bounds__(256) k_ke32b(MdArgs a) {
+    const int n = a.n;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        float k[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const int e = a.elem[i];
+            const float dtm = a.dtm32[e], m = (float)a.masses[e];
+            const float vx = fmaf(a.f32[i], dtm, a.v32[i]);
+            const float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
+            const float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
+            const float mx = m * vx, my = m * vy, mz = m * vz;
+            k[0] = fmaf(mx, vx, k[0]);
+            k[1] = fmaf(mx, vy, k[1]);
+            k[2] = fmaf(mx, vz, k[2]);
+            k[3] = fmaf(my, vy, k[3]);
+            k[4] = fmaf(my, vz, k[4]);
+            k[5] = fmaf(mz, vz, k[5]);
+        }
+        chunk_store<6>([&](int q) { return (double)k[q]; }, a.chunk_part + (size_t)ch * kChunkSlots + 7);
     }
 }
 
@@ -572,12 +638,8 @@ static void launch_step32(mappg_sys* s, const MdArgs& a) {
     launch_rebuild_chain(s);
     EamArgs e = eam_args(s);
     launch_density32(s, e);
-    e.md_tail = 1;
-    e.thermo = a.thermo;
-    e.nsteps = a.nsteps;
-    e.nhc = a.nhc;
-    for (int k = 0; k < s->ne; k++) e.dtm32[k] = a.dtm32[k];
     launch_force32(s, e);
+    k_close32<<<g, 256, 0, s->stream>>>(a);
 }
 
 static void launch_step32b(mappg_sys* s, const MdArgs& a) {
@@ -588,12 +650,12 @@ static void launch_step32b(mappg_sys* s, const MdArgs& a) {
     launch_rebuild_chain(s);
     EamArgs e = eam_args(s);
     launch_density32(s, e);
-    e.md_tail = 1;
+    launch_force32(s, e);
+    k_ke32b<<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a);
     e.thermo = a.thermo;
     e.nsteps = a.nsteps;
     e.nhc = a.nhc;
-    for (int k = 0; k < s->ne; k++) e.dtm32[k] = a.dtm32[k];
-    launch_force32(s, e);  // with the per-cell closing half (k_cells_done)
+    launch_cells_done(s, e, 2);  // kinetic tensors, each cell's closing half, thermo rows
 }
 
 struct NvtRun {

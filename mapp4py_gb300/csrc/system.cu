@@ -434,7 +434,9 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         const int nbx = BATCH ? cg->nb[0] : a.g.nb[0], nby = BATCH ? cg->nb[1] : a.g.nb[1],
                   nbz = BATCH ? cg->nb[2] : a.g.nb[2];
         const int bin_base = BATCH ? cg->bin_base : 0;
-        const double* h6 = BATCH ? cg->h6 : a.g.h6;
+        double h6[6];  // in registers: taking the address of a kernel argument would copy it to local memory
+#pragma unroll
+        for (int k = 0; k < 6; k++) h6[k] = BATCH ? cg->h6[k] : a.g.h6[k];
         float4 pi = a.p32[i];
         int ei = a.elem[i];
         int bc = a.binc[i];
@@ -691,8 +693,6 @@ EamArgs eam_args(mappg_sys* s) {
     a.rho32out = s->rho32;
     a.f = s->f;
     a.f32 = s->f32;
-    a.v32 = s->v32;
-    for (int e = 0; e < s->ne; e++) a.mass32[e] = (float)s->masses[e];
     a.partials = s->partials;
     a.sc = s->sc;
     a.ncell = s->ncell;

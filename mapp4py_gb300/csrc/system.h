@@ -150,12 +150,8 @@ struct EamArgs {
     float* f32;            // SoA 3n (mixed kernels)
     double* partials;
     DevScalars* sc;
-    // mixed MD tail of the force kernel (kinetic energy and thermostat)
-    const float* v32;      // SoA 3n
-    float dtm32[kMaxElem]; // dt/2/m
-    float mass32[kMaxElem];
+    // per-cell closing half of a batch MD step (k_cells_done)
     double* thermo;
-    int md_tail;
     long long nsteps;
     NhcParams nhc;
     // batch of cells (ncell > 1): per-atom cell, chunks, per-chunk sums
@@ -176,6 +172,7 @@ struct mappg_sys {
     int device = 0;
     int sm_count = 0;
     int tpa = 8;
+    int unroll = 1;  // neighbour entries per loop step of the mixed kernels (1 or 2)
     double skin = 0.5;
     double max_cut = 0.0;  // max cut + skin
     double cut_sq[mappg::kMaxElem * mappg::kMaxElem];
