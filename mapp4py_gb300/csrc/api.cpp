@@ -88,6 +88,17 @@ void upload_tables(mappg_ff* ff) {
         MAPPG_CUDA(cudaMalloc(dst, sizeof(float4) * n));
         MAPPG_CUDA(cudaMemcpy(*dst, f.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
     };
+    // setfl and funcfl density functions depend on the neighbour's element
+    // only (the reference aliases rho_arr[i][j] to rho_arr[i][0],
+    // import_eam.h:499-504); the kernels then read one row per e_j, which
+    // halves the density tables' share of the L1 cache for two elements
+    d.rho_ei = 0;
+    for (int ej = 0; ej < ne && !d.rho_ei; ej++)
+        for (int ei = 1; ei < ne; ei++)
+            if (memcmp(t.rho_at(ej, ei), t.rho_at(ej, 0), sizeof(double) * 4 * t.nr) != 0) {
+                d.rho_ei = 1;
+                break;
+            }
     up64(&d.rho64, t.rho, nrt);
     up64(&d.rphi64, t.rphi, nrt);
     up64(&d.F64, t.F, nFt);

@@ -151,7 +151,7 @@ __device__ __forceinline__ double density64_lane(const EamArgs& a, const Smem64&
         if (rsq < S.cut_sq[ei * a.ne + ej]) {
             double p;
             int m = knot64(sqrt(rsq), a, p);
-            acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+            acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
         }
     }
     return acc;
@@ -177,9 +177,9 @@ __device__ __forceinline__ void force64_lane(const EamArgs& a, const Smem64& S, 
             const double rinv = 1.0 / r;
             double p;
             const int m = knot64(r, a, p);
-            const double der_i = spl_der(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p) * dri;
+            const double der_i = spl_der(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p) * dri;
             double der_j = der_i;
-            if (ej != ei) der_j = spl_der(ldg4(a.rho64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) * dri;
+            if (ej != ei) der_j = spl_der(ldg4(a.rho64 + (size_t)(ei * a.ne + ej * a.rho_ei) * a.nr + m), p) * dri;
             const Dbl4 cz = ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m);
             const double z = spl_val(cz, p);
             const double zp = spl_der(cz, p) * dri;
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(256) k_descriptors(EamArgs a, const int* __res
                 if (rsq < S.cut_sq[ei * a.ne + ej]) {
                     double p;
                     const int m = knot64(sqrt(rsq), a, p);
-                    rho += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+                    rho += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
                 }
                 const float r = (float)sqrt(rsq);
                 if (r < kDescRc && ej < 2) {
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(256) k_energy64(EamArgs a) {
                     const double r = sqrt(rsq);
                     double p;
                     const int m = knot64(r, a, p);
-                    acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+                    acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
                     ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
                 }
             }
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(256) k_energy64b(EamArgs a, const int* __restr
                         const double r = sqrt(rsq);
                         double p;
                         const int m = knot64(r, a, p);
-                        acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei) * a.nr + m), p);
+                        acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
                         ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
                     }
                 }

@@ -40,6 +40,23 @@ struct Smem32 {
     }
 };
 
+// frame offset -8 d of a neighbour image from its entry's bin-step code
+// c = (d0+1) + 3(d1+1) + 9(d2+1), by integer arithmetic (c/9 = (57 c) >> 9
+// and r/3 = (11 r) >> 5 hold for c < 27, r < 9) and an exact int-to-float
+// through the float bits of 2^23 + k; cheaper on the L1 data pipe, which
+// bounds these kernels, than a table in shared memory
+__device__ __forceinline__ void image_offset(int e, float4& o) {
+    const int c = entry_code(e);
+    const int k2 = (c * 57) >> 9;
+    const int r = c - 9 * k2;
+    const int k1 = (r * 11) >> 5;
+    const int k0 = r - 3 * k1;
+    o.x = fmaf(__int_as_float(0x4B000000 + k0) - 8388608.0f, -8.0f, 8.0f);
+    o.y = fmaf(__int_as_float(0x4B000000 + k1) - 8388608.0f, -8.0f, 8.0f);
+    o.z = fmaf(__int_as_float(0x4B000000 + k2) - 8388608.0f, -8.0f, 8.0f);
+    o.w = 0.f;
+}
+
 // frame displacement (a,b,c) to Cartesian with the head + tail scale
 template <bool ORTHO, class FR>
 __device__ __forceinline__ void cart(const FR& fr, float a, float b, float c, float& x, float& y, float& z) {
@@ -151,17 +168,19 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
         ei = a.elem[i];
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
+        const float cut0 = S.cut_sq[0];
         auto pair = [&](int e, const float4& q) {
             const int ej = entry_elem(e);
-            const float4 o = S.off[entry_code(e)];
+            float4 o;
+            image_offset(e, o);
             float dx, dy, dz;
             cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < S.cut_sq[ei * a.ne + ej]) {
+            if (rsq < (a.cut_uniform ? cut0 : S.cut_sq[ei * a.ne + ej])) {
                 const float r = rsq * inv_sqrt(rsq);
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
                 acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
             }
         };
@@ -253,13 +272,15 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         ei = a.elem[i];
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
+        const float cut0 = S.cut_sq[0];
         auto pair = [&](int e, const float4& q) {
             const int t = ei * a.ne + entry_elem(e);
-            const float4 o = S.off[entry_code(e)];
+            float4 o;
+            image_offset(e, o);
             float dx, dy, dz;
             cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < S.cut_sq[t]) {
+            if (rsq < (a.cut_uniform ? cut0 : S.cut_sq[t])) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;
@@ -394,7 +415,8 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
             const int ej = entry_elem(e);
             const int t = ei * a.ne + ej;
             const float4 q = __ldg(a.p32 + entry_j(e));
-            const float4 o = S.off[entry_code(e)];
+            float4 o;
+            image_offset(e, o);
             float dx, dy, dz;
             cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -403,7 +425,7 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
                 const float r = rsq * rinv;
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei) * a.nr + m);
+                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
                 acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
                 const float4* rec = a.ftab + 2 * ((size_t)t * a.nr + m);
                 float4 r0, r1;

@@ -53,6 +53,37 @@ __device__ bool block_partials(double (&v)[K], double* partials, int slot0, unsi
     return last;
 }
 
+// block sums of K floats (FP32 within each warp, FP64 across warps and
+// blocks): for per-atom quantities whose warp sums need no more than FP32,
+// as kinetic tensors and displacement sums; FP64 work is scarce on this GPU
+template <int K>
+__device__ bool block_partials_f32(const float (&v)[K], double* partials, int slot0, unsigned* counter) {
+    __shared__ double red[32][K];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[w][k] = (double)t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int q = 0; q < nw; q++) t += red[q][threadIdx.x];
+        partials[blockIdx.x * kRedSlots + slot0 + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
 // the same with the K values produced on demand by get(k): only one of them
 // is live at a time, which keeps the register count of kernels with many
 // sums down

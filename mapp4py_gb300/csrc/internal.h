@@ -71,6 +71,7 @@ struct DevTables {
                                 // d = (c1, 2c2, 3c3)/dr of rho_{j->i} / rho_{i->j}
     float4* F32 = nullptr;      // embedding coefficients, [ne][nrho]
     float* F32lo = nullptr;     // c0 - (float)c0 of the embedding table
+    int rho_ei = 1;             // 0 when rho_{j->i} is the same table for every e_i
 };
 
 }  // namespace mappg

@@ -235,6 +235,7 @@ __global__ void k_step_open32(MdArgs a) {
     sc->rebuild = 0;
 }
 
+template <bool ORTHO>
 __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
     const int n = a.n;
     const double A = a.sc->kickA;
@@ -261,8 +262,9 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
         dsum2 = fmaf(vf[2], a.dt32, dsum2);
         // frame position and the skin test against the position at the build
         const int bc = a.binc[i];
-        const double u0 = a.bs[0] * xv[0] + (a.bs[1] * xv[1] + a.bs[2] * xv[2]);
-        const double u1 = a.bs[3] * xv[1] + a.bs[4] * xv[2];
+        // the scaled frame; for an orthorhombic box one product per axis
+        const double u0 = ORTHO ? a.bs[0] * xv[0] : a.bs[0] * xv[0] + (a.bs[1] * xv[1] + a.bs[2] * xv[2]);
+        const double u1 = ORTHO ? a.bs[3] * xv[1] : a.bs[3] * xv[1] + a.bs[4] * xv[2];
         const double u2 = a.bs[5] * xv[2];
         float4 p;
         p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
         const float4 q = a.p0[i];
         const float da = p.x - q.x, db = p.y - q.y, dc = p.z - q.z;
         float cx, cy, cz;
-        if (a.fr.ortho) {
+        if (ORTHO) {
             cx = da * a.fr.G[0][0];
             cy = db * a.fr.G[1][1];
             cz = dc * a.fr.G[2][2];
@@ -285,8 +287,8 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
         moved |= fmaf(cx, cx, fmaf(cy, cy, cz * cz)) > a.skin_sq32;
     }
     if (__syncthreads_or(moved) && threadIdx.x == 0) a.sc->rebuild = 1;
-    double dv[3] = {(double)dsum0, (double)dsum1, (double)dsum2};
-    if (md_block_partials<3>(dv, a.partials, &a.sc->counter[4]) && threadIdx.x < 32) {
+    const float dv[3] = {dsum0, dsum1, dsum2};
+    if (block_partials_f32<3>(dv, a.partials, 0, &a.sc->counter[4]) && threadIdx.x < 32) {
         double t[3];
         final_sums<3>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
@@ -322,8 +324,8 @@ __global__ void __launch_bounds__(256) k_close32(MdArgs a) {
         k4 = fmaf(my, vz, k4);
         k5 = fmaf(mz, vz, k5);
     }
-    double d[6] = {k0, k1, k2, k3, k4, k5};
-    if (md_block_partials<6>(d, a.partials, &a.sc->counter[5]) && threadIdx.x < 32) {
+    const float d[6] = {k0, k1, k2, k3, k4, k5};
+    if (block_partials_f32<6>(d, a.partials, 0, &a.sc->counter[5]) && threadIdx.x < 32) {
         double t[6];
         final_sums<6>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
@@ -489,8 +491,9 @@ __global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
             dsum1 = fmaf(vf[1], a.dt32, dsum1);
             dsum2 = fmaf(vf[2], a.dt32, dsum2);
             const int bc = a.binc[i];
-            const double u0 = g.bs[0] * xv[0] + (g.bs[1] * xv[1] + g.bs[2] * xv[2]);
-            const double u1 = g.bs[3] * xv[1] + g.bs[4] * xv[2];
+            const bool orth = g.ortho != 0;  // uniform over the chunk
+            const double u0 = orth ? g.bs[0] * xv[0] : g.bs[0] * xv[0] + (g.bs[1] * xv[1] + g.bs[2] * xv[2]);
+            const double u1 = orth ? g.bs[3] * xv[1] : g.bs[3] * xv[1] + g.bs[4] * xv[2];
             const double u2 = g.bs[5] * xv[2];
             float4 p;
             p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
@@ -634,7 +637,10 @@ static void launch_step64(mappg_sys* s, const MdArgs& a) {
 static void launch_step32(mappg_sys* s, const MdArgs& a) {
     int g = grid_for(s, s->n, 256);
     k_step_open32<<<1, 1, 0, s->stream>>>(a);
-    k_integrate32<<<g, 256, 0, s->stream>>>(a);
+    if (a.fr.ortho)
+        k_integrate32<true><<<g, 256, 0, s->stream>>>(a);
+    else
+        k_integrate32<false><<<g, 256, 0, s->stream>>>(a);
     launch_rebuild_chain(s);
     EamArgs e = eam_args(s);
     launch_density32(s, e);

@@ -680,10 +680,15 @@ EamArgs eam_args(mappg_sys* s) {
     a.fjtab = ff->dev.fjtab;
     a.F32 = ff->dev.F32;
     a.F32lo = ff->dev.F32lo;
+    a.rho_ei = ff->dev.rho_ei;
     a.dr_inv = ff->dev.dr_inv;
     a.drho_inv = ff->dev.drho_inv;
     a.rho_max = ff->dev.rho_max;
-    for (int p = 0; p < s->ne * s->ne; p++) a.cut_sq[p] = s->cut_sq[p];
+    a.cut_uniform = 1;
+    for (int p = 0; p < s->ne * s->ne; p++) {
+        a.cut_sq[p] = s->cut_sq[p];
+        if ((float)s->cut_sq[p] != (float)s->cut_sq[0]) a.cut_uniform = 0;
+    }
     memcpy(a.shift, s->shift, sizeof(a.shift));
     a.fr = s->frame;
     for (int d = 0; d < 3; d++) a.nb[d] = s->nb[d];

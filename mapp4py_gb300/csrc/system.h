@@ -138,6 +138,8 @@ struct EamArgs {
     const float4* fjtab;    // rho_{i->j} derivative per (pair type, knot)
     const float4* F32;
     const float* F32lo;
+    int rho_ei;              // 0: rho_{j->i} depends on e_j only (setfl, funcfl), read row e_j*ne
+    int cut_uniform;         // every pair type has the same cutoff
     double dr_inv, drho_inv, rho_max;
     double cut_sq[kMaxElem * kMaxElem];
     double shift[27][3];   // image shift n*H for image code (n0+1)+3(n1+1)+9(n2+1)
