@@ -413,15 +413,18 @@ __device__ __forceinline__ void frame_to_cart(const FR& fr, float a, float b, fl
 }
 
 // rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
-// candidates, ballots keep the row in (bin, index) order; x0 <- x
+// candidates, ballots keep the row in (bin step, bin order) order; x0 <- x
+// (blocks of 256 threads: eight warps, one per-warp bin table each)
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc) {
     if (!sc->rebuild) return;
     __shared__ float4 off[27];
+    __shared__ int s_pre[8][32], s_lo[8][32], s_img[8][32];  // per warp: the atom's 27 stencil bins
     if (threadIdx.x < 27)
         off[threadIdx.x] = make_float4(a.fr.off[threadIdx.x][0], a.fr.off[threadIdx.x][1], a.fr.off[threadIdx.x][2], 0.f);
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int n = a.n;
@@ -444,7 +447,12 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         double xi0 = a.x[i], xi1 = a.x[n + i], xi2 = a.x[2 * n + i];
         int cnt = 0;
         int* row = a.nbr + (size_t)i * a.maxnbr;
-        for (int c = 0; c < 27; c++) {
+        // the 27 stencil bins at once, lane c for bin step c: the candidates
+        // of all bins form one sequence (bin step, then bin order) that the
+        // warp walks 32 at a time, so lanes stay busy across bin borders
+        int lo = 0, ncand = 0, img = 0;
+        if (lane < 27) {
+            const int c = lane;
             int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
             int u0 = bi[0] + d0, u1 = bi[1] + d1, u2 = bi[2] + d2;
             int n0 = u0 < 0 ? -1 : (u0 >= nbx ? 1 : 0);
@@ -452,54 +460,75 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
             int n2 = u2 < 0 ? -1 : (u2 >= nbz ? 1 : 0);
             int w0 = u0 - n0 * nbx, w1 = u1 - n1 * nby, w2 = u2 - n2 * nbz;
             int b = bin_base + w0 + nbx * (w1 + nby * w2);
-            int lo = a.bin_start[b], hi = a.bin_start[b + 1];
-            float4 o = off[c];
-            bool self_img = (n0 | n1 | n2) == 0;
-            for (int k0 = lo; k0 < hi; k0 += 32) {
-                int k = k0 + lane;
-                bool keep = false;
-                int j = 0, ej = 0;
-                if (k < hi) {
-                    j = a.bin_atoms[k];
-                    if (!(self_img && j == i)) {
-                        float4 pj = a.p32[j];
-                        ej = a.elem[j];
-                        float dx, dy, dz;
-                        if (BATCH)
-                            frame_to_cart(*cg, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx,
-                                          dy, dz);
-                        else
-                            frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx,
-                                          dy, dz);
-                        float r2 = dx * dx + (dy * dy + dz * dz);
-                        int pe = ei * a.ne + ej;
-                        if (r2 < a.lo2[pe]) {
-                            keep = true;
-                        } else if (r2 <= a.hi2[pe]) {
-                            // exact reference predicate on S2X(s_j + n)
-                            double s0 = a.s[j], s1 = a.s[n + j], s2 = a.s[2 * n + j];
-                            if (n0 > 0) s0 = dadd(s0, 1.0);
-                            if (n0 < 0) s0 = dsub(s0, 1.0);
-                            if (n1 > 0) s1 = dadd(s1, 1.0);
-                            if (n1 < 0) s1 = dsub(s1, 1.0);
-                            if (n2 > 0) s2 = dadd(s2, 1.0);
-                            if (n2 < 0) s2 = dsub(s2, 1.0);
-                            double xj0, xj1, xj2;
-                            s2x(h6, s0, s1, s2, xj0, xj1, xj2);
-                            double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
-                            double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
-                            keep = rsq < a.cut_sk_sq[pe];
-                        }
+            lo = a.bin_start[b];
+            ncand = a.bin_start[b + 1] - lo;
+            img = (n0 + 1) | ((n1 + 1) << 2) | ((n2 + 1) << 4);
+        }
+        int incl = ncand;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        s_pre[wib][lane] = incl - ncand;
+        s_lo[wib][lane] = lo;
+        s_img[wib][lane] = img;
+        __syncwarp();
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            bool keep = false;
+            int j = 0, ej = 0, c = 0;
+            if (t < total) {
+                // the bin holding candidate t: the last c with pre[c] <= t
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (c + step < 27 && s_pre[wib][c + step] <= t) c += step;
+                const int k = s_lo[wib][c] + (t - s_pre[wib][c]);
+                const int im = s_img[wib][c];
+                const int n0 = (im & 3) - 1, n1 = ((im >> 2) & 3) - 1, n2 = ((im >> 4) & 3) - 1;
+                const float4 o = off[c];
+                const bool self_img = im == 21;  // no image shift
+                j = a.bin_atoms[k];
+                if (!(self_img && j == i)) {
+                    float4 pj = a.p32[j];
+                    ej = a.elem[j];
+                    float dx, dy, dz;
+                    if (BATCH)
+                        frame_to_cart(*cg, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
+                                      dz);
+                    else
+                        frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
+                                      dz);
+                    float r2 = dx * dx + (dy * dy + dz * dz);
+                    int pe = ei * a.ne + ej;
+                    if (r2 < a.lo2[pe]) {
+                        keep = true;
+                    } else if (r2 <= a.hi2[pe]) {
+                        // exact reference predicate on S2X(s_j + n)
+                        double s0 = a.s[j], s1 = a.s[n + j], s2 = a.s[2 * n + j];
+                        if (n0 > 0) s0 = dadd(s0, 1.0);
+                        if (n0 < 0) s0 = dsub(s0, 1.0);
+                        if (n1 > 0) s1 = dadd(s1, 1.0);
+                        if (n1 < 0) s1 = dsub(s1, 1.0);
+                        if (n2 > 0) s2 = dadd(s2, 1.0);
+                        if (n2 < 0) s2 = dsub(s2, 1.0);
+                        double xj0, xj1, xj2;
+                        s2x(h6, s0, s1, s2, xj0, xj1, xj2);
+                        double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
+                        double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
+                        keep = rsq < a.cut_sk_sq[pe];
                     }
                 }
-                unsigned m = __ballot_sync(0xffffffffu, keep);
-                if (keep) {
-                    int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                    if (pos < a.maxnbr) row[pos] = (j << kEntryShift) | (ej << 5) | c;
-                }
-                cnt += __popc(m);
             }
+            unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                if (pos < a.maxnbr) row[pos] = (j << kEntryShift) | (ej << 5) | c;
+            }
+            cnt += __popc(m);
         }
+        __syncwarp();  // the bin table is rewritten for the next atom
         if (lane == 0) {
             a.nnbr[i] = min(cnt, a.maxnbr);
             if (cnt > a.maxnbr) overflow = 1;

@@ -184,6 +184,35 @@ def test_lbfgs_converges_like_oracle(potentials):
     assert np.max(np.abs(d)) < 1e-8
 
 
+def test_per_pair_density_tables():
+    """Finnis-Sinclair-style tables, where the density of j at i depends on
+    both elements (rho_arr[e_j][e_i] differs across e_i, as ff_eam_fs
+    reads): FP64 forces, energy and virial match the oracle built from the
+    same knots, and the mixed path stays inside its error budget."""
+    dr, drho, F, rho1, rphi = synth.analytic_knots(("A", "B"))
+    nr = rho1.shape[1]
+    rho = np.zeros((2, 2, nr))
+    scale = np.array([[1.0, 0.8], [1.3, 1.1]])  # rho[i][j]: density of an i atom seen by a j atom
+    for i in range(2):
+        for j in range(2):
+            rho[i, j] = scale[i, j] * rho1[i]
+    nrho = F.shape[1]
+    ff = _lib.ForceField.knots(nr, nrho, dr, drho, F, rho, rphi)
+    e = O.Eam.knots(nr, nrho, dr, drho, F, rho, rphi)
+    c = synth.alloy((5, 5, 5), xB=0.4, sigma=0.08, seed=21, vac=0.02)
+    o = O.System(e, c.H, c.x, c.elem, c.masses)
+    pe_o, vir_o = o.force()
+    s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+    pe, vir = s.force()
+    assert abs(pe - pe_o) <= 1e-12 * abs(pe_o)
+    assert np.max(np.abs(vir - vir_o)) <= 1e-11 * np.max(np.abs(vir_o))
+    assert_forces(s.get_f(), o.f)
+    m = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+    pe_m, _ = m.force()
+    rms = np.sqrt(np.mean(np.sum((m.get_f() - o.f) ** 2, axis=1)))
+    assert rms < 1e-5 and abs(pe_m - pe_o) / c.natoms < 1e-7
+
+
 def test_cg_converges_like_oracle(potentials):
     """MinCG: the first iterations follow the oracle to rounding; the full
     run reaches the same minimum with the same iteration count."""
