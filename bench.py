@@ -265,6 +265,88 @@ def run_lbfgs(args, ff):
             "cell_253k": one(40, args.lbfgs_cap), "cell_4k": one(10, 5 * args.lbfgs_cap)}
 
 
+def run_accuracy(args, ff, cell, torch):
+    """The FP64 path on the same 2,048,000-atom cell (throughput), the mixed
+    path's error against it (force RMS, energy per atom), and the mixed NVE
+    energy drift (t_relax = inf, 1,000 steps of 1 fs)."""
+    from mapp4py_gb300 import _lib, synth
+
+    out = {}
+    s64 = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, precision=_lib.FP64)
+    s64.set_v(cell.v)
+    K = 10
+    s64.nvt_begin(T_K, synth.FS, synth.KB, K + 3)
+    st = torch.cuda.ExternalStream(s64.stream())
+    s64.nvt_steps(3)
+    s64.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    s64.nvt_steps(K)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    s64.nvt_end(K + 3)
+    out["fp64"] = {"value": cell.natoms / (ms / 1000.0), "unit": "atom-steps/s", "ms_per_step": ms, "steps": K}
+    # error of the mixed path against FP64 on the starting configuration
+    a = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, precision=_lib.FP64)
+    b = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, precision=_lib.MIXED)
+    pa, _ = a.force()
+    pb, _ = b.force()
+    fa, fb = a.get_f(), b.get_f()
+    out["mixed_vs_fp64"] = {"force_rms_eV_per_A": float(np.sqrt(np.mean(np.sum((fa - fb) ** 2, axis=1)))),
+                            "force_max_eV_per_A": float(np.max(np.abs(fa - fb))),
+                            "energy_eV_per_atom": float(abs(pa - pb) / cell.natoms)}
+    del a
+    # NVE drift of the mixed path
+    nsteps = args.nve_steps
+    b.set_v(cell.v)
+    th, _ = b.nvt_run(T_K, synth.FS, synth.KB, nsteps, t_relax=float("inf"), thermo=True)
+    etot = th[:, 0] + 0.5 * (th[:, 2] + th[:, 5] + th[:, 7])
+    t_ns = nsteps * 1e-6  # 1 fs steps
+    slope = np.polyfit(np.arange(nsteps + 1) * 1e-6, etot / cell.natoms, 1)[0]
+    out["nve"] = {"steps": nsteps, "dt_fs": 1.0, "drift_eV_per_atom_per_ns": float(slope),
+                  "max_deviation_eV_per_atom": float(np.max(np.abs(etot - etot[0])) / cell.natoms),
+                  "span_ns": t_ns}
+    return out
+
+
+def run_c1(args, ff_path, torch):
+    """The reference's CPU-runnable case: 4,000 atoms, FCC 10^3, NVE 100
+    steps, FP64, on the GPU and on the oracle (1 thread and all threads)."""
+    from mapp4py_gb300 import _lib, synth
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    c = synth.md_single((10, 10, 10), T=300.0, seed=0)
+    ff1 = _lib.ForceField.setfl(ff_path)
+    s = _lib.System(ff1, c.H, c.x, c.elem, c.masses)
+    s.set_v(c.v)
+    s.nvt_run(300.0, synth.FS, synth.KB, 5, t_relax=float("inf"))  # warm-up (graph, first launches)
+    s = _lib.System(ff1, c.H, c.x, c.elem, c.masses)
+    s.set_v(c.v)
+    s.nvt_begin(300.0, synth.FS, synth.KB, 100, t_relax=float("inf"))
+    st = torch.cuda.ExternalStream(s.stream())
+    s.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    s.nvt_steps(100)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    s.nvt_end(100)
+    out = {"workload": "4000-atom FCC 10^3, NVE 100 steps, FP64", "gpu": c.natoms * 100 / (ms / 1000.0)}
+    e = O.Eam.setfl(ff_path)
+    for name, threads in (("oracle_1_thread", 0), ("oracle_all_threads", os.cpu_count() or 1)):
+        o = O.System(e, c.H, c.x, c.elem, c.masses, pair_wise=threads == 0)
+        o.v = c.v
+        o.nvt_run(300.0, synth.FS, synth.KB, 100, t_relax=float("inf"), threads=threads)
+        out[name] = c.natoms * 100 / o.loop_seconds
+    out["unit"] = "atom-steps/s"
+    out["cores"] = os.cpu_count() or 1
+    return out
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
 
@@ -330,8 +412,8 @@ def run_gpu(args, rank, world, local_rank):
     # algorithmic bytes per launch (per atom: the row of 4*K entries plus the
     # atom's own streams; neighbour gathers are served by L2)
     if prec == _lib.MIXED:
-        b_force = N * (4 * kbar + 16 + 4 + 1 + 4 + 24)   # row, p32, dF32, elem, count, f (FP64)
-        b_density = N * (4 * kbar + 16 + 1 + 4 + 8 + 8 + 4)  # row, p32, elem, count, rho, dF, dF32
+        b_force = N * (4 * kbar + 16 + 1 + 4 + 12)   # row, q32 (position, F'), elem, count, f32 write
+        b_density = N * (4 * kbar + 16 + 1 + 4 + 16 + 4)  # row, p32, elem, count, q32 write, rho32 write
     else:
         b_force = N * (4 * kbar + 24 + 8 + 1 + 4 + 4 + 24)   # row, x, dF, elem, count, bins, f
         b_density = N * (4 * kbar + 24 + 1 + 4 + 4 + 8 + 8)
@@ -378,6 +460,11 @@ def run_gpu(args, rank, world, local_rank):
 
     batched = None if args.batch_steps <= 0 else run_batch(args, ff, torch)
     lbfgs = None if args.lbfgs_cap <= 0 else run_lbfgs(args, ff)
+    extras = None
+    if args.extras and rank == 0:
+        extras = run_accuracy(args, ff, cell, torch)
+        if not args.no_cpu:
+            extras["c1"] = run_c1(args, path, torch)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -393,6 +480,8 @@ def run_gpu(args, rank, world, local_rank):
             line["batched"] = batched
         if lbfgs is not None:
             line["lbfgs"] = lbfgs
+        if extras is not None:
+            line.update(extras)
         if not args.no_cpu and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline(path, cell, os.cpu_count() or 1)
@@ -416,6 +505,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=100,
                     help="steps of the 512-cell batch measurement (0 skips it)")
     ap.add_argument("--batch-cells", type=int, default=512)
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the FP64 run, the mixed-vs-FP64 error, the NVE drift and the 4,000-atom case")
+    ap.add_argument("--nve-steps", type=int, default=1000)
     ap.add_argument("--lbfgs-cap", type=int, default=1000,
                     help="iteration cap of the 253k-atom L-BFGS comparison (0 skips the L-BFGS part)")
     ap.add_argument("--cells", type=int, default=N_CELLS[0],

@@ -635,7 +635,10 @@ static void launch_step64(mappg_sys* s, const MdArgs& a) {
 }
 
 static void launch_step32(mappg_sys* s, const MdArgs& a) {
-    int g = grid_for(s, s->n, 256);
+    // streaming kernels with a last-block reduction: four blocks per SM keep
+    // loads in flight and the serial tail (the fixed-order sum over block
+    // partials) short
+    int g = std::min(grid_for(s, s->n, 256), 4 * s->sm_count);
     k_step_open32<<<1, 1, 0, s->stream>>>(a);
     if (a.fr.ortho)
         k_integrate32<true><<<g, 256, 0, s->stream>>>(a);

@@ -475,17 +475,24 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         s_lo[wib][lane] = lo;
         s_img[wib][lane] = img;
         __syncwarp();
+        // each lane's cursor into the bin sequence: candidate t lies in bin
+        // step c with pre[c] <= t < pre[c+1]; t grows by 32 per pass, so the
+        // cursor moves forward a bin or two at a time
+        int c = 0, cpre = 0, cnext = s_pre[wib][1], clo = s_lo[wib][0], cimg = s_img[wib][0];
         for (int t0 = 0; t0 < total; t0 += 32) {
             const int t = t0 + lane;
             bool keep = false;
-            int j = 0, ej = 0, c = 0;
+            int j = 0, ej = 0;
             if (t < total) {
-                // the bin holding candidate t: the last c with pre[c] <= t
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (c + step < 27 && s_pre[wib][c + step] <= t) c += step;
-                const int k = s_lo[wib][c] + (t - s_pre[wib][c]);
-                const int im = s_img[wib][c];
+                while (t >= cnext) {
+                    c++;
+                    cpre = cnext;
+                    cnext = c < 26 ? s_pre[wib][c + 1] : total;
+                    clo = s_lo[wib][c];
+                    cimg = s_img[wib][c];
+                }
+                const int k = clo + (t - cpre);
+                const int im = cimg;
                 const int n0 = (im & 3) - 1, n1 = ((im >> 2) & 3) - 1, n2 = ((im >> 4) & 3) - 1;
                 const float4 o = off[c];
                 const bool self_img = im == 21;  // no image shift
