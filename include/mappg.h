@@ -188,6 +188,13 @@ int mappg_nvt_begin(mappg_sys* sys, double T, double dt, double kB, double t_rel
 int mappg_nvt_steps(mappg_sys* sys, long long nsteps);
 int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
 
+/* Positions and velocities ([natoms][3] in the caller's order; either may
+ * be NULL) of a begun run after the steps enqueued so far, as MDNVT::run
+ * holds them when it writes its export (md_nvt.cpp:390,436,470): after the
+ * closing kick, before the deferred thermostat scale.  Waits for the steps;
+ * the run continues unchanged.  Single-cell systems only. */
+int mappg_nvt_snapshot(mappg_sys* sys, double* x, double* x_d);
+
 /* The system's CUDA stream (a cudaStream_t) and a wait on it. */
 int mappg_sys_stream(mappg_sys* sys, void** stream);
 int mappg_sys_sync(mappg_sys* sys);
@@ -221,6 +228,49 @@ int mappg_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f
  * it).  stats as mappg_lbfgs_run. */
 int mappg_cg_run(mappg_sys* sys, double e_tol, double max_dx, double f_tol, double c, double rho,
                  double min_alpha, int nsteps, double* stats);
+
+/* A function that mappg_lbfgs_run, mappg_lbfgs_run_precond and mappg_cg_run
+ * call after every nevery-th iteration's force call, with the number of
+ * iterations done; the system's positions and forces are then that
+ * iteration's and may be read from it (mappg_sys_get_x/get_f).  This is
+ * where the reference writes its periodic export (ExportHandler::print,
+ * min.h:216-220).  A non-zero return stops the run with MAPPG_ERR_ARG.
+ * hook NULL or nevery <= 0 removes it. */
+int mappg_sys_set_hook(mappg_sys* sys, int (*hook)(void* user, long long iteration), void* user, int nevery);
+
+/* --------------------------------------------------------- CFG snapshots */
+
+typedef struct mappg_cfg mappg_cfg;
+
+/* Read an AtomEye CFG file, standard or extended, as md.atoms.import_cfg
+ * (ImportCFGMD::operator(), import_cfg.cpp:496-595; header rules
+ * read_header 32-191; bodies read_body_ext 196-372 and read_body_std
+ * 377-478; Python entry 597-652).  The box is (H0 Transform) times
+ * sqrt(1 + 2 eta) when eta is given, made lower triangular (same row
+ * lengths and angles) and scaled by A; x = s H with s wrapped into [0,1);
+ * velocities, when the file has them, are x_d = s_d R H.  Elements are
+ * numbered in order of first appearance; a repeated name keeps its first
+ * mass.  Failures are MAPPG_ERR_FILE with the reference's messages. */
+int mappg_cfg_read(const char* path, mappg_cfg** out);
+/* Atom and element counts, whether velocities were read, the box (9). */
+int mappg_cfg_info(const mappg_cfg* cfg, int* natoms, int* nelem, int* has_vel, double* H);
+/* Mass and name of element i (name_len bytes including the terminator). */
+int mappg_cfg_element(const mappg_cfg* cfg, int i, double* mass, char* name, int name_len);
+/* Positions, velocities (NULL to skip) [natoms][3] and elements in file order. */
+int mappg_cfg_atoms(const mappg_cfg* cfg, double* x, double* x_d, unsigned char* elem);
+int mappg_cfg_destroy(mappg_cfg* cfg);
+
+/* Write an extended CFG file as ExportCFGMD::write (export_cfg_md.cpp:26-113,
+ * 167-193): A = 1, H0 = H (lower triangular), s = x H^-1 wrapped into
+ * [0,1), a mass and name line whenever the element changes along the atom
+ * order, then per atom s and the extra vectors (vec_dims[k] doubles each,
+ * [natoms][dim]) in the given order, all as "%.16lf ".  An extra vector
+ * named "x_d" is written as s_d = x_d H^-1 and the header then says
+ * "R = 1.0" instead of ".NO_VELOCITY."; the others are listed as
+ * auxiliary[k] = name_d. */
+int mappg_cfg_write(const char* path, int natoms, const double* H, const double* x, const unsigned char* elem,
+                    int nelem, const double* masses, const char* const* names, int nvec,
+                    const char* const* vec_names, const int* vec_dims, const double* const* vecs);
 
 /* ------------------------------------------------------- batches of cells */
 

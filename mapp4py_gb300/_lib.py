@@ -20,6 +20,7 @@ _I = C.POINTER(C.c_int)
 _U8 = C.POINTER(C.c_ubyte)
 _LL = C.POINTER(C.c_longlong)
 _VP = C.c_void_p
+_HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_longlong)
 
 # every exported entry point and its argument types (include/mappg.h)
 SIGNATURES = {
@@ -58,6 +59,15 @@ SIGNATURES = {
                                   C.c_longlong, _D, C.c_int]),
     "mappg_nvt_steps": (C.c_int, [_VP, C.c_longlong]),
     "mappg_nvt_end": (C.c_int, [_VP, _D, _D]),
+    "mappg_nvt_snapshot": (C.c_int, [_VP, _D, _D]),
+    "mappg_sys_set_hook": (C.c_int, [_VP, _VP, _VP, C.c_int]),
+    "mappg_cfg_read": (C.c_int, [C.c_char_p, C.POINTER(_VP)]),
+    "mappg_cfg_info": (C.c_int, [_VP, _I, _I, _I, _D]),
+    "mappg_cfg_element": (C.c_int, [_VP, C.c_int, _D, C.c_char_p, C.c_int]),
+    "mappg_cfg_atoms": (C.c_int, [_VP, _D, _D, _U8]),
+    "mappg_cfg_destroy": (C.c_int, [_VP]),
+    "mappg_cfg_write": (C.c_int, [C.c_char_p, C.c_int, _D, _D, _U8, C.c_int, _D, C.POINTER(C.c_char_p), C.c_int,
+                                  C.POINTER(C.c_char_p), _I, C.POINTER(_D)]),
     "mappg_sys_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "mappg_sys_sync": (C.c_int, [_VP]),
     "mappg_sys_enqueue": (C.c_int, [_VP, C.c_int]),
@@ -320,6 +330,41 @@ class System:
         check(load().mappg_nvt_end(self.h, dptr(eta), dptr(th) if th is not None else None))
         return th, eta
 
+    def nvt_snapshot(self):
+        """(x, x_d) of the begun run after the steps enqueued so far."""
+        x = np.empty((self.n, 3))
+        v = np.empty((self.n, 3))
+        check(load().mappg_nvt_snapshot(self.h, dptr(x), dptr(v)))
+        return x, v
+
+    def set_hook(self, fn, nevery):
+        """Call fn(iteration) after every nevery-th minimizer iteration
+        (None removes it); an exception in fn stops the run and is raised."""
+        if fn is None or nevery <= 0:
+            self._hook = None
+            check(load().mappg_sys_set_hook(self.h, None, None, 0))
+            return
+        box = {"error": None}
+
+        def call(_user, it):
+            try:
+                fn(int(it))
+                return 0
+            except BaseException as e:  # carried across the C frames
+                box["error"] = e
+                return 1
+
+        cb = _HOOK(call)
+        self._hook = (cb, box)
+        check(load().mappg_sys_set_hook(self.h, C.cast(cb, _VP), None, int(nevery)))
+
+    def _hook_error(self):
+        h = getattr(self, "_hook", None)
+        if h is not None and h[1]["error"] is not None:
+            e, h[1]["error"] = h[1]["error"], None
+            return e
+        return None
+
     def stream(self):
         p = _VP()
         check(load().mappg_sys_stream(self.h, C.byref(p)))
@@ -341,17 +386,24 @@ class System:
 
     def cg_run(self, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000):
         st = np.zeros(6)
-        check(load().mappg_cg_run(self.h, float(e_tol), float(max_dx), float(f_tol), float(c), float(rho),
-                                  float(min_alpha), int(nsteps), dptr(st)))
+        self._checked(load().mappg_cg_run(self.h, float(e_tol), float(max_dx), float(f_tol), float(c), float(rho),
+                                          float(min_alpha), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
 
     def lbfgs_run(self, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=100000):
         st = np.zeros(6)
-        check(load().mappg_lbfgs_run(self.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
-                                     float(rho), float(min_alpha), int(nsteps), dptr(st)))
+        self._checked(load().mappg_lbfgs_run(self.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
+                                             float(rho), float(min_alpha), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def _checked(self, rc):
+        # an exception raised by the iteration hook comes first
+        e = self._hook_error()
+        if e is not None:
+            raise e
+        return check(rc)
 
 
 class Batch(System):
@@ -511,8 +563,9 @@ def hessian_diag(system, color, h=1e-4):
 def lbfgs_run_precond(system, net, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0,
                       nsteps=100000):
     st = np.zeros(7)
-    check(load().mappg_lbfgs_run_precond(system.h, net.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
-                                         float(rho), float(min_alpha), int(nsteps), dptr(st)))
+    system._checked(load().mappg_lbfgs_run_precond(system.h, net.h, int(m), float(e_tol), float(max_dx),
+                                                   float(f_tol), float(c), float(rho), float(min_alpha), int(nsteps),
+                                                   dptr(st)))
     return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]), "n_energy": int(st[4]),
             "n_force": int(st[5]), "fallbacks": int(st[6])}
 
@@ -530,3 +583,46 @@ def device_info():
     sm = C.c_int()
     check(load().mappg_device_info(buf, 256, C.byref(sm)))
     return buf.value.decode(), sm.value
+
+
+def read_cfg(path):
+    """An AtomEye CFG file as a dict: H (lower triangular), x, x_d (None
+    without velocities), elem, names, masses."""
+    L = load()
+    h = _VP()
+    check(L.mappg_cfg_read(os.fsencode(path), C.byref(h)))
+    try:
+        n, ne, hv = C.c_int(), C.c_int(), C.c_int()
+        H = np.zeros((3, 3))
+        check(L.mappg_cfg_info(h, C.byref(n), C.byref(ne), C.byref(hv), dptr(H)))
+        x = np.zeros((n.value, 3))
+        v = np.zeros((n.value, 3)) if hv.value else None
+        elem = np.zeros(n.value, dtype=np.uint8)
+        check(L.mappg_cfg_atoms(h, dptr(x), dptr(v) if v is not None else None, elem.ctypes.data_as(_U8)))
+        names, masses = [], []
+        buf = C.create_string_buffer(4096)
+        m = C.c_double()
+        for i in range(ne.value):
+            check(L.mappg_cfg_element(h, i, C.byref(m), buf, 4096))
+            names.append(buf.value.decode())
+            masses.append(m.value)
+        return {"H": H, "x": x, "x_d": v, "elem": elem, "names": names, "masses": np.array(masses)}
+    finally:
+        L.mappg_cfg_destroy(h)
+
+
+def write_cfg(path, H, x, elem, masses, names, vecs=()):
+    """Write an extended CFG file; vecs is a sequence of (name, [n][dim])
+    extra per-atom vectors, "x_d" being written as reduced velocities."""
+    H = f64(H, (3, 3))
+    x = f64(x, (-1, 3))
+    n = x.shape[0]
+    elem = np.ascontiguousarray(elem, dtype=np.uint8)
+    masses = f64(masses)
+    arrs = [f64(a).reshape(n, -1) for _, a in vecs]
+    vnames = cstrings([nm for nm, _ in vecs])
+    dims = np.array([a.shape[1] for a in arrs] or [0], dtype=np.int32)
+    ptrs = (_D * max(1, len(arrs)))(*[dptr(a) for a in arrs])
+    check(load().mappg_cfg_write(os.fsencode(path), n, dptr(H), dptr(x), elem.ctypes.data_as(_U8), len(names),
+                                 dptr(masses), cstrings(names), len(arrs), vnames,
+                                 dims.ctypes.data_as(_I), ptrs))

@@ -33,6 +33,7 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
                const double* eta, bool thermo, const double* Tcell);
 void nvt_steps(mappg_sys* s, long long nsteps);
 void nvt_end(mappg_sys* s, double* eta, double* thermo);
+void nvt_snapshot(mappg_sys* s, double* x, double* v);
 void nvt_free(mappg_sys* s);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
@@ -41,25 +42,6 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls
 void launch_density_only(mappg_sys* s);
 void launch_force_only(mappg_sys* s);
 
-template <class F>
-static int guard(F&& f) {
-    try {
-        f();
-        return MAPPG_OK;
-    } catch (const Error& e) {
-        set_error(e.msg);
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        set_error("host allocation failed");
-        return MAPPG_ERR_ARG;
-    } catch (const std::exception& e) {
-        set_error(e.what());
-        return MAPPG_ERR_ARG;
-    } catch (...) {
-        set_error("unknown failure");
-        return MAPPG_ERR_ARG;
-    }
-}
 
 void upload_tables(mappg_ff* ff) {
     HostTables& t = ff->host;
@@ -644,6 +626,28 @@ int mappg_nvt_end(mappg_sys* s, double* eta, double* thermo) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         nvt_end(s, eta, thermo);
+    });
+}
+
+int mappg_nvt_snapshot(mappg_sys* s, double* x, double* x_d) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        nvt_snapshot(s, x, x_d);
+    });
+}
+
+int mappg_sys_set_hook(mappg_sys* s, int (*hook)(void*, long long), void* user, int nevery) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (hook && nevery > 0) {
+            s->hook = hook;
+            s->hook_user = user;
+            s->hook_every = nevery;
+        } else {
+            s->hook = nullptr;
+            s->hook_user = nullptr;
+            s->hook_every = 0;
+        }
     });
 }
 

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -26,6 +28,28 @@ struct Error {
     int code;
     std::string msg;
 };
+
+// Runs f; an exception becomes a negative status and the message of
+// mappg_last_error().  Every extern "C" entry point goes through it.
+template <class F>
+int guard(F&& f) {
+    try {
+        f();
+        return MAPPG_OK;
+    } catch (const Error& e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return MAPPG_ERR_ARG;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return MAPPG_ERR_ARG;
+    } catch (...) {
+        set_error("unknown failure");
+        return MAPPG_ERR_ARG;
+    }
+}
 
 #define MAPPG_CUDA(call)                                                                     \
     do {                                                                                     \

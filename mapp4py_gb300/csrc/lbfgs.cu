@@ -285,6 +285,15 @@ static void lb_force(mappg_sys* s, double* pe) {
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
 }
 
+// The caller's function after an iteration's force call, where the
+// reference writes its periodic export (ExportHandler::print, min.h:216-220)
+static void iteration_hook(mappg_sys* s, int istep) {
+    if (!s->hook || s->hook_every <= 0 || (istep + 1) % s->hook_every != 0) return;
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->hook(s->hook_user, (long long)istep + 1) != 0)
+        throw Error{MAPPG_ERR_ARG, "the iteration hook stopped the minimization"};
+}
+
 void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback) {
     enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
@@ -463,6 +472,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
         // search's energy, as in min_l-bfgs.h:181-188
         lb_force(s, &pe_force);
         n_fc++;
+        iteration_hook(s, istep);
         if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
         if (f_tol > 0.0) {
             read_prep(&fh, &hh, &hmax, &fmaxv);
@@ -693,6 +703,7 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls
         }
         lb_force(s, &pe_force);
         n_fc++;
+        iteration_hook(s, istep);
         if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
         if (f_tol > 0.0) {
             read_prep(&fh, &hh, &hmax, &fmaxv);

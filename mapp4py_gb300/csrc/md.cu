@@ -844,6 +844,51 @@ void nvt_end(mappg_sys* s, double* eta, double* thermo) {
     if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite position, energy or temperature during the run"};
 }
 
+// Positions (what = 0) or velocities (what = 1) of a run at a step boundary,
+// written in the caller's atom order.  They are the state MDNVT::run exports
+// between steps (md_nvt.cpp:390,436,470): after the closing kick, before the
+// deferred thermostat scale.  The mixed path keeps the mean displacement in
+// sc->drift and may hold the closing kick back (pending_kick); both are
+// applied to the copy here, the run's own state is left as it is.
+__global__ void k_snapshot(MdArgs a, const int* __restrict__ id, double* __restrict__ out, int what, int mixed) {
+    const int n = a.n;
+    const bool pend = mixed && a.sc->pending_kick != 0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+        const int i = q % n, c = q / n;
+        double val;
+        if (what == 0) {
+            val = a.x[q];
+            if (mixed) val -= a.sc->drift[c];
+        } else {
+            val = a.v[q];
+            if (pend) val += (double)a.f32[q] * a.dtm[a.elem[i]];
+        }
+        out[3 * (size_t)id[i] + c] = val;
+    }
+}
+
+void nvt_snapshot(mappg_sys* s, double* x, double* v) {
+    NvtRun* r = (NvtRun*)s->run;
+    if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
+    if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "snapshots are taken of single-cell runs"};
+    const int g = grid_for(s, 3LL * s->n, 256);
+    const int mixed = s->precision == MAPPG_MIXED ? 1 : 0;
+    double* out[2] = {x, v};
+    for (int what = 0; what < 2; what++) {
+        if (!out[what]) continue;
+        k_snapshot<<<g, 256, 0, s->stream>>>(r->a, s->id, s->stage, what, mixed);
+        MAPPG_CUDA(cudaGetLastError());
+        MAPPG_CUDA(cudaMemcpyAsync(out[what], s->stage, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyDeviceToHost,
+                                   s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    DevScalars h;
+    MAPPG_CUDA(cudaMemcpyAsync(&h, s->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    if (h.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during the run"};
+    if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite position, energy or temperature during the run"};
+}
+
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
              double* thermo, const double* Tcell) {
     nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo != nullptr, Tcell);

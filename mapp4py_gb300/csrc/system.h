@@ -237,6 +237,11 @@ struct mappg_sys {
     bool have_v = false;
     bool f_is_f32 = false;  // the newest forces are in f32 (mixed kernels)
     bool force64 = false;   // mixed system computing FP64 forces (end of a relaxation)
+    // called by the minimizers after every hook_every-th iteration's force
+    // call (mappg_sys_set_hook)
+    int (*hook)(void* user, long long iteration) = nullptr;
+    void* hook_user = nullptr;
+    int hook_every = 0;
     std::vector<int> host_id;  // sorted -> caller (host copy)
 };
 

@@ -10,6 +10,12 @@ Names, arguments and defaults follow the reference's Python types:
                        affine=False, max_dx=1.0, ls=ls_bt(); run(atoms, max_nsteps)
   ls_bt()              LineSearchBackTrack (ls.cpp:456-461): c=0.4, rho=0.5,
                        min_alpha=0.0
+  md.atoms.import_cfg  ImportCFGMD (import_cfg.cpp:496-652): an AtomEye CFG file
+                       (standard or extended) as an atoms object
+  md.export_cfg(...)   ExportCFGMD (export_cfg_md.cpp:9-16,167-226):
+                       file_pattern, nevery=10000, extra_vecs=[], sort=False;
+                       called as (atoms, file_name), or set as the .export of
+                       nvt / min_lbfgs / min_cg to write every nevery steps
 Additive: atoms.precision ('fp64' | 'mixed') selects the GPU arithmetic, and
 min_lbfgs.f_tol adds the max|F| stop.
 
@@ -72,6 +78,18 @@ class atoms:
     def vol(self):
         return float(self.H[0, 0] * self.H[1, 1] * self.H[2, 2])
 
+    @classmethod
+    def import_cfg(cls, cfg_file):
+        """The configuration of an AtomEye CFG file: elements in order of
+        first appearance with their masses, velocities when the file has
+        them (libmappg's mappg_cfg_read)."""
+        try:
+            d = _lib.read_cfg(cfg_file)
+        except _lib.MappgError as e:
+            raise TypeError(str(e)) from None
+        a = cls(d["H"], d["x"], d["elem"], elems=tuple(d["names"]), masses=d["masses"], x_d=d["x_d"])
+        return a
+
     # ---------------------------------------------------------- force fields
     def _remap(self, ff):
         # the file's elements become the system's; an existing element list
@@ -127,6 +145,53 @@ class atoms:
         return self._sys
 
 
+class export_cfg:
+    """Writer of extended AtomEye CFG files.  Called as (atoms, file_name) it
+    writes one file; as the .export of a run it writes
+    file_pattern.%09d.cfg (the step number) at the start, every nevery
+    steps and at the end.  extra_vecs lists per-atom vectors to add after
+    the positions: "x_d" (velocities, written in reduced units) and "f"."""
+
+    _VECS = ("x_d", "f")
+
+    def __init__(self, file_pattern, nevery=10000, extra_vecs=None, sort=False):
+        if not (int(nevery) > 0):
+            raise TypeError("nevery should be greater than 0")
+        self.file_pattern = str(file_pattern)
+        self.nevery = int(nevery)
+        self.extra_vecs = list(extra_vecs or [])
+        self.sort = bool(sort)
+
+    @property
+    def default_vecs(self):
+        # atoms keep the caller's order, which is already the id order that
+        # sort=True asks for
+        return ["elem", "x"] + (["id"] if self.sort else [])
+
+    def __call__(self, atoms, file_name):
+        self._write(atoms, file_name, atoms.x, atoms.x_d, atoms.f)
+
+    def _write_step(self, atoms, step, x, x_d, f):
+        self._write(atoms, "%s.%09d.cfg" % (self.file_pattern, step), x, x_d, f)
+
+    def _write(self, atoms, path, x, x_d, f):
+        vecs = []
+        for name in self.extra_vecs:
+            if name not in self._VECS:
+                raise TypeError("cannot export vector '%s' to file, it does not exist" % name)
+            arr = x_d if name == "x_d" else f
+            if arr is None:
+                raise TypeError("cannot export vector '%s' to file, it is empty" % name)
+            vecs.append((name, arr))
+        try:
+            _lib.write_cfg(path, atoms.H, x, atoms.elem, atoms.masses, list(atoms.elems), vecs)
+        except _lib.MappgError as e:
+            raise TypeError(str(e)) from None
+
+    def _wants_f(self):
+        return "f" in self.extra_vecs
+
+
 def _print_thermo(th, step0, ntally, vol):
     hdr = "%8s %14s %16s %12s %12s %12s" % ("step", "T", "PE", "S[0][0]", "S[1][1]", "S[2][2]")
     print(hdr)
@@ -169,8 +234,30 @@ class nvt:
         s = atoms._system()
         s.set_x(atoms.x)
         s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
-        th, self._eta = s.nvt_run(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L,
-                                  niters=self.niters, eta=self._eta, thermo=bool(self.ntally))
+        xprt = self.export
+        if xprt is None:
+            th, self._eta = s.nvt_run(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L,
+                                      niters=self.niters, eta=self._eta, thermo=bool(self.ntally))
+        else:
+            # MDNVT::run's exports (md_nvt.cpp:390,436,470): the run goes on
+            # the device in nevery-step pieces, each export is a snapshot
+            s.nvt_begin(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L, niters=self.niters,
+                        eta=self._eta, thermo=bool(self.ntally))
+            try:
+                def snap(step):
+                    x, v = s.nvt_snapshot()
+                    xprt._write_step(atoms, step, x, v, s.get_f() if xprt._wants_f() else None)
+
+                snap(atoms.step)
+                done = 0
+                while done < nsteps:
+                    k = min(xprt.nevery - done % xprt.nevery, nsteps - done)
+                    s.nvt_steps(k)
+                    done += k
+                    if done % xprt.nevery == 0 or done == nsteps:
+                        snap(atoms.step + done)
+            finally:
+                th, self._eta = s.nvt_end()
         s.get_x(atoms.x)
         if atoms.x_d is None:
             atoms.x_d = np.zeros_like(atoms.x)
@@ -189,6 +276,35 @@ class nvt:
 def _voigt_to_matrix(v):
     v = np.asarray(v)
     return np.array([[v[0], v[1], v[2]], [v[1], v[3], v[4]], [v[2], v[4], v[5]]])
+
+
+def _min_run(atoms, xprt, run):
+    """A minimizer run with the reference's exports (MinHelper::ExportHandler,
+    min.h:207-227): at the start, after every nevery-th iteration and at
+    the end when that step was not already written."""
+    s = atoms._system()
+    s.set_x(atoms.x)
+    if xprt is None:
+        return s, run(s)
+    step0 = atoms.step
+    f0 = None
+    if xprt._wants_f():
+        s.force()
+        f0 = s.get_f()
+    xprt._write_step(atoms, step0, atoms.x, atoms.x_d, f0)
+
+    def at(it):
+        xprt._write_step(atoms, step0 + it, s.get_x(), atoms.x_d, s.get_f() if xprt._wants_f() else None)
+
+    s.set_hook(at, xprt.nevery)
+    try:
+        r = run(s)
+    finally:
+        s.set_hook(None, 0)
+    if r["niter"] % xprt.nevery:
+        xprt._write_step(atoms, step0 + r["niter"], s.get_x(), atoms.x_d,
+                         s.get_f() if xprt._wants_f() else None)
+    return s, r
 
 
 class min_lbfgs:
@@ -221,10 +337,9 @@ class min_lbfgs:
             raise TypeError("max_nsteps should be greater than or equal to 0")
         if not isinstance(self.ls, ls_bt):
             raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
-        s = atoms._system()
-        s.set_x(atoms.x)
-        r = s.lbfgs_run(m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c,
-                        rho=self.ls.rho, min_alpha=self.ls.min_alpha, nsteps=max_nsteps)
+        s, r = _min_run(atoms, self.export, lambda s: s.lbfgs_run(
+            m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
+            min_alpha=self.ls.min_alpha, nsteps=max_nsteps))
         s.get_x(atoms.x)
         atoms.f = s.get_f()
         atoms.pe = r["pe"]
@@ -261,10 +376,9 @@ class min_cg:
             raise TypeError("max_nsteps should be greater than or equal to 0")
         if not isinstance(self.ls, ls_bt):
             raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
-        s = atoms._system()
-        s.set_x(atoms.x)
-        r = s.cg_run(e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
-                     min_alpha=self.ls.min_alpha, nsteps=max_nsteps)
+        s, r = _min_run(atoms, self.export, lambda s: s.cg_run(
+            e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
+            min_alpha=self.ls.min_alpha, nsteps=max_nsteps))
         s.get_x(atoms.x)
         atoms.f = s.get_f()
         atoms.pe = r["pe"]

@@ -1,0 +1,156 @@
+"""The mapp4py-style surface (mapp4py_gb300.md) on the GPU: md.atoms with a
+setfl force field, md.nvt / md.min_lbfgs / md.min_cg runs against the same
+runs through the system-level binding, CFG exports during runs
+(md.export_cfg as a run's .export: files at the start, every nevery steps
+and at the end, as MDNVT::run and MinHelper::ExportHandler write them), and
+md.atoms.import_cfg feeding a run."""
+import os
+
+import numpy as np
+import pytest
+
+from mapp4py_gb300 import _lib, md, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setfl(potentials):
+    return potentials[("A", "B")][0]
+
+
+def make_atoms(setfl, precision="fp64", n=(5, 5, 5), T=600.0, seed=3, sigma=0.05):
+    c = synth.alloy(n, xB=0.5, sigma=sigma, T=T, seed=seed)
+    a = md.atoms(c.H, c.x, c.elem, elems=("A", "B"), masses=c.masses, x_d=c.v)
+    a.ff_eam_setfl(setfl)
+    a.kB = synth.KB
+    a.precision = precision
+    return a
+
+
+def files(pattern):
+    d, base = os.path.split(pattern)
+    out = {}
+    for f in os.listdir(d):
+        if f.startswith(base + ".") and f.endswith(".cfg"):
+            out[int(f[len(base) + 1:-4])] = os.path.join(d, f)
+    return out
+
+
+def test_nvt_run_matches_system_binding(setfl):
+    a = make_atoms(setfl)
+    x0, v0 = a.x.copy(), a.x_d.copy()
+    integ = md.nvt(600.0, synth.FS)
+    integ.ntally = 0
+    integ.run(a, 40)
+    s = _lib.System(_lib.ForceField.setfl(setfl, ["A", "B"]), a.H, x0, a.elem, a.masses)
+    s.set_v(v0)
+    s.nvt_run(600.0, synth.FS, synth.KB, 40, t_relax=100 * synth.FS)
+    assert np.array_equal(a.x, s.get_x()) and np.array_equal(a.x_d, s.get_v())
+    assert a.step == 40 and np.isfinite(a.pe) and a.S_pe.shape == (3, 3)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nvt_export_every_nevery(setfl, tmp_path, precision):
+    a = make_atoms(setfl, precision)
+    b = make_atoms(setfl, precision)
+    pattern = str(tmp_path / "run")
+    integ = md.nvt(600.0, synth.FS)
+    integ.ntally = 0
+    integ.export = md.export_cfg(pattern, nevery=10, extra_vecs=["x_d"])
+    integ.run(a, 25)
+    plain = md.nvt(600.0, synth.FS)
+    plain.ntally = 0
+    plain.run(b, 25)
+    # the pieces and the snapshots leave the trajectory as it is
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.x_d, b.x_d)
+    got = files(pattern)
+    assert sorted(got) == [0, 10, 20, 25]
+    first = md.atoms.import_cfg(got[0])
+    d0 = first.x - make_atoms(setfl, precision).x
+    assert np.max(np.abs(d0 - np.round(d0 @ np.linalg.inv(a.H)) @ a.H)) < 1e-12
+    last = md.atoms.import_cfg(got[25])
+    d = last.x - a.x
+    d -= np.round(d @ np.linalg.inv(a.H)) @ a.H
+    assert np.max(np.abs(d)) < 1e-12
+    # the file holds the velocities before the run's final thermostat
+    # scale: one common factor close to 1 separates them
+    r = a.x_d / last.x_d
+    fac = np.median(r)
+    assert abs(fac - 1.0) < 1e-2 and np.max(np.abs(a.x_d - fac * last.x_d)) < 1e-12
+    # a second run continues the step numbering
+    integ.run(a, 10)
+    assert sorted(files(pattern)) == [0, 10, 20, 25, 30, 35]
+
+
+@pytest.mark.parametrize("kind", ["lbfgs", "cg"])
+def test_minimizer_export(setfl, tmp_path, kind):
+    def minimizer():
+        return md.min_lbfgs(m=5, e_tol=0.0) if kind == "lbfgs" else md.min_cg(e_tol=0.0)
+
+    a = make_atoms(setfl, T=0.0, sigma=0.1)
+    ref = make_atoms(setfl, T=0.0, sigma=0.1)
+    pattern = str(tmp_path / kind)
+    m = minimizer()
+    m.export = md.export_cfg(pattern, nevery=4, extra_vecs=["f"])
+    r = m.run(a, 10)
+    r_ref = minimizer().run(ref, 10)
+    assert r["niter"] == r_ref["niter"] == 10
+    assert np.array_equal(a.x, ref.x) and r["pe"] == r_ref["pe"]
+    got = files(pattern)
+    assert sorted(got) == [0, 4, 8, 10]
+    # the file of iteration 4 holds the positions after four iterations
+    four = make_atoms(setfl, T=0.0, sigma=0.1)
+    minimizer().run(four, 4)
+    snap = md.atoms.import_cfg(got[4])
+    d = snap.x - four.x
+    d -= np.round(d @ np.linalg.inv(a.H)) @ a.H
+    assert np.max(np.abs(d)) < 1e-12
+    # the forces column of the last file is the run's final force
+    with open(got[10]) as fh:
+        rows = [ln.split() for ln in fh if len(ln.split()) == 6]
+    f_file = np.array(rows, dtype=float)[:, 3:]
+    assert np.max(np.abs(f_file - a.f)) < 1e-12
+
+
+def test_export_failure_stops_the_run(setfl, tmp_path):
+    class Failing(md.export_cfg):
+        def _write_step(self, atoms, step, x, x_d, f):
+            if step == 4:
+                raise RuntimeError("disk full")
+            super()._write_step(atoms, step, x, x_d, f)
+
+    a = make_atoms(setfl, T=0.0, sigma=0.1)
+    m = md.min_lbfgs(m=5, e_tol=0.0)
+    m.export = Failing(str(tmp_path / "x"), nevery=2)
+    # the exception raised inside the iteration hook ends the device run
+    with pytest.raises(RuntimeError, match="disk full"):
+        m.run(a, 10)
+    assert sorted(files(str(tmp_path / "x"))) == [0, 2]
+    m.export = None
+    assert m.run(a, 3)["niter"] == 3  # the system is usable afterwards
+
+
+def test_import_cfg_runs(setfl, tmp_path):
+    a = make_atoms(setfl, T=300.0)
+    p = str(tmp_path / "start.cfg")
+    md.export_cfg("unused", extra_vecs=["x_d"])(a, p)
+    b = md.atoms.import_cfg(p)
+    b.ff_eam_setfl(setfl)
+    b.kB = synth.KB
+    assert b.elems == ("A", "B") or b.elems == ("B", "A")
+    integ = md.nvt(300.0, synth.FS)
+    integ.ntally = 0
+    integ.run(b, 20)
+    assert np.all(np.isfinite(b.x)) and np.isfinite(b.pe)
+    # same start, same elements: the run follows the original to the file's
+    # printed precision
+    c = make_atoms(setfl, T=300.0)
+    integ2 = md.nvt(300.0, synth.FS)
+    integ2.ntally = 0
+    integ2.run(c, 20)
+    order = np.array([b.elems.index(e) for e in c.elems])
+    assert np.array_equal(order[c.elem], b.elem)
+    d = b.x - c.x
+    d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
+    assert np.max(np.abs(d)) < 1e-8
