@@ -37,6 +37,10 @@ extern "C" {
 #define MAPPG_ERR_TIMEOUT -7  /* a bounded device wait gave up             */
 #define MAPPG_ERR_UNSUPP -8   /* feature outside this engine's scope       */
 
+#define MAPPG_LS_BT 0      /* back-tracking (ls_bt)            */
+#define MAPPG_LS_GOLDEN 1  /* golden section (ls_golden)       */
+#define MAPPG_LS_BRENT 2   /* Brent's method (ls_brent)        */
+
 #define MAPPG_FP64 0  /* FP64 everywhere (the reference's arithmetic)       */
 #define MAPPG_MIXED 1 /* FP32 pair math, FP64 state and global reductions   */
 
@@ -228,6 +232,29 @@ int mappg_lbfgs_run(mappg_sys* sys, int m, double e_tol, double max_dx, double f
  * it).  stats as mappg_lbfgs_run. */
 int mappg_cg_run(mappg_sys* sys, double e_tol, double max_dx, double f_tol, double c, double rho,
                  double min_alpha, int nsteps, double* stats);
+
+/* Line search of a minimizer (mapp4py.ls_bt / ls_golden / ls_brent,
+ * ls.cpp:95-100,262-268,456-461 for the defaults): kind is MAPPG_LS_*; c,
+ * rho, min_alpha are the back-tracking's (0.4, 0.5, 0); tol (sqrt(2 eps)),
+ * max_iter (5), bracket (1) and zeps (1e-3 eps, Brent only) the others'. */
+typedef struct mappg_ls {
+    int kind;
+    double c, rho, min_alpha;
+    double tol;
+    int max_iter;
+    int bracket;
+    double zeps;
+} mappg_ls;
+
+/* mappg_lbfgs_run and mappg_cg_run with any of the three line searches
+ * (LineSearchGoldenSection::min ls.h:340-515, LineSearchBrent::min
+ * ls.h:524-706, both after LineSearch::bracket ls.h:214-335 unless
+ * bracket = 0; back-tracking as mappg_lbfgs_run).  Stop codes add
+ * 8 = the bracketing found no lower energy (B_F_DOWNHILL). */
+int mappg_lbfgs_run_ls(mappg_sys* sys, int m, double e_tol, double max_dx, double f_tol, const mappg_ls* ls,
+                       int nsteps, double* stats);
+int mappg_cg_run_ls(mappg_sys* sys, double e_tol, double max_dx, double f_tol, const mappg_ls* ls, int nsteps,
+                    double* stats);
 
 /* A function that mappg_lbfgs_run, mappg_lbfgs_run_precond and mappg_cg_run
  * call after every nevery-th iteration's force call, with the number of

@@ -61,6 +61,8 @@ SIGNATURES = {
     "mappg_nvt_end": (C.c_int, [_VP, _D, _D]),
     "mappg_nvt_snapshot": (C.c_int, [_VP, _D, _D]),
     "mappg_sys_set_hook": (C.c_int, [_VP, _VP, _VP, C.c_int]),
+    "mappg_lbfgs_run_ls": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),
+    "mappg_cg_run_ls": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),
     "mappg_cfg_read": (C.c_int, [C.c_char_p, C.POINTER(_VP)]),
     "mappg_cfg_info": (C.c_int, [_VP, _I, _I, _I, _D]),
     "mappg_cfg_element": (C.c_int, [_VP, C.c_int, _D, C.c_char_p, C.c_int]),
@@ -106,6 +108,21 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+class LineSearch(C.Structure):
+    """mappg_ls: kind (LS_BT, LS_GOLDEN, LS_BRENT) and the parameters."""
+    _fields_ = [("kind", C.c_int), ("c", C.c_double), ("rho", C.c_double), ("min_alpha", C.c_double),
+                ("tol", C.c_double), ("max_iter", C.c_int), ("bracket", C.c_int), ("zeps", C.c_double)]
+
+
+LS_BT, LS_GOLDEN, LS_BRENT = 0, 1, 2
+
+
+def line_search(kind=LS_BT, c=0.4, rho=0.5, min_alpha=0.0, tol=(2.0 * np.finfo(float).eps) ** 0.5, max_iter=5,
+                bracket=True, zeps=np.finfo(float).eps * 1e-3):
+    return LineSearch(int(kind), float(c), float(rho), float(min_alpha), float(tol), int(max_iter),
+                      int(bool(bracket)), float(zeps))
 
 
 class MappgError(RuntimeError):
@@ -395,6 +412,21 @@ class System:
         st = np.zeros(6)
         self._checked(load().mappg_lbfgs_run(self.h, int(m), float(e_tol), float(max_dx), float(f_tol), float(c),
                                              float(rho), float(min_alpha), int(nsteps), dptr(st)))
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def lbfgs_run_ls(self, ls, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, nsteps=100000):
+        """L-BFGS with a given line search (line_search(...))."""
+        st = np.zeros(6)
+        self._checked(load().mappg_lbfgs_run_ls(self.h, int(m), float(e_tol), float(max_dx), float(f_tol),
+                                                C.cast(C.pointer(ls), _VP), int(nsteps), dptr(st)))
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def cg_run_ls(self, ls, e_tol=0.0, max_dx=1.0, f_tol=1e-4, nsteps=100000):
+        st = np.zeros(6)
+        self._checked(load().mappg_cg_run_ls(self.h, float(e_tol), float(max_dx), float(f_tol),
+                                             C.cast(C.pointer(ls), _VP), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
 

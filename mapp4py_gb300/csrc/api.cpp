@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "linesearch.h"
 #include "system.h"
 
 namespace mappg {
@@ -26,8 +27,8 @@ void sys_build(mappg_sys* s);
 void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total);
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
              double* thermo, const double* Tcell);
-void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
-               double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback);
+void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps,
+               double* stats, const double* P, long long* n_fallback);
 void lb_update(mappg_sys* s);
 void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
                const double* eta, bool thermo, const double* Tcell);
@@ -37,8 +38,7 @@ void nvt_snapshot(mappg_sys* s, double* x, double* v);
 void nvt_free(mappg_sys* s);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
-void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
-            int nsteps, double* stats);
+void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps, double* stats);
 void launch_density_only(mappg_sys* s);
 void launch_force_only(mappg_sys* s);
 
@@ -820,12 +820,44 @@ int mappg_sys_enqueue(mappg_sys* s, int what) {
     });
 }
 
+// line-search parameters as the Python types accept them (ls.cpp:190-260,
+// 358-450, 560-620)
+static LsParams ls_params(const mappg_ls* q) {
+    if (!q) throw Error{MAPPG_ERR_ARG, "null line search"};
+    LsParams p;
+    p.kind = q->kind;
+    p.c = q->c;
+    p.rho = q->rho;
+    p.min_alpha = q->min_alpha;
+    p.tol = q->tol;
+    p.max_iter = q->max_iter;
+    p.bracket = q->bracket != 0;
+    p.zeps = q->zeps;
+    if (p.kind == MAPPG_LS_BT) {
+        if (!(p.c > 0.0 && p.c < 1.0)) throw Error{MAPPG_ERR_ARG, "c must be in (0,1)"};
+        if (!(p.rho > 0.0 && p.rho < 1.0)) throw Error{MAPPG_ERR_ARG, "rho must be in (0,1)"};
+        if (!(p.min_alpha >= 0.0)) throw Error{MAPPG_ERR_ARG, "min_alpha must be >= 0"};
+    } else if (p.kind == MAPPG_LS_GOLDEN || p.kind == MAPPG_LS_BRENT) {
+        if (!(p.tol > 0.0)) throw Error{MAPPG_ERR_ARG, "tol must be > 0"};
+        if (p.max_iter <= 0) throw Error{MAPPG_ERR_ARG, "max_iter must be > 0"};
+        if (p.kind == MAPPG_LS_BRENT && !(p.zeps > 0.0)) throw Error{MAPPG_ERR_ARG, "zeps must be > 0"};
+    } else {
+        throw Error{MAPPG_ERR_ARG, "unknown line search"};
+    }
+    return p;
+}
+
+static LsParams bt_params(double c, double rho, double min_alpha) {
+    mappg_ls q{MAPPG_LS_BT, c, rho, min_alpha, 0.0, 0, 0, 0.0};
+    return ls_params(&q);
+}
+
 int mappg_cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c, double rho, double min_alpha,
                  int nsteps, double* stats) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "conjugate gradients run per single cell"};
-        cg_run(s, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats);
+        cg_run(s, e_tol, max_dx, f_tol, bt_params(c, rho, min_alpha), nsteps, stats);
     });
 }
 
@@ -834,7 +866,25 @@ int mappg_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_t
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "L-BFGS on a batch of cells runs with mappg_batch_lbfgs_run"};
-        lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, stats, nullptr, nullptr);
+        lbfgs_run(s, m, e_tol, max_dx, f_tol, bt_params(c, rho, min_alpha), nsteps, stats, nullptr, nullptr);
+    });
+}
+
+int mappg_cg_run_ls(mappg_sys* s, double e_tol, double max_dx, double f_tol, const mappg_ls* ls, int nsteps,
+                    double* stats) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "conjugate gradients run per single cell"};
+        cg_run(s, e_tol, max_dx, f_tol, ls_params(ls), nsteps, stats);
+    });
+}
+
+int mappg_lbfgs_run_ls(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, const mappg_ls* ls,
+                       int nsteps, double* stats) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "L-BFGS on a batch of cells runs with mappg_batch_lbfgs_run"};
+        lbfgs_run(s, m, e_tol, max_dx, f_tol, ls_params(ls), nsteps, stats, nullptr, nullptr);
     });
 }
 

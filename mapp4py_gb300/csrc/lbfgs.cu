@@ -19,6 +19,7 @@
 
 #include <vector>
 
+#include "linesearch.h"
 #include "system.h"
 
 namespace mappg {
@@ -294,9 +295,31 @@ static void iteration_hook(mappg_sys* s, int istep) {
         throw Error{MAPPG_ERR_ARG, "the iteration hook stopped the minimization"};
 }
 
-void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
-               double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback) {
-    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
+// The minimizers' line-search function (MinMDHandler::F and F_reset,
+// min_cg.h:260-276): a trial moves x to x0 + alpha h and evaluates the
+// energy; reset restores x0.
+struct TrialLine {
+    mappg_sys* s;
+    int N, grid;
+    const double* xs;  // x0
+    const double* h;
+    long long* n_en;
+    double F(double a) {
+        k_lb_trial<<<grid, 256, 0, s->stream>>>(N, s->x, xs, h, a);
+        (*n_en)++;
+        return lb_energy(s);
+    }
+    void reset() {
+        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, s->stream));
+        lb_update(s);
+    }
+};
+
+// a mixed-precision search that fails may be FP32 force noise, not a minimum
+static bool ls_failed(int err) { return err == LS_MIN_ALPHA || err == B_F_DOWNHILL; }
+
+void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps,
+               double* stats, const double* P, long long* n_fallback) {
     if (m < 0 || m > 64) throw Error{MAPPG_ERR_ARG, "m must be in 0..64"};
     if (!(max_dx > 0.0)) throw Error{MAPPG_ERR_ARG, "max_dx must be positive"};
     if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
@@ -387,6 +410,8 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
         }
         MAPPG_CUDA(cudaGetLastError());
     };
+    TrialLine line{s, N, grid, xs, h, &n_en};
+    LineSearch<TrialLine> search(ls, line);
     int istep = 0;
     for (; err == LS_S; istep++) {
         MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
@@ -405,7 +430,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             k = 0;
             read_prep(&fh, &hh, &hmax, &fmaxv);
         }
-        // LineSearchBackTrack::min, init_flag 0
+        // ls->min(&handler, e_curr, alpha_m, 0) (min_l-bfgs.h:173)
         double dfa = -fh, max_a;
         int lerr = LS_S;
         if (hh == 0.0) {
@@ -423,36 +448,10 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, d
             lerr = LS_MIN_ALPHA;
         else if (dfa >= 0.0)
             lerr = LS_F_DOWNHILL;
-        else {
-            max_a = fmin(max_a, 1.0);
-            if (max_a <= min_alpha)
-                lerr = LS_MIN_ALPHA;
-            else {
-                double a = max_a, init_energy = e_curr;
-                while (true) {
-                    double ideal = e_curr + a * c_ls * dfa;
-                    k_lb_trial<<<grid, 256, 0, st>>>(N, s->x, xs, h, a);
-                    double cur = lb_energy(s);
-                    n_en++;
-                    if (cur <= ideal) {
-                        e_curr = cur;
-                        lerr = LS_S;
-                        break;
-                    }
-                    a *= rho_ls;
-                    if (a <= min_alpha) {
-                        e_curr = init_energy;
-                        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-                        lb_update(s);
-                        lerr = LS_MIN_ALPHA;
-                        break;
-                    }
-                }
-                alpha_m = a;
-            }
-        }
+        else
+            lerr = search.min(dfa, max_a, e_curr, alpha_m, 0);
         err = lerr;
-        if (err == LS_MIN_ALPHA && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
+        if (ls_failed(err) && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
             s->force64 = true;
             lb_force(s, &pe_force);
             n_fc++;
@@ -565,9 +564,7 @@ __global__ void k_cg_dir(int N, double* __restrict__ h, const double* __restrict
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) h[q] = ratio * h[q] + f[q];
 }
 
-void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
-            int nsteps, double* stats) {
-    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
+void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps, double* stats) {
     if (!(max_dx > 0.0)) throw Error{MAPPG_ERR_ARG, "max_dx must be positive"};
     if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
@@ -617,7 +614,9 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls
     read_prep(&fh, &hh, &hmax, &fmaxv);
     if (err == LS_S && f_tol > 0.0 && fmaxv < f_tol) err = MIN_S_FTOL;
     double f0_f0 = fh;  // f.f with h = f
-    double prev_val = -1.0;
+    TrialLine line{s, N, grid, xs, h, &n_en};
+    LineSearch<TrialLine> search(ls, line);  // prev_val starts at -1 (LineSearch::reset)
+    double alpha = 0.0;
     struct Promote {
         mappg_sys* s;
         ~Promote() { s->force64 = false; }
@@ -654,36 +653,10 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls
             lerr = LS_MIN_ALPHA;
         else if (dfa >= 0.0)
             lerr = LS_F_DOWNHILL;
-        else {
-            if (prev_val > 0.0 && dfa < 0.0) max_a = fmin(max_a, -prev_val / dfa);
-            prev_val = -dfa;
-            if (max_a <= min_alpha)
-                lerr = LS_MIN_ALPHA;
-            else {
-                double a = max_a, init_energy = e_curr;
-                while (true) {
-                    double ideal = e_curr + a * c_ls * dfa;
-                    k_lb_trial<<<grid, 256, 0, st>>>(N, s->x, xs, h, a);
-                    double cur = lb_energy(s);
-                    n_en++;
-                    if (cur <= ideal) {
-                        prev_val *= a;
-                        e_curr = cur;
-                        break;
-                    }
-                    a *= rho_ls;
-                    if (a <= min_alpha) {
-                        e_curr = init_energy;
-                        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
-                        lb_update(s);
-                        lerr = LS_MIN_ALPHA;
-                        break;
-                    }
-                }
-            }
-        }
+        else
+            lerr = search.min(dfa, max_a, e_curr, alpha, 1);  // init_flag 1 (min_cg.h:504)
         err = lerr;
-        if (err == LS_MIN_ALPHA && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
+        if (ls_failed(err) && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
             // stalled on FP32 forces above f_tol: restart from x0 with FP64 forces
             s->force64 = true;
             lb_force(s, &pe_force);
@@ -692,7 +665,7 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, double c_ls
             MAPPG_CUDA(cudaMemcpyAsync(h, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
             read_prep(&fh, &hh, &hmax, &fmaxv);
             f0_f0 = fh;
-            prev_val = -1.0;
+            search.prev_val = -1.0;
             err = LS_S;
             istep--;
             continue;

@@ -9,6 +9,7 @@
 #include <random>
 #include <vector>
 
+#include "linesearch.h"
 #include "system.h"
 #include "tc.cuh"
 
@@ -496,8 +497,8 @@ namespace mappg {
 void launch_descriptors(mappg_sys* s, float* out);  // eam.cu
 void launch_force(mappg_sys* s);
 void sys_build(mappg_sys* s);
-void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
-               double min_alpha, int nsteps, double* stats, const double* P, long long* n_fallback);
+void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps,
+               double* stats, const double* P, long long* n_fallback);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
 
@@ -1013,7 +1014,11 @@ static void run_precond(mappg_sys* s, mappg_mlp* net, int m, double e_tol, doubl
             } else {
                 long long nfb = 0;
                 double st6[6];
-                lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, st6, P, &nfb);
+                LsParams ls;
+                ls.c = c;
+                ls.rho = rho;
+                ls.min_alpha = min_alpha;
+                lbfgs_run(s, m, e_tol, max_dx, f_tol, ls, nsteps, st6, P, &nfb);
                 if (stats) {
                     for (int k = 0; k < 6; k++) stats[k] = st6[k];
                     stats[6] = (double)nfb;

@@ -10,6 +10,10 @@ Names, arguments and defaults follow the reference's Python types:
                        affine=False, max_dx=1.0, ls=ls_bt(); run(atoms, max_nsteps)
   ls_bt()              LineSearchBackTrack (ls.cpp:456-461): c=0.4, rho=0.5,
                        min_alpha=0.0
+  ls_golden()          LineSearchGoldenSection (ls.cpp:95-100): tol=sqrt(2 eps),
+                       max_iter=5, bracket=True
+  ls_brent()           LineSearchBrent (ls.cpp:262-268): as ls_golden plus
+                       zeps=1e-3 eps
   md.atoms.import_cfg  ImportCFGMD (import_cfg.cpp:496-652): an AtomEye CFG file
                        (standard or extended) as an atoms object
   md.export_cfg(...)   ExportCFGMD (export_cfg_md.cpp:9-16,167-226):
@@ -44,6 +48,60 @@ class ls_bt:
         if min_alpha < 0.0:
             raise TypeError("min_alpha must be >= 0")
         self.c, self.rho, self.min_alpha = float(c), float(rho), float(min_alpha)
+
+
+class _bounded:
+    """A validated attribute of a line search (the reference's VarAPI logics)."""
+
+    def __init__(self, name, check, message, cast=float):
+        self.name, self.check, self.message, self.cast = "_" + name, check, message, cast
+
+    def __get__(self, obj, owner=None):
+        return self if obj is None else getattr(obj, self.name)
+
+    def __set__(self, obj, value):
+        value = self.cast(value)
+        if not self.check(value):
+            raise TypeError(self.message)
+        setattr(obj, self.name, value)
+
+
+class ls_golden:
+    """Golden-section line search (LineSearchGoldenSection, ls.h:340-515;
+    defaults ls.cpp:95-100), bracketed first unless bracket is False."""
+
+    tol = _bounded("tol", lambda v: v > 0.0, "tol should be greater than 0.0")
+    max_iter = _bounded("max_iter", lambda v: v > 0, "max_iter should be greater than 0", int)
+
+    def __init__(self, tol=math.sqrt(2.0 * sys.float_info.epsilon), max_iter=5, bracket=True):
+        self.tol, self.max_iter, self.bracket = tol, max_iter, bool(bracket)
+
+    def _struct(self):
+        return _lib.line_search(_lib.LS_GOLDEN, tol=self.tol, max_iter=self.max_iter, bracket=self.bracket)
+
+
+class ls_brent(ls_golden):
+    """Brent's line search (LineSearchBrent, ls.h:524-706; defaults
+    ls.cpp:262-268)."""
+
+    zeps = _bounded("zeps", lambda v: v > 0.0, "zeps should be greater than 0.0")
+
+    def __init__(self, tol=math.sqrt(2.0 * sys.float_info.epsilon), max_iter=5, bracket=True,
+                 zeps=sys.float_info.epsilon * 1.0e-3):
+        super().__init__(tol, max_iter, bracket)
+        self.zeps = zeps
+
+    def _struct(self):
+        return _lib.line_search(_lib.LS_BRENT, tol=self.tol, max_iter=self.max_iter, bracket=self.bracket,
+                                zeps=self.zeps)
+
+
+def _ls_struct(ls):
+    if isinstance(ls, ls_bt):
+        return _lib.line_search(_lib.LS_BT, c=ls.c, rho=ls.rho, min_alpha=ls.min_alpha)
+    if isinstance(ls, ls_golden):
+        return ls._struct()
+    raise TypeError("ls must be ls_bt, ls_golden or ls_brent")
 
 
 class atoms:
@@ -335,11 +393,9 @@ class min_lbfgs:
     def run(self, atoms, max_nsteps):
         if max_nsteps < 0:
             raise TypeError("max_nsteps should be greater than or equal to 0")
-        if not isinstance(self.ls, ls_bt):
-            raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
-        s, r = _min_run(atoms, self.export, lambda s: s.lbfgs_run(
-            m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
-            min_alpha=self.ls.min_alpha, nsteps=max_nsteps))
+        ls = _ls_struct(self.ls)
+        s, r = _min_run(atoms, self.export, lambda s: s.lbfgs_run_ls(
+            ls, m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, nsteps=max_nsteps))
         s.get_x(atoms.x)
         atoms.f = s.get_f()
         atoms.pe = r["pe"]
@@ -350,7 +406,7 @@ class min_lbfgs:
 
 class min_cg:
     """Polak-Ribiere conjugate-gradient minimization of positions
-    (MinCG::__run, min_cg.h:454-536) with the back-tracking line search;
+    (MinCG::__run, min_cg.h:454-536) with any of the three line searches;
     box degrees of freedom are not in this engine's scope."""
 
     def __init__(self, e_tol=math.sqrt(sys.float_info.epsilon), H_dof=None, affine=False, max_dx=1.0, ls=None,
@@ -374,11 +430,9 @@ class min_cg:
     def run(self, atoms, max_nsteps):
         if max_nsteps < 0:
             raise TypeError("max_nsteps should be greater than or equal to 0")
-        if not isinstance(self.ls, ls_bt):
-            raise TypeError("only the back-tracking line search (ls_bt) is on this engine's path")
-        s, r = _min_run(atoms, self.export, lambda s: s.cg_run(
-            e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, c=self.ls.c, rho=self.ls.rho,
-            min_alpha=self.ls.min_alpha, nsteps=max_nsteps))
+        ls = _ls_struct(self.ls)
+        s, r = _min_run(atoms, self.export, lambda s: s.cg_run_ls(
+            ls, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, nsteps=max_nsteps))
         s.get_x(atoms.x)
         atoms.f = s.get_f()
         atoms.pe = r["pe"]

@@ -19,6 +19,7 @@
  * multiply-adds, and the neighbour predicate is compared bit for bit.
  */
 #include <ctype.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -1241,16 +1242,310 @@ static double max_abs_f(orc_sys* s) {
     return m;
 }
 
+/* ---------------------------------------------------------------- line searches
+ * LineSearchBackTrack::min   ls.h:711-769
+ * LineSearch::bracket        ls.h:214-335
+ * LineSearchGoldenSection::min ls.h:340-515
+ * LineSearchBrent::min       ls.h:524-706
+ * Defaults: ls.cpp:7-11 (constants), 95-100, 262-268, 456-461.  The caller
+ * does MinMDHandler::ls_prep (min_cg.h:230-256) and its three early exits. */
+enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, B_S, B_F_MAX_ALPHA,
+       B_F_DOWNHILL, MIN_S_FTOL = 100 };
+
+typedef struct {
+    int kind; /* 0 back-tracking, 1 golden section, 2 Brent */
+    double c, rho, min_alpha, tol;
+    int max_iter, bracket;
+    double zeps;
+} orc_ls;
+
+typedef struct {
+    orc_sys* s;
+    const double* x0;
+    const double* h;
+    long* n_en;
+    double prev_val;
+} orc_line;
+
+static double lineF(orc_line* L, double a) {
+    (*L->n_en)++;
+    return ls_F(L->s, L->x0, L->h, a);
+}
+
+static void line_reset(orc_line* L) {
+    memcpy(L->s->x, L->x0, sizeof(double) * 3 * L->s->natms);
+    dynamic_update(L->s);
+}
+
+static int ls_backtrack(const orc_ls* p, orc_line* L, double dfa, double max_a, double* nrgy, double* alpha,
+                        int init_flag) {
+    double init_energy = *nrgy;
+    if (init_flag == 0) {
+        max_a = OMIN(max_a, 1.0);
+    } else if (init_flag == 1) {
+        if (L->prev_val > 0.0 && dfa < 0.0) max_a = OMIN(max_a, -L->prev_val / dfa);
+        L->prev_val = -dfa;
+    }
+    if (max_a <= p->min_alpha) return LS_MIN_ALPHA;
+    double a = max_a;
+    for (;;) {
+        double ideal = *nrgy + a * p->c * dfa;
+        double cur = lineF(L, a);
+        if (cur <= ideal) {
+            if (init_flag == 1) L->prev_val *= a;
+            *nrgy = cur;
+            *alpha = a;
+            return LS_S;
+        }
+        a *= p->rho;
+        if (a <= p->min_alpha) {
+            *nrgy = init_energy;
+            *alpha = a;
+            line_reset(L);
+            return LS_MIN_ALPHA;
+        }
+    }
+}
+
+static int ls_bracket(orc_line* L, double dfa, double max_a, double* pa, double* pb, double* pc, double* pfa,
+                      double* pfb, double* pfc) {
+    const double golden = 0.5 + 0.5 * sqrt(5.0), sqrt_eps = sqrt(DBL_EPSILON);
+    double a = *pa, b, c, fa = *pfa, fb, fc, u, fu, r, q;
+    int ret = B_S;
+    q = 1.0e-14 / (max_a * fabs(dfa));
+    if (0.01 < q && q < 1.0)
+        b = q * max_a;
+    else if (q >= 1.0)
+        b = max_a;
+    else
+        b = 0.01 * max_a;
+    fb = lineF(L, b);
+    c = b;
+    fc = fb;
+    if (fb >= fa) {
+        int iter = 20;
+        r = (fa - fc) / (c * dfa);
+        b = c * 0.5 / (1.0 + r);
+        while (fb >= fa && iter && b > DBL_EPSILON) {
+            fb = lineF(L, b);
+            if (fb < fa) continue;
+            c = b;
+            fc = fb;
+            iter--;
+            r = (fa - fc) / (c * dfa);
+            b = c * 0.5 / (1.0 + r);
+        }
+        if (fb >= fa) {
+            b = sqrt_eps < max_a ? sqrt_eps : max_a;
+            fb = lineF(L, b);
+            if (fb >= fa) ret = B_F_DOWNHILL;
+        }
+        goto done;
+    }
+    while (fb >= fc) {
+        c = b + golden * (b - a);
+        if (c >= max_a) {
+            c = max_a;
+            fc = lineF(L, c);
+            goto done;
+        }
+        fc = lineF(L, c);
+        if (fc > fb) continue;
+        double ulim = max_a;
+        r = (b - a) * (fb - fc);
+        q = (b - c) * (fb - fa);
+        u = b - ((b - c) * q - (b - a) * r) / (2.0 * (q - r));
+        if (b < u && u < c) {
+            fu = lineF(L, u);
+            if (fu < fc) {
+                a = b; b = u; fa = fb; fb = fu;
+                goto done;
+            } else if (fu > fb) {
+                c = u; fc = fu;
+                goto done;
+            }
+            a = b; b = c; fa = fb; fb = fc;
+        } else if (u > c) {
+            u = OMIN(u, ulim);
+            fu = lineF(L, u);
+            a = b; b = c; c = u; fa = fb; fb = fc; fc = fu;
+        } else {
+            a = b; b = c; fa = fb; fb = fc;
+        }
+    }
+done:
+    *pa = a; *pb = b; *pc = c; *pfa = fa; *pfb = fb; *pfc = fc;
+    return ret;
+}
+
+static int ls_golden(const orc_ls* p, orc_line* L, double dfa, double max_a, double* nrgy, double* alpha) {
+    const double gold = 0.61803399, cgold = 0.38196601;
+    int calc = 0;
+    double a = 0.0, b, c, fa = *nrgy, fb, fc, x0, x1, x2, x3, f1, f2;
+    if (p->bracket) {
+        int chk = ls_bracket(L, dfa, max_a, &a, &b, &c, &fa, &fb, &fc);
+        if (chk != B_S) {
+            line_reset(L);
+            return chk;
+        }
+        x0 = a;
+        x3 = c;
+        if (c - b > b - a) {
+            x1 = b; x2 = b + cgold * (c - b); f1 = fb; f2 = lineF(L, x2); calc = 2;
+        } else {
+            x1 = b + cgold * (a - b); x2 = b; f1 = lineF(L, x1); f2 = fb; calc = 1;
+        }
+        int iter = p->max_iter;
+        while (x3 - x0 > p->tol * (x1 + x2) && x3 - x0 > DBL_EPSILON && iter) {
+            if (f2 < f1) {
+                x0 = x1; x1 = x2; x2 = gold * x2 + cgold * x3; f1 = f2; f2 = lineF(L, x2); calc = 2;
+            } else {
+                x3 = x2; x2 = x1; x1 = gold * x1 + cgold * x0; f2 = f1; f1 = lineF(L, x1); calc = 1;
+            }
+            iter--;
+        }
+    } else {
+        double delta, f0, f3;
+        f1 = f2 = 0.0;
+        x0 = x1 = x2 = 0.0;
+        f0 = fa;
+        x3 = max_a;
+        f3 = lineF(L, x3);
+        int iter = p->max_iter, set_left = 0, set_right = 0;
+        while (x3 - x0 > p->tol * (x1 + x2) && x3 - x0 > DBL_EPSILON && iter) {
+            delta = cgold * (x3 - x0);
+            if (!set_left) { x1 = x0 + delta; f1 = lineF(L, x1); calc = 1; set_left = 1; }
+            if (!set_right) { x2 = x3 - delta; f2 = lineF(L, x2); calc = 2; set_right = 1; }
+            if ((f0 < f2 && f0 < f3) || (f1 < f2 && f1 < f3)) {
+                set_left = 0; x3 = x2; x2 = x1; f3 = f2; f2 = f1;
+            } else {
+                set_right = 0; x0 = x1; x1 = x2; f0 = f1; f1 = f2;
+            }
+            iter--;
+        }
+        if (!set_left) {
+            if (f0 < f1) {
+                if (x0 == 0.0) {
+                    line_reset(L);
+                    *alpha = 0.0;
+                    return LS_MIN_ALPHA;
+                }
+                x1 = x0; f1 = lineF(L, x1); calc = 1;
+            }
+        }
+        if (!set_right) {
+            if (f3 < f2) { x2 = x3; f2 = lineF(L, x2); calc = 2; }
+        }
+    }
+    if (f1 < f2) {
+        if (calc == 2) f1 = lineF(L, x1);
+        *nrgy = f1;
+        *alpha = x1;
+    } else {
+        if (calc == 1) f2 = lineF(L, x2);
+        *nrgy = f2;
+        *alpha = x2;
+    }
+    L->prev_val = -dfa * *alpha;
+    return LS_S;
+}
+
+static int ls_brent(const orc_ls* p, orc_line* L, double dfa, double max_a, double* nrgy, double* alpha) {
+    const double cgold = 0.38196601;
+    double a = 0.0, b = 0.0, fa = *nrgy, fb = 0.0, x = 0.0, fx = 0.0;
+    double d = 0.0, e = 0.0, etemp, fu = 0.0, fv, fw, r, q, pp, tol1, tol2, u = 0.0, v, w, xm;
+    if (p->bracket) {
+        int chk = ls_bracket(L, dfa, max_a, &a, &x, &b, &fa, &fx, &fb);
+        if (chk != B_S) {
+            line_reset(L);
+            return chk;
+        }
+    } else {
+        a = 0.0;
+        b = max_a;
+        x = cgold * (b - a);
+        fx = lineF(L, x);
+    }
+    w = v = x;
+    fw = fv = fx;
+    for (int iter = 0; iter < p->max_iter; iter++) {
+        xm = 0.5 * (a + b);
+        tol1 = p->tol * fabs(x) + p->zeps;
+        tol2 = 2.0 * tol1;
+        if (fabs(x - xm) <= (tol2 - 0.5 * (b - a))) {
+            if (u != x) lineF(L, x);
+            *nrgy = fx;
+            *alpha = x;
+            L->prev_val = x;
+            return LS_S;
+        }
+        if (fabs(e) > tol1) {
+            r = (x - w) * (fx - fv);
+            q = (x - v) * (fx - fw);
+            pp = (x - v) * q - (x - w) * r;
+            q = 2.0 * (q - r);
+            if (q > 0.0) pp = -pp;
+            q = fabs(q);
+            etemp = e;
+            e = d;
+            if (fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - x) || pp >= q * (b - x)) {
+                e = x >= xm ? a - x : b - x;
+                d = cgold * e;
+            } else {
+                d = pp / q;
+                u = x + d;
+                if (u - a < tol2 || b - u < tol2) d = (xm - x >= 0.0) ? fabs(tol1) : -fabs(tol1);
+            }
+        } else {
+            e = x >= xm ? a - x : b - x;
+            d = cgold * e;
+        }
+        if (fabs(d) >= tol1)
+            u = x + d;
+        else
+            u = d >= 0.0 ? x + fabs(tol1) : x - fabs(tol1);
+        fu = lineF(L, u);
+        if (fu <= fx) {
+            if (u >= x) a = x; else b = x;
+            v = w; w = x; x = u;
+            fv = fw; fw = fx; fx = fu;
+        } else {
+            if (u < x) a = u; else b = u;
+            if (fu <= fw || w == x) {
+                v = w; w = u; fv = fw; fw = fu;
+            } else if (fu <= fv || v == x || v == w) {
+                v = u; fv = fu;
+            }
+        }
+    }
+    if (fa < fx) {
+        line_reset(L);
+        *alpha = 0.0;
+        return LS_MIN_ALPHA;
+    }
+    if (u != x) lineF(L, x);
+    *nrgy = fx;
+    *alpha = x;
+    L->prev_val = x;
+    return LS_S;
+}
+
+static int ls_min(const orc_ls* p, orc_line* L, double dfa, double max_a, double* nrgy, double* alpha,
+                  int init_flag) {
+    if (p->kind == 1) return ls_golden(p, L, dfa, max_a, nrgy, alpha);
+    if (p->kind == 2) return ls_brent(p, L, dfa, max_a, nrgy, alpha);
+    return ls_backtrack(p, L, dfa, max_a, nrgy, alpha, init_flag);
+}
+
 /*
  * md.min_lbfgs(m,e_tol,max_dx,ls=ls_bt(c,rho,min_alpha)).run(atoms,nsteps),
  * plus the max|F| stop (f_tol > 0: stop once max_i |F_i,a| < f_tol, checked
  * after each accepted step).  stats out: [niter, pe, max|F|, err, n_energy,
  * n_force].  Returns 0 on success.
  */
-int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, double c_ls,
-                  double rho_ls, double min_alpha, int nsteps, double* stats) {
+int orc_lbfgs_run_ls(void* p, int m, double e_tol, double max_dx, double f_tol, const orc_ls* ls, int nsteps,
+                     double* stats) {
     orc_sys* s = (orc_sys*)p;
-    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
     int n3 = 3 * s->natms;
     if (orc_sys_init_dynamic(s)) return -1;
     double* f0 = (double*)malloc(sizeof(double) * n3);
@@ -1270,6 +1565,7 @@ int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, dou
     int k = 0;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
     if (err == LS_S && f_tol > 0.0 && max_abs_f(s) < f_tol) err = MIN_S_FTOL;
+    orc_line line = {s, x0, h, &n_en, -1.0};
     int istep = 0;
     for (; err == LS_S; istep++) {
         memcpy(x0, s->x, sizeof(double) * n3);
@@ -1291,7 +1587,7 @@ int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, dou
             k = 0;
             f_h = vdot(s->f, s->f, n3);
         }
-        /* LineSearchBackTrack::min with init_flag 0 */
+        /* ls->min(&handler, e_curr, alpha_m, 0)  min_l-bfgs.h:173 */
         {
             double h_norm = vdot(h, h, n3), dfa = -f_h, max_a;
             int lerr = LS_S;
@@ -1312,33 +1608,8 @@ int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, dou
                 lerr = LS_MIN_ALPHA;
             else if (dfa >= 0.0)
                 lerr = LS_F_DOWNHILL;
-            else {
-                max_a = OMIN(max_a, 1.0);
-                if (max_a <= min_alpha)
-                    lerr = LS_MIN_ALPHA;
-                else {
-                    double a = max_a, init_energy = e_curr;
-                    while (1) {
-                        double ideal = e_curr + a * c_ls * dfa;
-                        double cur = ls_F(s, x0, h, a);
-                        n_en++;
-                        if (cur <= ideal) {
-                            e_curr = cur;
-                            lerr = LS_S;
-                            break;
-                        }
-                        a *= rho_ls;
-                        if (a <= min_alpha) {
-                            e_curr = init_energy;
-                            memcpy(s->x, x0, sizeof(double) * n3);
-                            dynamic_update(s);
-                            lerr = LS_MIN_ALPHA;
-                            break;
-                        }
-                    }
-                    alpha_m = a;
-                }
-            }
+            else
+                lerr = ls_min(ls, &line, dfa, max_a, &e_curr, &alpha_m, 0);
             err = lerr;
         }
         if (err != LS_S) {
@@ -1396,17 +1667,16 @@ int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, dou
  * LineSearchBackTrack::min with init_flag 1  ls.h:711-769 (the first trial
  * step is capped by the previous step's decrease; LineSearch::reset sets
  * prev_val = -1, ls.h:42), plus the added stop at max|F| < f_tol. */
-int orc_cg_run(void* p, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
-               int nsteps, double* stats) {
+int orc_cg_run_ls(void* p, double e_tol, double max_dx, double f_tol, const orc_ls* ls, int nsteps, double* stats) {
     orc_sys* s = (orc_sys*)p;
-    enum { LS_S, LS_F_DOWNHILL, LS_F_GRAD0, LS_MIN_ALPHA, MIN_S_TOLERANCE, MIN_F_MAX_ITER, MIN_S_FTOL = 100 };
     int n3 = 3 * s->natms;
     if (orc_sys_init_dynamic(s)) return -1;
     double* f0 = (double*)malloc(sizeof(double) * n3);
     double* h = (double*)malloc(sizeof(double) * n3);
     double* x0 = (double*)malloc(sizeof(double) * n3);
     long n_en = 0, n_fc = 1;
-    double prev_val = -1.0;
+    orc_line line = {s, x0, h, &n_en, -1.0}; /* prev_val = -1 (LineSearch::reset) */
+    double alpha = 0.0;
     force_calc(s);
     double e_prev, e_curr = s->pe;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
@@ -1447,34 +1717,8 @@ int orc_cg_run(void* p, double e_tol, double max_dx, double f_tol, double c_ls, 
                 lerr = LS_MIN_ALPHA;
             else if (dfa >= 0.0)
                 lerr = LS_F_DOWNHILL;
-            else {
-                if (prev_val > 0.0 && dfa < 0.0) max_a = OMIN(max_a, -prev_val / dfa);
-                prev_val = -dfa;
-                if (max_a <= min_alpha)
-                    lerr = LS_MIN_ALPHA;
-                else {
-                    double a = max_a, init_energy = e_curr;
-                    while (1) {
-                        double ideal = e_curr + a * c_ls * dfa;
-                        double cur = ls_F(s, x0, h, a);
-                        n_en++;
-                        if (cur <= ideal) {
-                            prev_val *= a;
-                            e_curr = cur;
-                            lerr = LS_S;
-                            break;
-                        }
-                        a *= rho_ls;
-                        if (a <= min_alpha) {
-                            e_curr = init_energy;
-                            memcpy(s->x, x0, sizeof(double) * n3);
-                            dynamic_update(s);
-                            lerr = LS_MIN_ALPHA;
-                            break;
-                        }
-                    }
-                }
-            }
+            else
+                lerr = ls_min(ls, &line, dfa, max_a, &e_curr, &alpha, 1); /* min_cg.h:504 */
             err = lerr;
         }
         if (err != LS_S) {
@@ -1545,4 +1789,17 @@ int orc_create_temp(int natms, const unsigned char* elem, const double* masses, 
     }
 #undef UNIF
     return 0;
+}
+
+/* the back-tracking entry points (ls_bt) */
+int orc_lbfgs_run(void* p, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
+                  double min_alpha, int nsteps, double* stats) {
+    orc_ls ls = {0, c_ls, rho_ls, min_alpha, 0.0, 0, 0, 0.0};
+    return orc_lbfgs_run_ls(p, m, e_tol, max_dx, f_tol, &ls, nsteps, stats);
+}
+
+int orc_cg_run(void* p, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls, double min_alpha,
+               int nsteps, double* stats) {
+    orc_ls ls = {0, c_ls, rho_ls, min_alpha, 0.0, 0, 0, 0.0};
+    return orc_cg_run_ls(p, e_tol, max_dx, f_tol, &ls, nsteps, stats);
 }

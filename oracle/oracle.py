@@ -65,6 +65,9 @@ def lib():
                                     C.c_double, C.c_double, C.c_double, C.c_int, _D]
         L.orc_cg_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, C.POINTER(C.c_double)]
+        L.orc_lbfgs_run_ls.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(OrcLs), C.c_int, _D]
+        L.orc_cg_run_ls.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(OrcLs), C.c_int, _D]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
         _lib = L
     return _lib
@@ -72,6 +75,21 @@ def lib():
 
 def _dp(a):
     return a.ctypes.data_as(_D)
+
+
+class OrcLs(C.Structure):
+    """orc_ls: the line search of a minimizer (0 back-tracking, 1 golden
+    section, 2 Brent) and its parameters."""
+    _fields_ = [("kind", C.c_int), ("c", C.c_double), ("rho", C.c_double), ("min_alpha", C.c_double),
+                ("tol", C.c_double), ("max_iter", C.c_int), ("bracket", C.c_int), ("zeps", C.c_double)]
+
+
+LS_KINDS = {"bt": 0, "golden": 1, "brent": 2}
+
+
+def line_search(kind="bt", c=0.4, rho=0.5, min_alpha=0.0, tol=(2.0 * np.finfo(float).eps) ** 0.5, max_iter=5,
+                bracket=True, zeps=np.finfo(float).eps * 1e-3):
+    return OrcLs(LS_KINDS[kind], c, rho, min_alpha, tol, max_iter, int(bool(bracket)), zeps)
 
 
 def _err():
@@ -229,6 +247,24 @@ class System:
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
 
+    def lbfgs_run_ls(self, ls, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, nsteps=10000):
+        """L-BFGS with any line search (ls = line_search(...))."""
+        st = np.zeros(6)
+        r = lib().orc_lbfgs_run_ls(self.h, m, e_tol, max_dx, f_tol, C.byref(ls), nsteps, _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def cg_run_ls(self, ls, e_tol=0.0, max_dx=1.0, f_tol=1e-4, nsteps=10000):
+        st = np.zeros(6)
+        r = lib().orc_cg_run_ls(self.h, e_tol, max_dx, f_tol, C.byref(ls), nsteps, _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
 
     def cg_run(self, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0, nsteps=10000):
         st = np.zeros(6)

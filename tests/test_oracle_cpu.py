@@ -150,6 +150,35 @@ def test_cg_reaches_force_tolerance(potentials):
     assert abs(r["pe"] - rl["pe"]) < 1e-6 * abs(rl["pe"])
 
 
+@pytest.mark.parametrize("kind", ["golden", "brent"])
+def test_golden_and_brent_line_searches(potentials, kind):
+    """ls_golden / ls_brent (ls.h:214-706) in both minimizers: bracketed,
+    they reach the force tolerance at the same minimum as back-tracking;
+    the back-tracking entry with a line-search record is the plain one."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+
+    def fresh():
+        return O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+
+    ref = fresh().lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    assert fresh().lbfgs_run_ls(O.line_search("bt"), m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000) == ref
+    for run in ("lbfgs", "cg"):
+        s = fresh()
+        ls = O.line_search(kind)
+        r = (s.lbfgs_run_ls(ls, m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000) if run == "lbfgs"
+             else s.cg_run_ls(ls, e_tol=0.0, f_tol=1e-4, nsteps=5000))
+        assert r["err"] == 100 and r["fmax"] < 1e-4, r
+        assert abs(r["pe"] - ref["pe"]) < 1e-6 * abs(ref["pe"])
+        # a line minimization costs several energies per iteration
+        assert r["n_energy"] > 3 * r["niter"]
+        # without bracketing the search spans [0, max_dx/max|h|] in max_iter
+        # steps; the run stops on a failed search or descends
+        s = fresh()
+        r = s.lbfgs_run_ls(O.line_search(kind, bracket=False), m=10, e_tol=0.0, f_tol=1e-4, nsteps=50)
+        assert r["err"] in (3, 100, 5) and r["pe"] < ref["pe"] + 2.0
+
+
 REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
 
 
