@@ -108,7 +108,9 @@ def test_minimizer_export(setfl, tmp_path, kind):
     assert np.max(np.abs(d)) < 1e-12
     # the forces column of the last file is the run's final force
     with open(got[10]) as fh:
-        rows = [ln.split() for ln in fh if len(ln.split()) == 6]
+        lines = fh.read().splitlines()
+    body = lines[lines.index("auxiliary[2] = f_2 [reduced unit]") + 1:]
+    rows = [ln.split() for ln in body if len(ln.split()) == 6]
     f_file = np.array(rows, dtype=float)[:, 3:]
     assert np.max(np.abs(f_file - a.f)) < 1e-12
 
