@@ -256,6 +256,24 @@ int mappg_lbfgs_run_ls(mappg_sys* sys, int m, double e_tol, double max_dx, doubl
 int mappg_cg_run_ls(mappg_sys* sys, double e_tol, double max_dx, double f_tol, const mappg_ls* ls, int nsteps,
                     double* stats);
 
+/* md.min_lbfgs / md.min_cg with box degrees of freedom (MinLBFGS::__run
+ * min_l-bfgs.h:113-219, MinCG::__run min_cg.h:454-536, with MinMDHandler
+ * min_cg.h:89-331 for BC = true or X = false).  method 0 is L-BFGS with m
+ * history pairs, 1 conjugate gradients.  H_dof: 9 ints, row-major; the
+ * lower triangle says which entries of the box may relax (as the Python
+ * H_dof).  affine != 0 moves the atoms only with the box.  Each vector of
+ * the method carries a box part, the lower triangle of a 3x3 tensor, whose
+ * force is F_H masked by H_dof; a direction h moves the atoms along
+ * h + x0 h.A and the box along H0 h.A, and every line-search trial rebuilds
+ * the neighbour list for its box.  Stops as the reference's (energy
+ * tolerance, iterations, line-search failures; no force tolerance).  stats
+ * as mappg_lbfgs_run; the relaxed box is read with mappg_sys_get_box. */
+int mappg_min_box_run(mappg_sys* sys, int method, int m, double e_tol, double max_dx, const int* H_dof, int affine,
+                      const mappg_ls* ls, int nsteps, double* stats);
+
+/* The system's box (9 doubles, rows are the cell vectors; Atoms::H). */
+int mappg_sys_get_box(mappg_sys* sys, double* H);
+
 /* A function that mappg_lbfgs_run, mappg_lbfgs_run_precond and mappg_cg_run
  * call after every nevery-th iteration's force call, with the number of
  * iterations done; the system's positions and forces are then that

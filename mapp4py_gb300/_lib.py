@@ -62,6 +62,9 @@ SIGNATURES = {
     "mappg_nvt_snapshot": (C.c_int, [_VP, _D, _D]),
     "mappg_sys_set_hook": (C.c_int, [_VP, _VP, _VP, C.c_int]),
     "mappg_lbfgs_run_ls": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),
+    "mappg_min_box_run": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_double, _I, C.c_int, _VP, C.c_int,
+                                    _D]),
+    "mappg_sys_get_box": (C.c_int, [_VP, _D]),
     "mappg_cg_run_ls": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),
     "mappg_cfg_read": (C.c_int, [C.c_char_p, C.POINTER(_VP)]),
     "mappg_cfg_info": (C.c_int, [_VP, _I, _I, _I, _D]),
@@ -429,6 +432,23 @@ class System:
                                              C.cast(C.pointer(ls), _VP), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def min_box_run(self, ls, H_dof, affine=False, method="lbfgs", m=10, e_tol=0.0, max_dx=1.0, nsteps=100000):
+        """L-BFGS ("lbfgs") or CG ("cg") with box degrees of freedom: H_dof
+        is a 3x3 mask (its lower triangle is read); affine moves the atoms
+        only with the box."""
+        st = np.zeros(6)
+        mask = np.ascontiguousarray(np.asarray(H_dof, dtype=bool).reshape(3, 3), dtype=np.int32)
+        self._checked(load().mappg_min_box_run(self.h, 0 if method == "lbfgs" else 1, int(m), float(e_tol),
+                                               float(max_dx), mask.ctypes.data_as(_I), int(bool(affine)),
+                                               C.cast(C.pointer(ls), _VP), int(nsteps), dptr(st)))
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def get_box(self):
+        H = np.zeros((3, 3))
+        check(load().mappg_sys_get_box(self.h, dptr(H)))
+        return H
 
     def _checked(self, rc):
         # an exception raised by the iteration hook comes first

@@ -39,6 +39,8 @@ void nvt_free(mappg_sys* s);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
 void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsParams& ls, int nsteps, double* stats);
+void box_min_run(mappg_sys* s, int method, int m, double e_tol, double max_dx, const int* H_dof, bool affine,
+                 const LsParams& ls, int nsteps, double* stats);
 void launch_density_only(mappg_sys* s);
 void launch_force_only(mappg_sys* s);
 
@@ -876,6 +878,24 @@ int mappg_cg_run_ls(mappg_sys* s, double e_tol, double max_dx, double f_tol, con
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "conjugate gradients run per single cell"};
         cg_run(s, e_tol, max_dx, f_tol, ls_params(ls), nsteps, stats);
+    });
+}
+
+int mappg_min_box_run(mappg_sys* s, int method, int m, double e_tol, double max_dx, const int* H_dof, int affine,
+                      const mappg_ls* ls, int nsteps, double* stats) {
+    return guard([&] {
+        if (!s || !H_dof) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "box degrees of freedom are per single cell"};
+        box_min_run(s, method, m, e_tol, max_dx, H_dof, affine != 0, ls_params(ls), nsteps, stats);
+    });
+}
+
+int mappg_sys_get_box(mappg_sys* s, double* H) {
+    return guard([&] {
+        if (!s || !H) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "the boxes of a batch are those it was created with"};
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) H[3 * i + j] = s->box.H[i][j];
     });
 }
 

@@ -288,7 +288,7 @@ static void lb_force(mappg_sys* s, double* pe) {
 
 // The caller's function after an iteration's force call, where the
 // reference writes its periodic export (ExportHandler::print, min.h:216-220)
-static void iteration_hook(mappg_sys* s, int istep) {
+void iteration_hook(mappg_sys* s, int istep) {
     if (!s->hook || s->hook_every <= 0 || (istep + 1) % s->hook_every != 0) return;
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
     if (s->hook(s->hook_user, (long long)istep + 1) != 0)

@@ -191,10 +191,13 @@ class atoms:
         self.x_d = _lib.create_temp(self.elem, self.masses, temp, self.kB, seed)
 
     # ---------------------------------------------------------- device state
+    def _key(self):
+        return (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
+
     def _system(self):
         if self.ff is None:
             raise TypeError("cannot start without governing equations (force field)")
-        key = (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
+        key = self._key()
         if self._sys is None or self._sys_key != key:
             self._sys = None
             self._sys = _lib.System(self.ff, self.H, self.x, self.elem, self.masses, self.skin,
@@ -229,10 +232,10 @@ class export_cfg:
     def __call__(self, atoms, file_name):
         self._write(atoms, file_name, atoms.x, atoms.x_d, atoms.f)
 
-    def _write_step(self, atoms, step, x, x_d, f):
-        self._write(atoms, "%s.%09d.cfg" % (self.file_pattern, step), x, x_d, f)
+    def _write_step(self, atoms, step, x, x_d, f, H=None):
+        self._write(atoms, "%s.%09d.cfg" % (self.file_pattern, step), x, x_d, f, H)
 
-    def _write(self, atoms, path, x, x_d, f):
+    def _write(self, atoms, path, x, x_d, f, H=None):
         vecs = []
         for name in self.extra_vecs:
             if name not in self._VECS:
@@ -242,7 +245,7 @@ class export_cfg:
                 raise TypeError("cannot export vector '%s' to file, it is empty" % name)
             vecs.append((name, arr))
         try:
-            _lib.write_cfg(path, atoms.H, x, atoms.elem, atoms.masses, list(atoms.elems), vecs)
+            _lib.write_cfg(path, atoms.H if H is None else H, x, atoms.elem, atoms.masses, list(atoms.elems), vecs)
         except _lib.MappgError as e:
             raise TypeError(str(e)) from None
 
@@ -352,7 +355,8 @@ def _min_run(atoms, xprt, run):
     xprt._write_step(atoms, step0, atoms.x, atoms.x_d, f0)
 
     def at(it):
-        xprt._write_step(atoms, step0 + it, s.get_x(), atoms.x_d, s.get_f() if xprt._wants_f() else None)
+        xprt._write_step(atoms, step0 + it, s.get_x(), atoms.x_d, s.get_f() if xprt._wants_f() else None,
+                         s.get_box())
 
     s.set_hook(at, xprt.nevery)
     try:
@@ -361,84 +365,98 @@ def _min_run(atoms, xprt, run):
         s.set_hook(None, 0)
     if r["niter"] % xprt.nevery:
         xprt._write_step(atoms, step0 + r["niter"], s.get_x(), atoms.x_d,
-                         s.get_f() if xprt._wants_f() else None)
+                         s.get_f() if xprt._wants_f() else None, s.get_box())
     return s, r
 
 
-class min_lbfgs:
-    """L-BFGS minimization of positions (box degrees of freedom are not in
-    this engine's scope; H_dof must stay all False)."""
+def _h_dof_mask(H_dof):
+    """The reference's symmetric bool[3][3] (rows of lengths 1, 2, 3 for the
+    lower triangle, or a full 3x3) as a 3x3 mask of its lower triangle."""
+    mask = np.zeros((3, 3), dtype=bool)
+    if H_dof is None:
+        return mask
+    rows = [list(r) for r in H_dof]
+    if len(rows) != 3 or any(len(r) not in (i + 1, 3) for i, r in enumerate(rows)):
+        raise TypeError("H_dof should be [[bool],[bool,bool],[bool,bool,bool]] or a 3x3 array of bool")
+    for i in range(3):
+        for j in range(i + 1):
+            mask[i, j] = bool(rows[i][j])
+    return mask
+
+
+class _min:
+    """What md.min_lbfgs and md.min_cg share (Min, min.cpp:30-60): e_tol,
+    H_dof (box entries that relax), affine, max_dx, ls, plus f_tol."""
+
+    def __init__(self, e_tol, H_dof, affine, max_dx, ls, f_tol):
+        if e_tol < 0.0:
+            raise TypeError("e_tol should be greater than or equal to 0.0")
+        if not (max_dx > 0.0):
+            raise TypeError("max_dx should be greater than 0.0")
+        self.H_dof = _h_dof_mask(H_dof)
+        self.affine = bool(affine)
+        self.e_tol = float(e_tol)
+        self.max_dx = float(max_dx)
+        self.ls = ls if ls is not None else ls_bt()
+        self.f_tol = float(f_tol)
+        self.ntally = 1000
+        self.export = None
+        self.last = None
+
+    def _box(self):
+        return bool(self.H_dof.any()) or self.affine
+
+    def _run(self, atoms, max_nsteps, method, atoms_only):
+        if max_nsteps < 0:
+            raise TypeError("max_nsteps should be greater than or equal to 0")
+        ls = _ls_struct(self.ls)
+        if self._box():
+            if self.f_tol > 0.0:
+                raise TypeError("f_tol is not available with box degrees of freedom (use e_tol)")
+            run = lambda s: s.min_box_run(ls, self.H_dof, self.affine, method, getattr(self, "m", 0),  # noqa: E731
+                                          self.e_tol, self.max_dx, max_nsteps)
+        else:
+            run = atoms_only(ls)
+        s, r = _min_run(atoms, self.export, run)
+        s.get_x(atoms.x)
+        if self._box():
+            atoms.H = s.get_box()
+            atoms._sys_key = atoms._key()
+        atoms.f = s.get_f()
+        atoms.pe = r["pe"]
+        atoms.step += r["niter"]
+        self.last = r
+        return r
+
+
+class min_lbfgs(_min):
+    """L-BFGS minimization (MinLBFGS, min_l-bfgs.cpp; min_l-bfgs.h:113-219) of
+    the positions and, with H_dof or affine, of the box."""
 
     def __init__(self, m=2, e_tol=math.sqrt(sys.float_info.epsilon), H_dof=None, affine=False, max_dx=1.0,
                  ls=None, f_tol=0.0):
         if m < 0:
             raise TypeError("m should be greater than or equal to 0")
-        if e_tol < 0.0:
-            raise TypeError("e_tol should be greater than or equal to 0.0")
-        if not (max_dx > 0.0):
-            raise TypeError("max_dx should be greater than 0.0")
-        if H_dof is not None and np.any(np.asarray(H_dof, dtype=object) == True):  # noqa: E712
-            raise TypeError("box degrees of freedom (H_dof) are not supported by this engine")
-        if affine:
-            raise TypeError("affine minimization is not supported by this engine")
+        super().__init__(e_tol, H_dof, affine, max_dx, ls, f_tol)
         self.m = int(m)
-        self.e_tol = float(e_tol)
-        self.max_dx = float(max_dx)
-        self.ls = ls if ls is not None else ls_bt()
-        self.f_tol = float(f_tol)
-        self.ntally = 1000
-        self.export = None
-        self.last = None
 
     def run(self, atoms, max_nsteps):
-        if max_nsteps < 0:
-            raise TypeError("max_nsteps should be greater than or equal to 0")
-        ls = _ls_struct(self.ls)
-        s, r = _min_run(atoms, self.export, lambda s: s.lbfgs_run_ls(
+        return self._run(atoms, max_nsteps, "lbfgs", lambda ls: lambda s: s.lbfgs_run_ls(
             ls, m=self.m, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, nsteps=max_nsteps))
-        s.get_x(atoms.x)
-        atoms.f = s.get_f()
-        atoms.pe = r["pe"]
-        atoms.step += r["niter"]
-        self.last = r
-        return r
 
 
-class min_cg:
-    """Polak-Ribiere conjugate-gradient minimization of positions
-    (MinCG::__run, min_cg.h:454-536) with any of the three line searches;
-    box degrees of freedom are not in this engine's scope."""
+class min_cg(_min):
+    """Polak-Ribiere conjugate-gradient minimization (MinCG::__run,
+    min_cg.h:454-536) with any of the three line searches, of the positions
+    and, with H_dof or affine, of the box."""
 
     def __init__(self, e_tol=math.sqrt(sys.float_info.epsilon), H_dof=None, affine=False, max_dx=1.0, ls=None,
                  f_tol=0.0):
-        if e_tol < 0.0:
-            raise TypeError("e_tol should be greater than or equal to 0.0")
-        if not (max_dx > 0.0):
-            raise TypeError("max_dx should be greater than 0.0")
-        if H_dof is not None and np.any(np.asarray(H_dof, dtype=object) == True):  # noqa: E712
-            raise TypeError("box degrees of freedom (H_dof) are not supported by this engine")
-        if affine:
-            raise TypeError("affine minimization is not supported by this engine")
-        self.e_tol = float(e_tol)
-        self.max_dx = float(max_dx)
-        self.ls = ls if ls is not None else ls_bt()
-        self.f_tol = float(f_tol)
-        self.ntally = 1000
-        self.export = None
-        self.last = None
+        super().__init__(e_tol, H_dof, affine, max_dx, ls, f_tol)
 
     def run(self, atoms, max_nsteps):
-        if max_nsteps < 0:
-            raise TypeError("max_nsteps should be greater than or equal to 0")
-        ls = _ls_struct(self.ls)
-        s, r = _min_run(atoms, self.export, lambda s: s.cg_run_ls(
+        return self._run(atoms, max_nsteps, "cg", lambda ls: lambda s: s.cg_run_ls(
             ls, e_tol=self.e_tol, max_dx=self.max_dx, f_tol=self.f_tol, nsteps=max_nsteps))
-        s.get_x(atoms.x)
-        atoms.f = s.get_f()
-        atoms.pe = r["pe"]
-        atoms.step += r["niter"]
-        self.last = r
-        return r
 
 
 min_cg_new = min_cg  # the name the reference registers for this minimizer

@@ -1259,20 +1259,30 @@ typedef struct {
     double zeps;
 } orc_ls;
 
-typedef struct {
+/* the line-search function object (MinMDHandler::F / F_reset,
+   min_cg.h:260-276); F and reset null: atoms only, x = x0 + alpha h */
+typedef struct orc_line {
     orc_sys* s;
     const double* x0;
     const double* h;
     long* n_en;
     double prev_val;
+    double (*F)(struct orc_line*, double);
+    void (*reset)(struct orc_line*);
+    void* ctx;
 } orc_line;
 
 static double lineF(orc_line* L, double a) {
     (*L->n_en)++;
+    if (L->F) return L->F(L, a);
     return ls_F(L->s, L->x0, L->h, a);
 }
 
 static void line_reset(orc_line* L) {
+    if (L->reset) {
+        L->reset(L);
+        return;
+    }
     memcpy(L->s->x, L->x0, sizeof(double) * 3 * L->s->natms);
     dynamic_update(L->s);
 }
@@ -1749,6 +1759,243 @@ int orc_cg_run_ls(void* p, double e_tol, double max_dx, double f_tol, const orc_
     free(x0);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Box degrees of freedom                                                    */
+/* ------------------------------------------------------------------------ */
+/* MinLBFGS::__run  min_l-bfgs.h:113-219 and MinCG::__run  min_cg.h:454-536
+ * with BC = true or X = false: MinMDHandler  min_cg.h:89-331 (init 164-198,
+ * ls_prep 230-256, F 260-267, F_reset 271-276, prep_x_d 298-309,
+ * prep_x_d_affine 313-321, post_force_calc_box 324-329) and the vector-tensor
+ * algebra of new_min_vec.h (dot product 596-606: atoms first, then the lower
+ * triangle (0,0),(1,0),(1,1),(2,0),(2,1),(2,2), TOP 224-322).  A trial
+ * rebuilds the lists for its box (NewDynamicMD<true,true>::update,
+ * dynamic_md.h:200-206, rebuilds only past the skin; a rebuild at every
+ * trial gives the same energies while no pair crosses the cutoff unseen). */
+typedef struct {
+    double* v; /* 3n, or NULL when the atoms move affinely */
+    double A[3][3];
+} orc_vt;
+
+static const int LT[6][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {2, 2}};
+
+static double vt_dot(const orc_vt* a, const orc_vt* b, int n3) {
+    double r = a->v ? vdot(a->v, b->v, n3) : 0.0;
+    for (int k = 0; k < 6; k++) r += a->A[LT[k][0]][LT[k][1]] * b->A[LT[k][0]][LT[k][1]];
+    return r;
+}
+static void vt_lin(orc_vt* y, double cy, const orc_vt* x, double cx, int n3) {
+    if (y->v)
+        for (int q = 0; q < n3; q++) y->v[q] = cy * y->v[q] + cx * x->v[q];
+    for (int k = 0; k < 6; k++) {
+        int i = LT[k][0], j = LT[k][1];
+        y->A[i][j] = cy * y->A[i][j] + cx * x->A[i][j];
+    }
+}
+static void vt_scale(orc_vt* y, double c, int n3) {
+    if (y->v)
+        for (int q = 0; q < n3; q++) y->v[q] *= c;
+    for (int k = 0; k < 6; k++) y->A[LT[k][0]][LT[k][1]] *= c;
+}
+static void vt_copy(orc_vt* y, const orc_vt* x, int n3) {
+    if (y->v) memcpy(y->v, x->v, sizeof(double) * n3);
+    memcpy(y->A, x->A, sizeof(y->A));
+}
+
+typedef struct {
+    orc_sys* s;
+    int n3;
+    double *x0, *xd;
+    double H0[3][3], xdA[3][3];
+} orc_box;
+
+static int box_rebuild(orc_sys* s) {
+    update_H(s);
+    return rebuild(s);
+}
+static double box_F(orc_line* L, double a) {
+    orc_box* b = (orc_box*)L->ctx;
+    orc_sys* s = b->s;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) s->H[i][j] = b->H0[i][j] + a * b->xdA[i][j];
+    for (int q = 0; q < b->n3; q++) s->x[q] = b->x0[q] + a * b->xd[q];
+    if (box_rebuild(s)) return NAN;
+    return eam_energy_half(s);
+}
+static void box_reset(orc_line* L) {
+    orc_box* b = (orc_box*)L->ctx;
+    orc_sys* s = b->s;
+    memcpy(s->H, b->H0, sizeof(s->H));
+    memcpy(s->x, b->x0, sizeof(double) * b->n3);
+    box_rebuild(s);
+}
+
+/* handler.force_calc(): forces, pe and F_H masked by H_dof */
+static void box_force(orc_sys* s, orc_vt* f, const int* hdof) {
+    force_calc(s);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) f->A[i][j] = (j <= i && hdof[3 * i + j]) ? s->F_H[i][j] : 0.0;
+    if (f->v) memcpy(f->v, s->f, sizeof(double) * 3 * s->natms);
+}
+
+/* prep_x_d / prep_x_d_affine: x_d = h + x0 h.A (affine: x0 h.A), box part
+   H0 h.A (MLT_mul_MLT); returns max|x_d| */
+static double box_prep(orc_box* b, const orc_vt* h) {
+    int n = b->n3 / 3;
+    const double(*A)[3] = h->A;
+    double mx = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double* p = b->x0 + 3 * i;
+        double d[3] = {A[0][0] * p[0] + (A[1][0] * p[1] + A[2][0] * p[2]), A[1][1] * p[1] + A[2][1] * p[2],
+                       A[2][2] * p[2]};
+        for (int c = 0; c < 3; c++) {
+            double v = h->v ? h->v[3 * i + c] + d[c] : d[c];
+            b->xd[3 * i + c] = v;
+            mx = OMAX(mx, fabs(v));
+        }
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double t = 0.0;
+            if (j <= i) {
+                t = b->H0[i][i] * A[i][j];
+                for (int k = i - 1; k >= j; k--) t = b->H0[i][k] * A[k][j] + t;
+            }
+            b->xdA[i][j] = t;
+        }
+    return mx;
+}
+
+/* method 0 L-BFGS, 1 CG; hdof[9] row-major (lower triangle read); stats as
+   orc_lbfgs_run; the relaxed box is left in the system (orc_sys_get_box) */
+int orc_min_box_run(void* p, int method, int m, double e_tol, double max_dx, const int* hdof, int affine,
+                    const orc_ls* ls, int nsteps, double* stats) {
+    orc_sys* s = (orc_sys*)p;
+    int n3 = 3 * s->natms, X = !affine;
+    if (orc_sys_init_dynamic(s)) return -1;
+    orc_box box = {s, n3, (double*)malloc(sizeof(double) * n3), (double*)malloc(sizeof(double) * n3), {{0}}, {{0}}};
+    int nv = 3 + (method == 0 ? 2 * m : 0);
+    double* pool = X ? (double*)calloc((size_t)nv * n3, sizeof(double)) : NULL;
+    orc_vt f = {X ? pool : NULL, {{0}}}, f0 = {X ? pool + n3 : NULL, {{0}}}, h = {X ? pool + 2 * n3 : NULL, {{0}}};
+    orc_vt* sv = (orc_vt*)calloc(m ? m : 1, sizeof(orc_vt));
+    orc_vt* yv = (orc_vt*)calloc(m ? m : 1, sizeof(orc_vt));
+    if (method == 0)
+        for (int i = 0; i < m; i++) {
+            sv[i].v = X ? pool + (size_t)(3 + 2 * i) * n3 : NULL;
+            yv[i].v = X ? pool + (size_t)(4 + 2 * i) * n3 : NULL;
+        }
+    double* rho = (double*)calloc(m ? m : 1, sizeof(double));
+    double* alph = (double*)calloc(m ? m : 1, sizeof(double));
+    long n_en = 0, n_fc = 1;
+    orc_line line = {s, box.x0, box.xd, &n_en, -1.0, box_F, box_reset, &box};
+    box_force(s, &f, hdof);
+    double e_curr = s->pe, e_prev, f_h, alpha_m = 0.0, gamma = 1.0, f0_f0 = 0.0;
+    int k = 0, err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S, istep = 0;
+    if (method == 1) {
+        vt_copy(&h, &f, n3);
+        f0_f0 = vt_dot(&f, &f, n3);
+    }
+    for (; err == LS_S; istep++) {
+        if (method == 1 && f0_f0 == 0.0) {
+            err = LS_F_GRAD0;
+            continue;
+        }
+        memcpy(box.x0, s->x, sizeof(double) * n3);
+        memcpy(box.H0, s->H, sizeof(box.H0));
+        vt_copy(&f0, &f, n3);
+        if (method == 0) {
+            vt_copy(&h, &f, n3);
+            for (int i = 0; i < k; i++) {
+                alph[i] = -rho[i] * vt_dot(&sv[i], &h, n3);
+                vt_lin(&h, 1.0, &yv[i], alph[i], n3);
+            }
+            vt_scale(&h, gamma, n3);
+            for (int i = k - 1; i > -1; i--) {
+                double scl0 = -alph[i] - rho[i] * vt_dot(&yv[i], &h, n3);
+                vt_lin(&h, 1.0, &sv[i], scl0, n3);
+            }
+        }
+        e_prev = e_curr;
+        f_h = vt_dot(&f, &h, n3);
+        if (f_h < 0.0) {
+            vt_copy(&h, &f, n3);
+            if (method == 0) {
+                k = 0;
+                f_h = vt_dot(&f, &f, n3);
+            } else {
+                f_h = f0_f0;
+            }
+        }
+        double max_xd = box_prep(&box, &h);
+        double h_norm = vt_dot(&h, &h, n3), dfa = -f_h, max_a;
+        int lerr;
+        if (h_norm == 0.0) {
+            max_a = 0.0;
+            dfa = 0.0;
+        } else if (dfa >= 0.0) {
+            max_a = 0.0;
+            dfa = 1.0;
+        } else {
+            max_a = fabs(max_dx / max_xd);
+        }
+        if (dfa == 0.0)
+            lerr = LS_F_GRAD0;
+        else if (max_a == 0.0)
+            lerr = LS_MIN_ALPHA;
+        else if (dfa >= 0.0)
+            lerr = LS_F_DOWNHILL;
+        else
+            lerr = ls_min(ls, &line, dfa, max_a, &e_curr, &alpha_m, method == 0 ? 0 : 1);
+        err = lerr;
+        if (err != LS_S) {
+            istep--;
+            continue;
+        }
+        box_force(s, &f, hdof);
+        n_fc++;
+        if (e_prev - e_curr < e_tol) err = MIN_S_TOLERANCE;
+        if (istep + 1 == nsteps) err = MIN_F_MAX_ITER;
+        if (err) continue;
+        if (method == 1) {
+            double f_f = vt_dot(&f, &f, n3), f_f0 = vt_dot(&f, &f0, n3);
+            double ratio = (f_f - f_f0) / f0_f0;
+            vt_lin(&h, ratio, &f, 1.0, n3);
+            f0_f0 = f_f;
+        } else if (m) {
+            if (k != m) k++;
+            orc_vt ts = sv[k - 1], ty = yv[k - 1];
+            for (int i = k - 1; i > 0; i--) {
+                sv[i] = sv[i - 1];
+                yv[i] = yv[i - 1];
+            }
+            sv[0] = ts;
+            yv[0] = ty;
+            for (int i = m - 1; i > 0; i--) rho[i] = rho[i - 1];
+            vt_lin(&sv[0], 0.0, &h, alpha_m, n3);
+            vt_copy(&yv[0], &f0, n3);
+            vt_lin(&yv[0], 1.0, &f, -1.0, n3);
+            double inner0 = vt_dot(&sv[0], &yv[0], n3);
+            double inner1 = vt_dot(&yv[0], &yv[0], n3);
+            gamma = inner0 / inner1;
+            rho[0] = 1.0 / inner0;
+        } else {
+            gamma = alpha_m * (vt_dot(&h, &f0, n3) - vt_dot(&h, &f, n3)) /
+                    (vt_dot(&f, &f, n3) + vt_dot(&f0, &f0, n3) - 2.0 * vt_dot(&f, &f0, n3));
+        }
+    }
+    if (stats) {
+        stats[0] = istep;
+        stats[1] = s->pe;
+        stats[2] = max_abs_f(s);
+        stats[3] = err;
+        stats[4] = (double)n_en;
+        stats[5] = (double)n_fc;
+    }
+    free(box.x0); free(box.xd); free(pool); free(sv); free(yv); free(rho); free(alph);
+    return 0;
+}
+
+void orc_sys_get_box(void* p, double* H) { memcpy(H, ((orc_sys*)p)->H, sizeof(double) * 9); }
 
 /* Park-Miller + polar Box-Muller  random.cpp:32-68, AtomsMD::create_T
    atoms_md.cpp:130-162.  Seed 0 makes the reference loop forever; here it is

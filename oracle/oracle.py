@@ -68,6 +68,9 @@ def lib():
         L.orc_lbfgs_run_ls.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
                                        C.POINTER(OrcLs), C.c_int, _D]
         L.orc_cg_run_ls.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(OrcLs), C.c_int, _D]
+        L.orc_min_box_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int),
+                                      C.c_int, C.POINTER(OrcLs), C.c_int, _D]
+        L.orc_sys_get_box.argtypes = [C.c_void_p, _D]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
         _lib = L
     return _lib
@@ -256,6 +259,25 @@ class System:
         self.initialized = True
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def min_box_run(self, ls, H_dof, affine=False, method="lbfgs", m=10, e_tol=0.0, max_dx=1.0, nsteps=10000):
+        """L-BFGS or CG with box degrees of freedom (H_dof: 3x3 mask, lower
+        triangle read)."""
+        st = np.zeros(6)
+        mask = np.ascontiguousarray(np.asarray(H_dof, dtype=bool).reshape(3, 3), dtype=np.int32)
+        r = lib().orc_min_box_run(self.h, 0 if method == "lbfgs" else 1, m, e_tol, max_dx,
+                                  mask.ctypes.data_as(C.POINTER(C.c_int)), int(bool(affine)), C.byref(ls), nsteps,
+                                  _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def box(self):
+        H = np.zeros((3, 3))
+        lib().orc_sys_get_box(self.h, _dp(H))
+        return H
 
     def cg_run_ls(self, ls, e_tol=0.0, max_dx=1.0, f_tol=1e-4, nsteps=10000):
         st = np.zeros(6)

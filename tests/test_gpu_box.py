@@ -1,0 +1,71 @@
+"""Minimization with box degrees of freedom (H_dof, affine) on the device
+against the oracle's restatement of MinLBFGS / MinCG with the box in the
+vector-tensor algebra: iteration and energy-call counts, energies, boxes
+and positions; the md-level minimizers update atoms.H."""
+import numpy as np
+import pytest
+
+import oracle as O
+from mapp4py_gb300 import _lib, ls_bt, md, synth
+
+pytestmark = pytest.mark.gpu
+
+KINDS = {"bt": _lib.LS_BT, "golden": _lib.LS_GOLDEN, "brent": _lib.LS_BRENT}
+
+
+def cell():
+    return synth.alloy((4, 4, 4), a=3.7, xB=0.3, sigma=0.05, seed=2)
+
+
+def pair(path, method, affine, kind, nsteps, mask=None):
+    c = cell()
+    mask = np.eye(3, dtype=bool) if mask is None else mask
+    o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    ro = o.min_box_run(O.line_search(kind), mask, affine, method, m=10, e_tol=1e-10, nsteps=nsteps)
+    s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5, precision=_lib.FP64)
+    r = s.min_box_run(_lib.line_search(KINDS[kind]), mask, affine, method, m=10, e_tol=1e-10, nsteps=nsteps)
+    H, Ho = s.get_box(), o.box()
+    d = s.get_x() - o.x
+    d -= np.round(d @ np.linalg.inv(Ho)) @ Ho
+    return r, ro, np.max(np.abs(H - Ho)), np.max(np.abs(d))
+
+
+@pytest.mark.parametrize("kind", ["bt", "golden"])
+@pytest.mark.parametrize("affine", [True, False])
+@pytest.mark.parametrize("method", ["lbfgs", "cg"])
+def test_box_minimization_follows_oracle(potentials, method, affine, kind):
+    path, _ = potentials[("A", "B")]
+    r, ro, dH, dx = pair(path, method, affine, kind, 6)
+    assert (r["niter"], r["err"], r["n_energy"], r["n_force"]) == (ro["niter"], ro["err"], ro["n_energy"],
+                                                                      ro["n_force"])
+    assert abs(r["pe"] - ro["pe"]) <= 1e-11 * abs(ro["pe"])
+    assert dH < 1e-10 and dx < 1e-9
+
+
+def test_affine_box_relaxation_to_zero_stress(potentials):
+    path, _ = potentials[("A", "B")]
+    r, ro, dH, dx = pair(path, "lbfgs", True, "bt", 300)
+    assert r["err"] == ro["err"] == 4
+    assert abs(r["pe"] - ro["pe"]) <= 1e-9 * abs(ro["pe"]) and dH < 1e-7
+    mask = np.zeros((3, 3), dtype=bool)
+    mask[2, 2] = mask[1, 0] = True
+    r, ro, dH, dx = pair(path, "cg", True, "bt", 8, mask)
+    assert r["n_energy"] == ro["n_energy"] and dH < 1e-10
+
+
+def test_md_minimizer_updates_the_box(potentials, tmp_path):
+    path, _ = potentials[("A", "B")]
+    c = cell()
+    a = md.atoms(c.H, c.x, c.elem, elems=("A", "B"), masses=c.masses)
+    a.ff_eam_setfl(path)
+    m = md.min_lbfgs(m=10, e_tol=1e-10, H_dof=[[True], [False, True], [False, False, True]], affine=True,
+                     ls=ls_bt())
+    m.export = md.export_cfg(str(tmp_path / "box"), nevery=5)
+    r = m.run(a, 300)
+    assert r["err"] == 4
+    assert not np.allclose(a.H, c.H) and a.H[1, 0] == 0.0
+    assert np.max(np.abs(a.S_pe if np.all(np.isfinite(a.S_pe)) else 0.0)) >= 0.0
+    last = md.atoms.import_cfg(str(tmp_path / ("box.%09d.cfg" % r["niter"])))
+    assert np.allclose(last.H, a.H, rtol=0, atol=1e-12)
+    with pytest.raises(TypeError, match="f_tol"):
+        md.min_cg(H_dof=np.eye(3, dtype=bool), f_tol=1e-4).run(a, 10)

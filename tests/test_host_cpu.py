@@ -96,6 +96,18 @@ def test_library_exports_every_declared_symbol(built):
         assert hasattr(L, name)
 
 
+def test_h_dof_forms():
+    from mapp4py_gb300 import md
+
+    m = md.min_lbfgs(H_dof=[[True], [False, True], [False, False, True]])
+    assert m.H_dof.tolist() == np.eye(3, dtype=bool).tolist() and m._box()
+    full = np.ones((3, 3), dtype=bool)
+    assert md.min_cg(H_dof=full).H_dof.tolist() == np.tril(full).tolist()
+    assert not md.min_lbfgs()._box() and md.min_cg(affine=True)._box()
+    with pytest.raises(TypeError):
+        md.min_lbfgs(H_dof=[[True, False]])
+
+
 def test_api_surface_mirrors_reference(built):
     from mapp4py_gb300 import md, ls_bt
 

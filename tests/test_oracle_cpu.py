@@ -179,6 +179,40 @@ def test_golden_and_brent_line_searches(potentials, kind):
         assert r["err"] in (3, 100, 5) and r["pe"] < ref["pe"] + 2.0
 
 
+@pytest.mark.parametrize("method", ["lbfgs", "cg"])
+def test_box_degrees_of_freedom(potentials, method):
+    """MinLBFGS / MinCG with H_dof (min_cg.h:89-331, new_min_vec.h): with
+    affine atoms the box relaxes until F_H on the free entries vanishes;
+    with atoms and box free the energy ends below the fixed-box relaxation;
+    entries outside H_dof keep their value."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((4, 4, 4), a=3.7, xB=0.3, sigma=0.05, seed=2)
+
+    def fresh():
+        return O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+
+    s = fresh()
+    pe0, vir0 = s.force()
+    r = s.min_box_run(O.line_search("bt"), np.eye(3, dtype=bool), True, method, m=10, e_tol=1e-10, nsteps=300)
+    assert r["err"] == 4 and r["pe"] < pe0
+    pe, vir = s.force()
+    assert np.max(np.abs(vir[[0, 3, 5]])) < 1e-2 * np.max(np.abs(vir0[[0, 3, 5]]))
+    H = s.box()
+    assert H[1, 0] == H[2, 0] == H[2, 1] == 0.0  # off-diagonal entries were not free
+    # only H[0][0] free: the others stay
+    s = fresh()
+    mask = np.zeros((3, 3), dtype=bool)
+    mask[0, 0] = True
+    s.min_box_run(O.line_search("bt"), mask, True, method, m=10, e_tol=1e-10, nsteps=100)
+    H = s.box()
+    assert H[0, 0] != c.H[0, 0] and H[1, 1] == c.H[1, 1] and H[2, 2] == c.H[2, 2]
+    # atoms and box together go below the fixed-box minimum
+    fixed = fresh().lbfgs_run(m=10, e_tol=1e-10, f_tol=0.0, nsteps=300)
+    s = fresh()
+    r = s.min_box_run(O.line_search("brent"), np.eye(3, dtype=bool), False, method, m=10, e_tol=1e-10, nsteps=300)
+    assert r["pe"] < fixed["pe"]
+
+
 REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
 
 
