@@ -43,6 +43,7 @@
 namespace mappg {
 
 void launch_cells_done(mappg_sys* s, const EamArgs& a, int what);  // eam32.cu
+void lb_update(mappg_sys* s);                                       // lbfgs.cu
 
 struct MdArgs {
     int n;
@@ -770,7 +771,17 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     MAPPG_CUDA(cudaMemcpyAsync(s->sc->eta, eta_h, sizeof(double) * kMaxChain, cudaMemcpyHostToDevice, s->stream));
     k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
     k_mvv_init<<<g, 256, 0, s->stream>>>(a);
-    sys_build(s);
+    // MDNVT::run builds the list at its start.  A list built for this box
+    // whose atoms all stayed within half the skin of their positions at that
+    // build still holds every pair within the cutoff, so the skin test
+    // decides here (the forces are the same; only their summation order can
+    // differ from a fresh build's)
+    if (s->list_box) {
+        lb_update(s);
+        s->built = true;
+    } else {
+        sys_build(s);
+    }
     launch_force(s);
     k_run_begin<<<1, 1, 0, s->stream>>>(a);
     MAPPG_CUDA(cudaGetLastError());

@@ -95,6 +95,7 @@ void sys_set_box(mappg_sys* s, const double* H) {
     for (int i = 0; i < s->ne * s->ne; i++) csk = std::max(csk, s->cut_sk_sq[i]);
     s->band = 2e-5 * (csk + pmax * pmax);
     s->built = false;
+    s->list_box = false;
 }
 
 // a batch: every cell gets its own box, bins (a block of global bin ids) and
@@ -919,6 +920,7 @@ void sys_build(mappg_sys* s) {
         if (!h.overflow) {
             k_set_rebuild<<<1, 1, 0, s->stream>>>(s->sc, 0);
             s->built = true;
+            s->list_box = true;
             return;
         }
         int need = (int)h.maxrow;

@@ -234,6 +234,7 @@ struct mappg_sys {
 
     void* run = nullptr;  // an NVT run in progress (md.cu)
     bool built = false;
+    bool list_box = false;  // a neighbour list exists for the current box (skin test may reuse it)
     bool have_v = false;
     bool f_is_f32 = false;  // the newest forces are in f32 (mixed kernels)
     bool force64 = false;   // mixed system computing FP64 forces (end of a relaxation)

@@ -191,6 +191,14 @@ class atoms:
         self.x_d = _lib.create_temp(self.elem, self.masses, temp, self.kB, seed)
 
     # ---------------------------------------------------------- device state
+    def _f_out(self):
+        # the force array is refilled in place when it has the right shape
+        # (a caller may have given pinned memory)
+        f = self.f
+        if isinstance(f, np.ndarray) and f.shape == self.x.shape and f.dtype == np.float64 and f.flags.c_contiguous:
+            return f
+        return None
+
     def _key(self):
         return (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
 
@@ -323,7 +331,7 @@ class nvt:
         if atoms.x_d is None:
             atoms.x_d = np.zeros_like(atoms.x)
         s.get_v(atoms.x_d)
-        atoms.f = s.get_f()
+        atoms.f = s.get_f(atoms._f_out())
         if th is not None:
             _print_thermo(th, atoms.step, self.ntally, atoms.vol)
             atoms.pe = float(th[-1, 0])
@@ -422,7 +430,7 @@ class _min:
         if self._box():
             atoms.H = s.get_box()
             atoms._sys_key = atoms._key()
-        atoms.f = s.get_f()
+        atoms.f = s.get_f(atoms._f_out())
         atoms.pe = r["pe"]
         atoms.step += r["niter"]
         self.last = r

@@ -39,7 +39,7 @@ def test_box_minimization_follows_oracle(potentials, method, affine, kind):
     assert (r["niter"], r["err"], r["n_energy"], r["n_force"]) == (ro["niter"], ro["err"], ro["n_energy"],
                                                                       ro["n_force"])
     assert abs(r["pe"] - ro["pe"]) <= 1e-11 * abs(ro["pe"])
-    assert dH < 1e-10 and dx < 1e-9
+    assert dH < 1e-9 and dx < 1e-9
 
 
 def test_affine_box_relaxation_to_zero_stress(potentials):
