@@ -319,7 +319,7 @@ def run_c1(args, ff_path, torch):
     import oracle as O
 
     c = synth.md_single((10, 10, 10), T=300.0, seed=0)
-    ff1 = _lib.ForceField.setfl(ff_path)
+    ff1 = _lib.ForceField.setfl(ff_path, ["A"])  # the single-element case: element A of the file
     s = _lib.System(ff1, c.H, c.x, c.elem, c.masses)
     s.set_v(c.v)
     s.nvt_run(300.0, synth.FS, synth.KB, 5, t_relax=float("inf"))  # warm-up (graph, first launches)
@@ -337,8 +337,9 @@ def run_c1(args, ff_path, torch):
     s.nvt_end(100)
     out = {"workload": "4000-atom FCC 10^3, NVE 100 steps, FP64", "gpu": c.natoms * 100 / (ms / 1000.0)}
     e = O.Eam.setfl(ff_path)
+    masses = np.full(e.nelem, c.masses[0])  # one mass per element of the file (all atoms are A)
     for name, threads in (("oracle_1_thread", 0), ("oracle_all_threads", os.cpu_count() or 1)):
-        o = O.System(e, c.H, c.x, c.elem, c.masses, pair_wise=threads == 0)
+        o = O.System(e, c.H, c.x, c.elem, masses, pair_wise=threads == 0)
         o.v = c.v
         o.nvt_run(300.0, synth.FS, synth.KB, 100, t_relax=float("inf"), threads=threads)
         out[name] = c.natoms * 100 / o.loop_seconds
@@ -438,6 +439,7 @@ def run_gpu(args, rank, world, local_rank):
     vh[:] = cell.v
     at = md.atoms(cell.H, xh, cell.elem, elems=("A", "B"), masses=cell.masses, x_d=vh)
     at.x, at.x_d = xh, vh  # keep the pinned buffers
+    at.f = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()  # refilled in place
     at.kB = synth.KB
     at.precision = args.precision
     at.ff = ff
@@ -455,8 +457,9 @@ def run_gpu(args, rank, world, local_rank):
     te = max_over_ranks(te, dist, "cuda")
     e2e = {"value": throughput(N, E, world, 1000.0 * te), "unit": "atom-steps/s", "h2d_bytes_per_step": 48 * N,
            "d2h_bytes_per_step": 72 * N, "steps": E,
-           "call": "mapp4py_gb300.md.nvt(600,1fs).run(atoms,1): x,v in; x,v,f out; neighbour build + "
-                   "opening force call + one step per call, as MDNVT::run"}
+           "call": "mapp4py_gb300.md.nvt(600,1fs).run(atoms,1): x,v in; x,v,f out (pinned); skin test "
+                   "(list rebuilt when an atom moved more than skin/2) + opening force call + one step per "
+                   "call, as MDNVT::run"}
 
     batched = None if args.batch_steps <= 0 else run_batch(args, ff, torch)
     lbfgs = None if args.lbfgs_cap <= 0 else run_lbfgs(args, ff)

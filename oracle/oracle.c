@@ -1218,6 +1218,311 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
 }
 
 /* ------------------------------------------------------------------------ */
+/* NST molecular dynamics: MDNST::run  md_nst.cpp:374-450                    */
+/* ------------------------------------------------------------------------ */
+/* MDMath f, df, ddf  md_nst.cpp:848-873 */
+static double mdm_f(double x) {
+    if (fabs(x) < 0.015625) return 1.0 + x / 2.0 + x * x / 6.0 + x * x * x / 24.0;
+    return (exp(x) - 1.0) / x;
+}
+static double mdm_df(double x) {
+    if (fabs(x) < 0.015625) return 0.5 + x / 3.0 + x * x / 8.0 + x * x * x / 30.0;
+    double e = exp(x);
+    return (e - (e - 1.0) / x) / x;
+}
+static double mdm_ddf(double x) {
+    if (fabs(x) < 0.015625) return 1.0 / 3.0 + x / 4.0 + x * x / 10.0 + x * x * x / 36.0;
+    double e = exp(x);
+    return (e - 2.0 * ((e - (e - 1.0) / x) / x)) / x;
+}
+static double dd_exp(double x, double y, double fx, double fy) {
+    if (fabs(x - y) < sqrt(DBL_EPSILON)) return exp(0.5 * (x + y));
+    return (fx - fy) / (x - y);
+}
+static double dd_f(double x, double y, double fx, double fy) {
+    if (fabs(x - y) < sqrt(DBL_EPSILON * mdm_f(0.5 * (x + y)) / mdm_ddf(0.5 * (x + y)))) return mdm_df(0.5 * (x + y));
+    return (fx - fy) / (x - y);
+}
+static double dd_f3(double x, double y, double z, double f_yz, double f_zx, double f_xy) {
+    double d = mdm_ddf((x + y + z) / 3.0);
+    double lim = sqrt(DBL_EPSILON * mdm_f((x + y + z) / 3.0) / d);
+    if (fabs(x - z) > lim) return (f_xy - f_yz) / (x - z);
+    if (fabs(y - x) > lim) return (f_yz - f_zx) / (y - x);
+    if (fabs(z - y) > lim) return (f_zx - f_xy) / (z - y);
+    return d;
+}
+static double dd_exp3(double x, double y, double z, double f_yz, double f_zx, double f_xy) {
+    const double se = sqrt(DBL_EPSILON);
+    if (fabs(x - z) > se) return (f_xy - f_yz) / (x - z);
+    if (fabs(y - x) > se) return (f_yz - f_zx) / (y - x);
+    if (fabs(z - y) > se) return (f_zx - f_xy) / (z - y);
+    return exp((x + y + z) / 3.0);
+}
+
+/* MDMath::calc (3x3)  md_nst.cpp:887-1000: functions of the lower-
+   triangular A through divided differences: E = exp(-dt2 (A + a)),
+   F0 = dt2 f(-dt2 (A + a)) (off-diagonal sign as there), F1 = dt f(dt A) */
+static void mdm_calc(double a, double dt, double dt2, double A[3][3], double E[3][3], double F0[3][3],
+                     double F1[3][3]) {
+    double x = -dt2 * (A[0][0] + a), y = -dt2 * (A[1][1] + a), z = -dt2 * (A[2][2] + a);
+    double X = dt * A[0][0], Y = dt * A[1][1], Z = dt * A[2][2];
+    memset(E, 0, sizeof(double) * 9);
+    memset(F0, 0, sizeof(double) * 9);
+    memset(F1, 0, sizeof(double) * 9);
+    F0[0][0] = mdm_f(x); F0[1][1] = mdm_f(y); F0[2][2] = mdm_f(z);
+    F1[0][0] = mdm_f(X); F1[1][1] = mdm_f(Y); F1[2][2] = mdm_f(Z);
+    E[0][0] = exp(x); E[1][1] = exp(y); E[2][2] = exp(z);
+    double f_yz = 0, f_zx = 0, f_xy = 0, F_yz = 0, F_zx = 0, F_xy = 0, g_yz = 0, g_zx = 0, g_xy = 0;
+    if (A[2][1] != 0.0) {
+        f_yz = dd_f(y, z, F0[1][1], F0[2][2]);
+        F_yz = dd_f(Y, Z, F1[1][1], F1[2][2]);
+        g_yz = dd_exp(y, z, E[1][1], E[2][2]);
+    }
+    if (A[2][0] != 0.0) {
+        f_zx = dd_f(z, x, F0[2][2], F0[0][0]);
+        F_zx = dd_f(Z, X, F1[2][2], F1[0][0]);
+        g_zx = dd_exp(z, x, E[2][2], E[0][0]);
+    }
+    if (A[1][0] != 0.0) {
+        f_xy = dd_f(x, y, F0[0][0], F0[1][1]);
+        F_xy = dd_f(X, Y, F1[0][0], F1[1][1]);
+        g_xy = dd_exp(x, y, E[0][0], E[1][1]);
+    }
+    F0[0][0] *= dt2; F0[1][1] *= dt2; F0[2][2] *= dt2;
+    F0[2][1] = -A[2][1] * dt2 * dt2 * f_yz;
+    F0[2][0] = -A[2][0] * dt2 * dt2 * f_zx;
+    F0[1][0] = -A[1][0] * dt2 * dt2 * f_xy;
+    F1[0][0] *= dt; F1[1][1] *= dt; F1[2][2] *= dt;
+    F1[2][1] = A[2][1] * dt * dt * F_yz;
+    F1[2][0] = A[2][0] * dt * dt * F_zx;
+    F1[1][0] = A[1][0] * dt * dt * F_xy;
+    E[2][1] = -A[2][1] * dt2 * g_yz;
+    E[2][0] = -A[2][0] * dt2 * g_zx;
+    E[1][0] = -A[1][0] * dt2 * g_xy;
+    if (A[1][0] == 0.0 || A[2][1] == 0.0) return;
+    F0[2][0] += dt2 * dt2 * dt2 * A[2][1] * A[1][0] * dd_f3(x, y, z, f_yz, f_zx, f_xy);
+    F1[2][0] += dt * dt * dt * A[2][1] * A[1][0] * dd_f3(X, Y, Z, F_yz, F_zx, F_xy);
+    E[2][0] += dt2 * dt2 * A[2][1] * A[1][0] * dd_exp3(x, y, z, g_yz, g_zx, g_xy);
+}
+
+/* row vector times lower-triangular matrix, V_mul_MLT order */
+static void v_mlt(const double* v, double M[3][3], double* out) {
+    double o0 = M[0][0] * v[0] + (M[1][0] * v[1] + M[2][0] * v[2]);
+    double o1 = M[1][1] * v[1] + M[2][1] * v[2];
+    double o2 = M[2][2] * v[2];
+    out[0] = o0; out[1] = o1; out[2] = o2;
+}
+/* C = L R (lower triangular), MLT_mul_MLT order */
+static void mlt_mul(double L[3][3], double R[3][3], double C[3][3]) {
+    double T[3][3] = {{0}};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j <= i; j++) {
+            double t = R[i][j] * L[i][i];
+            for (int k = i - 1; k >= j; k--) t = R[k][j] * L[i][k] + t;
+            T[i][j] = t;
+        }
+    memcpy(C, T, sizeof(T));
+}
+
+typedef struct {
+    double T, dt, dt2, kB;
+    int ndof_part, ndof_baro;
+    double S[3][3], S_dev[3][3], s_hyd, tau[3][3], V_H[3][3], V_H_prefac[3][3];
+    int S_dof[3][3];
+    double B_ref[3][3], vol_ref, T_baro, T_part, mvv[6];
+} nst_t;
+
+/* MDNST::update_V_H  md_nst.cpp:315-341 */
+static void nst_update_V_H(nst_t* q, orc_sys* s) {
+    double M0[3][3], M1[3][3], M2[3][3];
+    mlt_mul(q->B_ref, s->H, M0);
+    /* MUT_mul_MSY_mul_MLT: M1 = S_dev M0, M2 = M0^T M1 */
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double t = 0.0;
+            for (int k = j; k < 3; k++) t += q->S_dev[i][k] * M0[k][j];
+            M1[i][j] = t;
+        }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double t = 0.0;
+            for (int k = i; k < 3; k++) t += M0[k][i] * M1[k][j];
+            M2[i][j] = t;
+        }
+    for (int i = 0; i < 3; i++)
+        if (q->S_dof[i][i]) q->V_H[i][i] += (q->kB * q->T_part + s->vol * q->s_hyd) * q->V_H_prefac[i][i] * q->dt2;
+    q->T_baro = 0.0;
+    static const int vo[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j <= i; j++)
+            if (q->S_dof[i][j]) {
+                q->V_H[i][j] += (q->vol_ref * M2[i][j] - s->vol * s->S_pe[i][j] + q->mvv[vo[i][j]]) *
+                                q->V_H_prefac[i][j] * q->dt2;
+                q->T_baro += q->V_H[i][j] * q->V_H[i][j] * q->tau[i][j] * q->tau[i][j];
+            }
+    q->T_baro *= q->ndof_part * q->T / q->ndof_baro;
+}
+
+/* MDNST::update_x_d__x__x_d  md_nst.cpp:70-145 (no per-atom dof mask) */
+static int nst_step_x(nst_t* q, orc_sys* s, double xi) {
+    double M0[3][3], M1[3][3], M2[3][3];
+    double tr = q->V_H[0][0] + q->V_H[1][1] + q->V_H[2][2];
+    mdm_calc(tr / q->ndof_part, q->dt, q->dt2, q->V_H, M0, M1, M2);
+    const int n = s->natms;
+    double dx[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++) {
+        double m_inv = 1.0 / s->masses[s->elem[i]];
+        double* xd = s->v + 3 * i;
+        double* xx = s->x + 3 * i;
+        double* ff = s->f + 3 * i;
+        double a[3], b[3], v0[3], w[3];
+        v_mlt(xd, M0, a);
+        v_mlt(ff, M1, b);
+        for (int k = 0; k < 3; k++) xd[k] = xi * a[k] + m_inv * b[k];
+        v_mlt(xx, q->V_H, v0);
+        for (int k = 0; k < 3; k++) v0[k] += xd[k];
+        v_mlt(v0, M2, w);
+        for (int k = 0; k < 3; k++) {
+            xx[k] += w[k];
+            dx[k] += w[k];
+        }
+    }
+    for (int k = 0; k < 3; k++) dx[k] /= (double)n;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) s->x[3 * i + k] -= dx[k];
+    /* H <- H (I + M2 V_H) */
+    double G[3][3];
+    mlt_mul(M2, q->V_H, G);
+    for (int k = 0; k < 3; k++) G[k][k] += 1.0;
+    mlt_mul(s->H, G, s->H);
+    update_H(s);
+    if (rebuild(s)) return -1;
+    force_calc(s);
+    for (int k = 0; k < 6; k++) q->mvv[k] = 0.0;
+    for (int i = 0; i < n; i++) {
+        double mi = s->masses[s->elem[i]], m_inv = 1.0 / mi;
+        double* xd = s->v + 3 * i;
+        double a[3], b[3];
+        v_mlt(xd, M0, a);
+        v_mlt(s->f + 3 * i, M1, b);
+        for (int k = 0; k < 3; k++) xd[k] = a[k] + m_inv * b[k];
+        dyadic_add(mi, xd, q->mvv);
+    }
+    q->T_part = (q->mvv[0] + (q->mvv[3] + q->mvv[5])) / (q->ndof_part * q->kB);
+    return 0;
+}
+
+/*
+ * md.nst(S,T,dt).run(atoms,nsteps).  S[9] row-major, NaN where the stress
+ * component is free (S_dof false); tau[9] the barostat relaxation times;
+ * t_relax_S and L_S/niters_S the barostat chain.  V_H[9] (box velocity),
+ * eta[L] and eta_S[L_S] are carried between runs (in/out).  thermo (may be
+ * NULL): nsteps+1 rows [pe, T_part, mvv(6), F_H(6), H(9)].
+ */
+int orc_md_nst_run(void* p, const double* S, const double* tau, double T, double dt, double kB, double t_relax,
+                   int L, int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps,
+                   double* V_H, double* eta, double* eta_S, double* thermo) {
+    orc_sys* s = (orc_sys*)p;
+    if (isnan(kB)) return fail("boltzmann constant should be set prior to MD");
+    nst_t q;
+    memset(&q, 0, sizeof(q));
+    q.T = T; q.dt = dt; q.dt2 = dt / 2.0; q.kB = kB;
+    const int n = s->natms;
+    q.ndof_part = 3 * n;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            q.S_dof[i][j] = !isnan(S[3 * i + j]);
+            q.S[i][j] = q.S_dof[i][j] ? S[3 * i + j] : NAN;
+            q.tau[i][j] = tau[3 * i + j];
+            q.V_H[i][j] = j <= i ? V_H[3 * i + j] : 0.0;
+        }
+    nhc_t tp, tb;
+    nhc_init(&tp, dt / 2.0, t_relax, L, niters);
+    nhc_init(&tb, dt / 2.0, t_relax_S, L_S, niters_S);
+    for (int i = 0; i < L; i++) tp.eta_d[i] = eta[i];
+    for (int i = 0; i < L_S; i++) tb.eta_d[i] = eta_S[i];
+    /* MDNVT::pre_init: mvv, T_part */
+    for (int i = 0; i < n; i++) dyadic_add(s->masses[s->elem[i]], s->v + 3 * i, q.mvv);
+    q.T_part = (q.mvv[0] + (q.mvv[3] + q.mvv[5])) / (q.ndof_part * kB);
+    /* MDNST::pre_init  md_nst.cpp:281-311 */
+    q.ndof_baro = 0;
+    q.T_baro = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j <= i; j++) {
+            if (q.S_dof[i][j]) {
+                q.V_H_prefac[i][j] = 1.0 / (q.tau[i][j] * q.tau[i][j] * q.ndof_part * kB * T);
+                q.ndof_baro++;
+                q.T_baro += q.V_H[i][j] * q.V_H[i][j] * q.tau[i][j] * q.tau[i][j];
+            } else {
+                q.S[i][j] = 0.0;
+                q.V_H[i][j] = 0.0;
+            }
+            q.S_dev[i][j] = q.S[i][j];
+        }
+    if (q.ndof_baro == 0) return fail("no stress component is set");
+    q.T_baro *= T * q.ndof_part * kB / q.ndof_baro;
+    q.s_hyd = (q.S[0][0] + q.S[1][1] + q.S[2][2]) / 3.0;
+    for (int i = 0; i < 3; i++) q.S_dev[i][i] = q.S[i][i] - q.s_hyd;
+    /* S_dev keeps only its lower triangle (pre_init fills it with DoLT), and
+       the stress product of update_V_H reads it as a square matrix */
+    /* DynamicMD::init, then run */
+    if (orc_sys_init_dynamic(s)) return -1;
+    force_calc(s);
+    int row = 0;
+#define NST_ROW()                                                              \
+    if (thermo) {                                                              \
+        double* tr = thermo + (size_t)23 * row;                                \
+        tr[0] = s->pe;                                                         \
+        tr[1] = q.T_part;                                                      \
+        for (int k = 0; k < 6; k++) tr[2 + k] = q.mvv[k];                      \
+        tr[8] = s->F_H[0][0]; tr[9] = s->F_H[0][1]; tr[10] = s->F_H[0][2];     \
+        tr[11] = s->F_H[1][1]; tr[12] = s->F_H[1][2]; tr[13] = s->F_H[2][2];   \
+        for (int k = 0; k < 9; k++) tr[14 + k] = s->H[k / 3][k % 3];           \
+    }                                                                          \
+    row++;
+    NST_ROW();
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) q.B_ref[i][j] = j <= i ? s->B[i][j] : 0.0;
+    q.vol_ref = s->vol;
+    double fac, fac_x_d = 1.0;
+    for (int istep = 0; istep < nsteps; istep++) {
+        fac = nhc_step(&tb, q.T_baro / T, q.ndof_baro);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j <= i; j++) q.V_H[i][j] *= fac;
+        q.T_baro *= fac * fac;
+        fac_x_d *= fac = nhc_step(&tp, q.T_part / T, q.ndof_part);
+        fac *= fac;
+        for (int k = 0; k < 6; k++) q.mvv[k] *= fac;
+        q.T_part *= fac;
+        nst_update_V_H(&q, s);
+        if (nst_step_x(&q, s, fac_x_d)) return -1;
+        nst_update_V_H(&q, s);
+        fac_x_d = fac = nhc_step(&tp, q.T_part / T, q.ndof_part);
+        fac *= fac;
+        for (int k = 0; k < 6; k++) q.mvv[k] *= fac;
+        q.T_part *= fac;
+        fac = nhc_step(&tb, q.T_baro / T, q.ndof_baro);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j <= i; j++) q.V_H[i][j] *= fac;
+        q.T_baro *= fac * fac;
+        if (nreset && (istep + 1) % nreset == 0) {
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) q.B_ref[i][j] = j <= i ? s->B[i][j] : 0.0;
+            q.vol_ref = s->vol;
+        }
+        NST_ROW();
+    }
+#undef NST_ROW
+    /* update_x_d_final */
+    for (int i = 0; i < 3 * n; i++) s->v[i] *= fac_x_d;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) V_H[3 * i + j] = q.V_H[i][j];
+    for (int i = 0; i < L; i++) eta[i] = tp.eta_d[i];
+    for (int i = 0; i < L_S; i++) eta_S[i] = tb.eta_d[i];
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* L-BFGS with back-tracking line search: MinLBFGS::__run                    */
 /* min_l-bfgs.h:113-219, MinMDHandler<false,true>  min_cg.h:215-309,          */
 /* LineSearchBackTrack::min  ls.h:711-769 (defaults ls.cpp:456-461)          */

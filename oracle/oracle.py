@@ -71,6 +71,8 @@ def lib():
         L.orc_min_box_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int),
                                       C.c_int, C.POINTER(OrcLs), C.c_int, _D]
         L.orc_sys_get_box.argtypes = [C.c_void_p, _D]
+        L.orc_md_nst_run.argtypes = [C.c_void_p, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                     C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
         _lib = L
     return _lib
@@ -273,6 +275,26 @@ class System:
         self.initialized = True
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def nst_run(self, S, T, dt, kB, nsteps, tau=None, t_relax=None, L=3, niters=1, t_relax_S=None, L_S=3,
+                niters_S=1, nreset=0, V_H=None, eta=None, eta_S=None):
+        """MDNST::run restated; S: 3x3 with NaN for components without a
+        degree of freedom.  Returns thermo rows [pe, T, mvv6, F_H6, H9] and
+        the carried state (V_H, eta, eta_S)."""
+        S = np.ascontiguousarray(S, dtype=np.float64).reshape(3, 3)
+        tau = np.full((3, 3), 1000.0 * dt) if tau is None else np.ascontiguousarray(tau, dtype=np.float64)
+        t_relax = 100.0 * dt if t_relax is None else t_relax
+        t_relax_S = 1000.0 * dt if t_relax_S is None else t_relax_S
+        V_H = np.zeros((3, 3)) if V_H is None else np.array(V_H, dtype=np.float64)
+        eta = np.zeros(L) if eta is None else np.array(eta, dtype=np.float64)
+        eta_S = np.zeros(L_S) if eta_S is None else np.array(eta_S, dtype=np.float64)
+        th = np.zeros((nsteps + 1, 23))
+        r = lib().orc_md_nst_run(self.h, _dp(S), _dp(tau), T, dt, kB, t_relax, L, niters, t_relax_S, L_S, niters_S,
+                                 nreset, nsteps, _dp(V_H), _dp(eta), _dp(eta_S), _dp(th))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return th, V_H, eta, eta_S
 
     def box(self):
         H = np.zeros((3, 3))

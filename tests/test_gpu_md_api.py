@@ -117,10 +117,10 @@ def test_minimizer_export(setfl, tmp_path, kind):
 
 def test_export_failure_stops_the_run(setfl, tmp_path):
     class Failing(md.export_cfg):
-        def _write_step(self, atoms, step, x, x_d, f):
+        def _write_step(self, atoms, step, x, x_d, f, H=None):
             if step == 4:
                 raise RuntimeError("disk full")
-            super()._write_step(atoms, step, x, x_d, f)
+            super()._write_step(atoms, step, x, x_d, f, H)
 
     a = make_atoms(setfl, T=0.0, sigma=0.1)
     m = md.min_lbfgs(m=5, e_tol=0.0)
