@@ -192,6 +192,23 @@ int mappg_nvt_begin(mappg_sys* sys, double T, double dt, double kB, double t_rel
 int mappg_nvt_steps(mappg_sys* sys, long long nsteps);
 int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
 
+/* md.nst(S,T,dt).run(atoms,nsteps): constant-stress MD (MDNST::run,
+ * md_nst.cpp:374-450; update_V_H 315-341; update_x_d__x__x_d 70-145;
+ * MDMath::calc 887-1000; pre_init 281-311).  S: 9 doubles, row-major, the
+ * lower triangle read, NaN where the box entry has no degree of freedom;
+ * tau: 9 relaxation times of the box (the reference's default 1000 dt).
+ * The particle chain (t_relax, L, niters) is md.nvt's; the box chain
+ * (t_relax_S, L_S, niters_S) is thermo_baro (default 1000 dt, 3, 1).
+ * nreset > 0 renews the reference box every nreset steps.  Carried between
+ * runs (in/out): V_H (9, the box velocity), eta (L), eta_S (L_S).  thermo
+ * (NULL to skip): (nsteps+1) rows of 23 doubles: pe, T, mvv (6), F_H (6),
+ * H (9).  The box moves every step and the neighbour list is rebuilt for it
+ * each step; FP64 systems only.  Positions, velocities and the box are read
+ * back with mappg_sys_get_x/get_v/get_box. */
+int mappg_nst_run(mappg_sys* sys, const double* S, const double* tau, double T, double dt, double kB, double t_relax,
+                  int L, int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps, double* V_H,
+                  double* eta, double* eta_S, double* thermo);
+
 /* Positions and velocities ([natoms][3] in the caller's order; either may
  * be NULL) of a begun run after the steps enqueued so far, as MDNVT::run
  * holds them when it writes its export (md_nvt.cpp:390,436,470): after the

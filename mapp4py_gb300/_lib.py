@@ -65,6 +65,8 @@ SIGNATURES = {
     "mappg_min_box_run": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_double, _I, C.c_int, _VP, C.c_int,
                                     _D]),
     "mappg_sys_get_box": (C.c_int, [_VP, _D]),
+    "mappg_nst_run": (C.c_int, [_VP, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D]),
     "mappg_cg_run_ls": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),
     "mappg_cfg_read": (C.c_int, [C.c_char_p, C.POINTER(_VP)]),
     "mappg_cfg_info": (C.c_int, [_VP, _I, _I, _I, _D]),
@@ -444,6 +446,25 @@ class System:
                                                C.cast(C.pointer(ls), _VP), int(nsteps), dptr(st)))
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def nst_run(self, S, T, dt, kB, nsteps, tau=None, t_relax=None, L=3, niters=1, t_relax_S=None, L_S=3,
+                niters_S=1, nreset=0, V_H=None, eta=None, eta_S=None, thermo=True):
+        """Constant-stress MD (mappg_nst_run).  S: 3x3, NaN where the box
+        entry has no degree of freedom.  Returns (thermo rows or None, V_H,
+        eta, eta_S)."""
+        S = f64(S, (3, 3))
+        tau = np.full((3, 3), 1000.0 * dt) if tau is None else f64(tau, (3, 3))
+        t_relax = 100.0 * dt if t_relax is None else t_relax
+        t_relax_S = 1000.0 * dt if t_relax_S is None else t_relax_S
+        V_H = np.zeros((3, 3)) if V_H is None else f64(V_H, (3, 3)).copy()
+        eta = np.zeros(L) if eta is None else f64(eta).copy()
+        eta_S = np.zeros(L_S) if eta_S is None else f64(eta_S).copy()
+        th = np.zeros((nsteps + 1, 23)) if thermo else None
+        check(load().mappg_nst_run(self.h, dptr(S), dptr(tau), float(T), float(dt), float(kB), float(t_relax),
+                                   int(L), int(niters), float(t_relax_S), int(L_S), int(niters_S), int(nreset),
+                                   int(nsteps), dptr(V_H), dptr(eta), dptr(eta_S),
+                                   dptr(th) if th is not None else None))
+        return th, V_H, eta, eta_S
 
     def get_box(self):
         H = np.zeros((3, 3))

@@ -35,6 +35,9 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
 void nvt_steps(mappg_sys* s, long long nsteps);
 void nvt_end(mappg_sys* s, double* eta, double* thermo);
 void nvt_snapshot(mappg_sys* s, double* x, double* v);
+void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double dt, double kB, double t_relax, int L,
+             int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps, double* V_H, double* eta,
+             double* eta_S, double* thermo);
 void nvt_free(mappg_sys* s);
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats);
@@ -628,6 +631,16 @@ int mappg_nvt_end(mappg_sys* s, double* eta, double* thermo) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         nvt_end(s, eta, thermo);
+    });
+}
+
+int mappg_nst_run(mappg_sys* s, const double* S, const double* tau, double T, double dt, double kB, double t_relax,
+                  int L, int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps, double* V_H,
+                  double* eta, double* eta_S, double* thermo) {
+    return guard([&] {
+        if (!s || !S || !tau || !V_H || !eta || !eta_S) throw Error{MAPPG_ERR_ARG, "null argument"};
+        nst_run(s, S, tau, T, dt, kB, t_relax, L, niters, t_relax_S, L_S, niters_S, nreset, nsteps, V_H, eta, eta_S,
+                thermo);
     });
 }
 

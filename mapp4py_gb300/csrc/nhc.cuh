@@ -8,12 +8,12 @@
 
 namespace mappg {
 
-__device__ __forceinline__ double nhc_f(double x) {
+__host__ __device__ __forceinline__ double nhc_f(double x) {
     if (fabs(x) < 0.015625) return 1.0 + x / 2.0 + x * x / 6.0 + x * x * x / 24.0;
     return (exp(x) - 1.0) / x;
 }
 
-__device__ inline double nhc_step(const NhcParams& P, double* eta, double T_r) {
+__host__ __device__ inline double nhc_step(const NhcParams& P, double* eta, double T_r) {
     double rescale = 1.0, prev_fac, tmp;
     const int L = P.L;
     if (L == 1) {

@@ -6,6 +6,8 @@ Names, arguments and defaults follow the reference's Python types:
                        create_temp (atoms_md.cpp:490-531), kB, skin, H, x, x_d
   md.nvt(T, dt)        MDNVT (md_nvt.cpp:14-26,493-881): t_relax=100*dt, L=3,
                        niters=1, ntally=10000, run(atoms, nsteps)
+  md.nst(S, T, dt)     MDNST (md_nst.cpp:10-38,374-450): as md.nvt plus S, tau,
+                       t_relax_s, nreset; moves the box (FP64 systems)
   md.min_lbfgs(...)    MinLBFGS (min_l-bfgs.cpp:69-127): m=2, e_tol=sqrt(eps),
                        affine=False, max_dx=1.0, ls=ls_bt(); run(atoms, max_nsteps)
   ls_bt()              LineSearchBackTrack (ls.cpp:456-461): c=0.4, rho=0.5,
@@ -340,6 +342,74 @@ class nvt:
             atoms.pe, F_H = s.force()
         atoms.S_pe = _voigt_to_matrix(-np.asarray(F_H) / atoms.vol)
         atoms.step += nsteps
+
+
+def _stress_arg(S):
+    """The reference's symmetric S (rows of lengths 1, 2, 3, or a full 3x3;
+    None or NaN where the box entry has no degree of freedom) as 3x3."""
+    rows = [list(r) for r in S]
+    if len(rows) != 3 or any(len(r) not in (i + 1, 3) for i, r in enumerate(rows)):
+        raise TypeError("S should be [[Sxx],[Syx,Syy],[Szx,Szy,Szz]] or a 3x3 array")
+    out = np.full((3, 3), np.nan)
+    for i in range(3):
+        for j in range(i + 1):
+            v = rows[i][j]
+            out[i, j] = out[j, i] = np.nan if v is None else float(v)
+    return out
+
+
+class nst(nvt):
+    """Constant-stress (NST) MD: MDNST (md_nst.cpp) with the particle chain
+    of md.nvt and a box chain (t_relax_s, default 1000 dt); S is the applied
+    stress, NaN (or None) where the box entry stays fixed; tau the box
+    relaxation times (default 1000 dt); nreset renews the reference box every
+    nreset steps (0: never).  FP64 systems only."""
+
+    def __init__(self, S, T, dt):
+        super().__init__(T, dt)
+        self.S = _stress_arg(S)
+        if np.all(np.isnan(self.S)):
+            raise TypeError("at least one component of S must be set")
+        self.tau = np.full((3, 3), 1000.0 * self.dt)
+        self.t_relax_s = 1000.0 * self.dt
+        self.nreset = 0
+        self._V_H = np.zeros((3, 3))
+        self._eta_s = np.zeros(3)
+
+    def run(self, atoms, nsteps):
+        if nsteps < 0:
+            raise TypeError("nsteps should be greater than or equal to 0")
+        if atoms.ff is None:
+            raise TypeError("cannot start md without governing equations (force field)")
+        if math.isnan(atoms.kB):
+            raise TypeError("boltzmann constant should be set prior to MD")
+        if atoms.precision != "fp64":
+            raise TypeError("md.nst runs in FP64 (atoms.precision = 'fp64')")
+        if self.export is not None:
+            raise TypeError("exports during md.nst runs are not available; export before and after the run")
+        if self._eta.shape[0] != self.L:
+            self._eta = np.zeros(self.L)
+        s = atoms._system()
+        s.set_x(atoms.x)
+        s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
+        th, self._V_H, self._eta, self._eta_s = s.nst_run(
+            self.S, self.T, self.dt, atoms.kB, nsteps, tau=self.tau, t_relax=self.t_relax, L=self.L,
+            niters=self.niters, t_relax_S=self.t_relax_s, nreset=self.nreset, V_H=self._V_H, eta=self._eta,
+            eta_S=self._eta_s, thermo=True)
+        s.get_x(atoms.x)
+        if atoms.x_d is None:
+            atoms.x_d = np.zeros_like(atoms.x)
+        s.get_v(atoms.x_d)
+        atoms.f = s.get_f(atoms._f_out())
+        atoms.H = s.get_box()
+        atoms._sys_key = atoms._key()
+        if self.ntally:
+            vol = float(atoms.H[0, 0] * atoms.H[1, 1] * atoms.H[2, 2])
+            _print_thermo(th[:, :14], atoms.step, self.ntally, vol)
+        atoms.pe = float(th[-1, 0])
+        atoms.S_pe = _voigt_to_matrix(-th[-1, 8:14] / atoms.vol)
+        atoms.step += nsteps
+        self.last_thermo = th
 
 
 def _voigt_to_matrix(v):

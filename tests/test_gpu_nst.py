@@ -1,0 +1,64 @@
+"""Constant-stress MD (md.nst; MDNST::run, md_nst.cpp) on the device against
+the oracle's restatement: energies, temperatures, boxes, positions and
+velocities over the first steps, for a diagonal and a sheared stress
+target; the md-level run updates atoms.H and carries the box velocity."""
+import numpy as np
+import pytest
+
+import oracle as O
+from mapp4py_gb300 import _lib, md, synth
+
+pytestmark = pytest.mark.gpu
+
+nan = np.nan
+
+
+def cell():
+    return synth.alloy((5, 5, 5), a=2.9, xB=0.3, sigma=0.02, T=300.0, seed=4)
+
+
+@pytest.mark.parametrize("shear", [False, True])
+def test_nst_follows_oracle(potentials, shear):
+    path, _ = potentials[("A", "B")]
+    c = cell()
+    S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, 0.0]])
+    if shear:
+        S[1, 0] = S[0, 1] = 0.0
+        S[2, 1] = S[1, 2] = 0.0
+    tau = np.full((3, 3), 50 * synth.FS)
+    o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    o.v = c.v
+    tho, VHo, eo, eSo = o.nst_run(S, 300.0, synth.FS, synth.KB, 30, tau=tau)
+    s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5, precision=_lib.FP64)
+    s.set_v(c.v)
+    th, VH, e, eS = s.nst_run(S, 300.0, synth.FS, synth.KB, 30, tau=tau)
+    # pe and T per step, boxes
+    assert np.max(np.abs(th[:, 0] - tho[:, 0])) <= 1e-9 * np.max(np.abs(tho[:, 0]))
+    assert np.max(np.abs(th[:, 1] - tho[:, 1])) <= 1e-8 * np.max(tho[:, 1])
+    assert np.max(np.abs(th[:, 14:] - tho[:, 14:])) < 1e-10
+    assert np.max(np.abs(VH - VHo)) <= 1e-9 * max(1e-30, np.max(np.abs(VHo)))
+    H = s.get_box()
+    d = s.get_x() - o.x
+    d -= np.round(d @ np.linalg.inv(H)) @ H
+    assert np.max(np.abs(d)) < 1e-9
+    assert np.max(np.abs(s.get_v() - o.v)) < 1e-10
+    assert np.max(np.abs(e - eo)) < 1e-9 and np.max(np.abs(eS - eSo)) < 1e-9
+
+
+def test_md_nst_updates_the_box(potentials):
+    path, _ = potentials[("A", "B")]
+    c = cell()
+    a = md.atoms(c.H, c.x, c.elem, elems=("A", "B"), masses=c.masses, x_d=c.v)
+    a.ff_eam_setfl(path)
+    a.kB = synth.KB
+    integ = md.nst([[0.0], [None, 0.0], [None, None, 0.0]], 300.0, synth.FS)
+    integ.tau = np.full((3, 3), 50 * synth.FS)
+    integ.ntally = 0
+    integ.run(a, 100)
+    assert np.max(np.abs(np.diag(a.H) - np.diag(c.H))) > 0.1 and a.step == 100
+    vh = integ._V_H.copy()
+    integ.run(a, 10)  # the box velocity carries over
+    assert np.any(vh != 0.0)
+    a.precision = "mixed"
+    with pytest.raises(TypeError, match="FP64"):
+        integ.run(a, 1)

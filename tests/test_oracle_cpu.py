@@ -213,6 +213,28 @@ def test_box_degrees_of_freedom(potentials, method):
     assert r["pe"] < fixed["pe"]
 
 
+def test_nst_relaxes_toward_the_applied_stress(potentials):
+    """MDNST restated (md_nst.cpp): a cell far from zero stress changes its
+    box until the pressure drops; the box entries without a degree of
+    freedom stay; the box velocity and both chains are carried out."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((5, 5, 5), a=2.9, xB=0.3, sigma=0.02, T=300.0, seed=4)
+    o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+    o.v = c.v
+    nan = np.nan
+    S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, 0.0]])
+    th, VH, eta, eta_S = o.nst_run(S, 300.0, synth.FS, synth.KB, 200, tau=np.full((3, 3), 50 * synth.FS))
+    H0, H = th[0, 14:].reshape(3, 3), th[-1, 14:].reshape(3, 3)
+    assert np.max(np.abs(np.diag(H) - np.diag(H0))) > 0.1
+    assert H[1, 0] == H[2, 0] == H[2, 1] == 0.0  # shear entries have no degree of freedom
+    p0 = -(th[0, 8] + th[0, 11] + th[0, 13])
+    p1 = -(th[-1, 8] + th[-1, 11] + th[-1, 13])
+    assert abs(p1) < abs(p0)
+    assert np.all(np.isfinite(th)) and np.any(VH != 0.0) and np.any(eta_S != 0.0)
+    with pytest.raises(RuntimeError, match="stress"):
+        o.nst_run(np.full((3, 3), nan), 300.0, synth.FS, synth.KB, 1)
+
+
 REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
 
 
