@@ -70,8 +70,9 @@ __device__ void nst_reduce(const NstAtoms& a, double (&v)[K]) {
     }
 }
 
-// first half of update_x_d__x__x_d (md_nst.cpp:70-118): v = xi v M0 +
-// f M1 / m, w = (x V_H + v) M2, x += w; the sum of w for the mean shift
+// first half of update_x_d__x__x_d (md_nst.cpp:70-118): v = v M0 (xi on
+// the z component) + f M1 / m, w = (x V_H + v) M2, x += w; the sum of w for
+// the mean shift
 __global__ void __launch_bounds__(256) k_nst_x(NstAtoms a) {
     double d[3] = {0.0, 0.0, 0.0};
     const int n = a.n;
@@ -81,9 +82,12 @@ __global__ void __launch_bounds__(256) k_nst_x(NstAtoms a) {
         double f[3] = {a.f[i], a.f[n + i], a.f[2 * n + i]};
         double x[3] = {a.x[i], a.x[n + i], a.x[2 * n + i]};
         double p[3], q[3], v0[3], w[3];
+        // the reference scales the velocity by xi in SCL_V_mul_MLT's in-place
+        // form, which applies xi to the last component only
         vmlt(v, a.M0.m, p);
+        p[2] = __dmul_rn(__dmul_rn(a.xi, v[2]), a.M0.m[2][2]);
         vmlt(f, a.M1.m, q);
-        for (int k = 0; k < 3; k++) v[k] = __dadd_rn(__dmul_rn(a.xi, p[k]), __dmul_rn(m_inv, q[k]));
+        for (int k = 0; k < 3; k++) v[k] = __dadd_rn(p[k], __dmul_rn(m_inv, q[k]));
         vmlt(x, a.VH.m, v0);
         for (int k = 0; k < 3; k++) v0[k] = __dadd_rn(v0[k], v[k]);
         vmlt(v0, a.M2.m, w);

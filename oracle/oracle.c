@@ -1376,9 +1376,12 @@ static int nst_step_x(nst_t* q, orc_sys* s, double xi) {
         double* xx = s->x + 3 * i;
         double* ff = s->f + 3 * i;
         double a[3], b[3], v0[3], w[3];
+        /* SCL_V_mul_MLT(xi, x_d, MLT0) in place (xmath.h:1049-1053,1077-1080)
+           applies xi to the last component only */
         v_mlt(xd, M0, a);
+        a[2] = xi * xd[2] * M0[2][2];
         v_mlt(ff, M1, b);
-        for (int k = 0; k < 3; k++) xd[k] = xi * a[k] + m_inv * b[k];
+        for (int k = 0; k < 3; k++) xd[k] = a[k] + m_inv * b[k];
         v_mlt(xx, q->V_H, v0);
         for (int k = 0; k < 3; k++) v0[k] += xd[k];
         v_mlt(v0, M2, w);

@@ -223,13 +223,14 @@ def test_nst_relaxes_toward_the_applied_stress(potentials):
     o.v = c.v
     nan = np.nan
     S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, 0.0]])
-    th, VH, eta, eta_S = o.nst_run(S, 300.0, synth.FS, synth.KB, 200, tau=np.full((3, 3), 50 * synth.FS))
+    th, VH, eta, eta_S = o.nst_run(S, 300.0, synth.FS, synth.KB, 1000, tau=np.full((3, 3), 50 * synth.FS))
     H0, H = th[0, 14:].reshape(3, 3), th[-1, 14:].reshape(3, 3)
-    assert np.max(np.abs(np.diag(H) - np.diag(H0))) > 0.1
+    assert np.max(np.abs(np.diag(H) - np.diag(H0))) > 0.1  # the cell transforms (FCC -> BCT for this alloy)
     assert H[1, 0] == H[2, 0] == H[2, 1] == 0.0  # shear entries have no degree of freedom
-    p0 = -(th[0, 8] + th[0, 11] + th[0, 13])
-    p1 = -(th[-1, 8] + th[-1, 11] + th[-1, 13])
-    assert abs(p1) < abs(p0)
+    # the virial pressure oscillates about the target and settles near it
+    vol = np.prod(th[:, [14, 18, 22]], axis=1)
+    p = -(th[:, 8] + th[:, 11] + th[:, 13]) / 3.0 / vol * 160.2  # GPa
+    assert abs(np.mean(p[500:])) < 1.5 and np.max(np.abs(p[:100])) > 5.0
     assert np.all(np.isfinite(th)) and np.any(VH != 0.0) and np.any(eta_S != 0.0)
     with pytest.raises(RuntimeError, match="stress"):
         o.nst_run(np.full((3, 3), nan), 300.0, synth.FS, synth.KB, 1)
