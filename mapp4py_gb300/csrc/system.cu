@@ -393,6 +393,7 @@ struct BuildArgs {
     Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
     double cut_sk_sq[kMaxElem * kMaxElem];
+    double prune2;         // above this squared gap a stencil bin holds no neighbour
     const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
     const int* cell_of;
 };
@@ -452,6 +453,8 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         // of all bins form one sequence (bin step, then bin order) that the
         // warp walks 32 at a time, so lanes stay busy across bin borders
         int lo = 0, ncand = 0, img = 0;
+        const bool ortho = BATCH ? cg->ortho != 0 : a.fr.ortho != 0;
+        const double si[3] = {a.s[i], a.s[n + i], a.s[2 * n + i]};
         if (lane < 27) {
             const int c = lane;
             int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
@@ -464,6 +467,22 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
             lo = a.bin_start[b];
             ncand = a.bin_start[b + 1] - lo;
             img = (n0 + 1) | ((n1 + 1) << 2) | ((n2 + 1) << 4);
+            if (ortho) {
+                // the gap between atom i and the stencil bin: a bin farther
+                // than cutoff + skin holds no neighbour, so it is skipped
+                // (the kept entries and their order are unchanged)
+                const int dd[3] = {d0, d1, d2}, nbv[3] = {nbx, nby, nbz};
+                const double L[3] = {h6[0], h6[3], h6[5]};
+                double g2 = 0.0;
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    if (dd[ax] == 0) continue;
+                    const double f = si[ax] * nbv[ax] - bi[ax];
+                    const double gap = (dd[ax] > 0 ? 1.0 - f : f) * (L[ax] / nbv[ax]);
+                    g2 += gap * gap;
+                }
+                if (g2 > a.prune2) ncand = 0;
+            }
         }
         int incl = ncand;
 #pragma unroll
@@ -670,11 +689,14 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.nnbr = s->nnbr;
     a.x0 = s->x0;
     a.g = g;
+    double maxc = 0.0;
     for (int p = 0; p < s->ne * s->ne; p++) {
         a.cut_sk_sq[p] = s->cut_sk_sq[p];
         a.lo2[p] = (float)(s->cut_sk_sq[p] - s->band);
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
+        maxc = std::max(maxc, s->cut_sk_sq[p]);
     }
+    a.prune2 = maxc * (1.0 + 1e-8) + 1e-12;
     a.fr = s->frame;
     a.cells = s->cells_dev;
     a.cell_of = s->cell_of;
