@@ -300,6 +300,17 @@ int mappg_sys_get_box(mappg_sys* sys, double* H);
  * hook NULL or nevery <= 0 removes it. */
 int mappg_sys_set_hook(mappg_sys* sys, int (*hook)(void* user, long long iteration), void* user, int nevery);
 
+/* The exchange-energy hooks of ForceFieldMD that grand-canonical Monte Carlo
+ * (GCMC) calls (init_xchng / fin_xchng / pre_xchng_energy / xchng_energy /
+ * post_xchng_energy, ff_md.h:19-21,49-50).  GCMC is outside this engine:
+ * each returns MAPPG_ERR_UNSUPP with a message, whatever its arguments
+ * (gcmc stands for the caller's GCMC object and is not read). */
+int mappg_sys_init_xchng(mappg_sys* sys);
+int mappg_sys_fin_xchng(mappg_sys* sys);
+int mappg_sys_pre_xchng_energy(mappg_sys* sys, void* gcmc);
+int mappg_sys_xchng_energy(mappg_sys* sys, void* gcmc, double* de);
+int mappg_sys_post_xchng_energy(mappg_sys* sys, void* gcmc);
+
 /* --------------------------------------------------------- CFG snapshots */
 
 typedef struct mappg_cfg mappg_cfg;

@@ -65,6 +65,11 @@ SIGNATURES = {
     "mappg_min_box_run": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_double, _I, C.c_int, _VP, C.c_int,
                                     _D]),
     "mappg_sys_get_box": (C.c_int, [_VP, _D]),
+    "mappg_sys_init_xchng": (C.c_int, [_VP]),
+    "mappg_sys_fin_xchng": (C.c_int, [_VP]),
+    "mappg_sys_pre_xchng_energy": (C.c_int, [_VP, _VP]),
+    "mappg_sys_xchng_energy": (C.c_int, [_VP, _VP, _D]),
+    "mappg_sys_post_xchng_energy": (C.c_int, [_VP, _VP]),
     "mappg_nst_run": (C.c_int, [_VP, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                 C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D]),
     "mappg_cg_run_ls": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, _VP, C.c_int, _D]),

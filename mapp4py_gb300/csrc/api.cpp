@@ -644,6 +644,18 @@ int mappg_nst_run(mappg_sys* s, const double* S, const double* tau, double T, do
     });
 }
 
+// GCMC exchange energies: outside this engine (ff_md.h:19-21,49-50)
+static int xchng_unsupported() {
+    return guard([] {
+        throw Error{MAPPG_ERR_UNSUPP, "GCMC exchange energies (ForceFieldMD::xchng_energy) are outside this engine"};
+    });
+}
+int mappg_sys_init_xchng(mappg_sys*) { return xchng_unsupported(); }
+int mappg_sys_fin_xchng(mappg_sys*) { return xchng_unsupported(); }
+int mappg_sys_pre_xchng_energy(mappg_sys*, void*) { return xchng_unsupported(); }
+int mappg_sys_xchng_energy(mappg_sys*, void*, double*) { return xchng_unsupported(); }
+int mappg_sys_post_xchng_energy(mappg_sys*, void*) { return xchng_unsupported(); }
+
 int mappg_nvt_snapshot(mappg_sys* s, double* x, double* x_d) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};

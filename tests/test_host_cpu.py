@@ -96,6 +96,16 @@ def test_library_exports_every_declared_symbol(built):
         assert hasattr(L, name)
 
 
+def test_gcmc_hooks_report_unsupported(built):
+    L = built
+    for name, args in (("mappg_sys_init_xchng", (None,)), ("mappg_sys_fin_xchng", (None,)),
+                       ("mappg_sys_pre_xchng_energy", (None, None)),
+                       ("mappg_sys_xchng_energy", (None, None, None)),
+                       ("mappg_sys_post_xchng_energy", (None, None))):
+        assert getattr(L, name)(*args) == -8  # MAPPG_ERR_UNSUPP
+        assert b"GCMC" in L.mappg_last_error()
+
+
 def test_h_dof_forms():
     from mapp4py_gb300 import md
 
