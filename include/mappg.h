@@ -168,6 +168,24 @@ int mappg_sys_stats(mappg_sys* sys, long long* out6);
 int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
                       double* v);
 
+/* create_temp with atoms.x_dof (AtomsMD::create_T, atoms_md.cpp:138-149):
+ * dof is [natoms][3], nonzero where the component is a degree of freedom;
+ * only those components draw a sample (in order), the others keep the value
+ * v holds.  dof NULL: as mappg_create_temp. */
+int mappg_create_temp_dof(int natoms, const unsigned char* elem, const double* masses, const unsigned char* dof,
+                          double T, double kB, int seed, double* v);
+
+/* atoms.x_dof: per atom and component (caller order, [natoms][3]), nonzero
+ * where it is a degree of freedom; NULL (or all nonzero) clears it.  Forces
+ * on frozen components are zero in every force call (ForceFieldMD::
+ * force_calc, ff_md.cpp:138-144), so the minimizers leave them in place.
+ * FP64 NVT runs take the reference's _w_dof steps (md_nvt.cpp:144-215): a
+ * frozen component is neither kicked nor thermostatted and keeps drifting
+ * with its velocity, leaves the degrees of freedom and the kinetic tensor,
+ * and the mean displacement is not removed along a component in which any
+ * atom is frozen.  Mixed-precision MD, md.nst and batches refuse it. */
+int mappg_sys_set_dof(mappg_sys* sys, const unsigned char* dof);
+
 /* ---------------------------------------------------------------- drivers */
 
 /* md.nvt(T,dt).run(atoms,nsteps): velocity Verlet with the Nose-Hoover

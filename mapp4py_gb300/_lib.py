@@ -65,6 +65,8 @@ SIGNATURES = {
     "mappg_min_box_run": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double, C.c_double, _I, C.c_int, _VP, C.c_int,
                                     _D]),
     "mappg_sys_get_box": (C.c_int, [_VP, _D]),
+    "mappg_sys_set_dof": (C.c_int, [_VP, _U8]),
+    "mappg_create_temp_dof": (C.c_int, [C.c_int, _U8, _D, _U8, C.c_double, C.c_double, C.c_int, _D]),
     "mappg_sys_init_xchng": (C.c_int, [_VP]),
     "mappg_sys_fin_xchng": (C.c_int, [_VP]),
     "mappg_sys_pre_xchng_energy": (C.c_int, [_VP, _VP]),
@@ -471,6 +473,14 @@ class System:
                                    dptr(th) if th is not None else None))
         return th, V_H, eta, eta_S
 
+    def set_dof(self, dof):
+        """atoms.x_dof: (n, 3) bool, True where the component is free; None clears."""
+        if dof is None:
+            check(load().mappg_sys_set_dof(self.h, None))
+            return
+        d = np.ascontiguousarray(np.asarray(dof, dtype=bool).reshape(self.n, 3), dtype=np.uint8)
+        check(load().mappg_sys_set_dof(self.h, d.ctypes.data_as(_U8)))
+
     def get_box(self):
         H = np.zeros((3, 3))
         check(load().mappg_sys_get_box(self.h, dptr(H)))
@@ -646,6 +656,16 @@ def lbfgs_run_precond(system, net, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.
                                                    dptr(st)))
     return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]), "n_energy": int(st[4]),
             "n_force": int(st[5]), "fallbacks": int(st[6])}
+
+
+def create_temp_dof(elem, masses, dof, T, kB, seed, v):
+    """create_temp for the free components of dof only; v holds the others."""
+    elem = np.ascontiguousarray(elem, dtype=np.uint8)
+    out = np.array(v, dtype=np.float64).reshape(-1, 3)
+    d = np.ascontiguousarray(np.asarray(dof, dtype=bool).reshape(-1, 3), dtype=np.uint8)
+    check(load().mappg_create_temp_dof(elem.shape[0], elem.ctypes.data_as(_U8), dptr(f64(masses)),
+                                       d.ctypes.data_as(_U8), float(T), float(kB), int(seed), dptr(out)))
+    return out
 
 
 def create_temp(elem, masses, T, kB, seed):

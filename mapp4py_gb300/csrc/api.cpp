@@ -562,6 +562,11 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
 
 int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
                       double* v) {
+    return mappg_create_temp_dof(natoms, elem, masses, nullptr, T, kB, seed, v);
+}
+
+int mappg_create_temp_dof(int natoms, const unsigned char* elem, const double* masses, const unsigned char* dof,
+                          double T, double kB, int seed, double* v) {
     return guard([&] {
         if (!elem || !masses || !v || natoms < 0) throw Error{MAPPG_ERR_ARG, "null argument"};
         if (seed == 0) throw Error{MAPPG_ERR_ARG, "seed 0 never yields a Gaussian sample"};
@@ -578,6 +583,7 @@ int mappg_create_temp(int natoms, const unsigned char* elem, const double* masse
         for (int i = 0; i < natoms; i++) {
             double fac = sqrt(kB * T / masses[elem[i]]);
             for (int j = 0; j < 3; j++) {
+                if (dof && !dof[3 * (size_t)i + j]) continue;  // kept (atoms_md.cpp:138-149)
                 double g;
                 if (gchk) {
                     gchk = false;
@@ -655,6 +661,37 @@ int mappg_sys_fin_xchng(mappg_sys*) { return xchng_unsupported(); }
 int mappg_sys_pre_xchng_energy(mappg_sys*, void*) { return xchng_unsupported(); }
 int mappg_sys_xchng_energy(mappg_sys*, void*, double*) { return xchng_unsupported(); }
 int mappg_sys_post_xchng_energy(mappg_sys*, void*) { return xchng_unsupported(); }
+
+int mappg_sys_set_dof(mappg_sys* s, const unsigned char* dof) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "frozen components (x_dof) are per single cell"};
+        if (s->run) throw Error{MAPPG_ERR_ARG, "an NVT run is in progress"};
+        if (s->dof) cudaFree(s->dof);
+        s->dof = nullptr;
+        for (int c = 0; c < 3; c++) s->dof_frozen[c] = 0;
+        if (!dof) return;
+        const int n = s->n;
+        std::vector<uint8_t> bits(n);
+        bool any = false;
+        for (int i = 0; i < n; i++) {
+            const int u = s->host_id[i];  // caller index of the atom at bin-order position i
+            uint8_t b = 0;
+            for (int c = 0; c < 3; c++) {
+                if (dof[3 * (size_t)u + c])
+                    b |= (uint8_t)(1u << c);
+                else
+                    s->dof_frozen[c]++;
+            }
+            bits[i] = b;
+            any |= b != 7;
+        }
+        if (!any) return;  // every component free: no mask
+        MAPPG_CUDA(cudaMalloc(&s->dof, n));
+        MAPPG_CUDA(cudaMemcpyAsync(s->dof, bits.data(), n, cudaMemcpyHostToDevice, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    });
+}
 
 int mappg_nvt_snapshot(mappg_sys* s, double* x, double* x_d) {
     return guard([&] {

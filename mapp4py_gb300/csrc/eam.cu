@@ -563,10 +563,32 @@ void launch_density_only(mappg_sys* s) {
     MAPPG_CUDA(cudaGetLastError());
 }
 
+// ForceFieldMD::force_calc (ff_md.cpp:138-144): components without a
+// degree of freedom carry no force
+template <class T>
+__global__ void k_dof_mask(int n, const uint8_t* __restrict__ dof, T* __restrict__ f) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned d = dof[i];
+        if (d == 7u) continue;
+        for (int c = 0; c < 3; c++)
+            if (!((d >> c) & 1u)) f[(size_t)c * n + i] = T(0);
+    }
+}
+
+void launch_dof_mask(mappg_sys* s, bool f32) {
+    if (!s->dof) return;
+    if (f32)
+        k_dof_mask<float><<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->dof, s->f32);
+    else
+        k_dof_mask<double><<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->dof, s->f);
+    MAPPG_CUDA(cudaGetLastError());
+}
+
 void launch_force_only(mappg_sys* s) {
     EamArgs a = eam_args(s);
     if (s->precision == MAPPG_MIXED && !s->force64) {
         launch_force32(s, a);
+        launch_dof_mask(s, true);
         s->f_is_f32 = true;
         return;
     }
@@ -578,6 +600,7 @@ void launch_force_only(mappg_sys* s) {
         MAPPG_TPA64(k_force64)
         MAPPG_CUDA(cudaGetLastError());
     }
+    launch_dof_mask(s, false);
     s->f_is_f32 = false;
 }
 

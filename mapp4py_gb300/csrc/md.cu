@@ -57,6 +57,8 @@ struct MdArgs {
     const int* binc;
     float4* p32;
     const float4* p0;
+    const uint8_t* dof;    // x_dof bits (null: every component free)
+    int com_on[3];         // the mean displacement is removed along c (no frozen atom along c)
     double masses[kMaxElem];
     double dtm[kMaxElem];  // dt2/m
     float dtm32[kMaxElem];
@@ -103,6 +105,12 @@ __global__ void k_mvv_init(MdArgs a) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double m = a.masses[a.elem[i]];
         double v0 = a.v[i], v1 = a.v[n + i], v2 = a.v[2 * n + i];
+        if (a.dof) {
+            const unsigned b = a.dof[i];
+            if (!(b & 1u)) v0 = 0.0;
+            if (!(b & 2u)) v1 = 0.0;
+            if (!(b & 4u)) v2 = 0.0;
+        }
         d[0] += __dmul_rn(__dmul_rn(v0, v0), m);
         d[1] += __dmul_rn(__dmul_rn(v0, v1), m);
         d[2] += __dmul_rn(__dmul_rn(v0, v2), m);
@@ -138,10 +146,13 @@ __global__ void __launch_bounds__(256) k_kick_drift64(MdArgs a) {
     double dsum[3] = {0, 0, 0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int e = a.elem[i];
+        const unsigned b = a.dof ? a.dof[i] : 7u;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             double vv = a.v[c * n + i], ff = a.f[c * n + i], xx = a.x[c * n + i];
-            vv = __dadd_rn(__dmul_rn(vv, fac), __ddiv_rn(__dmul_rn(ff, a.dt2), a.masses[e]));
+            // a frozen component keeps its velocity and still drifts
+            // (update_x_d__x_w_dof, md_nvt.cpp:144-180)
+            if ((b >> c) & 1u) vv = __dadd_rn(__dmul_rn(vv, fac), __ddiv_rn(__dmul_rn(ff, a.dt2), a.masses[e]));
             double dx = __dmul_rn(vv, a.dt);
             dsum[c] = __dadd_rn(dsum[c], dx);
             xx = __dadd_rn(xx, dx);
@@ -154,7 +165,7 @@ __global__ void __launch_bounds__(256) k_kick_drift64(MdArgs a) {
         final_sums<3>(a.partials, gridDim.x, t);
         if (threadIdx.x == 0) {
             double natms = (double)n;
-            for (int c = 0; c < 3; c++) a.sc->com[c] = t[c] / natms;
+            for (int c = 0; c < 3; c++) a.sc->com[c] = a.com_on[c] ? t[c] / natms : 0.0;
             a.sc->rebuild = 0;
             a.sc->counter[4] = 0;
         }
@@ -183,13 +194,20 @@ __global__ void __launch_bounds__(256) k_kick2_64(MdArgs a) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int e = a.elem[i];
         const double m = a.masses[e];
+        const unsigned b = a.dof ? a.dof[i] : 7u;
         double vv[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            double v0 = a.v[c * n + i], ff = a.f[c * n + i];
-            v0 = __dadd_rn(v0, __ddiv_rn(__dmul_rn(ff, a.dt2), m));
-            a.v[c * n + i] = v0;
-            vv[c] = v0;
+            // update_x_d_w_dof (md_nvt.cpp:184-215): frozen components are
+            // neither kicked nor counted in the kinetic tensor
+            if ((b >> c) & 1u) {
+                double v0 = a.v[c * n + i], ff = a.f[c * n + i];
+                v0 = __dadd_rn(v0, __ddiv_rn(__dmul_rn(ff, a.dt2), m));
+                a.v[c * n + i] = v0;
+                vv[c] = v0;
+            } else {
+                vv[c] = 0.0;
+            }
         }
         d[0] += __dmul_rn(__dmul_rn(vv[0], vv[0]), m);
         d[1] += __dmul_rn(__dmul_rn(vv[0], vv[1]), m);
@@ -218,7 +236,7 @@ __global__ void k_run_end64(MdArgs a) {
     const int n = a.n;
     const double fac = a.sc->fac_x_d;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n; i += gridDim.x * blockDim.x)
-        a.v[i] = __dmul_rn(a.v[i], fac);
+        if (!a.dof || ((a.dof[i % n] >> (i / n)) & 1u)) a.v[i] = __dmul_rn(a.v[i], fac);
 }
 
 // ------------------------------------------------------------------ mixed path
@@ -607,7 +625,12 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
     a.nhc.ddt2 = 0.5 * tdt / (double)niters;
     a.nhc.freq_sq = 1.0 / (t_relax * t_relax);
     a.nhc.kB = kB;
-    a.nhc.ndof = 3 * s->n;
+    // MDNVT::pre_init (md_nvt.cpp:264-291): frozen components leave the
+    // degrees of freedom, and the mean displacement is kept along a
+    // component in which any atom is frozen
+    a.dof = s->dof;
+    a.nhc.ndof = 3 * s->n - (s->dof_frozen[0] + s->dof_frozen[1] + s->dof_frozen[2]);
+    for (int c = 0; c < 3; c++) a.com_on[c] = s->dof_frozen[c] == 0;
     a.nhc.ndof_kB = a.nhc.ndof * kB;
     a.nhc.L = L;
     a.nhc.niters = niters;
@@ -709,6 +732,8 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     if (!(t_relax > 0.0)) throw Error{MAPPG_ERR_ARG, "t_relax must be positive"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
+    if (s->dof && s->precision == MAPPG_MIXED)
+        throw Error{MAPPG_ERR_UNSUPP, "MD with frozen components (x_dof) runs in FP64 (create the system with MAPPG_FP64)"};
     run_clear(s);
     double* tdev = nullptr;
     if (thermo) {

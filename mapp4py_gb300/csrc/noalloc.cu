@@ -60,15 +60,17 @@ static unsigned char* scratch_on(int device) {
 }
 
 // forces from bin order (structure of arrays) to the caller's order (x, y, z
-// per atom), energy and virial to the caller's 7 doubles
+// per atom), zero on components frozen by atoms.x_dof (dof null: none),
+// energy and virial to the caller's 7 doubles
 __global__ void k_noalloc_out(int n, const int* __restrict__ id, const double* __restrict__ f_bin,
-                              const DevScalars* __restrict__ sc, double* __restrict__ f_out,
-                              double* __restrict__ ev_out) {
+                              const uint8_t* __restrict__ dof, const DevScalars* __restrict__ sc,
+                              double* __restrict__ f_out, double* __restrict__ ev_out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const size_t u = 3 * (size_t)id[i];
-        f_out[u] = f_bin[i];
-        f_out[u + 1] = f_bin[n + i];
-        f_out[u + 2] = f_bin[2 * n + i];
+        const unsigned d = dof ? dof[i] : 7u;
+        f_out[u] = (d & 1u) ? f_bin[i] : 0.0;
+        f_out[u + 1] = (d & 2u) ? f_bin[n + i] : 0.0;
+        f_out[u + 2] = (d & 4u) ? f_bin[2 * n + i] : 0.0;
     }
     if (ev_out && blockIdx.x == 0 && threadIdx.x < 7)
         ev_out[threadIdx.x] = threadIdx.x == 0 ? sc->energy : sc->virial[threadIdx.x - 1];
@@ -98,7 +100,7 @@ extern "C" int mappg_sys_force_noalloc(mappg_sys* s, double* f_dev, double* ev_d
         a.partials = reinterpret_cast<double*>(base + kOffPart);
         a.sc = sc;
         launch_force64_args(s, a);
-        k_noalloc_out<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, a.f, sc, f_dev, ev_dev);
+        k_noalloc_out<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, a.f, s->dof, sc, f_dev, ev_dev);
         MAPPG_CUDA(cudaGetLastError());
         return MAPPG_OK;
     } catch (const Error& e) {

@@ -322,6 +322,7 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
     if (!(t_relax > 0.0) || !(t_relax_S > 0.0)) throw Error{MAPPG_ERR_ARG, "t_relax must be positive"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
+    if (s->dof) throw Error{MAPPG_ERR_UNSUPP, "md.nst with frozen components (x_dof) is not supported"};
     Nst q;
     q.s = s;
     q.T = T;

@@ -791,7 +791,7 @@ void sys_free(mappg_sys* s) {
                     s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
                     s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev, s->cells_dev, s->cell_of,
                     s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp, s->cmd,
-                    s->cell_out};
+                    s->cell_out, s->dof};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);

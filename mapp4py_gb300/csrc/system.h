@@ -244,6 +244,10 @@ struct mappg_sys {
     void* hook_user = nullptr;
     int hook_every = 0;
     std::vector<int> host_id;  // sorted -> caller (host copy)
+    // atoms.x_dof: bit c of dof[i] set when component c of atom i (bin
+    // order) is a degree of freedom; null when every component is
+    uint8_t* dof = nullptr;
+    int dof_frozen[3] = {0, 0, 0};  // atoms frozen per component
 };
 
 namespace mappg {

@@ -3,7 +3,8 @@
 Names, arguments and defaults follow the reference's Python types:
   md.atoms             AtomsMD (atoms_md.cpp); here built from arrays, with
                        ff_eam_setfl / ff_eam_funcfl / ff_eam_fs (ff_eam.cpp:594-801),
-                       create_temp (atoms_md.cpp:490-531), kB, skin, H, x, x_d
+                       create_temp (atoms_md.cpp:490-531), kB, skin, H, x, x_d,
+                       x_dof (frozen components: zero force, no kick)
   md.nvt(T, dt)        MDNVT (md_nvt.cpp:14-26,493-881): t_relax=100*dt, L=3,
                        niters=1, ntally=10000, run(atoms, nsteps)
   md.nst(S, T, dt)     MDNST (md_nst.cpp:10-38,374-450): as md.nvt plus S, tau,
@@ -127,8 +128,10 @@ class atoms:
         self.pe = float("nan")
         self.S_pe = np.full((3, 3), np.nan)
         self.ff = None
+        self.x_dof = None  # None, or [N][3] bool: True where a component is free
         self._sys = None
         self._sys_key = None
+        self._dof_set = None
 
     @property
     def natms(self):
@@ -190,7 +193,13 @@ class atoms:
     def create_temp(self, temp, seed):
         if math.isnan(self.kB):
             raise TypeError("boltzmann constant should be set prior to create_temp")
-        self.x_d = _lib.create_temp(self.elem, self.masses, temp, self.kB, seed)
+        dof = self._dof()
+        if dof is None:
+            self.x_d = _lib.create_temp(self.elem, self.masses, temp, self.kB, seed)
+        else:
+            # only the free components draw (AtomsMD::create_T, atoms_md.cpp:138-149)
+            v = self.x_d if self.x_d is not None else np.zeros_like(self.x)
+            self.x_d = _lib.create_temp_dof(self.elem, self.masses, dof, temp, self.kB, seed, v)
 
     # ---------------------------------------------------------- device state
     def _f_out(self):
@@ -200,6 +209,14 @@ class atoms:
         if isinstance(f, np.ndarray) and f.shape == self.x.shape and f.dtype == np.float64 and f.flags.c_contiguous:
             return f
         return None
+
+    def _dof(self):
+        if self.x_dof is None:
+            return None
+        d = np.asarray(self.x_dof, dtype=bool)
+        if d.shape != self.x.shape:
+            raise TypeError("x_dof should be an array of shape (natms, 3)")
+        return None if d.all() else np.ascontiguousarray(d)
 
     def _key(self):
         return (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
@@ -213,6 +230,12 @@ class atoms:
             self._sys = _lib.System(self.ff, self.H, self.x, self.elem, self.masses, self.skin,
                                     _PREC[self.precision])
             self._sys_key = key
+            self._dof_set = None
+        dof = self._dof()
+        dkey = None if dof is None else dof.tobytes()
+        if dkey != self._dof_set:
+            self._sys.set_dof(dof)
+            self._dof_set = dkey
         return self._sys
 
 

@@ -361,6 +361,7 @@ typedef struct {
     double vec[7];
     double pe, F_H[3][3], S_pe[3][3];
     int nrebuild;
+    unsigned char* dof; /* natms*3, nonzero: the component is a degree of freedom; NULL: all are */
 } orc_sys;
 
 /* Atoms::update_H  atoms.cpp:187-194 with MLT_inv / MLT_depth / MLT_det
@@ -454,7 +455,7 @@ void orc_sys_free(void* p) {
     free(s->x); free(s->elem); free(s->src); free(s->gdim); free(s->gsgn); free(s->owner);
     free(s->img); free(s->v); free(s->f); free(s->x0); free(s->masses); free(s->cut_sq);
     free(s->cut_sk_sq); free(s->nl_off); free(s->nl_cnt); free(s->nl); free(s->rho);
-    free(s->dF); free(s->drhoi); free(s->drhoj);
+    free(s->dF); free(s->drhoi); free(s->drhoj); free(s->dof);
     free(s);
 }
 
@@ -464,6 +465,16 @@ void orc_sys_set_v(void* p, const double* v) { memcpy(((orc_sys*)p)->v, v, sizeo
 void orc_sys_get_v(void* p, double* v) { memcpy(v, ((orc_sys*)p)->v, sizeof(double) * 3 * ((orc_sys*)p)->natms); }
 void orc_sys_get_f(void* p, double* f) { memcpy(f, ((orc_sys*)p)->f, sizeof(double) * 3 * ((orc_sys*)p)->natms); }
 void orc_sys_set_pair_wise(void* p, int pw) { ((orc_sys*)p)->pair_wise = pw; }
+/* atoms.x_dof: per atom and component, nonzero when it is a degree of
+   freedom; NULL clears it (every component free) */
+void orc_sys_set_dof(void* p, const unsigned char* dof) {
+    orc_sys* s = (orc_sys*)p;
+    free(s->dof);
+    s->dof = NULL;
+    if (!dof) return;
+    s->dof = (unsigned char*)malloc((size_t)3 * s->natms);
+    memcpy(s->dof, dof, (size_t)3 * s->natms);
+}
 int orc_sys_nghost(void* p) { return ((orc_sys*)p)->nghost; }
 int orc_sys_nrebuild(void* p) { return ((orc_sys*)p)->nrebuild; }
 
@@ -895,6 +906,10 @@ static void force_calc(orc_sys* s) {
     double vol_neg = -s->vol;
     for (int i = 0; i < 6; i++) vv[i + 1] /= vol_neg;
     for (int k = 0; k < 6; k++) s->S_pe[ia[k]][ja[k]] = s->S_pe[ja[k]][ia[k]] = vv[k + 1];
+    /* components without a degree of freedom carry no force  ff_md.cpp:138-144 */
+    if (s->dof)
+        for (int q = 0; q < 3 * s->natms; q++)
+            if (!s->dof[q]) s->f[q] = 0.0;
 }
 
 /* force_calc over the full list with nthreads threads (timing baseline);
@@ -1121,10 +1136,25 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
         for (int i = 0; i < L; i++) th.eta_d[i] = eta_io[i];
     const int n = s->natms;
     const double dt2 = dt / 2.0;
-    /* pre_init  md_nvt.cpp:256-340 */
+    /* pre_init  md_nvt.cpp:256-340 (with x_dof: the frozen components leave
+       the degrees of freedom and the kinetic tensor) */
+    const unsigned char* dof = s->dof;
+    if (dof && threads > 0) return fail("x_dof is restated on the serial path only");
     int ndof_part = n * 3;
+    int dofs[3] = {1, 1, 1};
+    if (dof)
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < 3; j++)
+                if (!dof[3 * i + j]) {
+                    ndof_part--;
+                    dofs[j] = 0;
+                }
     double mvv[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < n; i++) dyadic_add(s->masses[s->elem[i]], s->v + 3 * i, mvv);
+    for (int i = 0; i < n; i++) {
+        double w[3];
+        for (int j = 0; j < 3; j++) w[j] = (!dof || dof[3 * i + j]) ? s->v[3 * i + j] : 0.0;
+        dyadic_add(s->masses[s->elem[i]], w, mvv);
+    }
     double T_part = (mvv[0] + (mvv[3] + mvv[5])) / (ndof_part * kB);
     /* DynamicMD::init */
     if (orc_sys_init_dynamic(s)) return -1;
@@ -1173,32 +1203,42 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
             dxl[1] = d1;
             dxl[2] = d2;
         } else {
+            /* update_x_d__x(_w_dof)  md_nvt.cpp:70-102,144-180: a frozen
+               component keeps its velocity and still drifts */
             for (int i = 0; i < n; i++) {
                 double mi = s->masses[s->elem[i]];
                 double* xd = s->v + 3 * i;
                 double* xx = s->x + 3 * i;
                 double* ff = s->f + 3 * i;
                 for (int j = 0; j < 3; j++) {
-                    xd[j] = xd[j] * fac_x_d + ff[j] * dt2 / mi;
+                    if (!dof || dof[3 * i + j]) xd[j] = xd[j] * fac_x_d + ff[j] * dt2 / mi;
                     dxl[j] += xd[j] * dt;
                     xx[j] += xd[j] * dt;
                 }
             }
         }
         double natms = (double)n;
-        for (int j = 0; j < 3; j++) dxl[j] /= natms;
+        for (int j = 0; j < 3; j++) dxl[j] = dofs[j] ? dxl[j] / natms : 0.0;
         for (int i = 0; i < n; i++)
             for (int j = 0; j < 3; j++) s->x[3 * i + j] -= dxl[j];
         if (dynamic_update(s)) return -1;
         FORCE_CALC();
-        /* update_x_d  md_nvt.cpp:106-128 */
+        /* update_x_d(_w_dof)  md_nvt.cpp:106-128,184-215 */
         for (int k = 0; k < 6; k++) mvv[k] = 0.0;
         for (int i = 0; i < n; i++) {
             double mi = s->masses[s->elem[i]];
             double* xd = s->v + 3 * i;
             double* ff = s->f + 3 * i;
-            for (int j = 0; j < 3; j++) xd[j] += ff[j] * dt2 / mi;
-            dyadic_add(mi, xd, mvv);
+            double w[3];
+            for (int j = 0; j < 3; j++) {
+                if (!dof || dof[3 * i + j]) {
+                    xd[j] += ff[j] * dt2 / mi;
+                    w[j] = xd[j];
+                } else {
+                    w[j] = 0.0;
+                }
+            }
+            dyadic_add(mi, w, mvv);
         }
         T_part = (mvv[0] + (mvv[3] + mvv[5])) / (ndof_part * kB);
         fac_x_d = fac = nhc_step(&th, T_part / T, ndof_part);
@@ -1208,8 +1248,9 @@ int orc_md_nvt_run(void* p, double T, double dt, double kB, double t_relax, int 
         THERMO_ROW();
     }
     if (loop_seconds) *loop_seconds = now_seconds() - t0;
-    /* update_x_d_final  md_nvt.cpp:51-56 */
-    for (int i = 0; i < 3 * n; i++) s->v[i] *= fac_x_d;
+    /* update_x_d_final(_w_dof)  md_nvt.cpp:51-66 */
+    for (int i = 0; i < 3 * n; i++)
+        if (!dof || dof[i]) s->v[i] *= fac_x_d;
     if (eta_io)
         for (int i = 0; i < L; i++) eta_io[i] = th.eta_d[i];
 #undef THERMO_ROW
@@ -1427,6 +1468,7 @@ int orc_md_nst_run(void* p, const double* S, const double* tau, double T, double
                    double* V_H, double* eta, double* eta_S, double* thermo) {
     orc_sys* s = (orc_sys*)p;
     if (isnan(kB)) return fail("boltzmann constant should be set prior to MD");
+    if (s->dof) return fail("x_dof with md.nst is not restated");
     nst_t q;
     memset(&q, 0, sizeof(q));
     q.T = T; q.dt = dt; q.dt2 = dt / 2.0; q.kB = kB;
@@ -2308,8 +2350,16 @@ void orc_sys_get_box(void* p, double* H) { memcpy(H, ((orc_sys*)p)->H, sizeof(do
 /* Park-Miller + polar Box-Muller  random.cpp:32-68, AtomsMD::create_T
    atoms_md.cpp:130-162.  Seed 0 makes the reference loop forever; here it is
    rejected. */
+int orc_create_temp_dof(int natms, const unsigned char* elem, const double* masses, const unsigned char* dof,
+                        double T, double kB, int seed, double* v);
 int orc_create_temp(int natms, const unsigned char* elem, const double* masses, double T, double kB,
                     int seed, double* v) {
+    return orc_create_temp_dof(natms, elem, masses, NULL, T, kB, seed, v);
+}
+/* AtomsMD::create_T with x_dof (atoms_md.cpp:138-149): only the free
+   components draw a sample; the others keep their value */
+int orc_create_temp_dof(int natms, const unsigned char* elem, const double* masses, const unsigned char* dof,
+                        double T, double kB, int seed, double* v) {
     if (seed == 0) return fail("seed 0 never yields a Gaussian sample");
     int sd = seed, gchk = 0;
     double reserved = 0.0;
@@ -2323,6 +2373,7 @@ int orc_create_temp(int natms, const unsigned char* elem, const double* masses, 
     for (int i = 0; i < natms; i++) {
         double fac = sqrt(kB * T / masses[elem[i]]);
         for (int j = 0; j < 3; j++) {
+            if (dof && !dof[3 * i + j]) continue;
             double g;
             if (gchk) {
                 gchk = 0;

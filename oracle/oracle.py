@@ -74,6 +74,8 @@ def lib():
         L.orc_md_nst_run.argtypes = [C.c_void_p, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                      C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D]
         L.orc_create_temp.argtypes = [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]
+        L.orc_create_temp_dof.argtypes = [C.c_int, _U8, _D, _U8, C.c_double, C.c_double, C.c_int, _D]
+        L.orc_sys_set_dof.argtypes = [C.c_void_p, _U8]
         _lib = L
     return _lib
 
@@ -296,6 +298,15 @@ class System:
         self.initialized = True
         return th, V_H, eta, eta_S
 
+    def set_dof(self, dof):
+        """atoms.x_dof: (n, 3) bool, True where the component is free; None
+        clears it."""
+        if dof is None:
+            lib().orc_sys_set_dof(self.h, None)
+            return
+        d = np.ascontiguousarray(np.asarray(dof, dtype=bool).reshape(-1, 3), dtype=np.uint8)
+        lib().orc_sys_set_dof(self.h, d.ctypes.data_as(_U8))
+
     def box(self):
         H = np.zeros((3, 3))
         lib().orc_sys_get_box(self.h, _dp(H))
@@ -318,6 +329,19 @@ class System:
         self.initialized = True
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+
+def create_temp_dof(elem, masses, dof, T, kB, seed, v):
+    """AtomsMD::create_T with x_dof: free components drawn, the others kept."""
+    elem = np.ascontiguousarray(elem, dtype=np.uint8)
+    out = np.array(v, dtype=np.float64).reshape(-1, 3)
+    d = np.ascontiguousarray(np.asarray(dof, dtype=bool).reshape(-1, 3), dtype=np.uint8)
+    masses = np.ascontiguousarray(masses, dtype=np.float64)
+    r = lib().orc_create_temp_dof(elem.shape[0], elem.ctypes.data_as(_U8), _dp(masses), d.ctypes.data_as(_U8),
+                                  float(T), float(kB), int(seed), _dp(out))
+    if r != 0:
+        raise RuntimeError("oracle: " + _err())
+    return out
 
 
 def create_temp(elem, masses, T, kB, seed):

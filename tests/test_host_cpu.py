@@ -10,7 +10,7 @@ import pytest
 
 import oracle as O
 from conftest import ROOT
-from mapp4py_gb300 import _lib, synth
+from mapp4py_gb300 import _lib, md, synth
 
 
 @pytest.fixture(scope="module")
@@ -133,3 +133,28 @@ def test_api_surface_mirrors_reference(built):
     a = md.atoms(H, x, np.zeros(len(x), np.uint8))
     with pytest.raises(TypeError):
         a.create_temp(300.0, 1)  # kB not set
+
+
+def test_create_temp_dof_matches_oracle(built):
+    """create_temp with x_dof: free components drawn in order, the others
+    keep their value (atoms_md.cpp:138-149)."""
+    elem = (np.arange(600) % 2).astype(np.uint8)
+    masses = [63.5, 40.0]
+    rng = np.random.default_rng(1)
+    dof = rng.random((600, 3)) > 0.25
+    v0 = rng.normal(size=(600, 3))
+    v = _lib.create_temp_dof(elem, masses, dof, 300.0, synth.KB, 846244, v0)
+    vo = O.create_temp_dof(elem, masses, dof, 300.0, synth.KB, 846244, v0)
+    assert np.array_equal(v, vo) and np.array_equal(v[~dof], v0[~dof])
+    # all free: the plain draw
+    assert np.array_equal(_lib.create_temp_dof(elem, masses, np.ones((600, 3), bool), 300.0, synth.KB, 9, v0),
+                          _lib.create_temp(elem, masses, 300.0, synth.KB, 9))
+    a = md.atoms(np.eye(3) * 10.0, rng.random((600, 3)) * 10.0, elem, elems=("A", "B"), masses=masses)
+    a.kB = synth.KB
+    a.x_d = v0.copy()
+    a.x_dof = dof
+    a.create_temp(300.0, 846244)
+    assert np.array_equal(a.x_d, vo)
+    a.x_dof = np.ones((5, 3), bool)
+    with pytest.raises(TypeError):
+        a.create_temp(300.0, 1)

@@ -250,3 +250,68 @@ def test_cu_mishin_cohesive_energy():
     assert abs(pe / len(x) - (-3.54)) < 0.005
     # a0 is the energy minimum: the pressure (virial) nearly vanishes
     assert abs(vir[0]) / len(x) < 0.01
+
+
+def _dof_mask(n, seed=5):
+    """About a fifth of the atoms fully frozen, a few more frozen along one
+    component (z only for some, x only for others)."""
+    rng = np.random.default_rng(seed)
+    d = np.ones((n, 3), dtype=bool)
+    r = rng.random(n)
+    d[r < 0.2] = False
+    d[(r >= 0.2) & (r < 0.3), 2] = False
+    d[(r >= 0.3) & (r < 0.35), 0] = False
+    return d
+
+
+def test_x_dof_forces_minimizer_and_nvt(potentials):
+    """atoms.x_dof (ff_md.cpp:138-144, md_nvt.cpp:144-215): forces on frozen
+    components are zero, the minimizer leaves them in place, an NVT run
+    drifts them with their velocity without kicking or thermostatting them,
+    counts only the free components in the temperature, and draws only the
+    free components in create_temp."""
+    path, _ = potentials[("A", "B")]
+    e = O.Eam.setfl(path)
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, T=600.0, seed=2)
+    d = _dof_mask(c.natoms)
+    free = O.System(e, c.H, c.x, c.elem, c.masses)
+    pe0, vir0 = free.force()
+    s = O.System(e, c.H, c.x, c.elem, c.masses)
+    s.set_dof(d)
+    pe, vir = s.force()
+    assert pe == pe0 and np.array_equal(vir, vir0)
+    assert np.array_equal(s.f, np.where(d, free.f, 0.0))
+    # an all-free mask is the plain path, bit for bit
+    t = O.System(e, c.H, c.x, c.elem, c.masses)
+    t.set_dof(np.ones((c.natoms, 3), bool))
+    t.v = c.v
+    th_t, eta_t, _ = t.nvt_run(600.0, synth.FS, synth.KB, 30)
+    u = O.System(e, c.H, c.x, c.elem, c.masses)
+    u.v = c.v
+    th_u, eta_u, _ = u.nvt_run(600.0, synth.FS, synth.KB, 30)
+    assert np.array_equal(th_t, th_u) and np.array_equal(t.x, u.x)
+    # the minimizer: frozen components stay where they are, up to the
+    # rounding of the fractional-coordinate round trip at each rebuild
+    m = O.System(e, c.H, c.x, c.elem, c.masses)
+    m.set_dof(d)
+    r = m.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=3000)
+    assert r["err"] == 100
+    assert np.max(np.abs(m.x[~d] - c.x[~d])) < 1e-13
+    assert np.max(np.abs(m.f[d])) < 1e-4 and np.all(m.f[~d] == 0.0)
+    # NVT: frozen components keep their velocity and drift with it
+    v = O.create_temp_dof(c.elem, c.masses, d, 600.0, synth.KB, 77, np.full((c.natoms, 3), 1e-3))
+    assert np.all(v[~d] == 1e-3) and np.all(v[d] != 1e-3)
+    n = O.System(e, c.H, c.x, c.elem, c.masses)
+    n.set_dof(d)
+    n.v = v
+    nsteps = 40
+    th, eta, _ = n.nvt_run(600.0, synth.FS, synth.KB, nsteps, t_relax=20 * synth.FS)
+    assert np.all(n.v[~d] == 1e-3)
+    dx = n.x - c.x
+    dx -= np.round(dx @ np.linalg.inv(c.H)) @ c.H
+    assert np.max(np.abs(dx[~d] - nsteps * synth.FS * 1e-3)) < 1e-12
+    # the temperature column counts the free components only
+    vf = np.where(d, n.v, 0.0)
+    mvv = np.sum(c.masses[c.elem][:, None] * vf * vf)
+    assert abs(th[-1, 1] - mvv / (d.sum() * synth.KB)) < 1e-9 * th[-1, 1]
+    assert np.all(np.isfinite(eta))
