@@ -712,6 +712,10 @@ static void run_clear(mappg_sys* s) {
 
 void nvt_free(mappg_sys* s) { run_clear(s); }
 
+// runs this short launch their steps' kernels directly: capturing and
+// instantiating the step graph costs more than it saves over a few steps
+constexpr long long kGraphMinSteps = 8;
+
 // MDNVT::init + the opening force call of MDNVT::run, then the step graph
 void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
                const double* eta, bool thermo, const double* Tcell) {
@@ -810,6 +814,7 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     launch_force(s);
     k_run_begin<<<1, 1, 0, s->stream>>>(a);
     MAPPG_CUDA(cudaGetLastError());
+    if (nsteps < kGraphMinSteps) return;  // nvt_steps launches the kernels itself
     MAPPG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     try {
         if (s->precision == MAPPG_MIXED)
@@ -831,7 +836,14 @@ void nvt_steps(mappg_sys* s, long long nsteps) {
     NvtRun* r = (NvtRun*)s->run;
     if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
     if (r->done + nsteps > r->planned) throw Error{MAPPG_ERR_ARG, "more steps than the run was begun with"};
-    for (long long st = 0; st < nsteps; st++) MAPPG_CUDA(cudaGraphLaunch(r->exec, s->stream));
+    for (long long st = 0; st < nsteps; st++) {
+        if (r->exec)
+            MAPPG_CUDA(cudaGraphLaunch(r->exec, s->stream));
+        else if (s->precision == MAPPG_MIXED)
+            launch_step32(s, r->a);
+        else
+            launch_step64(s, r->a);
+    }
     r->done += nsteps;
 }
 

@@ -393,7 +393,7 @@ struct BuildArgs {
     Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
     double cut_sk_sq[kMaxElem * kMaxElem];
-    double prune2;         // above this squared gap a stencil bin holds no neighbour
+    float prune2f;         // above this squared gap (A^2) a stencil bin holds no neighbour
     const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
     const int* cell_of;
 };
@@ -454,7 +454,6 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
         // warp walks 32 at a time, so lanes stay busy across bin borders
         int lo = 0, ncand = 0, img = 0;
         const bool ortho = BATCH ? cg->ortho != 0 : a.fr.ortho != 0;
-        const double si[3] = {a.s[i], a.s[n + i], a.s[2 * n + i]};
         if (lane < 27) {
             const int c = lane;
             int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
@@ -470,18 +469,22 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
             if (ortho) {
                 // the gap between atom i and the stencil bin: a bin farther
                 // than cutoff + skin holds no neighbour, so it is skipped
-                // (the kept entries and their order are unchanged)
-                const int dd[3] = {d0, d1, d2}, nbv[3] = {nbx, nby, nbz};
-                const double L[3] = {h6[0], h6[3], h6[5]};
-                double g2 = 0.0;
+                // (the kept entries and their order are unchanged).  FP32 on
+                // the bin-relative position (0..8 per axis) and the frame's
+                // Cartesian scale; prune2f carries a margin far above the
+                // rounding of either, so a bin is only ever kept in doubt
+                const int dd[3] = {d0, d1, d2};
+                const float pa[3] = {pi.x, pi.y, pi.z};
+                float g2 = 0.f;
 #pragma unroll
                 for (int ax = 0; ax < 3; ax++) {
                     if (dd[ax] == 0) continue;
-                    const double f = si[ax] * nbv[ax] - bi[ax];
-                    const double gap = (dd[ax] > 0 ? 1.0 - f : f) * (L[ax] / nbv[ax]);
-                    g2 += gap * gap;
+                    const float w = BATCH ? cg->G[ax][ax] : a.fr.G[ax][ax];
+                    const float u = fmaxf(dd[ax] > 0 ? kBinW - pa[ax] : pa[ax], 0.f);
+                    const float gap = u * w;
+                    g2 = fmaf(gap, gap, g2);
                 }
-                if (g2 > a.prune2) ncand = 0;
+                if (g2 > a.prune2f) ncand = 0;
             }
         }
         int incl = ncand;
@@ -696,7 +699,10 @@ void launch_rebuild_chain(mappg_sys* s) {
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
         maxc = std::max(maxc, s->cut_sk_sq[p]);
     }
-    a.prune2 = maxc * (1.0 + 1e-8) + 1e-12;
+    // (cut + skin)^2 plus 1e-3 A^2 + 1e-5 relative: the FP32 gap of the
+    // builder errs by under 1e-4 A^2 (bin-relative positions to 1e-6 of a
+    // bin, sums of three squares)
+    a.prune2f = (float)(maxc * (1.0 + 1e-5) + 1e-3);
     a.fr = s->frame;
     a.cells = s->cells_dev;
     a.cell_of = s->cell_of;

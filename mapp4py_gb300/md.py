@@ -286,6 +286,9 @@ class export_cfg:
         return "f" in self.extra_vecs
 
 
+_ROWS_FOR_PE = 4096
+
+
 def _print_thermo(th, step0, ntally, vol):
     hdr = "%8s %14s %16s %12s %12s %12s" % ("step", "T", "PE", "S[0][0]", "S[1][1]", "S[2][2]")
     print(hdr)
@@ -328,15 +331,19 @@ class nvt:
         s = atoms._system()
         s.set_x(atoms.x)
         s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
+        # the per-step rows (14 doubles) also carry the last step's energy and
+        # virial, which atoms.pe / S_pe take; short runs keep them even
+        # without a tally instead of paying for one more force call
+        rows = bool(self.ntally) or nsteps <= _ROWS_FOR_PE
         xprt = self.export
         if xprt is None:
             th, self._eta = s.nvt_run(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L,
-                                      niters=self.niters, eta=self._eta, thermo=bool(self.ntally))
+                                      niters=self.niters, eta=self._eta, thermo=rows)
         else:
             # MDNVT::run's exports (md_nvt.cpp:390,436,470): the run goes on
             # the device in nevery-step pieces, each export is a snapshot
             s.nvt_begin(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L, niters=self.niters,
-                        eta=self._eta, thermo=bool(self.ntally))
+                        eta=self._eta, thermo=rows)
             try:
                 def snap(step):
                     x, v = s.nvt_snapshot()
@@ -358,7 +365,8 @@ class nvt:
         s.get_v(atoms.x_d)
         atoms.f = s.get_f(atoms._f_out())
         if th is not None:
-            _print_thermo(th, atoms.step, self.ntally, atoms.vol)
+            if self.ntally:
+                _print_thermo(th, atoms.step, self.ntally, atoms.vol)
             atoms.pe = float(th[-1, 0])
             F_H = th[-1, 8:14]
         else:

@@ -156,3 +156,48 @@ def test_import_cfg_runs(setfl, tmp_path):
     d = b.x - c.x
     d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
     assert np.max(np.abs(d)) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_short_runs_without_step_graph(setfl, precision):
+    """Runs of fewer than eight steps launch their kernels directly instead
+    of through the captured step graph; atoms.pe and S_pe of a run come from
+    its last step.  One 5-step run against the oracle (FP64) or the FP64 GPU
+    run (mixed, the mixed-precision budget), and run(atoms, 1) repeated
+    against one run of the same total length."""
+    import oracle as O
+
+    a = make_atoms(setfl, precision)
+    x0, v0 = a.x.copy(), a.x_d.copy()
+    integ = md.nvt(600.0, synth.FS)
+    integ.ntally = 0
+    integ.run(a, 5)
+    if precision == "fp64":
+        o = O.System(O.Eam.setfl(setfl), a.H, x0, a.elem, a.masses)
+        o.v = v0
+        th_o, _, _ = o.nvt_run(600.0, synth.FS, synth.KB, 5, t_relax=100 * synth.FS)
+        d = a.x - o.x
+        d -= np.round(d @ np.linalg.inv(a.H)) @ a.H
+        assert np.max(np.abs(d)) < 1e-9 and np.max(np.abs(a.x_d - o.v)) < 1e-9
+        assert abs(a.pe - th_o[-1, 0]) <= 1e-11 * abs(th_o[-1, 0])
+        F_H = th_o[-1, 8:14]
+        S = -np.array([[F_H[0], F_H[1], F_H[2]], [F_H[1], F_H[3], F_H[4]], [F_H[2], F_H[4], F_H[5]]]) / a.vol
+        assert np.max(np.abs(a.S_pe - S)) <= 1e-10 * np.max(np.abs(S))
+    else:
+        b = make_atoms(setfl, "fp64")
+        integ64 = md.nvt(600.0, synth.FS)
+        integ64.ntally = 0
+        integ64.run(b, 5)
+        assert np.max(np.abs(a.x - b.x)) < 1e-5
+        assert abs(a.pe - b.pe) / a.natms < 1e-6
+    # the energy the run reports is the energy of its final positions
+    s = a._system()
+    s.set_x(a.x)
+    pe, _ = s.force()
+    assert abs(pe - a.pe) <= (1e-11 * abs(pe) if precision == "fp64" else 1e-7 * a.natms)
+    c = make_atoms(setfl, precision)
+    one = md.nvt(600.0, synth.FS)
+    one.ntally = 0
+    for _ in range(3):
+        one.run(c, 1)
+    assert c.step == 3 and np.all(np.isfinite(c.x)) and np.isfinite(c.pe)
