@@ -179,11 +179,12 @@ int mappg_create_temp_dof(int natoms, const unsigned char* elem, const double* m
  * where it is a degree of freedom; NULL (or all nonzero) clears it.  Forces
  * on frozen components are zero in every force call (ForceFieldMD::
  * force_calc, ff_md.cpp:138-144), so the minimizers leave them in place.
- * FP64 NVT runs take the reference's _w_dof steps (md_nvt.cpp:144-215): a
+ * NVT runs take the reference's _w_dof steps (md_nvt.cpp:144-215): a
  * frozen component is neither kicked nor thermostatted and keeps drifting
  * with its velocity, leaves the degrees of freedom and the kinetic tensor,
  * and the mean displacement is not removed along a component in which any
- * atom is frozen.  Mixed-precision MD, md.nst and batches refuse it. */
+ * atom is frozen; mixed-precision MD takes the same branches in its FP32
+ * kernels.  md.nst and batches refuse it. */
 int mappg_sys_set_dof(mappg_sys* sys, const unsigned char* dof);
 
 /* ---------------------------------------------------------------- drivers */

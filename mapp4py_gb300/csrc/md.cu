@@ -264,11 +264,14 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int e = a.elem[i];
         const float kf = a.dtm32[e] * B;
+        const unsigned b = a.dof ? a.dof[i] : 7u;
         double xv[3];
         float vf[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            double v = fma(a.v[c * n + i], A, (double)(a.f32[c * n + i] * kf));
+            // a frozen component (atoms.x_dof) keeps its velocity and drifts
+            double v = a.v[c * n + i];
+            if ((b >> c) & 1u) v = fma(v, A, (double)(a.f32[c * n + i] * kf));
             double x = fma(v, a.dt, a.x[c * n + i]);
             a.v[c * n + i] = v;
             a.x[c * n + i] = x;
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
         if (threadIdx.x == 0) {
             const double natms = (double)n;
             for (int c = 0; c < 3; c++) {
-                a.sc->com[c] = t[c] / natms;
+                a.sc->com[c] = a.com_on[c] ? t[c] / natms : 0.0;
                 a.sc->drift[c] += a.sc->com[c];
             }
             a.sc->pending_kick = 0;
@@ -332,9 +335,15 @@ __global__ void __launch_bounds__(256) k_close32(MdArgs a) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int e = a.elem[i];
         const float dtm = a.dtm32[e], m = (float)a.masses[e];
-        const float vx = fmaf(a.f32[i], dtm, a.v32[i]);
-        const float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
-        const float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
+        float vx = fmaf(a.f32[i], dtm, a.v32[i]);
+        float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
+        float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
+        if (a.dof) {  // frozen components leave the kinetic tensor
+            const unsigned b = a.dof[i];
+            if (!(b & 1u)) vx = 0.f;
+            if (!(b & 2u)) vy = 0.f;
+            if (!(b & 4u)) vz = 0.f;
+        }
         const float mx = m * vx, my = m * vy, mz = m * vz;
         k0 = fmaf(mx, vx, k0);
         k1 = fmaf(mx, vy, k1);
@@ -394,10 +403,11 @@ __global__ void k_run_end32(MdArgs a) {
     const double fc = pend ? a.sc->fac_close : a.sc->fac_x_d;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
         const int i = q % n, c = q / n;
+        a.x[q] -= a.sc->drift[c];
+        if (a.dof && !((a.dof[i] >> c) & 1u)) continue;  // frozen: neither kicked nor scaled
         double v = a.v[q];
         if (pend) v += (double)a.f32[q] * a.dtm[a.elem[i]];
         a.v[q] = v * fc;
-        a.x[q] -= a.sc->drift[c];
     }
 }
 
@@ -736,8 +746,6 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
     if (!(t_relax > 0.0)) throw Error{MAPPG_ERR_ARG, "t_relax must be positive"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
-    if (s->dof && s->precision == MAPPG_MIXED)
-        throw Error{MAPPG_ERR_UNSUPP, "MD with frozen components (x_dof) runs in FP64 (create the system with MAPPG_FP64)"};
     run_clear(s);
     double* tdev = nullptr;
     if (thermo) {

@@ -414,6 +414,26 @@ __device__ __forceinline__ void frame_to_cart(const FR& fr, float a, float b, fl
     }
 }
 
+// the reference's predicate for a pair inside the FP32 band: x_j' =
+// S2X(s_j + n) in FP64 without fused multiply-adds, RSQ < (cut + skin)^2
+__device__ __forceinline__ bool exact_keep(const BuildArgs& a, const double* h6, double xi0, double xi1, double xi2,
+                                           int j, int im, int pe) {
+    const int n = a.n;
+    const int n0 = (im & 3) - 1, n1 = ((im >> 2) & 3) - 1, n2 = ((im >> 4) & 3) - 1;
+    double s0 = a.s[j], s1 = a.s[n + j], s2 = a.s[2 * n + j];
+    if (n0 > 0) s0 = dadd(s0, 1.0);
+    if (n0 < 0) s0 = dsub(s0, 1.0);
+    if (n1 > 0) s1 = dadd(s1, 1.0);
+    if (n1 < 0) s1 = dsub(s1, 1.0);
+    if (n2 > 0) s2 = dadd(s2, 1.0);
+    if (n2 < 0) s2 = dsub(s2, 1.0);
+    double xj0, xj1, xj2;
+    s2x(h6, s0, s1, s2, xj0, xj1, xj2);
+    double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
+    double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
+    return rsq < a.cut_sk_sq[pe];
+}
+
 // rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
 // candidates, ballots keep the row in (bin step, bin order) order; x0 <- x
 // (blocks of 256 threads: eight warps, one per-warp bin table each)
@@ -516,7 +536,6 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
                 }
                 const int k = clo + (t - cpre);
                 const int im = cimg;
-                const int n0 = (im & 3) - 1, n1 = ((im >> 2) & 3) - 1, n2 = ((im >> 4) & 3) - 1;
                 const float4 o = off[c];
                 const bool self_img = im == 21;  // no image shift
                 j = a.bin_atoms[k];
@@ -535,19 +554,7 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
                     if (r2 < a.lo2[pe]) {
                         keep = true;
                     } else if (r2 <= a.hi2[pe]) {
-                        // exact reference predicate on S2X(s_j + n)
-                        double s0 = a.s[j], s1 = a.s[n + j], s2 = a.s[2 * n + j];
-                        if (n0 > 0) s0 = dadd(s0, 1.0);
-                        if (n0 < 0) s0 = dsub(s0, 1.0);
-                        if (n1 > 0) s1 = dadd(s1, 1.0);
-                        if (n1 < 0) s1 = dsub(s1, 1.0);
-                        if (n2 > 0) s2 = dadd(s2, 1.0);
-                        if (n2 < 0) s2 = dsub(s2, 1.0);
-                        double xj0, xj1, xj2;
-                        s2x(h6, s0, s1, s2, xj0, xj1, xj2);
-                        double e0 = dsub(xi0, xj0), e1 = dsub(xi1, xj1), e2 = dsub(xi2, xj2);
-                        double rsq = dadd(dmul(e0, e0), dadd(dmul(e1, e1), dmul(e2, e2)));
-                        keep = rsq < a.cut_sk_sq[pe];
+                        keep = exact_keep(a, h6, xi0, xi1, xi2, j, im, pe);
                     }
                 }
             }
@@ -566,6 +573,160 @@ __global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc)
             sumrow += cnt;
         }
         if (lane < 3) a.x0[lane * n + i] = lane == 0 ? xi0 : (lane == 1 ? xi1 : xi2);
+    }
+    if (lane == 0) {
+        if (overflow) sc->overflow = 1;
+        if (maxrow) atomicMax(&sc->maxrow, maxrow);
+        if (sumrow) atomicAdd(&sc->sumrow, (unsigned long long)sumrow);
+    }
+}
+
+// rebuild step 5 for one cell: one warp per bin.  The candidates of the
+// bin's 27-bin stencil are read 32 at a time, once for all atoms of the bin,
+// and every atom of the bin tests them in turn, so a candidate's gathers and
+// its place in the bin sequence are paid once per bin instead of once per
+// atom.  Each row gets the entries of k_build_list in the same (bin step,
+// bin order) order; stencil bins are not pruned (a pruned bin holds no
+// neighbour, so testing it changes nothing).
+template <bool ORTHO>
+__global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    __shared__ float4 off[27];
+    __shared__ int s_pre[8][32], s_lo[8][32], s_img[8][32];  // per warp: the bin's 27 stencil bins
+    __shared__ float4 s_at[8][32];  // per warp: the bin's atoms (frame position, w = index << 3 | element)
+    __shared__ float s_lo2[kMaxElem * kMaxElem], s_hi2[kMaxElem * kMaxElem];
+    if (threadIdx.x < 27)
+        off[threadIdx.x] = make_float4(a.fr.off[threadIdx.x][0], a.fr.off[threadIdx.x][1], a.fr.off[threadIdx.x][2], 0.f);
+    if (threadIdx.x < a.ne * a.ne) {
+        s_lo2[threadIdx.x] = a.lo2[threadIdx.x];
+        s_hi2[threadIdx.x] = a.hi2[threadIdx.x];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = a.n;
+    const int nbx = a.g.nb[0], nby = a.g.nb[1], nbz = a.g.nb[2];
+    const int nbins = nbx * nby * nbz;
+    const float G0 = a.fr.G[0][0], G1 = a.fr.G[1][1], G2 = a.fr.G[2][2];
+    double h6[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) h6[k] = a.g.h6[k];
+    int maxrow = 0, overflow = 0;
+    long long sumrow = 0;
+    for (int b = warp; b < nbins; b += nw) {
+        const int a0 = a.bin_start[b];
+        const int na = a.bin_start[b + 1] - a0;
+        if (na == 0) continue;
+        const int b0 = b % nbx, b1 = (b / nbx) % nby, b2 = b / (nbx * nby);
+        int lo = 0, ncand = 0, img = 0;
+        if (lane < 27) {
+            const int c = lane;
+            int u0 = b0 + c % 3 - 1, u1 = b1 + (c / 3) % 3 - 1, u2 = b2 + c / 9 - 1;
+            int n0 = u0 < 0 ? -1 : (u0 >= nbx ? 1 : 0);
+            int n1 = u1 < 0 ? -1 : (u1 >= nby ? 1 : 0);
+            int n2 = u2 < 0 ? -1 : (u2 >= nbz ? 1 : 0);
+            int w = (u0 - n0 * nbx) + nbx * ((u1 - n1 * nby) + nby * (u2 - n2 * nbz));
+            lo = a.bin_start[w];
+            ncand = a.bin_start[w + 1] - lo;
+            img = (n0 + 1) | ((n1 + 1) << 2) | ((n2 + 1) << 4);
+        }
+        int incl = ncand;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        s_pre[wib][lane] = incl - ncand;
+        s_lo[wib][lane] = lo;
+        s_img[wib][lane] = img;
+        for (int g0 = 0; g0 < na; g0 += 32) {
+            const int ng = min(32, na - g0);
+            __syncwarp();  // the previous group's atoms are no longer read
+            if (lane < ng) {
+                const int i = a.bin_atoms[a0 + g0 + lane];
+                float4 p = a.p32[i];
+                p.w = __int_as_float((i << 3) | a.elem[i]);
+                s_at[wib][lane] = p;
+            }
+            __syncwarp();
+            int mycnt = 0;  // lane q: entries so far of the group's atom q
+            int c = 0, cpre = 0, cnext = s_pre[wib][1], clo = s_lo[wib][0], cimg = s_img[wib][0];
+            for (int t0 = 0; t0 < total; t0 += 32) {
+                const int t = t0 + lane;
+                const bool valid = t < total;
+                int j = -1, ej = 0, im = 21;
+                float qx = 0.f, qy = 0.f, qz = 0.f;  // candidate minus its bin-step offset
+                if (valid) {
+                    while (t >= cnext) {
+                        c++;
+                        cpre = cnext;
+                        cnext = c < 26 ? s_pre[wib][c + 1] : total;
+                        clo = s_lo[wib][c];
+                        cimg = s_img[wib][c];
+                    }
+                    j = a.bin_atoms[clo + (t - cpre)];
+                    const float4 pj = a.p32[j];
+                    const float4 o = off[c];
+                    ej = a.elem[j];
+                    im = cimg;
+                    qx = pj.x - o.x;
+                    qy = pj.y - o.y;
+                    qz = pj.z - o.z;
+                }
+                const int ent = valid ? (j << kEntryShift) | (ej << 5) | c : 0;
+                for (int q = 0; q < ng; q++) {
+                    const float4 pq = s_at[wib][q];
+                    const int iw = __float_as_int(pq.w);
+                    const int i = iw >> 3;
+                    bool keep = false;
+                    if (valid && !(im == 21 && j == i)) {
+                        float dx, dy, dz;
+                        if (ORTHO) {
+                            dx = (pq.x - qx) * G0;
+                            dy = (pq.y - qy) * G1;
+                            dz = (pq.z - qz) * G2;
+                        } else {
+                            frame_to_cart(a.fr, pq.x - qx, pq.y - qy, pq.z - qz, dx, dy, dz);
+                        }
+                        const float r2 = dx * dx + (dy * dy + dz * dz);
+                        const int pe = (iw & 7) * a.ne + ej;
+                        if (r2 < s_lo2[pe])
+                            keep = true;
+                        else if (r2 <= s_hi2[pe])
+                            keep = exact_keep(a, h6, a.x[i], a.x[n + i], a.x[2 * n + i], j, im, pe);
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, keep);
+                    if (m) {
+                        const int cnt = __shfl_sync(0xffffffffu, mycnt, q);
+                        if (keep) {
+                            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                            if (pos < a.maxnbr) a.nbr[(size_t)i * a.maxnbr + pos] = ent;
+                        }
+                        if (lane == q) mycnt = cnt + __popc(m);
+                    }
+                }
+            }
+            if (lane < ng) {
+                const int i = __float_as_int(s_at[wib][lane].w) >> 3;
+                a.nnbr[i] = min(mycnt, a.maxnbr);
+                if (mycnt > a.maxnbr) overflow = 1;
+                maxrow = max(maxrow, mycnt);
+                sumrow += mycnt;
+                a.x0[i] = a.x[i];
+                a.x0[n + i] = a.x[n + i];
+                a.x0[2 * n + i] = a.x[2 * n + i];
+            }
+        }
+        __syncwarp();  // the stencil table is rewritten for the next bin
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        maxrow = max(maxrow, __shfl_xor_sync(0xffffffffu, maxrow, o));
+        overflow |= __shfl_xor_sync(0xffffffffu, overflow, o);
+        sumrow += __shfl_xor_sync(0xffffffffu, sumrow, o);
     }
     if (lane == 0) {
         if (overflow) sc->overflow = 1;
@@ -710,7 +871,11 @@ void launch_rebuild_chain(mappg_sys* s) {
         k_build_list<true><<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
         k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->ncell);
     } else {
-        k_build_list<false><<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
+        const int gbins = grid_for(s, (long long)s->nbins * 32, B);
+        if (s->frame.ortho)
+            k_build_bins<true><<<gbins, B, 0, s->stream>>>(a, s->sc);
+        else
+            k_build_bins<false><<<gbins, B, 0, s->stream>>>(a, s->sc);
         k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
     }
     MAPPG_CUDA(cudaGetLastError());

@@ -141,12 +141,31 @@ def test_md_api_x_dof(potentials, cell):
     assert np.any(a.f[~d] != 0.0)
 
 
+def test_mixed_nvt_with_frozen_components(potentials, cell):
+    """The mixed-precision step kernels take the same dof branches: the run
+    follows the FP64 one within the mixed-precision budget, and frozen
+    components keep their velocity exactly."""
+    d = dof_mask(cell.natoms)
+    v = O.create_temp_dof(cell.elem, cell.masses, d, 600.0, synth.KB, 77, np.full((cell.natoms, 3), 1e-3))
+    runs = {}
+    for prec in (_lib.FP64, _lib.MIXED):
+        s, _ = pair(potentials, cell, d, prec)
+        s.set_v(v)
+        th, eta = s.nvt_run(600.0, synth.FS, synth.KB, 60, t_relax=20 * synth.FS, thermo=True)
+        runs[prec] = (s.get_x(), s.get_v(), th)
+    x64, v64, th64 = runs[_lib.FP64]
+    x32, v32, th32 = runs[_lib.MIXED]
+    assert np.all(v32[~d] == 1e-3)
+    dx = x32 - x64
+    dx -= np.round(dx @ np.linalg.inv(cell.H)) @ cell.H
+    assert np.max(np.abs(dx)) < 1e-5
+    assert np.max(np.abs(v32 - v64)) < 1e-5
+    assert np.max(np.abs(th32[:, 1] - th64[:, 1])) < 1e-4 * np.max(th64[:, 1])
+    assert np.max(np.abs(th32[:, 0] - th64[:, 0])) / cell.natoms < 1e-6
+
+
 def test_paths_without_x_dof_refuse_it(potentials, cell):
     d = dof_mask(cell.natoms)
-    s, _ = pair(potentials, cell, d, _lib.MIXED)
-    s.set_v(cell.v)
-    with pytest.raises(_lib.MappgError, match="x_dof"):
-        s.nvt_run(600.0, synth.FS, synth.KB, 5)
     t, _ = pair(potentials, cell, d)
     t.set_v(cell.v)
     S = np.full((3, 3), np.nan)
