@@ -106,6 +106,7 @@ void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) 
     s->cell_begin.assign(ncell + 1, 0);
     double band = 0.0;
     int bins = 0;
+    bool all_ortho = true;
     for (int c = 0; c < ncell; c++) {
         sys_set_box(s, H + 9 * (size_t)c);
         CellGeo& g = s->cells[c];
@@ -123,6 +124,7 @@ void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) 
         for (int d = 0; d < 3; d++) g.nb[d] = s->nb[d];
         g.bin_base = bins;
         g.ortho = s->frame.ortho;
+        all_ortho = all_ortho && g.ortho != 0;
         bins += s->nbins;
         band = std::max(band, s->band);
         s->cell_begin[c + 1] = s->cell_begin[c] + natoms[c];
@@ -132,6 +134,7 @@ void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) 
     sys_set_box(s, H);  // cell 0
     s->nbins = bins;
     s->band = band;
+    s->cells_ortho = all_ortho;
     // chunks of at most kChunk atoms, never across cells
     s->chunk_begin_h.clear();
     s->cell_chunk_h.assign(ncell + 1, 0);
@@ -393,7 +396,6 @@ struct BuildArgs {
     Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
     double cut_sk_sq[kMaxElem * kMaxElem];
-    float prune2f;         // above this squared gap (A^2) a stencil bin holds no neighbour
     const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
     const int* cell_of;
 };
@@ -434,162 +436,17 @@ __device__ __forceinline__ bool exact_keep(const BuildArgs& a, const double* h6,
     return rsq < a.cut_sk_sq[pe];
 }
 
-// rebuild step 5: one warp per atom walks the 27 bins around it; lanes test
-// candidates, ballots keep the row in (bin step, bin order) order; x0 <- x
-// (blocks of 256 threads: eight warps, one per-warp bin table each)
-template <bool BATCH>
-__global__ void __launch_bounds__(256) k_build_list(BuildArgs a, DevScalars* sc) {
-    if (!sc->rebuild) return;
-    __shared__ float4 off[27];
-    __shared__ int s_pre[8][32], s_lo[8][32], s_img[8][32];  // per warp: the atom's 27 stencil bins
-    if (threadIdx.x < 27)
-        off[threadIdx.x] = make_float4(a.fr.off[threadIdx.x][0], a.fr.off[threadIdx.x][1], a.fr.off[threadIdx.x][2], 0.f);
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int n = a.n;
-    int maxrow = 0;
-    long long sumrow = 0;
-    int overflow = 0;
-    for (int i = warp; i < n; i += nw) {
-        // the atom's cell: its bins, frame and box (the system's for one cell)
-        const CellGeo* cg = BATCH ? a.cells + a.cell_of[i] : nullptr;
-        const int nbx = BATCH ? cg->nb[0] : a.g.nb[0], nby = BATCH ? cg->nb[1] : a.g.nb[1],
-                  nbz = BATCH ? cg->nb[2] : a.g.nb[2];
-        const int bin_base = BATCH ? cg->bin_base : 0;
-        double h6[6];  // in registers: taking the address of a kernel argument would copy it to local memory
-#pragma unroll
-        for (int k = 0; k < 6; k++) h6[k] = BATCH ? cg->h6[k] : a.g.h6[k];
-        float4 pi = a.p32[i];
-        int ei = a.elem[i];
-        int bc = a.binc[i];
-        int bi[3] = {bc & 1023, (bc >> 10) & 1023, (bc >> 20) & 1023};
-        double xi0 = a.x[i], xi1 = a.x[n + i], xi2 = a.x[2 * n + i];
-        int cnt = 0;
-        int* row = a.nbr + (size_t)i * a.maxnbr;
-        // the 27 stencil bins at once, lane c for bin step c: the candidates
-        // of all bins form one sequence (bin step, then bin order) that the
-        // warp walks 32 at a time, so lanes stay busy across bin borders
-        int lo = 0, ncand = 0, img = 0;
-        const bool ortho = BATCH ? cg->ortho != 0 : a.fr.ortho != 0;
-        if (lane < 27) {
-            const int c = lane;
-            int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
-            int u0 = bi[0] + d0, u1 = bi[1] + d1, u2 = bi[2] + d2;
-            int n0 = u0 < 0 ? -1 : (u0 >= nbx ? 1 : 0);
-            int n1 = u1 < 0 ? -1 : (u1 >= nby ? 1 : 0);
-            int n2 = u2 < 0 ? -1 : (u2 >= nbz ? 1 : 0);
-            int w0 = u0 - n0 * nbx, w1 = u1 - n1 * nby, w2 = u2 - n2 * nbz;
-            int b = bin_base + w0 + nbx * (w1 + nby * w2);
-            lo = a.bin_start[b];
-            ncand = a.bin_start[b + 1] - lo;
-            img = (n0 + 1) | ((n1 + 1) << 2) | ((n2 + 1) << 4);
-            if (ortho) {
-                // the gap between atom i and the stencil bin: a bin farther
-                // than cutoff + skin holds no neighbour, so it is skipped
-                // (the kept entries and their order are unchanged).  FP32 on
-                // the bin-relative position (0..8 per axis) and the frame's
-                // Cartesian scale; prune2f carries a margin far above the
-                // rounding of either, so a bin is only ever kept in doubt
-                const int dd[3] = {d0, d1, d2};
-                const float pa[3] = {pi.x, pi.y, pi.z};
-                float g2 = 0.f;
-#pragma unroll
-                for (int ax = 0; ax < 3; ax++) {
-                    if (dd[ax] == 0) continue;
-                    const float w = BATCH ? cg->G[ax][ax] : a.fr.G[ax][ax];
-                    const float u = fmaxf(dd[ax] > 0 ? kBinW - pa[ax] : pa[ax], 0.f);
-                    const float gap = u * w;
-                    g2 = fmaf(gap, gap, g2);
-                }
-                if (g2 > a.prune2f) ncand = 0;
-            }
-        }
-        int incl = ncand;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        s_pre[wib][lane] = incl - ncand;
-        s_lo[wib][lane] = lo;
-        s_img[wib][lane] = img;
-        __syncwarp();
-        // each lane's cursor into the bin sequence: candidate t lies in bin
-        // step c with pre[c] <= t < pre[c+1]; t grows by 32 per pass, so the
-        // cursor moves forward a bin or two at a time
-        int c = 0, cpre = 0, cnext = s_pre[wib][1], clo = s_lo[wib][0], cimg = s_img[wib][0];
-        for (int t0 = 0; t0 < total; t0 += 32) {
-            const int t = t0 + lane;
-            bool keep = false;
-            int j = 0, ej = 0;
-            if (t < total) {
-                while (t >= cnext) {
-                    c++;
-                    cpre = cnext;
-                    cnext = c < 26 ? s_pre[wib][c + 1] : total;
-                    clo = s_lo[wib][c];
-                    cimg = s_img[wib][c];
-                }
-                const int k = clo + (t - cpre);
-                const int im = cimg;
-                const float4 o = off[c];
-                const bool self_img = im == 21;  // no image shift
-                j = a.bin_atoms[k];
-                if (!(self_img && j == i)) {
-                    float4 pj = a.p32[j];
-                    ej = a.elem[j];
-                    float dx, dy, dz;
-                    if (BATCH)
-                        frame_to_cart(*cg, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
-                                      dz);
-                    else
-                        frame_to_cart(a.fr, (pi.x - pj.x) + o.x, (pi.y - pj.y) + o.y, (pi.z - pj.z) + o.z, dx, dy,
-                                      dz);
-                    float r2 = dx * dx + (dy * dy + dz * dz);
-                    int pe = ei * a.ne + ej;
-                    if (r2 < a.lo2[pe]) {
-                        keep = true;
-                    } else if (r2 <= a.hi2[pe]) {
-                        keep = exact_keep(a, h6, xi0, xi1, xi2, j, im, pe);
-                    }
-                }
-            }
-            unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) {
-                int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                if (pos < a.maxnbr) row[pos] = (j << kEntryShift) | (ej << 5) | c;
-            }
-            cnt += __popc(m);
-        }
-        __syncwarp();  // the bin table is rewritten for the next atom
-        if (lane == 0) {
-            a.nnbr[i] = min(cnt, a.maxnbr);
-            if (cnt > a.maxnbr) overflow = 1;
-            maxrow = max(maxrow, cnt);
-            sumrow += cnt;
-        }
-        if (lane < 3) a.x0[lane * n + i] = lane == 0 ? xi0 : (lane == 1 ? xi1 : xi2);
-    }
-    if (lane == 0) {
-        if (overflow) sc->overflow = 1;
-        if (maxrow) atomicMax(&sc->maxrow, maxrow);
-        if (sumrow) atomicAdd(&sc->sumrow, (unsigned long long)sumrow);
-    }
-}
-
-// rebuild step 5 for one cell: one warp per bin.  The candidates of the
-// bin's 27-bin stencil are read 32 at a time, once for all atoms of the bin,
-// and every atom of the bin tests them in turn, so a candidate's gathers and
-// its place in the bin sequence are paid once per bin instead of once per
-// atom.  Each row gets the entries of k_build_list in the same (bin step,
-// bin order) order; stencil bins are not pruned (a pruned bin holds no
-// neighbour, so testing it changes nothing).
-template <bool ORTHO>
-__global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, DevScalars* sc) {
+// rebuild step 5: one warp per bin.  The candidates of the bin's 27-bin
+// stencil are read 32 at a time, once for all atoms of the bin, and every
+// atom of the bin tests them in turn, so a candidate's gathers and its place
+// in the bin sequence are paid once per bin instead of once per atom.  A
+// row lists its atom's neighbours in (bin step, bin order) order, bin steps
+// c = (d0+1) + 3(d1+1) + 9(d2+1); lanes test candidates and a ballot keeps
+// their order.  A batch finds the bin's cell through its first atom (the
+// bins of a cell hold only that cell's atoms).
+// ORTHO: every cell orthorhombic (one product per axis to Cartesian).
+template <bool BATCH, bool ORTHO>
+__global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevScalars* sc) {
     if (!sc->rebuild) return;
     __shared__ float4 off[27];
     __shared__ int s_pre[8][32], s_lo[8][32], s_img[8][32];  // per warp: the bin's 27 stencil bins
@@ -607,19 +464,23 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, DevScalars* sc)
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int n = a.n;
-    const int nbx = a.g.nb[0], nby = a.g.nb[1], nbz = a.g.nb[2];
-    const int nbins = nbx * nby * nbz;
-    const float G0 = a.fr.G[0][0], G1 = a.fr.G[1][1], G2 = a.fr.G[2][2];
-    double h6[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) h6[k] = a.g.h6[k];
     int maxrow = 0, overflow = 0;
     long long sumrow = 0;
     for (int b = warp; b < nbins; b += nw) {
         const int a0 = a.bin_start[b];
         const int na = a.bin_start[b + 1] - a0;
         if (na == 0) continue;
-        const int b0 = b % nbx, b1 = (b / nbx) % nby, b2 = b / (nbx * nby);
+        const CellGeo* cg = BATCH ? a.cells + a.cell_of[a.bin_atoms[a0]] : nullptr;
+        const int nbx = BATCH ? cg->nb[0] : a.g.nb[0], nby = BATCH ? cg->nb[1] : a.g.nb[1],
+                  nbz = BATCH ? cg->nb[2] : a.g.nb[2];
+        const int bin_base = BATCH ? cg->bin_base : 0;
+        const float G0 = BATCH ? cg->G[0][0] : a.fr.G[0][0], G1 = BATCH ? cg->G[1][1] : a.fr.G[1][1],
+                    G2 = BATCH ? cg->G[2][2] : a.fr.G[2][2];
+        double h6[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) h6[k] = BATCH ? cg->h6[k] : a.g.h6[k];
+        const int bl = b - bin_base;
+        const int b0 = bl % nbx, b1 = (bl / nbx) % nby, b2 = bl / (nbx * nby);
         int lo = 0, ncand = 0, img = 0;
         if (lane < 27) {
             const int c = lane;
@@ -627,7 +488,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, DevScalars* sc)
             int n0 = u0 < 0 ? -1 : (u0 >= nbx ? 1 : 0);
             int n1 = u1 < 0 ? -1 : (u1 >= nby ? 1 : 0);
             int n2 = u2 < 0 ? -1 : (u2 >= nbz ? 1 : 0);
-            int w = (u0 - n0 * nbx) + nbx * ((u1 - n1 * nby) + nby * (u2 - n2 * nbz));
+            int w = bin_base + (u0 - n0 * nbx) + nbx * ((u1 - n1 * nby) + nby * (u2 - n2 * nbz));
             lo = a.bin_start[w];
             ncand = a.bin_start[w + 1] - lo;
             img = (n0 + 1) | ((n1 + 1) << 2) | ((n2 + 1) << 4);
@@ -688,6 +549,8 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, DevScalars* sc)
                             dx = (pq.x - qx) * G0;
                             dy = (pq.y - qy) * G1;
                             dz = (pq.z - qz) * G2;
+                        } else if (BATCH) {
+                            frame_to_cart(*cg, pq.x - qx, pq.y - qy, pq.z - qz, dx, dy, dz);
                         } else {
                             frame_to_cart(a.fr, pq.x - qx, pq.y - qy, pq.z - qz, dx, dy, dz);
                         }
@@ -853,29 +716,26 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.nnbr = s->nnbr;
     a.x0 = s->x0;
     a.g = g;
-    double maxc = 0.0;
     for (int p = 0; p < s->ne * s->ne; p++) {
         a.cut_sk_sq[p] = s->cut_sk_sq[p];
         a.lo2[p] = (float)(s->cut_sk_sq[p] - s->band);
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
-        maxc = std::max(maxc, s->cut_sk_sq[p]);
     }
-    // (cut + skin)^2 plus 1e-3 A^2 + 1e-5 relative: the FP32 gap of the
-    // builder errs by under 1e-4 A^2 (bin-relative positions to 1e-6 of a
-    // bin, sums of three squares)
-    a.prune2f = (float)(maxc * (1.0 + 1e-5) + 1e-3);
     a.fr = s->frame;
     a.cells = s->cells_dev;
     a.cell_of = s->cell_of;
+    const int gbins = grid_for(s, (long long)s->nbins * 32, B);
     if (batch) {
-        k_build_list<true><<<grid_for(s, (long long)s->n * 32, B), B, 0, s->stream>>>(a, s->sc);
+        if (s->cells_ortho)
+            k_build_bins<true, true><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+        else
+            k_build_bins<true, false><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
         k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->ncell);
     } else {
-        const int gbins = grid_for(s, (long long)s->nbins * 32, B);
         if (s->frame.ortho)
-            k_build_bins<true><<<gbins, B, 0, s->stream>>>(a, s->sc);
+            k_build_bins<false, true><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
         else
-            k_build_bins<false><<<gbins, B, 0, s->stream>>>(a, s->sc);
+            k_build_bins<false, false><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
         k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
     }
     MAPPG_CUDA(cudaGetLastError());

@@ -248,6 +248,7 @@ struct mappg_sys {
     // order) is a degree of freedom; null when every component is
     uint8_t* dof = nullptr;
     int dof_frozen[3] = {0, 0, 0};  // atoms frozen per component
+    bool cells_ortho = false;       // batch: every cell's box orthorhombic
 };
 
 namespace mappg {
