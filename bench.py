@@ -325,6 +325,7 @@ def run_c1(args, ff_path, torch):
     s.nvt_run(300.0, synth.FS, synth.KB, 5, t_relax=float("inf"))  # warm-up (graph, first launches)
     s = _lib.System(ff1, c.H, c.x, c.elem, c.masses)
     s.set_v(c.v)
+    tpa, _, _ = s.autotune()  # lanes per atom for this small FP64 system
     s.nvt_begin(300.0, synth.FS, synth.KB, 100, t_relax=float("inf"))
     st = torch.cuda.ExternalStream(s.stream())
     s.sync()
@@ -335,7 +336,8 @@ def run_c1(args, ff_path, torch):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     s.nvt_end(100)
-    out = {"workload": "4000-atom FCC 10^3, NVE 100 steps, FP64", "gpu": c.natoms * 100 / (ms / 1000.0)}
+    out = {"workload": "4000-atom FCC 10^3, NVE 100 steps, FP64", "gpu": c.natoms * 100 / (ms / 1000.0),
+           "lanes_per_atom": tpa}
     e = O.Eam.setfl(ff_path)
     masses = np.full(e.nelem, c.masses[0])  # one mass per element of the file (all atoms are A)
     for name, threads in (("oracle_1_thread", 0), ("oracle_all_threads", os.cpu_count() or 1)):

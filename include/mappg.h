@@ -243,8 +243,10 @@ int mappg_sys_sync(mappg_sys* sys);
  * neighbour entries per loop step (1 or 2, mixed kernels) of the density and
  * force kernels by timing them on this system's atoms and neighbour list;
  * the choice is kept for the system.  tpa, unroll (may be NULL) receive it,
- * ms (6 doubles, may be NULL) the density+force time of each candidate
- * (4,1) (8,1) (16,1) (4,2) (8,2) (16,2).  No counterpart in the reference. */
+ * ms (7 doubles, may be NULL) the density+force time of each candidate
+ * (4,1) (8,1) (16,1) (4,2) (8,2) (16,2) (32,1); FP64 systems try the
+ * one-entry forms only (the others stay 0).  No counterpart in the
+ * reference. */
 int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
 
 /* Enqueue one kernel launch on the system's stream without waiting, for

@@ -405,9 +405,9 @@ class System:
     def autotune(self):
         """(lanes per atom, entries per step, {(lanes, entries): ms})"""
         tpa, unroll = C.c_int(), C.c_int()
-        ms = np.zeros(6)
+        ms = np.zeros(7)
         check(load().mappg_sys_autotune(self.h, C.byref(tpa), C.byref(unroll), dptr(ms)))
-        keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2))
+        keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2), (32, 1))
         return tpa.value, unroll.value, {k: v for k, v in zip(keys, ms) if v > 0}
 
     def enqueue(self, what):

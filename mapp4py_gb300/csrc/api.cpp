@@ -515,15 +515,18 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
         if (s->run) throw Error{MAPPG_ERR_ARG, "an NVT run is in progress"};
         if (!s->built) sys_build(s);
-        const int cand[6][2] = {{4, 1}, {8, 1}, {16, 1}, {4, 2}, {8, 2}, {16, 2}};
-        const int ncand = s->precision == MAPPG_MIXED ? 6 : 3;  // the FP64 kernels have no unrolled form
+        const int cand[7][2] = {{4, 1}, {8, 1}, {16, 1}, {4, 2}, {8, 2}, {16, 2}, {32, 1}};
+        // the FP64 kernels have no unrolled form; 32 lanes per atom spread a
+        // small system's FP64 work over more of the SMs
+        const bool mixed = s->precision == MAPPG_MIXED;
         cudaEvent_t e0, e1;
         MAPPG_CUDA(cudaEventCreate(&e0));
         MAPPG_CUDA(cudaEventCreate(&e1));
         double best = 1e30;
         int best_tpa = s->tpa, best_u = s->unroll;
         try {
-            for (int c = 0; c < ncand; c++) {
+            for (int c = 0; c < 7; c++) {
+                if (!mixed && cand[c][1] != 1) continue;
                 s->tpa = cand[c][0];
                 s->unroll = cand[c][1];
                 launch_density_only(s);  // warm-up (and first-use set-up)

@@ -264,3 +264,25 @@ def test_neighbor_capacity_grows(potentials):
     o = O.System(O.Eam.setfl(path), H, x, elem, [synth.MASS], skin=0.5, pair_wise=False)
     o.init_dynamic()
     assert np.array_equal(keys(*s.neighbors()), keys(*o.neighbors()))
+
+
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_autotune_keeps_the_forces(potentials, precision):
+    """mappg_sys_autotune only picks lanes per atom and entries per step:
+    the forces after it agree with those before it (FP64 to rounding, mixed
+    within its summation-order budget)."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((5, 5, 5), xB=0.4, sigma=0.08, seed=4)
+    s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, precision=precision)
+    pe0, _ = s.force()
+    f0 = s.get_f()
+    tpa, unroll, ms = s.autotune()
+    assert tpa in (4, 8, 16, 32) and unroll in (1, 2)
+    assert (32, 1) in ms and all(v > 0 for v in ms.values())
+    if precision == _lib.FP64:
+        assert set(ms) == {(4, 1), (8, 1), (16, 1), (32, 1)}
+    pe1, _ = s.force()
+    f1 = s.get_f()
+    tol = 1e-10 if precision == _lib.FP64 else 1e-5
+    assert np.max(np.abs(f1 - f0)) <= tol * max(1.0, np.max(np.abs(f0)))
+    assert abs(pe1 - pe0) <= (1e-12 if precision == _lib.FP64 else 1e-7) * abs(pe0)
