@@ -199,6 +199,17 @@ int mappg_sys_set_dof(mappg_sys* sys, const unsigned char* dof);
 int mappg_nvt_run(mappg_sys* sys, double T, double dt, double kB, double t_relax, int L,
                   int niters, int nsteps, double* eta, double* thermo);
 
+/* MDNVT::run with the atoms' host arrays (md_nvt.cpp:383-480): x_in and
+ * v_in ([natoms][3], caller order) are uploaded, the run goes as
+ * mappg_nvt_run, and the final positions, velocities and forces are written
+ * to x_out, v_out, f_out (each may be NULL, and may be the input array).
+ * The velocity upload overlaps the list check and the opening force call;
+ * the downloads are queued together and the call returns once they are
+ * done.  Pinned host memory makes the copies asynchronous.  Single cells. */
+int mappg_nvt_run_host(mappg_sys* sys, const double* x_in, const double* v_in, double T, double dt, double kB,
+                       double t_relax, int L, int niters, int nsteps, double* eta, double* thermo, double* x_out,
+                       double* v_out, double* f_out);
+
 /* The same run in three parts, for callers that time or interleave the
  * steps: mappg_nvt_begin does MDNVT::init and the opening force call (a
  * neighbour build, then the step is captured as a CUDA graph) for a run of

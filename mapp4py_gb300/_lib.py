@@ -53,6 +53,8 @@ SIGNATURES = {
     "mappg_sys_neighbors": (C.c_int, [_VP, _I, _I, _LL]),
     "mappg_sys_stats": (C.c_int, [_VP, _LL]),
     "mappg_create_temp": (C.c_int, [C.c_int, _U8, _D, C.c_double, C.c_double, C.c_int, _D]),
+    "mappg_nvt_run_host": (C.c_int, [_VP, _D, _D, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                     C.c_int, _D, _D, _D, _D, _D]),
     "mappg_nvt_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                 _D, _D]),
     "mappg_nvt_begin": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
@@ -338,6 +340,27 @@ class System:
         th = np.zeros((nsteps + 1, 14)) if thermo else None
         check(load().mappg_nvt_run(self.h, float(T), float(dt), float(kB), float(t_relax), int(L), int(niters),
                                    int(nsteps), dptr(eta_a), dptr(th) if th is not None else None))
+        return th, eta_a
+
+    def nvt_run_host(self, x, v, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False,
+                     x_out=None, v_out=None, f_out=None):
+        """nvt_run with host arrays in and out in one call (mappg_nvt_run_host):
+        x, v (n, 3) in; x_out, v_out, f_out (n, 3) C-contiguous float64 arrays
+        written in place (None: not returned).  Returns (thermo rows, eta)."""
+        if t_relax is None:
+            t_relax = 100.0 * dt
+        eta_a = np.zeros(max(L, 1)) if eta is None else f64(eta).copy()
+        th = np.zeros((nsteps + 1, 14)) if thermo else None
+        for o in (x_out, v_out, f_out):
+            if o is not None and not (isinstance(o, np.ndarray) and o.dtype == np.float64 and o.flags.c_contiguous
+                                      and o.flags.writeable and o.size == 3 * self.n):
+                raise ValueError("outputs must be writable C-contiguous float64 arrays of shape (n, 3)")
+        check(load().mappg_nvt_run_host(self.h, dptr(f64(x, (-1, 3))), dptr(f64(v, (-1, 3))), float(T), float(dt),
+                                        float(kB), float(t_relax), int(L), int(niters), int(nsteps), dptr(eta_a),
+                                        dptr(th) if th is not None else None,
+                                        None if x_out is None else dptr(x_out),
+                                        None if v_out is None else dptr(v_out),
+                                        None if f_out is None else dptr(f_out)))
         return th, eta_a
 
     def nvt_begin(self, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False):

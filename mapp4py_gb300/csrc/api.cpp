@@ -23,6 +23,9 @@ void sys_alloc_nbr(mappg_sys* s, int maxnbr);
 void sys_free(mappg_sys* s);
 void sys_upload(mappg_sys* s, const double* host, double* dev);
 void sys_download(mappg_sys* s, const double* dev, double* host);
+void sys_upload_side(mappg_sys* s, const double* host, double* dev);
+void sys_join_side(mappg_sys* s);
+void sys_download_async(mappg_sys* s, const double* dev, double* host);
 void sys_build(mappg_sys* s);
 void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total);
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
@@ -616,6 +619,33 @@ int mappg_nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, 
         if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
         if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells runs with mappg_batch_nvt_run"};
         nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, nullptr);
+    });
+}
+
+int mappg_nvt_run_host(mappg_sys* s, const double* x_in, const double* v_in, double T, double dt, double kB,
+                       double t_relax, int L, int niters, int nsteps, double* eta, double* thermo, double* x_out,
+                       double* v_out, double* f_out) {
+    return guard([&] {
+        if (!s || !x_in || !v_in) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_ARG, "a batch of cells runs with mappg_batch_nvt_run"};
+        try {
+            sys_upload(s, x_in, s->x);
+            s->built = false;
+            sys_upload_side(s, v_in, s->v);  // joined before the run reads velocities
+            s->have_v = true;
+            nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, nullptr);
+        } catch (...) {
+            if (s->side) cudaStreamSynchronize(s->side);
+            s->v_pending = false;
+            throw;
+        }
+        if (x_out) sys_download_async(s, s->x, x_out);
+        if (v_out) sys_download_async(s, s->v, v_out);
+        if (f_out) {
+            sync_forces64(s);
+            sys_download_async(s, s->f, f_out);
+        }
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
     });
 }
 

@@ -722,6 +722,8 @@ static void run_clear(mappg_sys* s) {
 
 void nvt_free(mappg_sys* s) { run_clear(s); }
 
+void sys_join_side(mappg_sys* s);  // system.cu
+
 // runs this short launch their steps' kernels directly: capturing and
 // instantiating the step graph costs more than it saves over a few steps
 constexpr long long kGraphMinSteps = 8;
@@ -807,7 +809,6 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
         for (int k = 0; k < L; k++) eta_h[k] = eta[k];
     MAPPG_CUDA(cudaMemcpyAsync(s->sc->eta, eta_h, sizeof(double) * kMaxChain, cudaMemcpyHostToDevice, s->stream));
     k_clear_drift<<<1, 1, 0, s->stream>>>(s->sc);
-    k_mvv_init<<<g, 256, 0, s->stream>>>(a);
     // MDNVT::run builds the list at its start.  A list built for this box
     // whose atoms all stayed within half the skin of their positions at that
     // build still holds every pair within the cutoff, so the skin test
@@ -820,6 +821,10 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
         sys_build(s);
     }
     launch_force(s);
+    // the list and the opening force do not read velocities: an upload of
+    // them on the side stream (nvt_run_host) overlaps them and is joined here
+    sys_join_side(s);
+    k_mvv_init<<<g, 256, 0, s->stream>>>(a);
     k_run_begin<<<1, 1, 0, s->stream>>>(a);
     MAPPG_CUDA(cudaGetLastError());
     if (nsteps < kGraphMinSteps) return;  // nvt_steps launches the kernels itself

@@ -822,9 +822,12 @@ void sys_free(mappg_sys* s) {
                     s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
                     s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev, s->cells_dev, s->cell_of,
                     s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp, s->cmd,
-                    s->cell_out, s->dof};
+                    s->cell_out, s->dof, s->stage2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (s->ev_main) cudaEventDestroy(s->ev_main);
+    if (s->ev_side) cudaEventDestroy(s->ev_side);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -951,6 +954,39 @@ void sys_upload(mappg_sys* s, const double* host, double* dev) {
     MAPPG_CUDA(cudaMemcpyAsync(s->stage, host, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
     k_gather_aos<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, s->stage, dev);
     MAPPG_CUDA(cudaGetLastError());
+}
+
+// upload on the side stream, after the work queued on s->stream so far;
+// s->v_pending marks the target as unfinished until s->stream waits on it
+void sys_upload_side(mappg_sys* s, const double* host, double* dev) {
+    if (!s->side) {
+        MAPPG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+        MAPPG_CUDA(cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming));
+        MAPPG_CUDA(cudaEventCreateWithFlags(&s->ev_side, cudaEventDisableTiming));
+        dev_alloc((void**)&s->stage2, sizeof(double) * 3 * (size_t)s->n);
+    }
+    MAPPG_CUDA(cudaEventRecord(s->ev_main, s->stream));
+    MAPPG_CUDA(cudaStreamWaitEvent(s->side, s->ev_main, 0));
+    MAPPG_CUDA(cudaMemcpyAsync(s->stage2, host, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyHostToDevice, s->side));
+    k_gather_aos<<<grid_for(s, s->n, 256), 256, 0, s->side>>>(s->n, s->id, s->stage2, dev);
+    MAPPG_CUDA(cudaGetLastError());
+    MAPPG_CUDA(cudaEventRecord(s->ev_side, s->side));
+    s->v_pending = true;
+}
+
+// s->stream waits for the side-stream upload (if one is pending)
+void sys_join_side(mappg_sys* s) {
+    if (!s->v_pending) return;
+    MAPPG_CUDA(cudaStreamWaitEvent(s->stream, s->ev_side, 0));
+    s->v_pending = false;
+}
+
+// queue a caller-order download without waiting for it (the stage array is
+// reused in stream order by the next one)
+void sys_download_async(mappg_sys* s, const double* dev, double* host) {
+    k_scatter_aos<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->id, dev, s->stage);
+    MAPPG_CUDA(cudaGetLastError());
+    MAPPG_CUDA(cudaMemcpyAsync(host, s->stage, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
 }
 
 void sys_download(mappg_sys* s, const double* dev, double* host) {

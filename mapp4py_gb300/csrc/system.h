@@ -249,6 +249,12 @@ struct mappg_sys {
     uint8_t* dof = nullptr;
     int dof_frozen[3] = {0, 0, 0};  // atoms frozen per component
     bool cells_ortho = false;       // batch: every cell's box orthorhombic
+    // second stream for an upload that runs under other work (nvt_run_host),
+    // its staging array, and the events that order it with s->stream
+    cudaStream_t side = nullptr;
+    double* stage2 = nullptr;
+    cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+    bool v_pending = false;  // s->v is being written on `side` until ev_side
 };
 
 namespace mappg {

@@ -289,6 +289,14 @@ class export_cfg:
 _ROWS_FOR_PE = 4096
 
 
+def _inplace(a):
+    """a, when a run can write its result into it directly."""
+    if isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.flags.writeable \
+            and a.ndim == 2 and a.shape[1] == 3:
+        return a
+    return None
+
+
 def _print_thermo(th, step0, ntally, vol):
     hdr = "%8s %14s %16s %12s %12s %12s" % ("step", "T", "PE", "S[0][0]", "S[1][1]", "S[2][2]")
     print(hdr)
@@ -329,17 +337,28 @@ class nvt:
         if self._eta.shape[0] != self.L:
             self._eta = np.zeros(self.L)
         s = atoms._system()
-        s.set_x(atoms.x)
-        s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
+        v_in = atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x)
         # the per-step rows (14 doubles) also carry the last step's energy and
         # virial, which atoms.pe / S_pe take; short runs keep them even
         # without a tally instead of paying for one more force call
         rows = bool(self.ntally) or nsteps <= _ROWS_FOR_PE
         xprt = self.export
         if xprt is None:
-            th, self._eta = s.nvt_run(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L,
-                                      niters=self.niters, eta=self._eta, thermo=rows)
+            # one call: x, v in, the run, x, v, f out (the arrays refilled in
+            # place when they have the right form)
+            x_out = _inplace(atoms.x)
+            v_out = _inplace(atoms.x_d) if atoms.x_d is not None else None
+            x_out = x_out if x_out is not None else np.empty_like(atoms.x, dtype=np.float64)
+            v_out = v_out if v_out is not None else np.empty((atoms.natms, 3))
+            f_out = atoms._f_out()
+            f_out = f_out if f_out is not None else np.empty((atoms.natms, 3))
+            th, self._eta = s.nvt_run_host(atoms.x, v_in, self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax,
+                                           L=self.L, niters=self.niters, eta=self._eta, thermo=rows, x_out=x_out,
+                                           v_out=v_out, f_out=f_out)
+            atoms.x, atoms.x_d, atoms.f = x_out, v_out, f_out
         else:
+            s.set_x(atoms.x)
+            s.set_v(v_in)
             # MDNVT::run's exports (md_nvt.cpp:390,436,470): the run goes on
             # the device in nevery-step pieces, each export is a snapshot
             s.nvt_begin(self.T, self.dt, atoms.kB, nsteps, t_relax=self.t_relax, L=self.L, niters=self.niters,
@@ -359,11 +378,11 @@ class nvt:
                         snap(atoms.step + done)
             finally:
                 th, self._eta = s.nvt_end()
-        s.get_x(atoms.x)
-        if atoms.x_d is None:
-            atoms.x_d = np.zeros_like(atoms.x)
-        s.get_v(atoms.x_d)
-        atoms.f = s.get_f(atoms._f_out())
+            s.get_x(atoms.x)
+            if atoms.x_d is None:
+                atoms.x_d = np.zeros_like(atoms.x)
+            s.get_v(atoms.x_d)
+            atoms.f = s.get_f(atoms._f_out())
         if th is not None:
             if self.ntally:
                 _print_thermo(th, atoms.step, self.ntally, atoms.vol)

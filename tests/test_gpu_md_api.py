@@ -201,3 +201,37 @@ def test_short_runs_without_step_graph(setfl, precision):
     for _ in range(3):
         one.run(c, 1)
     assert c.step == 3 and np.all(np.isfinite(c.x)) and np.isfinite(c.pe)
+
+
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_nvt_run_host_matches_separate_calls(setfl, precision):
+    """mappg_nvt_run_host (x, v in; run; x, v, f out in one call, the
+    velocity upload on a second stream) gives the bits of set_x, set_v,
+    nvt_run, get_x, get_v, get_f; outputs may alias the inputs."""
+    c = synth.alloy((5, 5, 5), xB=0.5, sigma=0.05, T=600.0, seed=8)
+    ff = _lib.ForceField.setfl(setfl, ["A", "B"])
+    runs = []
+    for one_call in (False, True):
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=precision)
+        for _ in range(2):  # a second run reuses the list and the side stream
+            x = c.x.copy()
+            v = c.v.copy()
+            if one_call:
+                f = np.empty_like(x)
+                th, eta = s.nvt_run_host(x, v, 600.0, synth.FS, synth.KB, 12, thermo=True, x_out=x, v_out=v,
+                                         f_out=f)
+            else:
+                s.set_x(x)
+                s.set_v(v)
+                th, eta = s.nvt_run(600.0, synth.FS, synth.KB, 12, thermo=True)
+                x, v, f = s.get_x(), s.get_v(), s.get_f()
+        runs.append((x, v, f, th, eta))
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+    with pytest.raises(ValueError):
+        s.nvt_run_host(c.x, c.v, 600.0, synth.FS, synth.KB, 1, x_out=np.empty((3, 3)))
+    with pytest.raises(_lib.MappgError):
+        s.nvt_run_host(c.x, c.v, -1.0, synth.FS, synth.KB, 1)
+    # the system stays usable after the refused run
+    th, _ = s.nvt_run_host(c.x, c.v, 600.0, synth.FS, synth.KB, 2, thermo=True)
+    assert np.all(np.isfinite(th))
