@@ -156,10 +156,13 @@ __device__ __forceinline__ CellFrame cell_frame(const CellGeo* g) {
     return f;
 }
 
-// one atom's density row (TPA lanes), its embedding terms and q32 record
-template <int TPA, bool ORTHO, int U, class FR>
+// one atom's density row (TPA lanes), its embedding terms and q32 record;
+// SM: the density records of knots from a.rho_mlo on come from the
+// shared-memory copy stab (k_density32s), lower knots from global memory
+template <int TPA, bool ORTHO, int U, class FR, bool SM = false>
 __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
-                                             int i, int lane, bool active, float& es, float& ec) {
+                                             int i, int lane, bool active, float& es, float& ec,
+                                             const float4* stab = nullptr) {
     float acc = 0.f;
     int ei = 0;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -180,7 +183,12 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
                 const float r = rsq * inv_sqrt(rsq);
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
-                const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
+                float4 c;
+                const int ms = m - a.rho_mlo;
+                if (SM && ms >= 0)
+                    c = stab[(a.rho_ei ? ej * a.ne + ei : ej) * a.rho_w + ms];
+                else
+                    c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
                 acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
             }
         };
@@ -228,6 +236,43 @@ __global__ void __launch_bounds__(256) k_density32(EamArgs a) {
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
         density_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec);
+    }
+    double v[1] = {(double)es - (double)ec};
+    if (block_partials<1>(v, a.partials, 0, &a.sc->counter[1]) && threadIdx.x < 32) {
+        double tot[1];
+        final_sums<1>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            a.sc->e_embed = tot[0];
+            a.sc->counter[1] = 0;
+        }
+    }
+}
+
+// k_density32 with the density tables in shared memory: one 1024-thread
+// block per SM copies the knots rho_mlo.. of every density table (94 KB)
+// and reads its spline records there instead of through L1; pairs closer
+// than the first copied knot read global memory
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(1024, 1) k_density32s(EamArgs a) {
+    extern __shared__ float4 stab[];
+    const int W = a.rho_w, ntab = a.rho_ntab;
+    for (int k = threadIdx.x; k < ntab * W; k += blockDim.x) {
+        const int ts = k / W, w = k - ts * W;
+        const int gt = a.rho_ei ? ts : ts * a.ne;
+        stab[k] = __ldg(a.rho32 + (size_t)gt * a.nr + a.rho_mlo + w);
+    }
+    __shared__ Smem32 S;
+    S.fill(a);  // ends with __syncthreads
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    float es = 0.f, ec = 0.f;
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        density_atom<TPA, ORTHO, U, Frame, true>(a, S, K, a.fr, i, lane, active, es, ec, stab);
     }
     double v[1] = {(double)es - (double)ec};
     if (block_partials<1>(v, a.partials, 0, &a.sc->counter[1]) && threadIdx.x < 32) {
@@ -545,9 +590,14 @@ __global__ void k_cells_done(EamArgs a, const int* __restrict__ cell_chunk, Cell
 // loop step U); TPA and U come from the system (mappg_sys_autotune)
 template <int TPA, bool ORTHO, int U>
 static void density_t(mappg_sys* s, const EamArgs& a) {
-    static int grid = 0;
-    if (!grid) grid = occupancy_grid(s, k_density32<TPA, ORTHO, U>, 256);
-    k_density32<TPA, ORTHO, U><<<grid, 256, 0, s->stream>>>(a);
+    static bool attr = false;
+    if (!attr) {
+        MAPPG_CUDA(cudaFuncSetAttribute(k_density32s<TPA, ORTHO, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kDensSmemBytes));
+        attr = true;
+    }
+    const size_t bytes = sizeof(float4) * (size_t)a.rho_ntab * a.rho_w;
+    k_density32s<TPA, ORTHO, U><<<s->sm_count, 1024, bytes, s->stream>>>(a);
 }
 
 template <int TPA, bool ORTHO, int U>

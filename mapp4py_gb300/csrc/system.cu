@@ -771,6 +771,9 @@ EamArgs eam_args(mappg_sys* s) {
     a.F32 = ff->dev.F32;
     a.F32lo = ff->dev.F32lo;
     a.rho_ei = ff->dev.rho_ei;
+    a.rho_ntab = a.rho_ei ? s->ne * s->ne : s->ne;
+    a.rho_w = std::min(a.nr - 1, (int)(kDensSmemBytes / (sizeof(float) * 4 * a.rho_ntab)));
+    a.rho_mlo = (a.nr - 1) - a.rho_w;  // knots up to nr - 2, the last one a pair can use
     a.dr_inv = ff->dev.dr_inv;
     a.drho_inv = ff->dev.drho_inv;
     a.rho_max = ff->dev.rho_max;

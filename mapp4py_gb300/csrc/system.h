@@ -121,6 +121,10 @@ constexpr int kChunkSlots = 16;
 constexpr int kMaxCells = 1 << 16;
 
 // arguments of the EAM kernels (passed by value)
+// shared memory given to the density tables of k_density32s: the rest of
+// the SM's 256 KB stays L1 for the neighbour-position gathers
+constexpr size_t kDensSmemBytes = 94 * 1024;
+
 struct EamArgs {
     int n, maxnbr, ne, nr, nrho;
     const int* nbr;
@@ -139,6 +143,9 @@ struct EamArgs {
     const float4* F32;
     const float* F32lo;
     int rho_ei;              // 0: rho_{j->i} depends on e_j only (setfl, funcfl), read row e_j*ne
+    // density tables held in shared memory by k_density32s: knots
+    // rho_mlo .. rho_mlo + rho_w - 1 of each of rho_ntab tables
+    int rho_mlo, rho_w, rho_ntab;
     int cut_uniform;         // every pair type has the same cutoff
     double dr_inv, drho_inv, rho_max;
     double cut_sq[kMaxElem * kMaxElem];
