@@ -233,8 +233,8 @@ int mappg_nvt_end(mappg_sys* sys, double* eta, double* thermo);
  * runs (in/out): V_H (9, the box velocity), eta (L), eta_S (L_S).  thermo
  * (NULL to skip): (nsteps+1) rows of 23 doubles: pe, T, mvv (6), F_H (6),
  * H (9).  The box moves every step and the neighbour list is rebuilt for it
- * each step; FP64 systems only.  Positions, velocities and the box are read
- * back with mappg_sys_get_x/get_v/get_box. */
+ * each step; mixed-precision systems take the FP32 force passes.  Positions,
+ * velocities and the box are read back with mappg_sys_get_x/get_v/get_box. */
 int mappg_nst_run(mappg_sys* sys, const double* S, const double* tau, double T, double dt, double kB, double t_relax,
                   int L, int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps, double* V_H,
                   double* eta, double* eta_S, double* thermo);

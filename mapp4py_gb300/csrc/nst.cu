@@ -11,7 +11,10 @@
 // per step brings back the kinetic tensor, the energy and the virial.  As the
 // box changes each step, the neighbour list is rebuilt for the new box at
 // every step (the reference rebuilds only past the skin; the forces are the
-// same while no pair crosses the cutoff unseen).  FP64 systems only.
+// same while no pair crosses the cutoff unseen).  In mixed precision the
+// density and force passes are the FP32 kernels, whose forces are converted
+// into the FP64 array that the per-atom updates read; the state, the box
+// algebra and the chains stay FP64.
 #include <math.h>
 #include <string.h>
 
@@ -314,7 +317,6 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
              int niters, double t_relax_S, int L_S, int niters_S, int nreset, int nsteps, double* V_H, double* eta,
              double* eta_S, double* thermo) {
     if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "NST runs on a single cell"};
-    if (s->precision != MAPPG_FP64) throw Error{MAPPG_ERR_UNSUPP, "NST runs in FP64 (create the system with MAPPG_FP64)"};
     if (!(kB == kB)) throw Error{MAPPG_ERR_ARG, "boltzmann constant should be set prior to MD"};
     if (!(T > 0.0) || !(dt > 0.0)) throw Error{MAPPG_ERR_ARG, "T and dt must be positive"};
     if (L < 1 || L > kMaxChain || L_S < 1 || L_S > kMaxChain) throw Error{MAPPG_ERR_ARG, "L must be in 1..16"};
@@ -443,6 +445,7 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
     MAPPG_CUDA(cudaGetLastError());
     sys_build(s);
     launch_force(s);
+    sync_forces64(s);  // mixed precision: the FP32 forces as the FP64 array the updates read
     read_force(true);
     q.T_part = (q.mvv[0] + (q.mvv[3] + q.mvv[5])) / (q.ndof_part * kB);
     thermo_row();
@@ -488,6 +491,7 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
         set_box(Hn);
         sys_build(s);
         launch_force(s);
+        sync_forces64(s);
         k_nst_v<<<grid, 256, 0, st>>>(a);
         MAPPG_CUDA(cudaGetLastError());
         read_force(true);

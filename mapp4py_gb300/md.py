@@ -8,7 +8,7 @@ Names, arguments and defaults follow the reference's Python types:
   md.nvt(T, dt)        MDNVT (md_nvt.cpp:14-26,493-881): t_relax=100*dt, L=3,
                        niters=1, ntally=10000, run(atoms, nsteps)
   md.nst(S, T, dt)     MDNST (md_nst.cpp:10-38,374-450): as md.nvt plus S, tau,
-                       t_relax_s, nreset; moves the box (FP64 systems)
+                       t_relax_s, nreset; moves the box
   md.min_lbfgs(...)    MinLBFGS (min_l-bfgs.cpp:69-127): m=2, e_tol=sqrt(eps),
                        affine=False, max_dx=1.0, ls=ls_bt(); run(atoms, max_nsteps)
   ls_bt()              LineSearchBackTrack (ls.cpp:456-461): c=0.4, rho=0.5,
@@ -413,7 +413,7 @@ class nst(nvt):
     of md.nvt and a box chain (t_relax_s, default 1000 dt); S is the applied
     stress, NaN (or None) where the box entry stays fixed; tau the box
     relaxation times (default 1000 dt); nreset renews the reference box every
-    nreset steps (0: never).  FP64 systems only."""
+    nreset steps (0: never)."""
 
     def __init__(self, S, T, dt):
         super().__init__(T, dt)
@@ -433,8 +433,6 @@ class nst(nvt):
             raise TypeError("cannot start md without governing equations (force field)")
         if math.isnan(atoms.kB):
             raise TypeError("boltzmann constant should be set prior to MD")
-        if atoms.precision != "fp64":
-            raise TypeError("md.nst runs in FP64 (atoms.precision = 'fp64')")
         if self.export is not None:
             raise TypeError("exports during md.nst runs are not available; export before and after the run")
         if self._eta.shape[0] != self.L:
