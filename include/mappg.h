@@ -328,8 +328,11 @@ int mappg_sys_get_box(mappg_sys* sys, double* H);
  * iterations done; the system's positions and forces are then that
  * iteration's and may be read from it (mappg_sys_get_x/get_f).  This is
  * where the reference writes its periodic export (ExportHandler::print,
- * min.h:216-220).  A non-zero return stops the run with MAPPG_ERR_ARG.
- * hook NULL or nevery <= 0 removes it. */
+ * min.h:216-220).  mappg_nst_run calls it after every nevery-th step and
+ * after its last step, with positions, velocities (before the run's final
+ * velocity scale), forces and box of that step (MDNST::run's exports).  A
+ * non-zero return stops the run with MAPPG_ERR_ARG.  hook NULL or
+ * nevery <= 0 removes it. */
 int mappg_sys_set_hook(mappg_sys* sys, int (*hook)(void* user, long long iteration), void* user, int nevery);
 
 /* The exchange-energy hooks of ForceFieldMD that grand-canonical Monte Carlo

@@ -490,10 +490,10 @@ class System:
         eta = np.zeros(L) if eta is None else f64(eta).copy()
         eta_S = np.zeros(L_S) if eta_S is None else f64(eta_S).copy()
         th = np.zeros((nsteps + 1, 23)) if thermo else None
-        check(load().mappg_nst_run(self.h, dptr(S), dptr(tau), float(T), float(dt), float(kB), float(t_relax),
-                                   int(L), int(niters), float(t_relax_S), int(L_S), int(niters_S), int(nreset),
-                                   int(nsteps), dptr(V_H), dptr(eta), dptr(eta_S),
-                                   dptr(th) if th is not None else None))
+        self._checked(load().mappg_nst_run(self.h, dptr(S), dptr(tau), float(T), float(dt), float(kB),
+                                           float(t_relax), int(L), int(niters), float(t_relax_S), int(L_S),
+                                           int(niters_S), int(nreset), int(nsteps), dptr(V_H), dptr(eta),
+                                           dptr(eta_S), dptr(th) if th is not None else None))
         return th, V_H, eta, eta_S
 
     def set_dof(self, dof):

@@ -292,7 +292,7 @@ void iteration_hook(mappg_sys* s, int istep) {
     if (!s->hook || s->hook_every <= 0 || (istep + 1) % s->hook_every != 0) return;
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
     if (s->hook(s->hook_user, (long long)istep + 1) != 0)
-        throw Error{MAPPG_ERR_ARG, "the iteration hook stopped the minimization"};
+        throw Error{MAPPG_ERR_ARG, "the iteration hook stopped the run"};
 }
 
 // The minimizers' line-search function (MinMDHandler::F and F_reset,

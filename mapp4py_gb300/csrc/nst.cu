@@ -506,6 +506,14 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
             q.vol_ref = s->box.vol;
         }
         thermo_row();
+        // MDNST::run's exports (md_nst.cpp:374-450): the host hook after every
+        // hook_every-th step and after the last one, before the final
+        // velocity scale, as md.nvt's snapshots
+        if (s->hook && s->hook_every > 0 && ((istep + 1) % s->hook_every == 0 || istep + 1 == nsteps)) {
+            MAPPG_CUDA(cudaStreamSynchronize(st));
+            if (s->hook(s->hook_user, (long long)istep + 1) != 0)
+                throw Error{MAPPG_ERR_ARG, "the iteration hook stopped the run"};
+        }
     }
     // update_x_d_final
     k_scale<<<grid, 256, 0, st>>>(3 * n, s->v, fac_x_d);

@@ -433,17 +433,35 @@ class nst(nvt):
             raise TypeError("cannot start md without governing equations (force field)")
         if math.isnan(atoms.kB):
             raise TypeError("boltzmann constant should be set prior to MD")
-        if self.export is not None:
-            raise TypeError("exports during md.nst runs are not available; export before and after the run")
         if self._eta.shape[0] != self.L:
             self._eta = np.zeros(self.L)
         s = atoms._system()
         s.set_x(atoms.x)
         s.set_v(atoms.x_d if atoms.x_d is not None else np.zeros_like(atoms.x))
-        th, self._V_H, self._eta, self._eta_s = s.nst_run(
-            self.S, self.T, self.dt, atoms.kB, nsteps, tau=self.tau, t_relax=self.t_relax, L=self.L,
-            niters=self.niters, t_relax_S=self.t_relax_s, nreset=self.nreset, V_H=self._V_H, eta=self._eta,
-            eta_S=self._eta_s, thermo=True)
+        xprt = self.export
+        step0 = atoms.step
+        if xprt is not None:
+            # MDNST::run's exports: the start, every nevery steps and the last
+            # step (the library calls the hook after those steps)
+            f0 = None
+            if xprt._wants_f():
+                s.force()
+                f0 = s.get_f()
+            xprt._write_step(atoms, step0, atoms.x, atoms.x_d, f0)
+
+            def at(it):
+                xprt._write_step(atoms, step0 + it, s.get_x(), s.get_v(),
+                                 s.get_f() if xprt._wants_f() else None, s.get_box())
+
+            s.set_hook(at, xprt.nevery)
+        try:
+            th, self._V_H, self._eta, self._eta_s = s.nst_run(
+                self.S, self.T, self.dt, atoms.kB, nsteps, tau=self.tau, t_relax=self.t_relax, L=self.L,
+                niters=self.niters, t_relax_S=self.t_relax_s, nreset=self.nreset, V_H=self._V_H, eta=self._eta,
+                eta_S=self._eta_s, thermo=True)
+        finally:
+            if xprt is not None:
+                s.set_hook(None, 0)
         s.get_x(atoms.x)
         if atoms.x_d is None:
             atoms.x_d = np.zeros_like(atoms.x)

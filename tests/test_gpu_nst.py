@@ -93,3 +93,51 @@ def test_mixed_nst_follows_fp64(potentials):
     assert np.max(np.abs(d)) < 5e-5 and np.max(np.abs(v32 - v64)) < 5e-5
     # the box moved: the test compares a live relaxation, not a fixed box
     assert np.max(np.abs(H64 - c.H)) > 1e-3
+
+
+def test_md_nst_exports(potentials, tmp_path):
+    """md.nst with an export: files at the start, every nevery steps and at
+    the last step, each with that step's box; the run is unchanged by them."""
+    import os
+
+    path, _ = potentials[("A", "B")]
+    c = cell()
+
+    def atoms():
+        a = md.atoms(c.H, c.x, c.elem, elems=("A", "B"), masses=c.masses, x_d=c.v)
+        a.ff_eam_setfl(path)
+        a.kB = synth.KB
+        return a
+
+    def integ():
+        i = md.nst([[0.0], [None, 0.0], [None, None, 0.0]], 300.0, synth.FS)
+        i.tau = np.full((3, 3), 50 * synth.FS)
+        i.ntally = 0
+        return i
+
+    a, b = atoms(), atoms()
+    ia = integ()
+    pattern = str(tmp_path / "nst")
+    ia.export = md.export_cfg(pattern, nevery=10, extra_vecs=["x_d", "f"])
+    ia.run(a, 25)
+    integ().run(b, 25)
+    assert np.array_equal(a.x, b.x) and np.array_equal(a.H, b.H)
+    got = sorted(int(f.split(".")[-2]) for f in os.listdir(tmp_path) if f.startswith("nst."))
+    assert got == [0, 10, 20, 25]
+    last = md.atoms.import_cfg(pattern + ".%09d.cfg" % 25)
+    assert np.max(np.abs(last.H - a.H)) < 1e-9
+    d = last.x - a.x
+    d -= np.round(d @ np.linalg.inv(a.H)) @ a.H
+    assert np.max(np.abs(d)) < 1e-9
+    mid = md.atoms.import_cfg(pattern + ".%09d.cfg" % 10)
+    assert np.max(np.abs(mid.H - c.H)) > 0.0 and np.max(np.abs(mid.H - a.H)) > 0.0
+
+    class Failing(md.export_cfg):
+        def _write_step(self, atoms, step, x, x_d, f, H=None):
+            if step == 10:
+                raise RuntimeError("disk full")
+            super()._write_step(atoms, step, x, x_d, f, H)
+
+    ia.export = Failing(str(tmp_path / "fail"), nevery=5)
+    with pytest.raises(RuntimeError, match="disk full"):
+        ia.run(atoms(), 20)
