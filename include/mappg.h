@@ -184,7 +184,10 @@ int mappg_create_temp_dof(int natoms, const unsigned char* elem, const double* m
  * with its velocity, leaves the degrees of freedom and the kinetic tensor,
  * and the mean displacement is not removed along a component in which any
  * atom is frozen; mixed-precision MD takes the same branches in its FP32
- * kernels.  md.nst and batches refuse it. */
+ * kernels.  md.nst takes MDNST's handling (md_nst.cpp:259-279,374-476):
+ * frozen components leave the degrees of freedom and carry no force, and a
+ * stress along a direction in which an atom is frozen is refused.  Batches
+ * refuse a mask. */
 int mappg_sys_set_dof(mappg_sys* sys, const unsigned char* dof);
 
 /* ---------------------------------------------------------------- drivers */

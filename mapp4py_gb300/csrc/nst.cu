@@ -41,6 +41,7 @@ struct NstAtoms {
     double* v;
     const double* f;
     const uint8_t* elem;
+    const uint8_t* dof;  // x_dof bits, read by the opening kinetic tensor only (null: all free)
     double masses[kMaxElem];
     M3 M0, M1, M2, VH;
     double xi;
@@ -142,7 +143,13 @@ __global__ void k_nst_kinetic(NstAtoms a) {
     const int n = a.n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double m = a.masses[a.elem[i]];
-        const double v0 = a.v[i], v1 = a.v[n + i], v2 = a.v[2 * n + i];
+        double v0 = a.v[i], v1 = a.v[n + i], v2 = a.v[2 * n + i];
+        if (a.dof) {  // MDNVT::pre_init leaves frozen components out (md_nvt.cpp:318-330)
+            const unsigned b = a.dof[i];
+            if (!(b & 1u)) v0 = 0.0;
+            if (!(b & 2u)) v1 = 0.0;
+            if (!(b & 4u)) v2 = 0.0;
+        }
         t[0] += m * v0 * v0;
         t[1] += m * v0 * v1;
         t[2] += m * v0 * v2;
@@ -324,7 +331,6 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
     if (!(t_relax > 0.0) || !(t_relax_S > 0.0)) throw Error{MAPPG_ERR_ARG, "t_relax must be positive"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     if (!s->have_v) throw Error{MAPPG_ERR_ARG, "velocities must be set before MD"};
-    if (s->dof) throw Error{MAPPG_ERR_UNSUPP, "md.nst with frozen components (x_dof) is not supported"};
     Nst q;
     q.s = s;
     q.T = T;
@@ -332,7 +338,10 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
     q.dt2 = dt / 2.0;
     q.kB = kB;
     const int n = s->n;
-    q.ndof_part = 3 * n;
+    // x_dof: frozen components leave the degrees of freedom (MDNVT::pre_init,
+    // md_nvt.cpp:265-291); their forces are zero, and otherwise the steps
+    // treat them as MDNST::run does (update_x_d__x__x_d, update_x_d_final)
+    q.ndof_part = 3 * n - (s->dof_frozen[0] + s->dof_frozen[1] + s->dof_frozen[2]);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
             const int lo = j <= i ? 3 * i + j : 3 * j + i;
@@ -341,6 +350,17 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
             q.tau[i][j] = tau[lo];
             if (j <= i) q.VH[i][j] = V_H[3 * i + j];
         }
+    // MDNST::pre_run_chk (md_nst.cpp:259-279): no stress along a direction in
+    // which an atom is frozen
+    std::string chk;
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++)
+            if (q.S_dof[i][j] && s->dof_frozen[i]) {
+                if (!chk.empty()) chk += "\n";
+                chk += "cannot impose stress component [" + std::to_string(i) + "][" + std::to_string(j) +
+                       "] while any of the atoms do not have degree freedom in " + std::to_string(i) + " direction";
+            }
+    if (!chk.empty()) throw Error{MAPPG_ERR_ARG, chk};
     // MDNST::pre_init (md_nst.cpp:281-311)
     for (int i = 0; i < 3; i++)
         for (int j = 0; j <= i; j++) {
@@ -399,6 +419,7 @@ void nst_run(mappg_sys* s, const double* S, const double* tau, double T, double 
     a.v = s->v;
     a.f = s->f;
     a.elem = s->elem;
+    a.dof = s->dof;
     for (int e = 0; e < kMaxElem; e++) a.masses[e] = s->masses[e];
     a.part = (double*)dalloc(sizeof(double) * kRedSlots * grid);
     a.counter = (unsigned*)dalloc(sizeof(unsigned));

@@ -1468,12 +1468,18 @@ int orc_md_nst_run(void* p, const double* S, const double* tau, double T, double
                    double* V_H, double* eta, double* eta_S, double* thermo) {
     orc_sys* s = (orc_sys*)p;
     if (isnan(kB)) return fail("boltzmann constant should be set prior to MD");
-    if (s->dof) return fail("x_dof with md.nst is not restated");
     nst_t q;
     memset(&q, 0, sizeof(q));
     q.T = T; q.dt = dt; q.dt2 = dt / 2.0; q.kB = kB;
     const int n = s->natms;
-    q.ndof_part = 3 * n;
+    /* x_dof (MDNVT::pre_init md_nvt.cpp:265-291): frozen components leave
+     * the degrees of freedom; MDNST::run itself keeps the plain updates */
+    int frozen[3] = {0, 0, 0};
+    if (s->dof)
+        for (int i = 0; i < n; i++)
+            for (int c = 0; c < 3; c++)
+                if (!s->dof[3 * i + c]) frozen[c]++;
+    q.ndof_part = 3 * n - (frozen[0] + frozen[1] + frozen[2]);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
             q.S_dof[i][j] = !isnan(S[3 * i + j]);
@@ -1481,13 +1487,23 @@ int orc_md_nst_run(void* p, const double* S, const double* tau, double T, double
             q.tau[i][j] = tau[3 * i + j];
             q.V_H[i][j] = j <= i ? V_H[3 * i + j] : 0.0;
         }
+    /* MDNST::pre_run_chk md_nst.cpp:259-279 */
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++)
+            if (q.S_dof[i][j] && frozen[i])
+                return fail("cannot impose stress component while any of the atoms do not have degree freedom "
+                            "in its direction");
     nhc_t tp, tb;
     nhc_init(&tp, dt / 2.0, t_relax, L, niters);
     nhc_init(&tb, dt / 2.0, t_relax_S, L_S, niters_S);
     for (int i = 0; i < L; i++) tp.eta_d[i] = eta[i];
     for (int i = 0; i < L_S; i++) tb.eta_d[i] = eta_S[i];
-    /* MDNVT::pre_init: mvv, T_part */
-    for (int i = 0; i < n; i++) dyadic_add(s->masses[s->elem[i]], s->v + 3 * i, q.mvv);
+    /* MDNVT::pre_init: mvv (frozen components left out, md_nvt.cpp:318-330), T_part */
+    for (int i = 0; i < n; i++) {
+        double v[3];
+        for (int c = 0; c < 3; c++) v[c] = (!s->dof || s->dof[3 * i + c]) ? s->v[3 * i + c] : 0.0;
+        dyadic_add(s->masses[s->elem[i]], v, q.mvv);
+    }
     q.T_part = (q.mvv[0] + (q.mvv[3] + q.mvv[5])) / (q.ndof_part * kB);
     /* MDNST::pre_init  md_nst.cpp:281-311 */
     q.ndof_baro = 0;

@@ -168,9 +168,45 @@ def test_paths_without_x_dof_refuse_it(potentials, cell):
     d = dof_mask(cell.natoms)
     t, _ = pair(potentials, cell, d)
     t.set_v(cell.v)
-    S = np.full((3, 3), np.nan)
-    S[0, 0] = S[1, 1] = S[2, 2] = 0.0
-    with pytest.raises(_lib.MappgError, match="x_dof"):
-        t.nst_run(S, 600.0, synth.FS, synth.KB, 5)
     with pytest.raises(ValueError):
         t.set_dof(np.ones((cell.natoms + 1, 3), bool))
+
+
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_nst_with_frozen_components(potentials, precision):
+    """md.nst with x_dof against the oracle (FP64) or the FP64 GPU run
+    (mixed): frozen components leave ndof and carry no force; a stress along
+    a frozen direction is refused with the reference's message."""
+    path = potentials[("A", "B")][0]
+    c = synth.alloy((5, 5, 5), a=2.9, xB=0.3, sigma=0.02, T=300.0, seed=4)
+    d = np.ones((c.natoms, 3), bool)
+    d[::5, 2] = False
+    nan = np.nan
+    S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, nan]])
+    tau = np.full((3, 3), 50 * synth.FS)
+    o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses)
+    o.set_dof(d)
+    o.v = c.v
+    tho, VHo, _, _ = o.nst_run(S, 300.0, synth.FS, synth.KB, 30, tau=tau)
+    s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, precision=precision)
+    s.set_dof(d)
+    s.set_v(c.v)
+    th, VH, _, _ = s.nst_run(S, 300.0, synth.FS, synth.KB, 30, tau=tau)
+    assert np.all(s.get_f()[~d] == 0.0)
+    if precision == _lib.FP64:
+        assert np.max(np.abs(th[:, 0] - tho[:, 0])) <= 1e-9 * np.max(np.abs(tho[:, 0]))
+        assert np.max(np.abs(th[:, 1] - tho[:, 1])) <= 1e-8 * np.max(tho[:, 1])
+        assert np.max(np.abs(th[:, 14:] - tho[:, 14:])) < 1e-10
+        d_x = s.get_x() - o.x
+        H = s.get_box()
+        d_x -= np.round(d_x @ np.linalg.inv(H)) @ H
+        assert np.max(np.abs(d_x)) < 1e-9 and np.max(np.abs(s.get_v() - o.v)) < 1e-10
+    else:
+        assert np.max(np.abs(th[:, 0] - tho[:, 0])) / c.natoms < 1e-6
+        assert np.max(np.abs(th[:, 14:] - tho[:, 14:])) < 2e-6 * np.max(np.abs(c.H))
+    S[2, 2] = 0.0
+    t = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, precision=precision)
+    t.set_dof(d)
+    t.set_v(c.v)
+    with pytest.raises(_lib.MappgError, match=r"cannot impose stress component \[2\]\[2\]"):
+        t.nst_run(S, 300.0, synth.FS, synth.KB, 1)

@@ -315,3 +315,28 @@ def test_x_dof_forces_minimizer_and_nvt(potentials):
     mvv = np.sum(c.masses[c.elem][:, None] * vf * vf)
     assert abs(th[-1, 1] - mvv / (d.sum() * synth.KB)) < 1e-9 * th[-1, 1]
     assert np.all(np.isfinite(eta))
+
+
+def test_x_dof_with_nst(potentials):
+    """MDNST with x_dof (md_nst.cpp:259-279, md_nvt.cpp:265-330): frozen
+    components leave the degrees of freedom, carry no force, and no stress
+    may act along a direction in which an atom is frozen."""
+    path, _ = potentials[("A", "B")]
+    e = O.Eam.setfl(path)
+    c = synth.alloy((4, 4, 4), a=2.9, xB=0.3, sigma=0.02, T=300.0, seed=4)
+    d = np.ones((c.natoms, 3), bool)
+    d[::5, 2] = False
+    nan = np.nan
+    s = O.System(e, c.H, c.x, c.elem, c.masses)
+    s.set_dof(d)
+    s.v = c.v
+    S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, nan]])
+    th, VH, _, _ = s.nst_run(S, 300.0, synth.FS, synth.KB, 20, tau=np.full((3, 3), 50 * synth.FS))
+    assert np.all(np.isfinite(th)) and np.all(s.f[~d] == 0.0)
+    assert th[-1, 14 + 8] == c.H[2, 2]  # no stress along z: that box entry stays
+    S[2, 2] = 0.0
+    t = O.System(e, c.H, c.x, c.elem, c.masses)
+    t.set_dof(d)
+    t.v = c.v
+    with pytest.raises(RuntimeError, match="degree freedom"):
+        t.nst_run(S, 300.0, synth.FS, synth.KB, 1)
