@@ -385,7 +385,6 @@ struct BuildArgs {
     const double* x;
     const double* s;
     const float4* p32;
-    const int* binc;
     const uint8_t* elem;
     const int* bin_start;
     const int* bin_atoms;
@@ -708,7 +707,6 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.x = s->x;
     a.s = s->s;
     a.p32 = s->p32;
-    a.binc = s->binc;
     a.elem = s->elem;
     a.bin_start = s->bin_start;
     a.bin_atoms = s->bin_atoms;
