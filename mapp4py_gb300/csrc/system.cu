@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "system.h"
@@ -444,7 +445,8 @@ __device__ __forceinline__ bool exact_keep(const BuildArgs& a, const double* h6,
 // their order.  A batch finds the bin's cell through its first atom (the
 // bins of a cell hold only that cell's atoms).
 // ORTHO: every cell orthorhombic (one product per axis to Cartesian).
-template <bool BATCH, bool ORTHO>
+// UNI: every pair type has the same list cutoff (thresholds in registers).
+template <bool BATCH, bool ORTHO, bool UNI>
 __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevScalars* sc) {
     if (!sc->rebuild) return;
     __shared__ float4 off[27];
@@ -463,6 +465,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int n = a.n;
+    const float lo2u = a.lo2[0], hi2u = a.hi2[0];
     int maxrow = 0, overflow = 0;
     long long sumrow = 0;
     for (int b = warp; b < nbins; b += nw) {
@@ -518,6 +521,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                 const int t = t0 + lane;
                 const bool valid = t < total;
                 int j = -1, ej = 0, im = 21;
+                int selfq = -1;  // the group atom this candidate is (its own bin, no image shift)
                 float qx = 0.f, qy = 0.f, qz = 0.f;  // candidate minus its bin-step offset
                 if (valid) {
                     while (t >= cnext) {
@@ -532,6 +536,8 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                     const float4 o = off[c];
                     ej = a.elem[j];
                     im = cimg;
+                    // the bin's own atoms appear once unshifted, as bin step 13
+                    if (c == 13 && im == 21) selfq = (t - cpre) - g0;
                     qx = pj.x - o.x;
                     qy = pj.y - o.y;
                     qz = pj.z - o.z;
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                     const int iw = __float_as_int(pq.w);
                     const int i = iw >> 3;
                     bool keep = false;
-                    if (valid && !(im == 21 && j == i)) {
+                    if (valid && q != selfq) {
                         float dx, dy, dz;
                         if (ORTHO) {
                             dx = (pq.x - qx) * G0;
@@ -554,11 +560,12 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                             frame_to_cart(a.fr, pq.x - qx, pq.y - qy, pq.z - qz, dx, dy, dz);
                         }
                         const float r2 = dx * dx + (dy * dy + dz * dz);
-                        const int pe = (iw & 7) * a.ne + ej;
-                        if (r2 < s_lo2[pe])
+                        const int pe = UNI ? 0 : (iw & 7) * a.ne + ej;
+                        if (r2 < (UNI ? lo2u : s_lo2[pe]))
                             keep = true;
-                        else if (r2 <= s_hi2[pe])
-                            keep = exact_keep(a, h6, a.x[i], a.x[n + i], a.x[2 * n + i], j, im, pe);
+                        else if (r2 <= (UNI ? hi2u : s_hi2[pe]))
+                            keep = exact_keep(a, h6, a.x[i], a.x[n + i], a.x[2 * n + i], j, im,
+                                              UNI ? (iw & 7) * a.ne + ej : pe);
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
                     if (m) {
@@ -723,17 +730,29 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.cells = s->cells_dev;
     a.cell_of = s->cell_of;
     const int gbins = grid_for(s, (long long)s->nbins * 32, B);
+    bool uni = true;
+    for (int p = 1; p < s->ne * s->ne; p++) uni = uni && a.lo2[p] == a.lo2[0] && a.hi2[p] == a.hi2[0];
+    auto launch = [&](auto BT, auto OT, auto UT) {
+        k_build_bins<decltype(BT)::value, decltype(OT)::value, decltype(UT)::value>
+            <<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+    };
+    auto by_uni = [&](auto BT, auto OT) {
+        if (uni)
+            launch(BT, OT, std::true_type());
+        else
+            launch(BT, OT, std::false_type());
+    };
     if (batch) {
         if (s->cells_ortho)
-            k_build_bins<true, true><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+            by_uni(std::true_type(), std::true_type());
         else
-            k_build_bins<true, false><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+            by_uni(std::true_type(), std::false_type());
         k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->ncell);
     } else {
         if (s->frame.ortho)
-            k_build_bins<false, true><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+            by_uni(std::false_type(), std::true_type());
         else
-            k_build_bins<false, false><<<gbins, B, 0, s->stream>>>(a, s->nbins, s->sc);
+            by_uni(std::false_type(), std::false_type());
         k_rebuild_done<<<1, 1, 0, s->stream>>>(s->sc);
     }
     MAPPG_CUDA(cudaGetLastError());
