@@ -131,6 +131,7 @@ class atoms:
         self.x_dof = None  # None, or [N][3] bool: True where a component is free
         self._sys = None
         self._sys_key = None
+        self._sys_elem = None
         self._dof_set = None
 
     @property
@@ -219,17 +220,27 @@ class atoms:
         return None if d.all() else np.ascontiguousarray(d)
 
     def _key(self):
-        return (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes(), self.elem.tobytes())
+        # elem by content (compared against the copy kept with the key)
+        return (id(self.ff), self.natms, self.precision, self.skin, self.H.tobytes())
+
+    def _same_system(self):
+        return self._sys is not None and self._sys_key == self._key() and self._sys_elem is not None \
+            and self._sys_elem.shape == self.elem.shape and np.array_equal(self._sys_elem, self.elem)
 
     def _system(self):
         if self.ff is None:
             raise TypeError("cannot start without governing equations (force field)")
         key = self._key()
-        if self._sys is None or self._sys_key != key:
+        if not self._same_system():
             self._sys = None
             self._sys = _lib.System(self.ff, self.H, self.x, self.elem, self.masses, self.skin,
                                     _PREC[self.precision])
+            if self.precision == "mixed" and self.natms >= _AUTOTUNE_ATOMS:
+                # lanes per atom and entries per step of the density and force
+                # passes, timed once on this system's own list (~20 passes)
+                self._sys.autotune()
             self._sys_key = key
+            self._sys_elem = self.elem.copy()
             self._dof_set = None
         dof = self._dof()
         dkey = None if dof is None else dof.tobytes()
@@ -287,6 +298,7 @@ class export_cfg:
 
 
 _ROWS_FOR_PE = 4096
+_AUTOTUNE_ATOMS = 50000  # mixed systems from this size are autotuned when created
 
 
 def _inplace(a):
