@@ -26,6 +26,8 @@ void sys_download(mappg_sys* s, const double* dev, double* host);
 void sys_upload_side(mappg_sys* s, const double* host, double* dev);
 void sys_join_side(mappg_sys* s);
 void sys_download_async(mappg_sys* s, const double* dev, double* host);
+void nvt_run_xout(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps,
+                  double* eta, double* thermo, double* x_out);
 void sys_build(mappg_sys* s);
 void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total);
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
@@ -633,19 +635,23 @@ int mappg_nvt_run_host(mappg_sys* s, const double* x_in, const double* v_in, dou
             s->built = false;
             sys_upload_side(s, v_in, s->v);  // joined before the run reads velocities
             s->have_v = true;
-            nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, nullptr);
+            if (x_out && nsteps > 0)
+                nvt_run_xout(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, x_out);
+            else
+                nvt_run(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo, nullptr);
         } catch (...) {
             if (s->side) cudaStreamSynchronize(s->side);
             s->v_pending = false;
             throw;
         }
-        if (x_out) sys_download_async(s, s->x, x_out);
+        if (x_out && nsteps == 0) sys_download_async(s, s->x, x_out);
         if (v_out) sys_download_async(s, s->v, v_out);
         if (f_out) {
             sync_forces64(s);
             sys_download_async(s, s->f, f_out);
         }
         MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->side));  // the positions' copy
     });
 }
 

@@ -658,17 +658,20 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
     return a;
 }
 
-static void launch_step64(mappg_sys* s, const MdArgs& a) {
+// mark: record s->ev_main once the step's positions are final (after the
+// list check; the passes after it do not move the atoms)
+static void launch_step64(mappg_sys* s, const MdArgs& a, bool mark = false) {
     int g = grid_for(s, s->n, 256);
     k_step_open<<<1, 1, 0, s->stream>>>(a);
     k_kick_drift64<<<g, 256, 0, s->stream>>>(a);
     k_com_skin64<<<g, 256, 0, s->stream>>>(a);
     launch_rebuild_chain(s);
+    if (mark) MAPPG_CUDA(cudaEventRecord(s->ev_main, s->stream));
     launch_force(s);
     k_kick2_64<<<g, 256, 0, s->stream>>>(a);
 }
 
-static void launch_step32(mappg_sys* s, const MdArgs& a) {
+static void launch_step32(mappg_sys* s, const MdArgs& a, bool mark = false) {
     // streaming kernels with a last-block reduction: four blocks per SM keep
     // loads in flight and the serial tail (the fixed-order sum over block
     // partials) short
@@ -679,6 +682,7 @@ static void launch_step32(mappg_sys* s, const MdArgs& a) {
     else
         k_integrate32<false><<<g, 256, 0, s->stream>>>(a);
     launch_rebuild_chain(s);
+    if (mark) MAPPG_CUDA(cudaEventRecord(s->ev_main, s->stream));
     EamArgs e = eam_args(s);
     launch_density32(s, e);
     launch_force32(s, e);
@@ -864,6 +868,7 @@ void nvt_steps(mappg_sys* s, long long nsteps) {
 void nvt_end(mappg_sys* s, double* eta, double* thermo) {
     NvtRun* r = (NvtRun*)s->run;
     if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
+    sys_join_side(s);  // a side-stream read of the positions (nvt_run_xout) comes first
     int g = grid_for(s, 3LL * s->n, 256);
     if (s->ncell > 1) {
         k_run_end32b<<<g, 256, 0, s->stream>>>(r->a);
@@ -948,6 +953,46 @@ void nvt_snapshot(mappg_sys* s, double* x, double* v) {
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
     if (h.overflow) throw Error{MAPPG_ERR_NBR, "neighbour list capacity exceeded during the run"};
     if (h.bad) throw Error{MAPPG_ERR_NAN, "non-finite position, energy or temperature during the run"};
+}
+
+// positions in the caller's order less the mean displacement not yet
+// removed (sc->drift; zero on the FP64 path): what the run's end leaves in x
+__global__ void k_scatter_x_final(int n, const int* __restrict__ id, const double* __restrict__ x,
+                                  const DevScalars* __restrict__ sc, double* __restrict__ out) {
+    const double d0 = sc->drift[0], d1 = sc->drift[1], d2 = sc->drift[2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const size_t u = 3 * (size_t)id[i];
+        out[u] = x[i] - d0;
+        out[u + 1] = x[n + i] - d1;
+        out[u + 2] = x[2 * n + i] - d2;
+    }
+}
+
+// nvt_run whose final positions go to the host array x_out during the last
+// step: they are final once that step's list check is done, so the side
+// stream gathers them then and copies them out under the density and force
+// passes; the run's end (which removes sc->drift from x) waits for the
+// gather only.  Needs the side stream (sys_upload_side made it).
+void nvt_run_xout(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps,
+                  double* eta, double* thermo, double* x_out) {
+    nvt_begin(s, T, dt, kB, t_relax, L, niters, nsteps, eta, thermo != nullptr, nullptr);
+    NvtRun* r = (NvtRun*)s->run;
+    if (nsteps > 0) {
+        nvt_steps(s, nsteps - 1);
+        if (s->precision == MAPPG_MIXED)
+            launch_step32(s, r->a, true);
+        else
+            launch_step64(s, r->a, true);
+        r->done += 1;
+        MAPPG_CUDA(cudaStreamWaitEvent(s->side, s->ev_main, 0));
+        k_scatter_x_final<<<grid_for(s, s->n, 256), 256, 0, s->side>>>(s->n, s->id, s->x, s->sc, s->stage2);
+        MAPPG_CUDA(cudaGetLastError());
+        MAPPG_CUDA(cudaEventRecord(s->ev_side, s->side));
+        s->v_pending = true;
+        MAPPG_CUDA(cudaMemcpyAsync(x_out, s->stage2, sizeof(double) * 3 * (size_t)s->n, cudaMemcpyDeviceToHost,
+                                   s->side));
+    }
+    nvt_end(s, eta, thermo);
 }
 
 void nvt_run(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, int nsteps, double* eta,
