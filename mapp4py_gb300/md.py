@@ -360,7 +360,7 @@ class nvt:
             # place when they have the right form)
             x_out = _inplace(atoms.x)
             v_out = _inplace(atoms.x_d) if atoms.x_d is not None else None
-            x_out = x_out if x_out is not None else np.empty_like(atoms.x, dtype=np.float64)
+            x_out = x_out if x_out is not None else np.empty((atoms.natms, 3))
             v_out = v_out if v_out is not None else np.empty((atoms.natms, 3))
             f_out = atoms._f_out()
             f_out = f_out if f_out is not None else np.empty((atoms.natms, 3))

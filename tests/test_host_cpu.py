@@ -158,3 +158,60 @@ def test_create_temp_dof_matches_oracle(built):
     a.x_dof = np.ones((5, 3), bool)
     with pytest.raises(TypeError):
         a.create_temp(300.0, 1)
+
+
+class _FakeSystem:
+    """Stands in for _lib.System in md.nvt.run's host logic: records the
+    call and writes recognisable outputs."""
+
+    def __init__(self, n):
+        self.n = n
+        self.calls = []
+
+    def nvt_run_host(self, x, v, T, dt, kB, nsteps, t_relax=None, L=3, niters=1, eta=None, thermo=False,
+                     x_out=None, v_out=None, f_out=None):
+        self.calls.append(dict(x=np.array(x), v=np.array(v), nsteps=nsteps, thermo=thermo, L=L, eta=np.array(eta)))
+        x_out[:] = x + 1.0
+        v_out[:] = v * 2.0
+        f_out[:] = 3.0
+        th = np.zeros((nsteps + 1, 14))
+        th[-1, 0] = -7.5
+        th[-1, 8:14] = [1.0, 0.1, 0.2, 2.0, 0.3, 3.0]
+        return th, np.full(L, 0.25)
+
+
+def test_md_nvt_run_host_logic(monkeypatch):
+    """md.nvt.run without an export: one nvt_run_host call; the atoms'
+    arrays are refilled in place when they are C-contiguous float64 (n, 3),
+    replaced otherwise; pe and S_pe come from the last thermo row; the chain
+    state is carried; step advances."""
+    n = 6
+    H = np.diag([10.0, 11.0, 12.0])
+    x = np.arange(3 * n, dtype=np.float64).reshape(n, 3)
+    a = md.atoms(H, x, np.zeros(n, np.uint8), masses=(50.0,), x_d=np.ones((n, 3)))
+    a.kB = synth.KB
+    a.ff = object()
+    fake = _FakeSystem(n)
+    monkeypatch.setattr(a, "_system", lambda: fake)
+    x_obj, v_obj = a.x, a.x_d
+    a.f = np.zeros((n, 3))
+    f_obj = a.f
+    integ = md.nvt(300.0, synth.FS)
+    integ.ntally = 0
+    integ.run(a, 3)
+    assert len(fake.calls) == 1 and fake.calls[0]["nsteps"] == 3 and fake.calls[0]["thermo"]
+    assert a.x is x_obj and a.x_d is v_obj and a.f is f_obj  # refilled in place
+    assert np.array_equal(a.x, x + 1.0) and np.all(a.x_d == 2.0) and np.all(a.f == 3.0)
+    assert a.pe == -7.5 and a.step == 3
+    vol = 10.0 * 11.0 * 12.0
+    assert np.allclose(a.S_pe, -np.array([[1.0, 0.1, 0.2], [0.1, 2.0, 0.3], [0.2, 0.3, 3.0]]) / vol)
+    assert np.all(integ._eta == 0.25)
+    integ.run(a, 2)
+    assert np.all(fake.calls[1]["eta"] == 0.25) and a.step == 5  # the chain state carries over
+    # arrays that cannot take the result in place are replaced
+    a.x = np.asfortranarray(a.x)
+    a.x_d = a.x_d.astype(np.float32)
+    xf = a.x.copy()
+    integ.run(a, 1)
+    assert a.x.flags.c_contiguous and a.x.dtype == np.float64 and np.array_equal(a.x, xf + 1.0)
+    assert a.x_d.dtype == np.float64
