@@ -272,6 +272,9 @@ class System:
             self.h = None
 
     def _get(self, fn, out=None):
+        if out is not None and not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.flags.c_contiguous
+                                    and out.flags.writeable and out.size == 3 * self.n):
+            raise ValueError("out must be a writable C-contiguous float64 array of shape (n, 3)")
         a = np.empty((self.n, 3)) if out is None else out
         check(fn(self.h, dptr(a)))
         return a

@@ -211,6 +211,13 @@ class atoms:
             return f
         return None
 
+    def _download(self, s):
+        """x, x_d and f from the system, into the atoms' arrays when they can
+        take them in place (C-contiguous float64 (n, 3)), else new arrays"""
+        self.x = s.get_x(_inplace(self.x))
+        self.x_d = s.get_v(_inplace(self.x_d) if self.x_d is not None else None)
+        self.f = s.get_f(self._f_out())
+
     def _dof(self):
         if self.x_dof is None:
             return None
@@ -390,11 +397,7 @@ class nvt:
                         snap(atoms.step + done)
             finally:
                 th, self._eta = s.nvt_end()
-            s.get_x(atoms.x)
-            if atoms.x_d is None:
-                atoms.x_d = np.zeros_like(atoms.x)
-            s.get_v(atoms.x_d)
-            atoms.f = s.get_f(atoms._f_out())
+            atoms._download(s)
         if th is not None:
             if self.ntally:
                 _print_thermo(th, atoms.step, self.ntally, atoms.vol)
@@ -474,11 +477,7 @@ class nst(nvt):
         finally:
             if xprt is not None:
                 s.set_hook(None, 0)
-        s.get_x(atoms.x)
-        if atoms.x_d is None:
-            atoms.x_d = np.zeros_like(atoms.x)
-        s.get_v(atoms.x_d)
-        atoms.f = s.get_f(atoms._f_out())
+        atoms._download(s)
         atoms.H = s.get_box()
         atoms._sys_key = atoms._key()
         if self.ntally:
@@ -574,7 +573,7 @@ class _min:
         else:
             run = atoms_only(ls)
         s, r = _min_run(atoms, self.export, run)
-        s.get_x(atoms.x)
+        atoms.x = s.get_x(_inplace(atoms.x))
         if self._box():
             atoms.H = s.get_box()
             atoms._sys_key = atoms._key()

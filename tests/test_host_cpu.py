@@ -215,3 +215,15 @@ def test_md_nvt_run_host_logic(monkeypatch):
     integ.run(a, 1)
     assert a.x.flags.c_contiguous and a.x.dtype == np.float64 and np.array_equal(a.x, xf + 1.0)
     assert a.x_d.dtype == np.float64
+
+
+def test_system_download_targets_are_checked():
+    """System._get refuses an output array it would fill in the wrong layout
+    (no device work is reached: the check comes first)."""
+    s = _lib.System.__new__(_lib.System)
+    s.n = 4
+    s.h = None
+    for bad in (np.zeros((4, 3), np.float32), np.asfortranarray(np.zeros((4, 3))), np.zeros((5, 3)),
+                np.zeros((4, 3))[:, :2]):
+        with pytest.raises(ValueError):
+            s._get(None, bad)
