@@ -289,9 +289,9 @@ __global__ void __launch_bounds__(256) k_integrate32(MdArgs a) {
         const double u1 = ORTHO ? a.bs[3] * xv[1] : a.bs[3] * xv[1] + a.bs[4] * xv[2];
         const double u2 = a.bs[5] * xv[2];
         float4 p;
-        p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
-        p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
-        p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+        p.x = (float)(u0 - (double)(8 * (bc & 1023)));
+        p.y = (float)(u1 - (double)(8 * ((bc >> 10) & 1023)));
+        p.z = (float)(u2 - (double)(8 * ((bc >> 20) & 1023)));
         p.w = 0.f;
         a.p32[i] = p;
         const float4 q = a.p0[i];
@@ -525,9 +525,9 @@ __global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
             const double u1 = orth ? g.bs[3] * xv[1] : g.bs[3] * xv[1] + g.bs[4] * xv[2];
             const double u2 = g.bs[5] * xv[2];
             float4 p;
-            p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
-            p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
-            p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+            p.x = (float)(u0 - (double)(8 * (bc & 1023)));
+            p.y = (float)(u1 - (double)(8 * ((bc >> 10) & 1023)));
+            p.z = (float)(u2 - (double)(8 * ((bc >> 20) & 1023)));
             p.w = 0.f;
             a.p32[i] = p;
             const float4 q = a.p0[i];

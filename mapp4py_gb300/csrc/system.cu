@@ -350,9 +350,9 @@ __device__ __forceinline__ float4 frame_pos(const Geo& g, double x0, double x1, 
     double u1 = g.bs[3] * x1 + g.bs[4] * x2;
     double u2 = g.bs[5] * x2;
     float4 p;
-    p.x = (float)(u0 - 8.0 * (double)(bc & 1023));
-    p.y = (float)(u1 - 8.0 * (double)((bc >> 10) & 1023));
-    p.z = (float)(u2 - 8.0 * (double)((bc >> 20) & 1023));
+    p.x = (float)(u0 - (double)(8 * (bc & 1023)));
+    p.y = (float)(u1 - (double)(8 * ((bc >> 10) & 1023)));
+    p.z = (float)(u2 - (double)(8 * ((bc >> 20) & 1023)));
     p.w = 0.f;
     return p;
 }
