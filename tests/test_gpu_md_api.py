@@ -235,3 +235,27 @@ def test_nvt_run_host_matches_separate_calls(setfl, precision):
     # the system stays usable after the refused run
     th, _ = s.nvt_run_host(c.x, c.v, 600.0, synth.FS, synth.KB, 2, thermo=True)
     assert np.all(np.isfinite(th))
+
+
+def test_mixed_md_in_a_triclinic_box(setfl):
+    """Mixed-precision NVT in a sheared (triclinic) box: the non-orthogonal
+    frame of the integrator and of the list builder, over enough steps for
+    list rebuilds, against the FP64 run of the same cell."""
+    strain = [[0.0, 0.0, 0.0], [0.06, 0.0, 0.0], [-0.04, 0.05, 0.0]]
+    c = synth.alloy((6, 6, 6), xB=0.4, sigma=0.05, T=1200.0, seed=12, strain=strain)
+    assert c.H[1, 0] != 0.0 and c.H[2, 1] != 0.0
+    ff = _lib.ForceField.setfl(setfl, ["A", "B"])
+    out = {}
+    for prec in (_lib.FP64, _lib.MIXED):
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=prec)
+        s.set_v(c.v)
+        th, _ = s.nvt_run(1200.0, synth.FS, synth.KB, 300, thermo=True)
+        out[prec] = (th, s.get_x(), s.get_v(), s.stats()["rebuilds"])
+    th64, x64, v64, nreb64 = out[_lib.FP64]
+    th32, x32, v32, nreb32 = out[_lib.MIXED]
+    assert nreb64 >= 2 and nreb32 >= 2  # the run crossed list rebuilds
+    d = x32 - x64
+    d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
+    assert np.max(np.abs(d)) < 1e-4 and np.max(np.abs(v32 - v64)) < 1e-4
+    assert np.max(np.abs(th32[:, 0] - th64[:, 0])) / c.natoms < 1e-6
+    assert np.max(np.abs(th32[:, 1] - th64[:, 1])) < 1e-3 * np.max(th64[:, 1])
