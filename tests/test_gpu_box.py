@@ -69,3 +69,22 @@ def test_md_minimizer_updates_the_box(potentials, tmp_path):
     assert np.allclose(last.H, a.H, rtol=0, atol=1e-12)
     with pytest.raises(TypeError, match="f_tol"):
         md.min_cg(H_dof=np.eye(3, dtype=bool), f_tol=1e-4).run(a, 10)
+
+
+def test_mixed_precision_box_relaxation(potentials):
+    """Box degrees of freedom on a mixed-precision system (FP32 forces made
+    FP64 for the vectors, FP64 line-search energies): the relaxation reaches
+    the FP64 run's box and energy."""
+    path, _ = potentials[("A", "B")]
+    c = cell()
+    res = {}
+    for prec in (_lib.FP64, _lib.MIXED):
+        s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5, precision=prec)
+        r = s.min_box_run(_lib.line_search(_lib.LS_BT), np.eye(3, dtype=bool), True, "lbfgs", m=10, e_tol=1e-10,
+                          nsteps=300)
+        res[prec] = (r, s.get_box())
+    (r64, H64), (r32, H32) = res[_lib.FP64], res[_lib.MIXED]
+    assert r64["err"] == 4 and r32["err"] in (4, 3)  # energy tolerance, or the line search ran out of step
+    assert abs(r32["pe"] - r64["pe"]) / c.natoms < 1e-7
+    assert np.max(np.abs(H32 - H64)) < 1e-4 * np.max(np.abs(H64))
+    assert np.max(np.abs(H64 - c.H)) > 1e-3  # the box did relax
