@@ -81,3 +81,25 @@ def test_md_minimizers_take_every_line_search(potentials):
     assert max(pes) - min(pes) < 1e-6 * abs(pes[0])
     with pytest.raises(TypeError):
         md.min_lbfgs(ls=object()).run(a, 1)
+
+
+@pytest.mark.parametrize("kind,minimizer", [("brent", "lbfgs"), ("golden", "cg")])
+def test_mixed_precision_line_searches(potentials, kind, minimizer):
+    """Golden-section and Brent searches on a mixed-precision system (FP64
+    trial energies, FP32-computed forces): the run reaches max|F| < 1e-4 at
+    the FP64 run's energy."""
+    path, _ = potentials[("A", "B")]
+    c = cell()
+    out = {}
+    for prec in (_lib.FP64, _lib.MIXED):
+        s = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5, precision=prec)
+        ls = _lib.line_search(KINDS[kind])
+        if minimizer == "lbfgs":
+            out[prec] = s.lbfgs_run_ls(ls, m=10, e_tol=0.0, f_tol=1e-4, nsteps=5000)
+        else:
+            out[prec] = s.cg_run_ls(ls, e_tol=0.0, f_tol=1e-4, nsteps=5000)
+    r64, r32 = out[_lib.FP64], out[_lib.MIXED]
+    assert r64["err"] == 100 and r32["err"] == 100
+    assert r32["fmax"] < 1e-4
+    # the mixed-precision energy budget (1e-7 eV/atom against FP64)
+    assert abs(r32["pe"] - r64["pe"]) / c.natoms < 1e-7
