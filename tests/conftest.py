@@ -8,6 +8,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLDEN)
+# The reference tree (its src/ and examples/), when a test may read it in
+# place; tests that need it skip where the variable is unset.
+REF_ROOT = os.environ.get("MAPPG_REFERENCE_ROOT") or None
 
 
 def pytest_configure(config):

@@ -1,0 +1,195 @@
+"""Regenerate the reference-pinned fixtures (ref_*.npz) from MAPP itself.
+
+    MAPPG_REFERENCE_ROOT=/path/to/mapp4py python tests/golden/make_ref_golden.py
+
+The reference is compiled from its own sources into oracle/_ref (recipe
+oracle/ref.mk) and driven through its Python API (md.atoms, md.nvt,
+md.min_lbfgs, atoms.create_temp) plus the probe of oracle/refshim, which
+sets exact states and reads ForceFieldMD::force_calc's forces.  Nothing here
+runs where the reference tree is absent; the fixtures it writes are what the
+tests compare the oracle and the GPU against there.
+
+Fixtures:
+  ref_synth.npz      the analytic-potential cases of make_golden.py (forces,
+                     energy, stress), the 256-atom NVT run's end state, the
+                     first L-BFGS iterates of two cells, create_temp draws
+  ref_extrap.npz     an FCC cell whose host densities exceed rho_max
+                     (linear extrapolation of F, ff_eam.cpp:188-189)
+  ref_pot_<name>.npz the knot values of a potential file shipped with the
+                     reference's examples, seeded cells on it and the
+                     reference's forces, energy, stress (and a short NVT run
+                     on Cu)
+"""
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from mapp4py_gb300 import synth  # noqa: E402
+import potfile  # noqa: E402
+import refmod  # noqa: E402
+import make_golden  # noqa: E402
+
+EXTRAP_DRHO = 0.002  # rho_max = 5000 * 0.002 = 10 < the FCC host density (~17)
+
+POTENTIALS = {
+    # name: (path under the reference tree, kind)
+    "cu": ("examples/diff/potentials/Cu_mishin.eam.alloy", "setfl"),
+    "nial": ("examples/dmd/potentials/NiAl.eam.alloy", "setfl"),
+    "feh": ("examples/beginner-tutorial/potentials/FeH-sina.eam.alloy", "setfl"),
+    "feh_fs": ("examples/diff/potentials/Fe-H.eam.fs", "fs"),
+}
+
+
+def bcc_fe_h(n, a, nh, sigma, seed):
+    """BCC Fe (n^3 cells) with nh H atoms at octahedral sites, noise sigma."""
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    s = (g[:, None, :] + np.array([[0, 0, 0], [0.5, 0.5, 0.5]])[None]).reshape(-1, 3)
+    cells = rng.choice(g.shape[0], nh, replace=False)
+    sh = g[cells] + np.array([0.5, 0.5, 0.0])
+    x = np.concatenate([s, sh]) * a
+    elem = np.concatenate([np.zeros(s.shape[0], np.uint8), np.ones(nh, np.uint8)])
+    H = np.diag([n * a] * 3).astype(np.float64)
+    x = synth.wrap(H, x + rng.normal(0.0, sigma, x.shape))
+    return H, x, elem
+
+
+def fcc_cell(n, a, xB, sigma, seed, strain=None):
+    c = synth.alloy(n, a=a, xB=xB, sigma=sigma, strain=strain, seed=seed)
+    return c.H, c.x, c.elem
+
+
+def ref_force(H, x, elem, masses, names, path, kind, v=None):
+    r = refmod.RefSystem(H, x, elem, masses, names, path, kind=kind, v=v)
+    pe, S, val, f = r.force()
+    return r, {"pe": pe, "S_pe": S, "energy": val, "f": f}
+
+
+def synth_cases(tmp):
+    out = {}
+    pots = {}
+    for elems in (("A",), ("A", "B")):
+        pots[elems] = make_golden.potential(tmp, elems)
+    for name, (elems, c) in make_golden.cases().items():
+        path, digest = pots[elems]
+        names = list(elems)
+        _, res = ref_force(c.H, c.x, c.elem, c.masses, names, path, "setfl")
+        for k, v in res.items():
+            out[name + "/" + k] = v
+        out[name + "/sha256"] = np.array(digest)
+        print(name, res["pe"])
+    # NVT: the nvt_a_256 case (NHC at 300 K, t_relax = 100 dt, 40 steps)
+    path, digest = pots[("A",)]
+    c = synth.md_single((4, 4, 4), T=300.0, seed=21)
+    r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A"], path, v=c.v, kB=synth.KB)
+    H, x, v = r.nvt(300.0, synth.FS, 40, t_relax=100.0 * synth.FS, L=3, niters=1)
+    out.update({"nvt_a_256/x_end": x, "nvt_a_256/v_end": v, "nvt_a_256/pe_end": r.force()[0]})
+    # NVE: 4,000-atom single-element FCC (the plain FP64 MD workload), 100 steps of
+    # 1 fs at a 300 K start, thermostat off (t_relax = inf)
+    c = synth.md_single((10, 10, 10), T=300.0, seed=0)
+    r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A"], path, v=c.v, kB=synth.KB)
+    H, x, v = r.nvt(300.0, synth.FS, 100, t_relax=float("inf"), L=3, niters=1)
+    out.update({"nve_a_4000/x_end": x, "nve_a_4000/v_end": v, "nve_a_4000/pe_end": r.force()[0]})
+    print("nve_a_4000 pe", out["nve_a_4000/pe_end"])
+    # L-BFGS: iterates of the plain minimizer with back-tracking (m = 10)
+    pathAB, digestAB = pots[("A", "B")]
+    for name, (cell, iters) in {
+        "lbfgs_ab_256": (synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=51), (1, 5, 20, 60)),
+        "lbfgs_ab_475": (synth.alloy((5, 5, 5), xB=0.4, sigma=0.15, vac=0.05, seed=31), (1, 3, 8)),
+    }.items():
+        for it in iters:
+            r = refmod.RefSystem(cell.H, cell.x, cell.elem, cell.masses, ["A", "B"], pathAB)
+            H, x, v = r.lbfgs(it, m=10, e_tol=0.0)
+            out["%s/x_%d" % (name, it)] = x
+            out["%s/pe_%d" % (name, it)] = r.force()[0]
+        out[name + "/iters"] = np.array(iters)
+        out[name + "/H"] = cell.H
+        out[name + "/x"] = cell.x
+        out[name + "/elem"] = cell.elem
+        out[name + "/masses"] = cell.masses
+        print(name, [out["%s/pe_%d" % (name, it)] for it in iters])
+    # create_temp: the Park-Miller / Box-Muller draw (two masses); the atoms are
+    # in element order so the reference's local order is the caller's
+    c = synth.alloy((3, 3, 3), xB=0.5, seed=61)
+    elem = np.sort(c.elem)
+    masses = np.array([63.5, 27.0])
+    r = refmod.RefSystem(c.H, c.x, elem, masses, ["A", "B"], pathAB, kB=synth.KB)
+    out.update({"create_temp/elem": elem, "create_temp/masses": masses, "create_temp/T": 450.0,
+                "create_temp/seed": 987654, "create_temp/v": r.create_temp(450.0, 987654)})
+    out["sha256_A"] = np.array(pots[("A",)][1])
+    out["sha256_AB"] = np.array(digestAB)
+    return out
+
+
+def extrap_case(tmp):
+    path = os.path.join(tmp, "A_extrap.setfl")
+    synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
+    H, x, elem = fcc_cell((4, 4, 4), 3.615, 0.0, 0.1, 71)
+    elem = np.zeros_like(elem)
+    masses = np.array([synth.MASS])
+    _, res = ref_force(H, x, elem, masses, ["A"], path, "setfl")
+    print("extrap pe", res["pe"])
+    return dict(H=H, x=x, elem=elem, masses=masses, drho=EXTRAP_DRHO, **res)
+
+
+def potential_case(tmp, name, root):
+    rel, kind = POTENTIALS[name]
+    src = os.path.join(root, rel)
+    d = potfile.parse(src, kind)
+    path = os.path.join(tmp, os.path.basename(src))
+    potfile.write(path, d)  # the tests run on this rewrite of the file
+    out = potfile.to_fixture(d)
+    masses = d["masses"]
+    names = d["names"]
+    cells = {}
+    if name == "cu":
+        cells["c0"] = fcc_cell((4, 4, 4), 3.615, 0.0, 0.1, 81)
+        cells["thin"] = fcc_cell((2, 2, 3), 3.615, 0.0, 0.08, 82)
+        cells["dense"] = fcc_cell((5, 5, 5), 2.9, 0.0, 0.05, 83)  # host densities beyond rho_max
+    elif name == "nial":
+        cells["c0"] = fcc_cell((5, 5, 5), 3.52, 0.25, 0.08, 84)
+        cells["tric"] = fcc_cell((5, 5, 6), 3.52, 0.5, 0.08, 85,
+                                 strain=[[0.01, 0, 0], [0.02, -0.01, 0], [-0.015, 0.01, 0.004]])
+    else:
+        cells["c0"] = bcc_fe_h(5, 2.8553, 12, 0.05, 86)
+    for cname, (H, x, elem) in cells.items():
+        elem = np.asarray(elem, np.uint8)
+        if name == "cu":
+            elem = np.zeros_like(elem)
+        r, res = ref_force(H, x, elem, masses, names, path, kind)
+        out.update({cname + "/H": H, cname + "/x": x, cname + "/elem": elem})
+        for k, v in res.items():
+            out[cname + "/" + k] = v
+        print(name, cname, x.shape[0], res["pe"] / x.shape[0])
+        if name == "cu" and cname == "c0":
+            rng = np.random.default_rng(87)
+            v0 = synth.maxwell(rng, masses[elem], 600.0)
+            r.set_state(x, v0)
+            H1, x1, v1 = r.nvt(600.0, synth.FS, 40, t_relax=100.0 * synth.FS)
+            out.update({"nvt/v0": v0, "nvt/x_end": x1, "nvt/v_end": v1, "nvt/T": 600.0, "nvt/nsteps": 40})
+    out["cells"] = np.array(list(cells))
+    return out
+
+
+def main():
+    root = refmod.ref_root()
+    if root is None:
+        raise SystemExit("set MAPPG_REFERENCE_ROOT to the reference tree")
+    refmod.build(root)
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, "ref_synth.npz"), **synth_cases(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_extrap.npz"), **extrap_case(tmp))
+        for name in POTENTIALS:
+            np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
+
+
+if __name__ == "__main__":
+    main()

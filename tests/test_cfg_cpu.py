@@ -12,9 +12,10 @@ import numpy as np
 import pytest
 
 import cfg_ref as R
+from conftest import REF_ROOT
 from mapp4py_gb300 import _lib, md
 
-REF_EXAMPLES = "/root/reference/examples"
+REF_EXAMPLES = os.path.join(REF_ROOT, "examples") if REF_ROOT else None
 
 
 @pytest.fixture(scope="module")
@@ -205,7 +206,7 @@ def test_edge_rules_match_oracle(built, tmp_path):
     assert np.array_equal(results["std_ok"]["x_d"][1], [4e-3 * 1.0, 0.0, -8e-3])
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+@pytest.mark.skipif(not (REF_EXAMPLES and os.path.isdir(REF_EXAMPLES)), reason="MAPPG_REFERENCE_ROOT unset")
 def test_reference_example_files(built):
     files = sorted(glob.glob(os.path.join(REF_EXAMPLES, "**", "*.cfg"), recursive=True))
     assert files

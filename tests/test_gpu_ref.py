@@ -1,0 +1,152 @@
+"""GPU parity against MAPP itself: libmappg through its C ABI against the
+fixtures of the reference compiled from its own sources
+(tests/golden/make_ref_golden.py).
+
+Covers the potential files shipped with the reference's examples, written
+back from their knots and read by the library's own parsers: Cu_mishin
+(setfl, nr = 10,001, a cell thinner than two cutoffs, a compressed cell with
+host densities beyond rho_max), NiAl and FeH-sina (two elements with
+per-pair cutoffs, one triclinic cell), Fe-H (Finnis-Sinclair per-pair
+densities); the analytic potential's static cases, a cell where every host
+density is extrapolated, md.nvt/NVE trajectories and md.min_lbfgs iterates.
+
+Tolerances: FP64 forces 1e-10 relative to the largest force component,
+energy 1e-12 relative, stress 1e-11 relative; mixed precision force RMS
+<= 1e-5 eV/A and energy <= 1e-7 eV/atom against the reference; trajectories
+1e-9 A after 40-100 steps; L-BFGS iterates 1e-8 A after up to 20 iterations.
+"""
+import numpy as np
+import pytest
+
+import potfile
+from conftest import golden
+from mapp4py_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+STATIC = ["fcc_a_256", "alloy_ab_475", "thin_a_32", "tric_ab_240"]
+POTS = ["cu", "nial", "feh", "feh_fs"]
+
+
+def stress(vir, H):
+    F = np.array([[vir[0], vir[1], vir[2]], [vir[1], vir[3], vir[4]], [vir[2], vir[4], vir[5]]])
+    return -F / np.linalg.det(H)
+
+
+def assert_forces(fg, fr, rel=1e-10):
+    scale = max(1.0, np.max(np.abs(fr)))
+    err = np.max(np.abs(fg - fr))
+    assert err <= rel * scale, "max force error %.3e > %.1e x %.3e" % (err, rel, scale)
+
+
+def force_field(d, path):
+    return _lib.ForceField.setfl(path) if d["kind"] == "setfl" else _lib.ForceField.fs(path)
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return golden("ref_synth")
+
+
+@pytest.mark.parametrize("name", STATIC)
+def test_fp64_matches_reference_static(potentials, ref, name):
+    g = golden(name)
+    path, digest = potentials[tuple(str(e) for e in g["elems"])]
+    assert str(ref[name + "/sha256"]) == digest
+    s = _lib.System(_lib.ForceField.setfl(path), g["H"], g["x"], g["elem"], g["masses"])
+    pe, vir = s.force()
+    assert abs(pe - ref[name + "/pe"]) <= 1e-12 * abs(pe)
+    assert abs(s.energy() - ref[name + "/energy"]) <= 1e-12 * abs(pe)
+    assert_forces(s.get_f(), ref[name + "/f"])
+    S = ref[name + "/S_pe"]
+    assert np.max(np.abs(stress(vir, g["H"]) - S)) <= 1e-11 * np.max(np.abs(S))
+
+
+@pytest.mark.parametrize("pot", POTS)
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_reference_potential_files(tmp_path, pot, precision):
+    g = golden("ref_pot_" + pot)
+    d = potfile.from_fixture(g)
+    path = potfile.write(str(tmp_path / (pot + ".pot")), d)
+    ff = force_field(d, path)
+    for cell in [str(c) for c in g["cells"]]:
+        H, x, elem = g[cell + "/H"], g[cell + "/x"], g[cell + "/elem"]
+        s = _lib.System(ff, H, x, elem, d["masses"], precision=precision)
+        pe, vir = s.force()
+        pe_r, f_r, S_r = float(g[cell + "/pe"]), g[cell + "/f"], g[cell + "/S_pe"]
+        if precision == _lib.FP64:
+            assert abs(pe - pe_r) <= 1e-12 * abs(pe_r), cell
+            assert_forces(s.get_f(), f_r)
+            assert np.max(np.abs(stress(vir, H) - S_r)) <= 1e-11 * np.max(np.abs(S_r)), cell
+            assert abs(s.energy() - float(g[cell + "/energy"])) <= 1e-12 * abs(pe_r), cell
+        else:
+            rms = np.sqrt(np.mean(np.sum((s.get_f() - f_r) ** 2, axis=1)))
+            assert rms <= 1e-5, (cell, rms)
+            assert abs(pe - pe_r) / x.shape[0] <= 1e-7, (cell, pe - pe_r)
+
+
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_extrapolated_embedding_matches_reference(tmp_path, precision):
+    """Every host density above rho_max: F(rho) continued linearly."""
+    g = golden("ref_extrap")
+    path = str(tmp_path / "extrap.setfl")
+    synth.write_setfl(path, ("A",), drho=float(g["drho"]))
+    s = _lib.System(_lib.ForceField.setfl(path), g["H"], g["x"], g["elem"], g["masses"], precision=precision)
+    pe, vir = s.force()
+    if precision == _lib.FP64:
+        assert abs(pe - g["pe"]) <= 1e-12 * abs(g["pe"])
+        assert_forces(s.get_f(), g["f"])
+    else:
+        rms = np.sqrt(np.mean(np.sum((s.get_f() - g["f"]) ** 2, axis=1)))
+        assert rms <= 1e-5 and abs(pe - g["pe"]) / g["x"].shape[0] <= 1e-7, (rms, pe - g["pe"])
+
+
+def test_nvt_matches_reference(potentials, ref):
+    """md.nvt(300 K, 1 fs): 40 NHC steps on 256 atoms; 100 NVE steps on the
+    4,000-atom FCC cell (t_relax = inf)."""
+    path, digest = potentials[("A",)]
+    assert str(ref["sha256_A"]) == digest
+    ff = _lib.ForceField.setfl(path)
+    c = synth.md_single((4, 4, 4), T=300.0, seed=21)
+    s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+    s.set_v(c.v)
+    s.nvt_run(300.0, synth.FS, synth.KB, 40)
+    assert np.max(np.abs(s.get_x() - ref["nvt_a_256/x_end"])) <= 1e-9
+    assert np.max(np.abs(s.get_v() - ref["nvt_a_256/v_end"])) <= 1e-9
+    c = synth.md_single((10, 10, 10), T=300.0, seed=0)
+    s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+    s.set_v(c.v)
+    s.nvt_run(300.0, synth.FS, synth.KB, 100, t_relax=float("inf"))
+    assert np.max(np.abs(s.get_x() - ref["nve_a_4000/x_end"])) <= 1e-9
+    assert np.max(np.abs(s.get_v() - ref["nve_a_4000/v_end"])) <= 1e-9
+    pe, _ = s.force()
+    assert abs(pe - ref["nve_a_4000/pe_end"]) <= 1e-11 * abs(pe)
+
+
+def test_nvt_on_cu_mishin_matches_reference(tmp_path):
+    """40 NHC steps at 600 K on the Cu setfl file (nr = 10,001)."""
+    g = golden("ref_pot_cu")
+    d = potfile.from_fixture(g)
+    path = potfile.write(str(tmp_path / "cu.setfl"), d)
+    s = _lib.System(_lib.ForceField.setfl(path), g["c0/H"], g["c0/x"], g["c0/elem"], d["masses"])
+    s.set_v(g["nvt/v0"])
+    s.nvt_run(float(g["nvt/T"]), synth.FS, synth.KB, int(g["nvt/nsteps"]))
+    assert np.max(np.abs(s.get_x() - g["nvt/x_end"])) <= 1e-9
+    assert np.max(np.abs(s.get_v() - g["nvt/v_end"])) <= 1e-9
+
+
+def test_lbfgs_iterates_match_reference(potentials, ref):
+    """md.min_lbfgs(m=10, e_tol=0) with ls_bt: positions and energy after 1, 5
+    and 20 iterations of the reference."""
+    path, _ = potentials[("A", "B")]
+    ff = _lib.ForceField.setfl(path)
+    name = "lbfgs_ab_256"
+    H = ref[name + "/H"]
+    for it in [int(i) for i in ref[name + "/iters"] if i <= 20]:
+        s = _lib.System(ff, H, ref[name + "/x"], ref[name + "/elem"], ref[name + "/masses"])
+        r = s.lbfgs_run(m=10, e_tol=0.0, f_tol=0.0, nsteps=it)
+        assert r["niter"] == it
+        d = (s.get_x() - ref["%s/x_%d" % (name, it)]) @ np.linalg.inv(H)
+        d = (d - np.round(d)) @ H
+        assert np.max(np.abs(d)) <= 1e-8, (it, np.max(np.abs(d)))
+        assert abs(r["pe"] - ref["%s/pe_%d" % (name, it)]) <= 1e-11 * abs(r["pe"])

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import golden, golden_potential
+from conftest import REF_ROOT, golden, golden_potential
 from mapp4py_gb300 import synth
 
 STATIC = ["fcc_a_256", "alloy_ab_475", "thin_a_32", "tric_ab_240"]
@@ -236,10 +236,10 @@ def test_nst_relaxes_toward_the_applied_stress(potentials):
         o.nst_run(np.full((3, 3), nan), 300.0, synth.FS, synth.KB, 1)
 
 
-REF_CU = "/root/reference/examples/diff/potentials/Cu_mishin.eam.alloy"
+REF_CU = os.path.join(REF_ROOT, "examples/diff/potentials/Cu_mishin.eam.alloy") if REF_ROOT else None
 
 
-@pytest.mark.skipif(not os.path.exists(REF_CU), reason="reference tree not present")
+@pytest.mark.skipif(not (REF_CU and os.path.exists(REF_CU)), reason="MAPPG_REFERENCE_ROOT unset or without the example")
 def test_cu_mishin_cohesive_energy():
     """Mishin et al. (2001) Cu: FCC a0 = 3.615 A, E_coh = -3.54 eV/atom; the
     setfl file shipped with the reference, read by the oracle."""
