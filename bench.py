@@ -131,10 +131,13 @@ def throughput(natoms, steps, world, ms):
     return natoms * steps * world / (ms / 1000.0)
 
 
-def workload_config(natoms, cells, precision, world):
+def workload_config(natoms, cells, world):
+    """The workload both arms run (the arithmetic is the line's `precision`
+    and `dtype`, outside the config, so the two arms' configs compare equal)."""
     return {"workload": "EAM NVT MD, %d-atom A/B alloy (FCC %d^3, seed 1)" % (natoms, cells),
-            "natoms": natoms, "precision": precision, "dt_fs": 1.0, "T_K": T_K,
-            "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None}
+            "natoms": natoms, "dt_fs": 1.0, "T_K": T_K,
+            "parallelism": "replicas x%d" % world, "global_batch": None, "seq_len": None,
+            "l2": "inputs larger than L2 (the neighbour list alone is ~%.0f MB)" % (natoms * 78 * 4 / 1e6)}
 
 
 def make_cell(cells=80):
@@ -169,6 +172,9 @@ def cpu_baseline(path, cell, threads, steps=5, natoms_cap=256000):
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores: the oracle's full-list
+    OpenMP restatement of ForceFieldEAM/MDNVT (pinned to the reference itself
+    by the ref_*.npz fixtures), FP64, on the whole workload cell."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
@@ -178,7 +184,7 @@ def run_reference(args, rank, world):
         import oracle as O
         from mapp4py_gb300 import synth
 
-        c = synth.alloy((40, 40, 40), xB=0.5, sigma=0.05, T=T_K, seed=1)
+        c = make_cell(args.cells)
         e = O.Eam.setfl(path)
         o = O.System(e, c.H, c.x, c.elem, c.masses, skin=0.5, pair_wise=False)
         o.v = c.v
@@ -187,13 +193,13 @@ def run_reference(args, rank, world):
         o.nvt_run(T_K, synth.FS, synth.KB, args.steps, threads=threads)
         secs = o.loop_seconds
     value = c.natoms * args.steps / secs
-    sample = ("each step: one NVT step of a 256,000-atom (FCC 40^3) block of the %d-atom alloy; "
-              "the reference does not build here (MPI and Python<=3.10 C-API), so this is the oracle's "
-              "OpenMP restatement" % (args.cells ** 3 * 4))
-    config = workload_config(args.cells ** 3 * 4, args.cells, args.precision, world)
+    sample = ("%d NVT steps of the whole %d-atom cell (after %d warm-up steps) on %d host threads: the "
+              "oracle's OpenMP restatement of the reference's CPU path, FP64; the reference itself builds only "
+              "where its sources are (x86 here, not on this host)" % (args.steps, c.natoms, args.warmup, threads))
+    config = workload_config(c.natoms, args.cells, world)
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "precision": "fp64",
             "data": "synthetic", "config": config,
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": sample},
@@ -267,8 +273,8 @@ def run_lbfgs(args, ff):
 
 def run_accuracy(args, ff, cell, torch):
     """The FP64 path on the same 2,048,000-atom cell (throughput), the mixed
-    path's error against it (force RMS, energy per atom), and the mixed NVE
-    energy drift (t_relax = inf, 1,000 steps of 1 fs)."""
+    path's error against it (force RMS, energy per atom), and the NVE energy
+    drift of both paths (run_nve)."""
     from mapp4py_gb300 import _lib, synth
 
     out = {}
@@ -296,17 +302,32 @@ def run_accuracy(args, ff, cell, torch):
     out["mixed_vs_fp64"] = {"force_rms_eV_per_A": float(np.sqrt(np.mean(np.sum((fa - fb) ** 2, axis=1)))),
                             "force_max_eV_per_A": float(np.max(np.abs(fa - fb))),
                             "energy_eV_per_atom": float(abs(pa - pb) / cell.natoms)}
-    del a
-    # NVE drift of the mixed path
-    nsteps = args.nve_steps
-    b.set_v(cell.v)
-    th, _ = b.nvt_run(T_K, synth.FS, synth.KB, nsteps, t_relax=float("inf"), thermo=True)
-    etot = th[:, 0] + 0.5 * (th[:, 2] + th[:, 5] + th[:, 7])
-    t_ns = nsteps * 1e-6  # 1 fs steps
-    slope = np.polyfit(np.arange(nsteps + 1) * 1e-6, etot / cell.natoms, 1)[0]
-    out["nve"] = {"steps": nsteps, "dt_fs": 1.0, "drift_eV_per_atom_per_ns": float(slope),
-                  "max_deviation_eV_per_atom": float(np.max(np.abs(etot - etot[0])) / cell.natoms),
-                  "span_ns": t_ns}
+    del a, b
+    out["nve"] = run_nve(args, ff)
+    return out
+
+
+def run_nve(args, ff):
+    """NVE energy drift (t_relax = inf, dt = 1 fs) on a 32,000-atom cell of
+    the workload's recipe (FCC 20^3, 50/50 A/B, 0.05 A noise, 600 K start):
+    mixed precision over args.nve_ps picoseconds, FP64 over a fifth of that.
+    Drift = slope of a straight-line fit of the total energy per atom."""
+    from mapp4py_gb300 import _lib, synth
+
+    c = synth.alloy((20, 20, 20), xB=0.5, sigma=0.05, T=T_K, seed=1)
+    out = {"workload": "%d-atom cell of the same recipe (FCC 20^3)" % c.natoms, "dt_fs": 1.0}
+    for name, prec, ps in (("mixed", _lib.MIXED, args.nve_ps), ("fp64", _lib.FP64, args.nve_ps / 5.0)):
+        nsteps = int(round(ps * 1000))
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=prec)
+        s.set_v(c.v)
+        t0 = time.perf_counter()
+        th, _ = s.nvt_run(T_K, synth.FS, synth.KB, nsteps, t_relax=float("inf"), thermo=True)
+        secs = time.perf_counter() - t0
+        etot = (th[:, 0] + 0.5 * (th[:, 2] + th[:, 5] + th[:, 7])) / c.natoms
+        t_ns = np.arange(nsteps + 1) * 1e-6
+        slope = np.polyfit(t_ns, etot, 1)[0]
+        out[name] = {"steps": nsteps, "span_ns": nsteps * 1e-6, "drift_eV_per_atom_per_ns": float(slope),
+                     "max_deviation_eV_per_atom": float(np.max(np.abs(etot - etot[0]))), "seconds": secs}
     return out
 
 
@@ -474,11 +495,11 @@ def run_gpu(args, rank, world, local_rank):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "data": "synthetic",
-                "config": dict(workload_config(N, args.cells, args.precision, world),
-                               l2="inputs larger than L2 (neighbour list %.0f MB)" % (N * kbar * 4 / 1e6),
-                               lanes_per_atom=tpa, entries_per_step=unroll,
-                               autotune_ms={"%d,%d" % k: round(v, 4) for k, v in tune_ms.items()}),
+                "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "precision": args.precision,
+                "data": "synthetic",
+                "config": workload_config(N, args.cells, world),
+                "tuning": {"lanes_per_atom": tpa, "entries_per_step": unroll,
+                           "autotune_ms": {"%d,%d" % k: round(v, 4) for k, v in tune_ms.items()}},
                 "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP[args.precision] * K,
                 "neighbor": {"rebuilds_in_run": st["rebuilds"], "max_row": st["max_row"], "capacity": st["capacity"]}}
         if batched is not None:
@@ -492,6 +513,11 @@ def run_gpu(args, rank, world, local_rank):
                 line["cpu_baseline"] = cpu_baseline(path, cell, os.cpu_count() or 1)
             except Exception as ex:  # reported, not fatal
                 line["cpu_baseline"] = {"value": None, "error": str(ex)}
+            cpu = line["cpu_baseline"].get("value")
+            if cpu and "fp64" in line:
+                # the same FP64 arithmetic on both sides: GPU FP64 path against the CPU port
+                line["fp64_gpu_vs_cpu"] = {"gpu_fp64": line["fp64"]["value"], "cpu_fp64": cpu,
+                                           "ratio": line["fp64"]["value"] / cpu}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -512,7 +538,8 @@ def main():
     ap.add_argument("--batch-cells", type=int, default=512)
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the FP64 run, the mixed-vs-FP64 error, the NVE drift and the 4,000-atom case")
-    ap.add_argument("--nve-steps", type=int, default=1000)
+    ap.add_argument("--nve-ps", type=float, default=50.0,
+                    help="length of the mixed-precision NVE drift run in ps (1 fs steps)")
     ap.add_argument("--lbfgs-cap", type=int, default=1000,
                     help="iteration cap of the 253k-atom L-BFGS comparison (0 skips the L-BFGS part)")
     ap.add_argument("--cells", type=int, default=N_CELLS[0],

@@ -53,6 +53,13 @@ const char* mappg_last_error(void);
 /* Device name and SM count of the current CUDA device. */
 int mappg_device_info(char* name, int name_len, int* sm_count);
 
+/* The current GPU's FP64 fused multiply-add rate in TFLOP/s (2 flops per
+ * FMA), measured with a kernel of independent FMA chains and no memory
+ * traffic: the arithmetic roof of the FP64 path (its kernels are bounded by
+ * FP64 issue, not HBM).  No counterpart in the reference.  iters: FMA
+ * iterations per thread per launch; reps: timed launches (best counts). */
+int mappg_fp64_fma_rate(int iters, int reps, double* tflops);
+
 /* ---------------------------------------------------------------- tables */
 
 /* Read a DYNAMO setfl file.  Replaces ImportEAM::setfl (import_eam.h:348-613)
@@ -145,7 +152,11 @@ int mappg_sys_energy(mappg_sys* sys, double* pe);
  * about 11 MB (10.5 MiB) that every GPU using this call holds until the process
  * exits; the first call on each device looks up that array's address and
  * loads the kernels, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race and must be serialised. */
+ * array: calls that overlap on the GPU race and must be serialised.  The
+ * call runs on the system's device, which must be the calling thread's
+ * current device (checked on every call).  Because it returns before the
+ * work completes, it makes no finiteness check (mappg_sys_force returns
+ * MAPPG_ERR_NAN for a non-finite energy): check ev_dev[0] after waiting. */
 int mappg_sys_force_noalloc(mappg_sys* sys, double* f_dev, double* ev_dev);
 
 /* Per-atom host density rho and F'(rho) from the last force call. */
@@ -267,6 +278,16 @@ int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
  * timing: 0 density + embedding, 1 force/virial (uses the last F'(rho)),
  * 2 energy only, 3 neighbour rebuild. */
 int mappg_sys_enqueue(mappg_sys* sys, int what);
+
+/* The energy change E(x + alpha h) - E(x) of a mixed-precision system, as
+ * the line searches of its minimizers take it: formed pair by pair from the
+ * displacement change (an FP32 difference of two FP32 energies would carry
+ * rounding of the size of the decreases near convergence), the embedding
+ * change in FP64.  No counterpart in the reference, whose line searches
+ * compare FP64 energies (MinMDHandler::F, min_cg.h:260-267).  h is
+ * [natoms][3] in the caller's order; atoms do not move.  Refused when
+ * alpha*h would take an atom beyond half the neighbour list's skin. */
+int mappg_sys_energy_delta(mappg_sys* sys, const double* h, double alpha, double* de);
 
 /* md.min_lbfgs(m,e_tol,max_dx,ls=ls_bt(c,rho,min_alpha)).run(atoms,nsteps)
  * (MinLBFGS::__run, min_l-bfgs.h:113-219; LineSearchBackTrack::min,

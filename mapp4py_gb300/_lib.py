@@ -26,6 +26,7 @@ _HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_longlong)
 SIGNATURES = {
     "mappg_last_error": (C.c_char_p, []),
     "mappg_device_info": (C.c_int, [C.c_char_p, C.c_int, _I]),
+    "mappg_fp64_fma_rate": (C.c_int, [C.c_int, C.c_int, _D]),
     "mappg_ff_setfl": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
     "mappg_ff_fs": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
     "mappg_ff_funcfl": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
@@ -49,6 +50,7 @@ SIGNATURES = {
     "mappg_sys_force": (C.c_int, [_VP, _D, _D]),
     "mappg_sys_force_noalloc": (C.c_int, [_VP, _VP, _VP]),
     "mappg_sys_energy": (C.c_int, [_VP, _D]),
+    "mappg_sys_energy_delta": (C.c_int, [_VP, _D, C.c_double, _D]),
     "mappg_sys_get_rho": (C.c_int, [_VP, _D, _D]),
     "mappg_sys_neighbors": (C.c_int, [_VP, _I, _I, _LL]),
     "mappg_sys_stats": (C.c_int, [_VP, _LL]),
@@ -315,6 +317,13 @@ class System:
         pe = C.c_double()
         check(load().mappg_sys_energy(self.h, C.byref(pe)))
         return pe.value
+
+    def energy_delta(self, h, alpha):
+        """E(x + alpha h) - E(x) as the mixed minimizers' line searches take it."""
+        h = f64(h, (self.n, 3))
+        de = C.c_double()
+        self._checked(load().mappg_sys_energy_delta(self.h, dptr(h), float(alpha), C.byref(de)))
+        return de.value
 
     def rho_dF(self):
         rho = np.zeros(self.n)
@@ -700,6 +709,13 @@ def create_temp(elem, masses, T, kB, seed):
     check(load().mappg_create_temp(elem.shape[0], elem.ctypes.data_as(_U8), dptr(f64(masses)), float(T),
                                    float(kB), int(seed), dptr(v)))
     return v
+
+
+def fp64_fma_rate(iters=4096, reps=5):
+    """FP64 FMA throughput of the current GPU in TFLOP/s (measured)."""
+    t = C.c_double()
+    check(load().mappg_fp64_fma_rate(int(iters), int(reps), C.byref(t)))
+    return t.value
 
 
 def device_info():

@@ -31,6 +31,8 @@ void launch_force(mappg_sys* s);
 void launch_energy(mappg_sys* s);
 void sync_forces64(mappg_sys* s);
 void launch_energy64(mappg_sys* s);
+void launch_energy32(mappg_sys* s, const EamArgs& a);  // eam32.cu
+void launch_de32b(mappg_sys* s, const double* cell_alpha);
 
 constexpr int kBlMaxHist = 32;
 enum BlState { BL_RUN = 0, BL_PLAIN = 1, BL_LS = 2, BL_ACCEPT = 3, BL_DONE = 4 };
@@ -41,8 +43,13 @@ struct BlCell {
     double dot;
     double fh, hh, hmax, fmax;
     double e_curr, e_prev, e0, a, dfa, pe;
+    double dxmax;  // max |x - x_build| component over the cell's atoms
+    double e0_32;  // FP32 energy of x0 (searches of FP32 energy differences)
     int k, head, state, err, niter, n_en, n_fc, nfb;
 };
+
+// how a line search of mixed-precision cells takes trial energies
+enum BlEnergy { BL_E64 = 0, BL_EDELTA = 1, BL_E32DIFF = 2 };
 
 struct BlArgs {
     int n, ncell, nchunk, m;
@@ -59,6 +66,11 @@ struct BlArgs {
     int* count;      // cells still searching
     double c_ls, rho_ls, min_alpha, max_dx, e_tol, f_tol;
     int nsteps;
+    int emode;              // BlEnergy of the current search
+    const double* xb;       // neighbour list build positions
+    double skin_half;
+    uint8_t* active;        // per cell: the chunk kernels work on it
+    double* alpha_cell;     // per cell trial step (energy differences)
 };
 
 __device__ __forceinline__ int slot_of(const BlCell& c, int i, int m) { return (c.head - i + m) % m; }
@@ -280,13 +292,16 @@ __global__ void k_bl_trial(BlArgs a) {
     }
 }
 
-// Armijo test of every searching cell on its trial energy
+// Armijo test of every searching cell on its trial energy: the FP64
+// energy, x0's energy plus the energy difference of the trial, or plus the
+// difference of two FP32 energies
 __global__ void k_bl_cells_ls(BlArgs a) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= a.ncell) return;
     BlCell& cs = a.cs[c];
     if (cs.state != BL_LS) return;
-    const double cur = a.cmd[c].energy;
+    const double e = a.cmd[c].energy;
+    const double cur = a.emode == BL_EDELTA ? cs.e0 + e : a.emode == BL_E32DIFF ? cs.e0 + (e - cs.e0_32) : e;
     cs.n_en++;
     if (cur <= cs.e0 + cs.a * a.c_ls * cs.dfa) {
         cs.e_curr = cur;
@@ -424,6 +439,57 @@ __global__ void k_bl_revive(BlArgs a) {
     atomicAdd(a.count, 1);
 }
 
+// the chunk kernels' cell mask: cells in state st
+__global__ void k_bl_active(BlArgs a, int st) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < a.ncell) a.active[c] = a.cs[c].state == st ? 1 : 0;
+}
+
+// per-chunk max |x - x_build| of the searching cells into part[ch][0]
+__global__ void __launch_bounds__(256) k_bl_dx(BlArgs a) {
+    const int n = a.n;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const bool on = a.cs[a.chunk_cell[ch]].state == BL_LS;
+        double v[1] = {0.0};
+        for (int ii = a.chunk_begin[ch] + threadIdx.x; on && ii < a.chunk_begin[ch + 1]; ii += blockDim.x)
+            for (int q = 0; q < 3; q++) {
+                const size_t j = (size_t)q * n + ii;
+                v[0] = fmax(v[0], fabs(a.x[j] - a.xb[j]));
+            }
+        const int op[1] = {1};
+        bl_store<1>(v, op, a.part + (size_t)ch * 4);
+    }
+}
+
+// counts the searching cells whose first (largest) trial could take an atom
+// beyond half the skin of the list's build positions
+__global__ void k_bl_cells_bound(BlArgs a) {
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.ncell) return;
+    const double dx = bl_cell_total(a, c, 0, true);
+    if ((threadIdx.x & 31) != 0) return;
+    BlCell& cs = a.cs[c];
+    if (cs.state != BL_LS) return;
+    cs.dxmax = dx;
+    if (!(1.7320508075688772 * (cs.a * cs.hmax + dx) < a.skin_half)) atomicAdd(a.count, 1);
+}
+
+// per-cell trial steps for the energy-difference pass; FP32 energies of x0
+__global__ void k_bl_alpha(BlArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < a.ncell) a.alpha_cell[c] = a.cs[c].state == BL_LS ? a.cs[c].a : 0.0;
+}
+
+__global__ void k_bl_e0_32(BlArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < a.ncell && a.cs[c].state == BL_LS) a.cs[c].e0_32 = a.cmd[c].energy;
+}
+
+__global__ void k_lb_h32b(int n, const double* __restrict__ h, float4* __restrict__ h32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        h32[i] = make_float4((float)h[i], (float)h[n + i], (float)h[2 * n + i], 0.f);
+}
+
 __global__ void k_bl_count(BlArgs a, int st) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < a.ncell && a.cs[c].state == st) atomicAdd(a.count, 1);
@@ -480,6 +546,23 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
     a.e_tol = e_tol;
     a.f_tol = f_tol;
     a.nsteps = nsteps;
+    a.xb = s->x0;
+    a.skin_half = 0.5 * s->skin;
+    a.active = (uint8_t*)dalloc(nc);
+    a.alpha_cell = (double*)dalloc(sizeof(double) * nc);
+    const bool mixed = s->precision == MAPPG_MIXED;
+    float4* h32 = mixed ? (float4*)dalloc(sizeof(float4) * (size_t)n) : nullptr;
+    // the masks and the kept density belong to this run only
+    struct Masks {
+        mappg_sys* s;
+        ~Masks() {
+            s->cell_active = nullptr;
+            s->keep_rho64 = false;
+            s->h32 = nullptr;
+        }
+    } masks{s};
+    s->keep_rho64 = mixed;
+    s->h32 = h32;
     cudaStream_t st = s->stream;
     const int gc = std::min(s->nchunk, s->sm_count * 8);
     const int ga = grid_for(s, n, 256);
@@ -551,11 +634,46 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
         k_bl_prep<<<gc, 256, 0, st>>>(a, -1);
         k_bl_cells_ls_init<<<gw, 256, 0, st>>>(a);
         MAPPG_CUDA(cudaGetLastError());
-        // line search over all searching cells
+        // line search over all searching cells.  Mixed cells take energy
+        // differences on x0's lists when every searching cell's trials stay
+        // within half the skin (BL_EDELTA), else differences of FP32
+        // energies with rebuilds (large steps, where the differences are
+        // large); FP64 systems and FP64-force cells compare FP64 energies.
+        const int gb = (nc + 255) / 256;
+        a.emode = BL_E64;
+        if (mixed && !s->force64) {
+            MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+            k_bl_dx<<<gc, 256, 0, st>>>(a);
+            k_bl_cells_bound<<<gw, 256, 0, st>>>(a);
+            int wide = 0;
+            MAPPG_CUDA(cudaMemcpyAsync(&wide, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+            MAPPG_CUDA(cudaStreamSynchronize(st));
+            a.emode = wide == 0 ? BL_EDELTA : BL_E32DIFF;
+            k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
+            s->cell_active = a.active;
+            if (a.emode == BL_EDELTA) {
+                k_lb_h32b<<<ga, 256, 0, st>>>(n, a.h, h32);
+            } else {
+                launch_energy32(s, eam_args(s));
+                k_bl_e0_32<<<gb, 256, 0, st>>>(a);
+            }
+            MAPPG_CUDA(cudaGetLastError());
+        }
         while (true) {
             k_bl_trial<<<ga, 256, 0, st>>>(a);
-            lb_update(s);
-            launch_energy64(s);
+            if (a.emode == BL_EDELTA) {
+                k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
+                k_bl_alpha<<<gb, 256, 0, st>>>(a);
+                launch_de32b(s, a.alpha_cell);
+            } else {
+                lb_update(s);
+                if (a.emode == BL_E32DIFF) {
+                    k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
+                    launch_energy32(s, eam_args(s));
+                } else {
+                    launch_energy64(s);
+                }
+            }
             MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
             k_bl_cells_ls<<<g1, 256, 0, st>>>(a);
             int left = 0;
@@ -565,9 +683,16 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
         }
         k_bl_restore<<<ga, 256, 0, st>>>(a);
         lb_update(s);
-        // force pass, tolerances and history
+        // force pass of the cells that took a step, tolerances and history
+        if (mixed && !s->force64) {
+            k_bl_active<<<gb, 256, 0, st>>>(a, BL_ACCEPT);
+            s->cell_active = a.active;
+        } else {
+            s->cell_active = nullptr;
+        }
         launch_force(s);
         sync_forces64(s);
+        s->cell_active = nullptr;
         k_bl_hist<<<gc, 256, 0, st>>>(a);
         k_bl_cells_step<<<gw, 256, 0, st>>>(a);
         MAPPG_CUDA(cudaGetLastError());

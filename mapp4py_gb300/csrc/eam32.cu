@@ -10,9 +10,13 @@
 //                gather plus the record
 //   k_energy32   energy only (line-search trials)
 //
-// Precision: every per-pair term is FP32; per-atom sums are FP32 within a
-// lane group; energies are accumulated per lane with compensated FP32 sums
-// and reduced in FP64 across lanes and blocks.  Constants shared by many
+// Precision: every per-pair term is computed in FP32; every sum of them is
+// accumulated with compensation (Kahan: an FP32 sum and an FP32 correction
+// holding its lost low part), which carries the sum of FP32 terms as an FP64
+// accumulator would: per-atom density, force and pair energy within a lane,
+// the virial across all pairs a thread visits.  Lane partials are reduced in
+// FP64 (shuffles of doubles), block and grid totals in FP64 in a fixed
+// order.  The embedding takes the FP64 density.  Constants shared by many
 // pairs (1/dr, the frame-to-Cartesian scale, the spline constant terms) are
 // carried as head + tail so their rounding does not bias the totals.
 //
@@ -103,27 +107,49 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 }
 
 struct Consts32 {
-    float dri, dri_lo, drhoi, drhoi_lo, rho_max;
+    float dri, dri_lo;
     __device__ Consts32(const EamArgs& a) {
         dri = (float)a.dr_inv;
         dri_lo = (float)(a.dr_inv - (double)dri);
-        drhoi = (float)a.drho_inv;
-        drhoi_lo = (float)(a.drho_inv - (double)drhoi);
-        rho_max = (float)a.rho_max;
     }
 };
 
-// embedding F and F' from the FP32 table, constant term as head + tail;
-// linear extrapolation above rho_max as ff_eam.cpp:180-191
-__device__ __forceinline__ void embed32(const EamArgs& a, const Consts32& K, int ei, float rho, float& Fv,
-                                        float& dFv) {
-    float fr;
-    const int m = knot32(fmaf(rho, K.drhoi, rho * K.drhoi_lo), a.nrho - 2, fr);
+// a lane's compensated partial (s, c), reduced over the TPA lanes of one
+// atom in FP64
+template <int TPA>
+__device__ __forceinline__ double lane_sum64(float s, float c) {
+    double v = (double)s - (double)c;
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, TPA);
+    return v;
+}
+
+// embedding F and F' of the FP64 density: knot and fraction from rho/drho
+// in FP64, then the FP32 table with its constant term as head + tail
+// (ff_eam.cpp:180-187).  Above rho_max every atom uses the last knot's
+// record at p = 1 and extrapolates linearly (ff_eam.cpp:188-189); one FP32
+// copy of that single record would bias all such atoms alike, so this rare
+// branch reads the FP64 record.
+__device__ __forceinline__ void embed32(const EamArgs& a, int ei, double rho, float& Fv, float& dFv) {
+    if (rho > a.rho_max) {
+        const Dbl4 c = ldg4(a.F64 + (size_t)ei * a.nrho + (a.nrho - 2));
+        const double d1 = ((3.0 * c.w + 2.0 * c.z) + c.y) * a.drho_inv;
+        const double f0 = ((c.w + c.z) + c.y) + c.x;
+        dFv = (float)d1;
+        Fv = (float)(f0 + d1 * (rho - a.rho_max));
+        return;
+    }
+    const double p = rho * a.drho_inv;
+    int m = (int)p;
+    float fr = (float)(p - (double)m);
+    if (m > a.nrho - 2) {
+        m = a.nrho - 2;
+        fr = 1.0f;
+    }
     const size_t k = (size_t)ei * a.nrho + m;
     const float4 c = __ldg(a.F32 + k);
-    dFv = fmaf(fmaf(3.0f * c.w, fr, 2.0f * c.z), fr, c.y) * K.drhoi;
+    dFv = fmaf(fmaf(3.0f * c.w, fr, 2.0f * c.z), fr, c.y) * (float)a.drho_inv;
     Fv = c.x + (__ldg(a.F32lo + k) + fr * fmaf(fmaf(c.w, fr, c.z), fr, c.y));
-    if (rho > K.rho_max) Fv += dFv * (rho - K.rho_max);
 }
 
 // per-kernel persistent grid: as many blocks as fit on the GPU at once
@@ -163,7 +189,7 @@ template <int TPA, bool ORTHO, int U, class FR, bool SM = false>
 __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
                                              int i, int lane, bool active, float& es, float& ec,
                                              const float4* stab = nullptr) {
-    float acc = 0.f;
+    float acc = 0.f, acc_c = 0.f;
     int ei = 0;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) {
@@ -189,7 +215,7 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
                     c = stab[(a.rho_ei ? ej * a.ne + ei : ej) * a.rho_w + ms];
                 else
                     c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
-                acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+                kahan_add(acc, acc_c, fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x));
             }
         };
         if (U == 1) {
@@ -211,13 +237,13 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
             }
         }
     }
-#pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
+    const double rho = lane_sum64<TPA>(acc, acc_c);
     if (active && lane == 0) {
         float Fv, dFv;
-        embed32(a, K, ei, acc, Fv, dFv);
+        embed32(a, ei, rho, Fv, dFv);
         a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
-        a.rho32out[i] = acc;
+        a.rho32out[i] = (float)rho;
+        if (a.rho_keep) a.rho_keep[i] = rho;
         kahan_add(es, ec, Fv);
     }
 }
@@ -294,6 +320,7 @@ __global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
         float es = 0.f, ec = 0.f;
@@ -308,8 +335,10 @@ __global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
 // one atom's force row (TPA lanes): force, pair energy and virial
 template <int TPA, bool ORTHO, int U, class FR>
 __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
-                                           int i, int lane, bool active, float& es, float& ec, float (&w)[6]) {
+                                           int i, int lane, bool active, float& es, float& ec, float (&w)[6],
+                                           float (&wc)[6]) {
     float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
+    float fxc = 0.f, fyc = 0.f, fzc = 0.f, epc = 0.f;
     int ei = 0;
     if (active) {
         const float4 pi = __ldg(a.q32 + i);
@@ -346,16 +375,16 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 const float dphi = (zp - phi) * rinv;
                 const float fp = -fmaf(dFi, der_i, fmaf(q.w, der_j, dphi)) * rinv;
                 const float fdx = fp * dx, fdy = fp * dy, fdz = fp * dz;
-                fx += fdx;
-                fy += fdy;
-                fz += fdz;
-                ep += phi;
-                w[0] = fmaf(fdx, dx, w[0]);
-                w[1] = fmaf(fdx, dy, w[1]);
-                w[2] = fmaf(fdx, dz, w[2]);
-                w[3] = fmaf(fdy, dy, w[3]);
-                w[4] = fmaf(fdy, dz, w[4]);
-                w[5] = fmaf(fdz, dz, w[5]);
+                kahan_add(fx, fxc, fdx);
+                kahan_add(fy, fyc, fdy);
+                kahan_add(fz, fzc, fdz);
+                kahan_add(ep, epc, phi);
+                kahan_add(w[0], wc[0], fdx * dx);
+                kahan_add(w[1], wc[1], fdx * dy);
+                kahan_add(w[2], wc[2], fdx * dz);
+                kahan_add(w[3], wc[3], fdy * dy);
+                kahan_add(w[4], wc[4], fdy * dz);
+                kahan_add(w[5], wc[5], fdz * dz);
             }
         };
         if (U == 1) {
@@ -376,22 +405,18 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
             }
         }
         kahan_add(es, ec, ep);
+        ec += epc;  // the atom's own correction (small): the thread total is es - ec
     }
-#pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) {
-        fx += __shfl_xor_sync(0xffffffffu, fx, o, TPA);
-        fy += __shfl_xor_sync(0xffffffffu, fy, o, TPA);
-        fz += __shfl_xor_sync(0xffffffffu, fz, o, TPA);
-    }
+    const double gx = lane_sum64<TPA>(fx, fxc), gy = lane_sum64<TPA>(fy, fyc), gz = lane_sum64<TPA>(fz, fzc);
     if (active && lane == 0) {
-        a.f32[i] = fx;
-        a.f32[a.n + i] = fy;
-        a.f32[2 * a.n + i] = fz;
+        a.f32[i] = (float)gx;
+        a.f32[a.n + i] = (float)gy;
+        a.f32[2 * a.n + i] = (float)gz;
     }
 }
 
 template <int TPA, bool ORTHO, int U>
-__global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32(EamArgs a) {
+__global__ void __launch_bounds__(256, 4) k_force32(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
@@ -399,15 +424,15 @@ __global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32(EamArgs a) {
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
     float es = 0.f, ec = 0.f;  // pair energy, compensated
-    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, wc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // virial
     for (int base = 0;; base += stride) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        force_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec, w);
+        force_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec, w, wc);
     }
     auto sum_k = [&](int k) -> double {
-        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1];
+        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * ((double)w[k - 1] - (double)wc[k - 1]);
     };
     __shared__ double tot[7];
     if (block_partials_fn<7>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
@@ -423,23 +448,26 @@ __global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32(EamArgs a) {
 
 // batch: chunk slots 0 pair energy, 1-6 virial
 template <int TPA, bool ORTHO, int U>
-__global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32b(EamArgs a) {
+__global__ void __launch_bounds__(256, 4) k_force32b(EamArgs a) {
     __shared__ Smem32 S;
     S.fill(a);
     const Consts32 K(a);
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
         float es = 0.f, ec = 0.f;
-        float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, wc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (int i0 = lo; i0 < hi; i0 += apb) {
             const int i = i0 + (int)threadIdx.x / TPA;
-            force_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec, w);
+            force_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec, w, wc);
         }
         chunk_store<7>(
-            [&](int k) -> double { return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1]; },
+            [&](int k) -> double {
+                return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * ((double)w[k - 1] - (double)wc[k - 1]);
+            },
             a.chunk_part + (size_t)ch * kChunkSlots);
     }
 }
@@ -448,7 +476,7 @@ __global__ void __launch_bounds__(256, U == 1 ? 5 : 4) k_force32b(EamArgs a) {
 template <int TPA, bool ORTHO, class FR>
 __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
                                             int i, int lane, bool active, float& es, float& ec) {
-    float acc = 0.f, ep = 0.f;
+    float acc = 0.f, acc_c = 0.f, ep = 0.f, epc = 0.f;
     int ei = 0;
     if (active) {
         const float4 pi = __ldg(a.p32 + i);
@@ -471,21 +499,23 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
                 const float4 c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
-                acc += fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x);
+                kahan_add(acc, acc_c, fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x));
                 const float4* rec = a.ftab + 2 * ((size_t)t * a.nr + m);
                 float4 r0, r1;
                 ldg8(rec, r0, r1);
                 const float z = r0.w + fmaf(fr, fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x), r1.w);
-                ep += 0.5f * z * rinv;
+                kahan_add(ep, epc, 0.5f * z * rinv);
             }
         }
     }
-#pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPA);
-    if (active) kahan_add(es, ec, ep);
+    const double rho = lane_sum64<TPA>(acc, acc_c);
+    if (active) {
+        kahan_add(es, ec, ep);
+        ec += epc;
+    }
     if (active && lane == 0) {
         float Fv, dFv;
-        embed32(a, K, ei, acc, Fv, dFv);
+        embed32(a, ei, rho, Fv, dFv);
         kahan_add(es, ec, Fv);
     }
 }
@@ -525,12 +555,213 @@ __global__ void __launch_bounds__(256) k_energy32b(EamArgs a) {
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
         float es = 0.f, ec = 0.f;
         for (int i0 = lo; i0 < hi; i0 += apb) {
             const int i = i0 + (int)threadIdx.x / TPA;
             energy_atom<TPA, ORTHO>(a, S, K, fr, i, lane, i < hi, es, ec);
+        }
+        chunk_store<1>([&](int) { return (double)es - (double)ec; }, a.chunk_part + (size_t)ch * kChunkSlots);
+    }
+}
+
+// ------------------------------------------------------------------ energy differences
+// dE = E(x0 + alpha h) - E(x0) for the line-search trials of a mixed-
+// precision minimizer.  FP32 energies of the two configurations each carry
+// ~1e-4 eV of rounding at 10^5 atoms (mostly from r, whose relative error is
+// ~1e-7, through rho'(r) and phi'(r)), as much as the energy decrease the
+// Armijo test has to resolve near max|F| = 1e-4.  Differences are therefore
+// formed pair by pair, where they are small, instead of between totals:
+//   d' = d + alpha (h_i - h_j)                       (displacement, Cartesian)
+//   r'^2 - r^2 = dd . (2 d + dd),  r' - r = (r'^2 - r^2) / (r + r')
+//   g(r') - g(r) of a cubic spline from the knot fraction p and its change
+//   dp = (r' - r)/dr: dp (c1 + c2 (p + p') + c3 (p^2 + p p' + p'^2)) inside
+//   an interval, split at the knot when the step crosses one
+//   phi' - phi = (dz r - z dr) / (r r'),  z = r phi
+// so each term, and the total, is accurate relative to the difference itself.
+// The embedding change F(rho0 + drho) - F(rho0) is taken per atom in FP64
+// from the FP64 density of x0 (kept by the density pass) and the FP64 table.
+// The neighbour rows and the FP32 frame positions are those of x0; the
+// caller guarantees that x0 and the trial stay within half the skin of the
+// list's build positions, so every pair inside the cutoff at either end is
+// in the rows.
+
+// change of one cubic c0 + c1 p + c2 p^2 + c3 p^3 from p to p + dp
+__device__ __forceinline__ float cubic_step(float c1, float c2, float c3, float p, float dp) {
+    const float q = p + dp;
+    return dp * fmaf(c3, fmaf(p, p + q, q * q), fmaf(c2, p + q, c1));
+}
+
+// g(knot m1, p1) - g(knot m, p) of one spline whose knot-m coefficients are
+// returned by coef(m) as (c0, c1, c2, c3): within one interval or across one
+// knot by the step formula, otherwise (steps of more than one interval,
+// where the difference is large) as the difference of the two values
+template <class Coef>
+__device__ __forceinline__ float spline_step(Coef coef, int m, float p, float dp, int mmax, int m1, float p1) {
+    const float t = p + dp;
+    const float4 c = coef(m);
+    if (t >= 0.f && t < 1.f) return cubic_step(c.y, c.z, c.w, p, dp);
+    if (t >= 1.f && t < 2.f && m + 1 <= mmax) {
+        const float4 d = coef(m + 1);
+        return cubic_step(c.y, c.z, c.w, p, 1.f - p) + cubic_step(d.y, d.z, d.w, 0.f, t - 1.f);
+    }
+    if (t < 0.f && t >= -1.f && m >= 1) {
+        const float4 d = coef(m - 1);
+        return cubic_step(c.y, c.z, c.w, p, -p) + cubic_step(d.y, d.z, d.w, 1.f, t);
+    }
+    const float4 d = coef(m1);
+    const float g1 = fmaf(fmaf(fmaf(d.w, p1, d.z), p1, d.y), p1, d.x);
+    const float g0 = fmaf(fmaf(fmaf(c.w, p, c.z), p, c.y), p, c.x);
+    return g1 - g0;
+}
+
+// F(rho) in FP64 with the reference's clamps and linear extrapolation
+// (ff_eam.cpp:180-189)
+__device__ __forceinline__ double embed64(const EamArgs& a, int ei, double rho) {
+    const double p = rho * a.drho_inv;
+    int m = (int)p;
+    if (m > a.nrho - 2) m = a.nrho - 2;
+    double q = p - (double)m;
+    if (q > 1.0) q = 1.0;
+    const Dbl4 c = ldg4(a.F64 + (size_t)ei * a.nrho + m);
+    double F = ((c.w * q + c.z) * q + c.y) * q + c.x;
+    if (rho > a.rho_max) F += ((3.0 * c.w * q + 2.0 * c.z) * q + c.y) * a.drho_inv * (rho - a.rho_max);
+    return F;
+}
+
+template <int TPA, bool ORTHO, class FR>
+__device__ __forceinline__ void de_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr, int i,
+                                        int lane, bool active, float alpha, float& es, float& ec) {
+    float dr = 0.f, drc = 0.f, dp = 0.f, dpc = 0.f;  // density change, pair-energy change (compensated)
+    int ei = 0;
+    if (active) {
+        const float4 pi = __ldg(a.p32 + i);
+        const float4 hi = __ldg(a.h32 + i);
+        ei = a.elem[i];
+        const int nn = __ldg(a.nnbr + i);
+        const int* row = a.nbr + (size_t)i * a.maxnbr;
+        const int mmax = a.nr - 2;
+        for (int k = lane; k < nn; k += TPA) {
+            const int e = __ldg(row + k);
+            const int j = entry_j(e), ej = entry_elem(e);
+            const int t = ei * a.ne + ej;
+            const float4 q = __ldg(a.p32 + j);
+            const float4 hj = __ldg(a.h32 + j);
+            float4 o;
+            image_offset(e, o);
+            float dx, dy, dz;
+            cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
+            const float ux = alpha * (hi.x - hj.x), uy = alpha * (hi.y - hj.y), uz = alpha * (hi.z - hj.z);
+            const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float drsq = fmaf(ux, fmaf(2.f, dx, ux), fmaf(uy, fmaf(2.f, dy, uy), uz * fmaf(2.f, dz, uz)));
+            const float rsq1 = rsq + drsq;
+            const float cut = S.cut_sq[t];
+            const bool in0 = rsq < cut, in1 = rsq1 < cut;
+            if (!(in0 || in1)) continue;
+            const float rinv = inv_sqrt(rsq), rinv1 = inv_sqrt(rsq1);
+            const float r = rsq * rinv, r1 = rsq1 * rinv1;
+            float p0, p1;
+            const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), mmax, p0);
+            const int m1 = knot32(fmaf(r1, K.dri, r1 * K.dri_lo), mmax, p1);
+            const float4* rt = a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr;
+            const float4* ft = a.ftab + 2 * (size_t)t * a.nr;
+            // the rphi record: (c0 head in .w of the first half, c1 c2 c3 and
+            // the c0 tail in the second half)
+            auto zc = [&](int mm) {
+                float4 r0, r1r;
+                ldg8(ft + 2 * (size_t)mm, r0, r1r);
+                return make_float4(r0.w + r1r.w, r1r.x, r1r.y, r1r.z);
+            };
+            auto rc = [&](int mm) { return __ldg(rt + mm); };
+            float drho, dphi;
+            if (in0 && in1) {
+                const float ddr = drsq / (r + r1);
+                const float dpk = fmaf(ddr, K.dri, ddr * K.dri_lo);
+                drho = spline_step(rc, m, p0, dpk, mmax, m1, p1);
+                float4 r0, r1r;
+                ldg8(ft + 2 * (size_t)m, r0, r1r);
+                const float z = r0.w + fmaf(p0, fmaf(fmaf(r1r.z, p0, r1r.y), p0, r1r.x), r1r.w);
+                const float dz = spline_step(zc, m, p0, dpk, mmax, m1, p1);
+                dphi = fmaf(dz, r, -z * ddr) * (rinv * rinv1);
+            } else {
+                // the pair enters or leaves the cutoff: the change is the
+                // (small, near-cutoff) value at the end inside
+                const int mm = in1 ? m1 : m;
+                const float pp = in1 ? p1 : p0, ri = in1 ? rinv1 : rinv, sg = in1 ? 1.f : -1.f;
+                const float4 c = rc(mm);
+                drho = sg * fmaf(fmaf(fmaf(c.w, pp, c.z), pp, c.y), pp, c.x);
+                float4 r0, r1r;
+                ldg8(ft + 2 * (size_t)mm, r0, r1r);
+                const float z = r0.w + fmaf(pp, fmaf(fmaf(r1r.z, pp, r1r.y), pp, r1r.x), r1r.w);
+                dphi = sg * z * ri;
+            }
+            kahan_add(dr, drc, drho);
+            kahan_add(dp, dpc, dphi);
+        }
+    }
+    const double drho_i = lane_sum64<TPA>(dr, drc);
+    if (active) {
+        kahan_add(es, ec, 0.5f * dp);
+        ec += 0.5f * dpc;
+    }
+    if (active && lane == 0) {
+        const double r0 = a.rho0[i];
+        const double dF = embed64(a, ei, r0 + drho_i) - embed64(a, ei, r0);
+        // dF carries FP64 precision; added as head and tail
+        const float h = (float)dF;
+        kahan_add(es, ec, h);
+        kahan_add(es, ec, (float)(dF - (double)h));
+    }
+}
+
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_de32(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const float alpha = (float)a.alpha;
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    float es = 0.f, ec = 0.f;
+    for (int base = 0;; base += stride) {
+        const int i = gid + base;
+        const bool active = i < a.n;
+        if (!__any_sync(0xffffffffu, active)) break;
+        de_atom<TPA, ORTHO>(a, S, K, a.fr, i, lane, active, alpha, es, ec);
+    }
+    double v[1] = {(double)es - (double)ec};
+    if (block_partials<1>(v, a.partials, 0, &a.sc->counter[6]) && threadIdx.x < 32) {
+        double tot[1];
+        final_sums<1>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            a.sc->de = tot[0];
+            a.sc->counter[6] = 0;
+        }
+    }
+}
+
+// batch: the chunk's energy difference goes to slot 0 (cells in
+// cell_active only)
+template <int TPA, bool ORTHO>
+__global__ void __launch_bounds__(256) k_de32b(EamArgs a) {
+    __shared__ Smem32 S;
+    S.fill(a);
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int apb = blockDim.x / TPA;
+    for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        const int cell = a.chunk_cell[ch];
+        if (a.cell_active && !a.cell_active[cell]) continue;
+        const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
+        const CellFrame fr = cell_frame<ORTHO>(a.cells + cell);
+        const float alpha = (float)a.cell_alpha[cell];
+        float es = 0.f, ec = 0.f;
+        for (int i0 = lo; i0 < hi; i0 += apb) {
+            const int i = i0 + (int)threadIdx.x / TPA;
+            de_atom<TPA, ORTHO>(a, S, K, fr, i, lane, i < hi, alpha, es, ec);
         }
         chunk_store<1>([&](int) { return (double)es - (double)ec; }, a.chunk_part + (size_t)ch * kChunkSlots);
     }
@@ -615,6 +846,20 @@ static void energy_t(mappg_sys* s, const EamArgs& a) {
 }
 
 template <int TPA, bool ORTHO, int U>
+static void de_t(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_de32<TPA, ORTHO>, 256);
+    k_de32<TPA, ORTHO><<<grid, 256, 0, s->stream>>>(a);
+}
+
+template <int TPA, bool ORTHO, int U>
+static void de_b(mappg_sys* s, const EamArgs& a) {
+    static int grid = 0;
+    if (!grid) grid = occupancy_grid(s, k_de32b<TPA, ORTHO>, 256);
+    k_de32b<TPA, ORTHO><<<std::min(grid, a.nchunk), 256, 0, s->stream>>>(a);
+}
+
+template <int TPA, bool ORTHO, int U>
 static void density_b(mappg_sys* s, const EamArgs& a) {
     static int grid = 0;
     if (!grid) grid = occupancy_grid(s, k_density32b<TPA, ORTHO, U>, 256);
@@ -689,6 +934,23 @@ void launch_force32(mappg_sys* s, const EamArgs& a) {
         MAPPG_TPA32(force_t);
     }
 }
+// E(x0 + alpha h) - E(x0) into sc->de (one cell; p32, rows and rho of x0,
+// h32 set by the caller)
+void launch_de32(mappg_sys* s, double alpha) {
+    EamArgs a = eam_args(s);
+    a.alpha = alpha;
+    MAPPG_TPA32(de_t);
+}
+
+// batch: per-cell energy differences with each cell's trial step
+// cell_alpha[c], for the cells in cell_active, into CellMd::energy
+void launch_de32b(mappg_sys* s, const double* cell_alpha) {
+    EamArgs a = eam_args(s);
+    a.cell_alpha = cell_alpha;
+    MAPPG_TPA32B(de_b);
+    cells_done(s, a, 1);
+}
+
 void launch_energy32(mappg_sys* s, const EamArgs& a) {
     if (s->ncell > 1) {
         MAPPG_TPA32B(energy_b);

@@ -17,6 +17,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "linesearch.h"
@@ -34,7 +35,8 @@ struct LbScal {
     double alpha[64];
     double gamma;
     double fh, hh, hmax, fmax;
-    double tau;  // scale of the learned diagonal, (s.y)/(y.P.y)
+    double tau;    // scale of the learned diagonal, (s.y)/(y.P.y)
+    double dxmax;  // max |x - x_build| component (list validity of line-search trials)
 };
 
 __device__ __forceinline__ void warp_sum(double& t) {
@@ -128,25 +130,29 @@ __global__ void __launch_bounds__(256) k_lb_axpy_dot(int N, double* __restrict__
     }
 }
 
-// dots f.h, h.h and max|h| (line-search preparation) and max|f|
+// dots f.h, h.h and max|h| (line-search preparation) and max|f|; with x
+// and xb (the neighbour list's build positions) also max|x - xb| over
+// components
 __global__ void __launch_bounds__(256) k_lb_prep(int N, const double* __restrict__ f, const double* __restrict__ h,
+                                                 const double* __restrict__ x, const double* __restrict__ xb,
                                                  LbScal* L, double* partials, unsigned* counter) {
     double v[2] = {0.0, 0.0};
-    double mx[2] = {0.0, 0.0};
+    double mx[3] = {0.0, 0.0, 0.0};
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x) {
         double hv = h[q], fv = f[q];
         v[0] += fv * hv;
         v[1] += hv * hv;
         mx[0] = fmax(mx[0], fabs(hv));
         mx[1] = fmax(mx[1], fabs(fv));
+        if (x) mx[2] = fmax(mx[2], fabs(x[q] - xb[q]));
     }
-    // sums into slots 0,1 and maxima into slots 2,3 of the same partial row
-    __shared__ double red[32][4];
+    // sums into slots 0,1 and maxima into slots 2,3,4 of the same partial row
+    __shared__ double red[32][5];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double t[4] = {v[0], v[1], mx[0], mx[1]};
+    double t[5] = {v[0], v[1], mx[0], mx[1], mx[2]};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 5; k++) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             double u = __shfl_xor_sync(0xffffffffu, t[k], o);
@@ -155,7 +161,7 @@ __global__ void __launch_bounds__(256) k_lb_prep(int N, const double* __restrict
         if (lane == 0) red[w][k] = t[k];
     }
     __syncthreads();
-    if (threadIdx.x < 4) {
+    if (threadIdx.x < 5) {
         double r = 0.0;
         for (int q = 0; q < nw; q++) r = threadIdx.x < 2 ? r + red[q][threadIdx.x] : fmax(r, red[q][threadIdx.x]);
         partials[blockIdx.x * kRedSlots + threadIdx.x] = r;
@@ -165,29 +171,36 @@ __global__ void __launch_bounds__(256) k_lb_prep(int N, const double* __restrict
     if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
     __syncthreads();
     if (last && threadIdx.x < 32) {
-        double s2[2], m2[2];
+        double s2[2], m3[3];
         for (int k = 0; k < 2; k++) {
-            double a = 0.0, b = 0.0;
-            for (int bb = lane; bb < (int)gridDim.x; bb += 32) {
-                a += partials[bb * kRedSlots + k];
-                b = fmax(b, partials[bb * kRedSlots + 2 + k]);
-            }
+            double a = 0.0;
+            for (int bb = lane; bb < (int)gridDim.x; bb += 32) a += partials[bb * kRedSlots + k];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
-            }
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
             s2[k] = a;
-            m2[k] = b;
+        }
+        for (int k = 0; k < 3; k++) {
+            double b = 0.0;
+            for (int bb = lane; bb < (int)gridDim.x; bb += 32) b = fmax(b, partials[bb * kRedSlots + 2 + k]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+            m3[k] = b;
         }
         if (threadIdx.x == 0) {
             L->fh = s2[0];
             L->hh = s2[1];
-            L->hmax = m2[0];
-            L->fmax = m2[1];
+            L->hmax = m3[0];
+            L->fmax = m3[1];
+            L->dxmax = m3[2];
             *counter = 0;
         }
     }
+}
+
+// the search direction as one float4 per atom (Cartesian) for k_de32
+__global__ void k_lb_h32(int n, const double* __restrict__ h, float4* __restrict__ h32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        h32[i] = make_float4((float)h[i], (float)h[n + i], (float)h[2 * n + i], 0.f);
 }
 
 // x = x0 + alpha*h  (MinMDHandler::F, min_cg.h:260-267)
@@ -246,6 +259,7 @@ struct LbState {
 };
 
 void launch_energy64(mappg_sys* s);  // eam.cu
+void launch_de32(mappg_sys* s, double alpha);  // eam32.cu
 
 static double lb_energy(mappg_sys* s) {
     // skin test and (gated) rebuild, then the energy kernel; mixed systems
@@ -297,21 +311,49 @@ void iteration_hook(mappg_sys* s, int istep) {
 
 // The minimizers' line-search function (MinMDHandler::F and F_reset,
 // min_cg.h:260-276): a trial moves x to x0 + alpha h and evaluates the
-// energy; reset restores x0.
+// energy; reset restores x0.  Trial energies by mode:
+//   E64      the FP64 energy (FP64 systems; mixed systems on FP64 forces)
+//   DELTA    e0 + dE, dE from the energy-difference pass (launch_de32) on
+//            x0's rows and frame positions; no skin test or rebuild (the
+//            caller has checked that every trial stays within the skin)
+//   E32DIFF  e0 + (E32(trial) - E32(x0)) with the skin test and rebuilds:
+//            searches whose first step is too long for DELTA, where the
+//            energy changes are large next to the FP32 rounding
 struct TrialLine {
+    enum Mode { E64, DELTA, E32DIFF };
     mappg_sys* s;
     int N, grid;
     const double* xs;  // x0
     const double* h;
     long long* n_en;
+    Mode mode = E64;
+    double e0 = 0.0;     // energy of x0 (DELTA, E32DIFF)
+    double e0_32 = 0.0;  // FP32 energy of x0 (E32DIFF)
     double F(double a) {
         k_lb_trial<<<grid, 256, 0, s->stream>>>(N, s->x, xs, h, a);
         (*n_en)++;
-        return lb_energy(s);
+        if (mode == E64) return lb_energy(s);
+        double e;
+        if (mode == DELTA) {
+            launch_de32(s, a);
+            MAPPG_CUDA(cudaMemcpyAsync(&e, &s->sc->de, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+            return e0 + e;
+        }
+        return e0 + (energy32(s) - e0_32);
     }
     void reset() {
         MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, s->stream));
+        if (mode != DELTA) lb_update(s);
+    }
+    // skin test, gated rebuild, then the FP32 energy
+    static double energy32(mappg_sys* s) {
         lb_update(s);
+        launch_energy(s);
+        double e;
+        MAPPG_CUDA(cudaMemcpyAsync(&e, &s->sc->energy, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        return e;
     }
 };
 
@@ -362,6 +404,21 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
     } promote{s};
     cudaStream_t st = s->stream;
     double* part = s->partials;
+    // mixed systems: line-search trials inside the skin take energy
+    // differences (TrialLine delta mode), which need x0's FP64 density and
+    // the direction as float4
+    const bool mixed = s->precision == MAPPG_MIXED;
+    struct KeepRho {
+        mappg_sys* s;
+        ~KeepRho() {
+            s->keep_rho64 = false;
+            s->h32 = nullptr;
+        }
+    } keep_rho{s};
+    if (mixed) {
+        s->keep_rho64 = true;
+        s->h32 = (float4*)dalloc(sizeof(float4) * (size_t)s->n);
+    }
 
     // NewDynamicMD::init then the opening force call
     sys_build(s);
@@ -373,16 +430,18 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
     double e_prev, alpha_m = 0.0;
     int k = 0;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
+    double dxmax = 0.0;
     auto read_prep = [&](double* fh, double* hh, double* hmax, double* fmax_) {
-        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, L, part, counter);
+        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, s->x, s->x0, L, part, counter);
         MAPPG_CUDA(cudaGetLastError());
-        double buf[4];
+        double buf[6];
         MAPPG_CUDA(cudaMemcpyAsync(buf, &L->fh, sizeof(buf), cudaMemcpyDeviceToHost, st));
         MAPPG_CUDA(cudaStreamSynchronize(st));
         *fh = buf[0];
         *hh = buf[1];
         *hmax = buf[2];
         *fmax_ = buf[3];
+        dxmax = buf[5];
     };
     double fh, hh, hmax, fmaxv;
     if (err == LS_S && f_tol > 0.0) {
@@ -442,6 +501,23 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
         } else {
             max_a = fabs(max_dx / hmax);
         }
+        // mixed: trials that keep every atom within half the skin of the
+        // list's build positions (the first, largest trial moves an atom by
+        // at most sqrt(3) alpha max|h_c|) take energy differences on x0's
+        // list; longer searches take differences of FP32 energies
+        line.mode = TrialLine::E64;
+        if (mixed && !s->force64 && dfa < 0.0 && max_a > 0.0) {
+            line.e0 = e_curr;
+            const double a1 = std::min(max_a, 1.0);
+            if (1.7320508075688772 * (a1 * hmax + dxmax) < 0.5 * s->skin) {
+                line.mode = TrialLine::DELTA;
+                k_lb_h32<<<grid_for(s, s->n, 256), 256, 0, st>>>(s->n, h, s->h32);
+                MAPPG_CUDA(cudaGetLastError());
+            } else {
+                line.mode = TrialLine::E32DIFF;
+                line.e0_32 = TrialLine::energy32(s);
+            }
+        }
         if (dfa == 0.0)
             lerr = LS_F_GRAD0;
         else if (max_a == 0.0)
@@ -451,6 +527,11 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
         else
             lerr = search.min(dfa, max_a, e_curr, alpha_m, 0);
         err = lerr;
+        if (line.mode == TrialLine::DELTA) {
+            // the accepted (or restored) positions: skin test, and the FP32
+            // frame positions the force call reads
+            lb_update(s);
+        }
         if (ls_failed(err) && s->precision == MAPPG_MIXED && !s->force64 && f_tol > 0.0) {
             s->force64 = true;
             lb_force(s, &pe_force);
@@ -592,16 +673,18 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsPar
     MAPPG_CUDA(cudaMemsetAsync(L, 0, sizeof(LbScal), st));
     MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned) * 4, st));
     double* part = s->partials;
+    double dxmax = 0.0;
     auto read_prep = [&](double* fh, double* hh, double* hmax, double* fmax_) {
-        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, L, part, counter);
+        k_lb_prep<<<grid, 256, 0, st>>>(N, s->f, h, s->x, s->x0, L, part, counter);
         MAPPG_CUDA(cudaGetLastError());
-        double buf[4];
+        double buf[6];
         MAPPG_CUDA(cudaMemcpyAsync(buf, &L->fh, sizeof(buf), cudaMemcpyDeviceToHost, st));
         MAPPG_CUDA(cudaStreamSynchronize(st));
         *fh = buf[0];
         *hh = buf[1];
         *hmax = buf[2];
         *fmax_ = buf[3];
+        dxmax = buf[5];
     };
     sys_build(s);
     long long n_en = 0, n_fc = 1;
@@ -712,3 +795,69 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsPar
 }
 
 }  // namespace mappg
+
+// ------------------------------------------------------------------ C entry
+namespace mappg {
+void sys_upload(mappg_sys* s, const double* host, double* dev);  // system.cu
+}
+
+// The energy change E(x + alpha h) - E(x) of a mixed-precision system as its
+// minimizers' line searches take it (k_de32), without moving the atoms.
+extern "C" int mappg_sys_energy_delta(mappg_sys* s, const double* h, double alpha, double* de) {
+    using namespace mappg;
+    try {
+        if (!s || !h || !de) throw Error{MAPPG_ERR_ARG, "null argument"};
+        if (s->precision != MAPPG_MIXED) throw Error{MAPPG_ERR_ARG, "energy differences are for mixed-precision systems"};
+        if (s->ncell > 1) throw Error{MAPPG_ERR_UNSUPP, "energy differences run per single cell"};
+        if (!s->built) sys_build(s);
+        const int n = s->n;
+        double* hd = nullptr;
+        float4* h32 = nullptr;
+        MAPPG_CUDA(cudaMalloc(&hd, sizeof(double) * 3 * (size_t)n));
+        MAPPG_CUDA(cudaMalloc(&h32, sizeof(float4) * (size_t)n));
+        struct Free {
+            double* a;
+            float4* b;
+            mappg_sys* s;
+            ~Free() {
+                cudaFree(a);
+                cudaFree(b);
+                s->h32 = nullptr;
+                s->keep_rho64 = false;
+            }
+        } fr{hd, h32, s};
+        // the list must hold every pair inside the cutoff at x and at x + alpha h
+        double hmax = 0.0;
+        for (size_t q = 0; q < 3 * (size_t)n; q++) hmax = std::max(hmax, std::fabs(h[q]));
+        lb_update(s);
+        sys_upload(s, h, hd);
+        const int N = 3 * n, grid = grid_for(s, N, 256);
+        LbScal* L = nullptr;
+        unsigned* counter = nullptr;
+        MAPPG_CUDA(cudaMalloc(&L, sizeof(LbScal)));
+        MAPPG_CUDA(cudaMalloc(&counter, sizeof(unsigned)));
+        MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s->stream));
+        k_lb_prep<<<grid, 256, 0, s->stream>>>(N, hd, hd, s->x, s->x0, L, s->partials, counter);
+        double dxmax = 0.0;
+        MAPPG_CUDA(cudaMemcpyAsync(&dxmax, &L->dxmax, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        cudaFree(L);
+        cudaFree(counter);
+        if (!(1.7320508075688772 * (std::fabs(alpha) * hmax + dxmax) < 0.5 * s->skin))
+            throw Error{MAPPG_ERR_ARG, "alpha*h moves atoms beyond the neighbour list's skin"};
+        s->keep_rho64 = true;
+        s->h32 = h32;
+        launch_force(s);  // density of x kept in FP64, F'(rho) and forces of x
+        k_lb_h32<<<grid_for(s, n, 256), 256, 0, s->stream>>>(n, hd, h32);
+        launch_de32(s, alpha);
+        MAPPG_CUDA(cudaMemcpyAsync(de, &s->sc->de, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        return MAPPG_OK;
+    } catch (const Error& e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return MAPPG_ERR_ARG;
+    }
+}

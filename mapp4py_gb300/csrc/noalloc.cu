@@ -46,11 +46,13 @@ static std::mutex g_scratch_mu;
 
 static unsigned char* scratch_on(int device) {
     if (device < 0 || device >= kMaxDevices) throw Error{MAPPG_ERR_ARG, "device ordinal out of range"};
+    int cur = -1;
+    MAPPG_CUDA(cudaGetDevice(&cur));
+    if (cur != device)
+        throw Error{MAPPG_ERR_ARG, "mappg_sys_force_noalloc: the system lives on device " + std::to_string(device) +
+                                       " but the calling thread's current device is " + std::to_string(cur)};
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch_dev[device]) {
-        int cur = -1;
-        MAPPG_CUDA(cudaGetDevice(&cur));
-        if (cur != device) throw Error{MAPPG_ERR_ARG, "the system's device is not the current device"};
         void* p = nullptr;
         MAPPG_CUDA(cudaGetSymbolAddress(&p, g_scratch));
         preload_force64();

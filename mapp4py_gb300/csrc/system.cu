@@ -804,6 +804,11 @@ EamArgs eam_args(mappg_sys* s) {
     for (int d = 0; d < 3; d++) a.nb[d] = s->nb[d];
     a.q32 = s->q32;
     a.rho = s->rho;
+    a.rho_keep = s->keep_rho64 ? s->rho : nullptr;
+    a.rho0 = s->rho;
+    a.h32 = s->h32;
+    a.alpha = 0.0;
+    a.cell_active = s->cell_active;
     a.dF = s->dF;
     a.rho32out = s->rho32;
     a.f = s->f;

@@ -55,6 +55,7 @@ struct DevScalars {
     unsigned counter[8];  // last-block-done counters, one per reduction site
     double energy;     // last force/energy call
     double e_embed;    // embedding energy of the last mixed density pass
+    double de;         // last energy difference of a line-search trial (k_de32)
     double virial[6];  // F_H voigt
     double com[3];     // mean displacement of the step
     double drift[3];   // mixed MD: displacement not yet removed from x
@@ -159,6 +160,14 @@ struct EamArgs {
     float* f32;            // SoA 3n (mixed kernels)
     double* partials;
     DevScalars* sc;
+    // line searches of mixed-precision minimizers: the density pass also
+    // writes the FP64 density here when non-null; the energy-difference pass
+    // (k_de32) reads it with the search direction h (float4 per atom,
+    // Cartesian) and the trial step alpha
+    double* rho_keep;
+    const double* rho0;
+    const float4* h32;
+    double alpha;
     // per-cell closing half of a batch MD step (k_cells_done)
     double* thermo;
     long long nsteps;
@@ -169,6 +178,8 @@ struct EamArgs {
     const int* chunk_begin;   // nchunk + 1 atom offsets
     const int* chunk_cell;
     double* chunk_part;       // nchunk x kChunkSlots
+    const uint8_t* cell_active;  // batch minimizers: cells the chunk kernels work on (null: all)
+    const double* cell_alpha;    // batch energy differences: trial step per cell
 };
 
 }  // namespace mappg
@@ -235,6 +246,7 @@ struct mappg_sys {
     int* chunk_cell = nullptr;
     int* cell_chunk = nullptr;           // ncell + 1
     double* chunk_part = nullptr;
+    uint8_t* cell_active = nullptr;      // batch minimizer in progress: cells still working (null: all)
     double* chunk_disp = nullptr;        // nchunk x 4 (integrator displacement sums)
     mappg::CellMd* cmd = nullptr;        // per-cell MD state
     double* cell_out = nullptr;          // ncell x 8 (pe, virial6, spare) staging
@@ -245,6 +257,10 @@ struct mappg_sys {
     bool have_v = false;
     bool f_is_f32 = false;  // the newest forces are in f32 (mixed kernels)
     bool force64 = false;   // mixed system computing FP64 forces (end of a relaxation)
+    // mixed minimizer in progress: the density pass keeps the FP64 density
+    // (rho) and h32 holds the search direction for energy differences
+    bool keep_rho64 = false;
+    float4* h32 = nullptr;
     // called by the minimizers after every hook_every-th iteration's force
     // call (mappg_sys_set_hook)
     int (*hook)(void* user, long long iteration) = nullptr;

@@ -6,13 +6,16 @@
  * libmappg C ABI) links, loads or calls this file.  Only tests/, the smoke
  * check and the CPU-baseline leg of bench.py use it, as the checker.
  *
- * Parity status: parity unpinned.  The reference ships no test vectors for
- * this path and cannot be compiled here as shipped (it needs an MPI library
- * and a Python <= 3.10 / NumPy 1.x C-API).  This file restates the cited
- * reference code step by step in the reference's own operation order and is
- * cross-checked by finite differences, lattice symmetry, Newton's third law,
- * energy conservation and the published cohesive energy of the Cu potential
- * file shipped with the reference.
+ * Parity status: pinned to the reference itself.  The reference ships no
+ * test vectors for this path; it is compiled from its own sources with a
+ * single-rank MPI stand-in (ref.mk, refshim/), and the fixtures
+ * tests/golden/ref_*.npz hold its forces, energies, stresses, NVT/NVE
+ * trajectories, L-BFGS iterates and create_temp draws on the analytic
+ * potential and on the four potential files of its examples.  This file
+ * restates the cited reference code step by step in the reference's own
+ * operation order and reproduces those fixtures to 1e-14 (bit for bit for
+ * NVE and create_temp); it is also cross-checked by finite differences,
+ * lattice symmetry, Newton's third law and energy conservation.
  *
  * Reference files cited below are relative to the mapp4py source tree.
  * Build with -ffp-contract=off: the reference's own x86 build never fuses

@@ -55,7 +55,7 @@ def test_single_process_helpers():
 
     assert bench.max_over_ranks(3.5) == 3.5
     assert bench.throughput(1000, 10, 1, 1000.0) == 10000.0
-    c = bench.workload_config(2048000, 80, "mixed", 1)
+    c = bench.workload_config(2048000, 80, 1)
     assert c["natoms"] == 2048000 and "80^3" in c["workload"]
 
 

@@ -110,6 +110,26 @@ def test_mixed_precision_error_budget(potentials):
     assert abs(s32.energy() - pe64) / c.natoms <= 1e-7
 
 
+def test_mixed_precision_error_budget_full_workload_cell(potentials):
+    """The bar on the MD workload cell itself: 2,048,000-atom 50/50 A/B alloy
+    (FCC 80^3, a = 3.615 A, seed 1, 0.05 A noise), mixed precision against
+    the FP64 GPU path on the same configuration."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((80, 80, 80), xB=0.5, sigma=0.05, seed=1)
+    ff = _lib.ForceField.setfl(path)
+    s64 = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+    pe64, vir64 = s64.force()
+    f64 = s64.get_f()
+    del s64
+    s32 = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
+    pe32, vir32 = s32.force()
+    f32 = s32.get_f()
+    rms = np.sqrt(np.mean(np.sum((f64 - f32) ** 2, axis=1)))
+    assert rms <= 1e-5, "force RMS error %.3e" % rms
+    assert abs(pe32 - pe64) / c.natoms <= 1e-7, (pe32 - pe64) / c.natoms
+    assert np.max(np.abs(vir32 - vir64)) <= 1e-6 * np.max(np.abs(vir64))
+
+
 def test_nvt_trajectory_matches_golden(potentials):
     g = golden("nvt_a_256")
     path, digest = potentials[("A",)]

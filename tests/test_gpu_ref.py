@@ -12,7 +12,8 @@ density is extrapolated, md.nvt/NVE trajectories and md.min_lbfgs iterates.
 
 Tolerances: FP64 forces 1e-10 relative to the largest force component,
 energy 1e-12 relative, stress 1e-11 relative; mixed precision force RMS
-<= 1e-5 eV/A and energy <= 1e-7 eV/atom against the reference; trajectories
+<= 1e-5 eV/A (or 3e-6 of the RMS force, for the compressed cell) and energy
+<= 1e-7 eV/atom against the reference; trajectories
 1e-9 A after 40-100 steps; L-BFGS iterates 1e-8 A after up to 20 iterations.
 """
 import numpy as np
@@ -80,8 +81,12 @@ def test_reference_potential_files(tmp_path, pot, precision):
             assert np.max(np.abs(stress(vir, H) - S_r)) <= 1e-11 * np.max(np.abs(S_r)), cell
             assert abs(s.energy() - float(g[cell + "/energy"])) <= 1e-12 * abs(pe_r), cell
         else:
+            # FP32 distances carry ~6e-8 relative rounding, so the force error
+            # grows with the stiffness: 1e-5 eV/A near equilibrium, 3e-6 of the
+            # RMS force in strongly compressed cells (dense Cu: 6.4 eV/A RMS)
             rms = np.sqrt(np.mean(np.sum((s.get_f() - f_r) ** 2, axis=1)))
-            assert rms <= 1e-5, (cell, rms)
+            frms = np.sqrt(np.mean(np.sum(f_r ** 2, axis=1)))
+            assert rms <= max(1e-5, 3e-6 * frms), (cell, rms, frms)
             assert abs(pe - pe_r) / x.shape[0] <= 1e-7, (cell, pe - pe_r)
 
 

@@ -57,6 +57,35 @@ def test_noalloc_matches_force_on_consecutive_calls(potentials):
     _check_against_force(a)
 
 
+def test_noalloc_calls_after_the_first_allocate_nothing(potentials):
+    """The promise itself: once the first call on the device has done its
+    set-up, further calls leave the device's free memory and torch's pool
+    exactly as they were."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    ff = _lib.ForceField.setfl(potentials[("A", "B")][0])
+    c = synth.alloy((6, 6, 6), xB=0.4, sigma=0.06, seed=21)
+    s = _lib.System(ff, c.H, c.x, c.elem, c.masses)
+    s.build()
+    f = torch.empty((s.n, 3), dtype=torch.float64, device="cuda")
+    ev = torch.empty(7, dtype=torch.float64, device="cuda")
+    fp, evp = C.c_void_p(f.data_ptr()), C.c_void_p(ev.data_ptr())
+    _lib.check(L.mappg_sys_force_noalloc(s.h, fp, evp))  # first call: set-up
+    s.sync()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for _ in range(5):
+        _lib.check(L.mappg_sys_force_noalloc(s.h, fp, evp))
+    s.sync()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "device free memory changed by %d bytes" % (free0 - free1)
+    assert torch.cuda.memory_reserved() == reserved0
+    pe, _ = s.force()
+    assert abs(float(ev[0].item()) - pe) <= 1e-12 * abs(pe)
+
+
 def test_noalloc_refuses_what_it_cannot_do(potentials):
     torch = pytest.importorskip("torch")
     L = _lib.load()
