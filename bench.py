@@ -209,18 +209,22 @@ def run_reference(args, rank, world):
 
 def run_batch(args, ff, torch):
     """512 independent A/B alloy cells (log-uniform 500-32,000 atoms, random
-    composition, vacancies, temperatures 100-1200 K) advanced together, one
-    CUDA graph per step over all cells; device-timed like the main line."""
+    composition, vacancies, temperatures 100-1200 K) advanced together.  A
+    3-step warm-up run, then the timed run: its args.batch_steps steps of
+    every cell are one CUDA graph, launched once; device-timed like the main
+    line."""
     from mapp4py_gb300 import _lib, synth
 
     cells, temps = synth.batch_cells(args.batch_cells, seed=7)
     b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
     b.set_v(np.concatenate([c.v for c in cells]))
-    tpa, unroll, _ = b.autotune()
+    tpa, unroll, tune = b.autotune()
     K, W = args.batch_steps, 3
-    b.nvt_begin(temps, synth.FS, synth.KB, W + K)
-    stream = torch.cuda.ExternalStream(b.stream())
+    b.nvt_begin(temps, synth.FS, synth.KB, W)
     b.nvt_steps(W)
+    b.nvt_end(W)
+    b.nvt_begin(temps, synth.FS, synth.KB, K)  # captures the K steps as one graph
+    stream = torch.cuda.ExternalStream(b.stream())
     b.sync()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -229,12 +233,14 @@ def run_batch(args, ff, torch):
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    b.nvt_end(W + K)
+    b.nvt_end(K)
     st = b.stats()
     return {"workload": "%d independent cells, %d atoms (%d-%d per cell), NVT at 100-1200 K, mixed precision"
                         % (len(cells), b.n, int(b.natoms.min()), int(b.natoms.max())),
             "value": b.n * K / (ms / 1000.0), "unit": "atom-steps/s", "steps": K, "ms_per_step": ms / K,
-            "rebuilds_in_run": st["rebuilds"], "lanes_per_atom": tpa, "entries_per_step": unroll}
+            "graph_launches": 1 if K <= 512 else -(-K // 512), "rebuilds_in_run": st["rebuilds"],
+            "lanes_per_atom": tpa, "entries_per_step": unroll, "atoms_per_chunk": b.chunk_atoms,
+            "autotune_ms": {"%d,%d,%d" % k: round(v, 4) for k, v in tune.items()}}
 
 
 def run_lbfgs(args, ff):
@@ -271,7 +277,7 @@ def run_lbfgs(args, ff):
             "cell_253k": one(40, args.lbfgs_cap), "cell_4k": one(10, 5 * args.lbfgs_cap)}
 
 
-def run_accuracy(args, ff, cell, torch):
+def run_accuracy(args, ff, path, cell, torch):
     """The FP64 path on the same 2,048,000-atom cell (throughput), the mixed
     path's error against it (force RMS, energy per atom), and the NVE energy
     drift of both paths (run_nve)."""
@@ -303,31 +309,38 @@ def run_accuracy(args, ff, cell, torch):
                             "force_max_eV_per_A": float(np.max(np.abs(fa - fb))),
                             "energy_eV_per_atom": float(abs(pa - pb) / cell.natoms)}
     del a, b
-    out["nve"] = run_nve(args, ff)
+    out["nve"] = run_nve(args, path)
     return out
 
 
-def run_nve(args, ff):
-    """NVE energy drift (t_relax = inf, dt = 1 fs) on a 32,000-atom cell of
-    the workload's recipe (FCC 20^3, 50/50 A/B, 0.05 A noise, 600 K start):
-    mixed precision over args.nve_ps picoseconds, FP64 over a fifth of that.
-    Drift = slope of a straight-line fit of the total energy per atom."""
+def run_nve(args, ff_path):
+    """NVE energy drift (t_relax = inf, dt = 1 fs) over args.nve_ps
+    picoseconds, mixed and FP64, on the 4,000-atom single-element FCC cell
+    of the plain FP64 workload (300 K start).  The 50/50 alloy of the MD
+    workload is metastable under this potential: NVE runs of it (and of the
+    single-element crystal from 600 K) collapse within a few ps into a denser
+    structure (rows 78 -> 125 entries, 0.7-1 eV/atom released; the oracle
+    shows the same), so a drift over tens of ps is only meaningful on a cell
+    that stays crystalline.  Drift = slope of a straight-line fit of the
+    total energy per atom."""
     from mapp4py_gb300 import _lib, synth
 
-    c = synth.alloy((20, 20, 20), xB=0.5, sigma=0.05, T=T_K, seed=1)
-    out = {"workload": "%d-atom cell of the same recipe (FCC 20^3)" % c.natoms, "dt_fs": 1.0}
-    for name, prec, ps in (("mixed", _lib.MIXED, args.nve_ps), ("fp64", _lib.FP64, args.nve_ps / 5.0)):
-        nsteps = int(round(ps * 1000))
-        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=prec)
+    c = synth.md_single((10, 10, 10), T=300.0, seed=0)
+    ff1 = _lib.ForceField.setfl(ff_path, ["A"])
+    out = {"workload": "%d-atom single-element FCC 10^3, 300 K start" % c.natoms, "dt_fs": 1.0}
+    for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
+        nsteps = int(round(args.nve_ps * 1000))
+        s = _lib.System(ff1, c.H, c.x, c.elem, c.masses, precision=prec)
         s.set_v(c.v)
         t0 = time.perf_counter()
-        th, _ = s.nvt_run(T_K, synth.FS, synth.KB, nsteps, t_relax=float("inf"), thermo=True)
+        th, _ = s.nvt_run(300.0, synth.FS, synth.KB, nsteps, t_relax=float("inf"), thermo=True)
         secs = time.perf_counter() - t0
         etot = (th[:, 0] + 0.5 * (th[:, 2] + th[:, 5] + th[:, 7])) / c.natoms
         t_ns = np.arange(nsteps + 1) * 1e-6
         slope = np.polyfit(t_ns, etot, 1)[0]
         out[name] = {"steps": nsteps, "span_ns": nsteps * 1e-6, "drift_eV_per_atom_per_ns": float(slope),
-                     "max_deviation_eV_per_atom": float(np.max(np.abs(etot - etot[0]))), "seconds": secs}
+                     "max_deviation_eV_per_atom": float(np.max(np.abs(etot - etot[0]))),
+                     "T_end_K": float(th[-1, 1]), "seconds": secs}
     return out
 
 
@@ -488,7 +501,7 @@ def run_gpu(args, rank, world, local_rank):
     lbfgs = None if args.lbfgs_cap <= 0 else run_lbfgs(args, ff)
     extras = None
     if args.extras and rank == 0:
-        extras = run_accuracy(args, ff, cell, torch)
+        extras = run_accuracy(args, ff, path, cell, torch)
         if not args.no_cpu:
             extras["c1"] = run_c1(args, path, torch)
 
@@ -533,7 +546,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--batch-steps", type=int, default=100,
+    ap.add_argument("--batch-steps", type=int, default=500,
                     help="steps of the 512-cell batch measurement (0 skips it)")
     ap.add_argument("--batch-cells", type=int, default=512)
     ap.add_argument("--no-extras", dest="extras", action="store_false",

@@ -274,6 +274,14 @@ int mappg_sys_sync(mappg_sys* sys);
  * reference. */
 int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
 
+/* A batch of cells (mappg_batch_create): the atoms per chunk (128, 256 or
+ * 512: the atoms a block of the batch kernels works through before it takes
+ * another chunk) together with mappg_sys_autotune's lanes per atom and
+ * entries per loop step, each of the 21 candidates timed on the batch's own
+ * cells and neighbour lists; the fastest is kept.  No counterpart in the
+ * reference (it runs one cell).  ms_out: NULL or 21 doubles, chunk-major. */
+int mappg_batch_autotune(mappg_sys* sys, int* tpa, int* unroll, int* chunk_atoms, double* ms_out);
+
 /* Enqueue one kernel launch on the system's stream without waiting, for
  * timing: 0 density + embedding, 1 force/virial (uses the last F'(rho)),
  * 2 energy only, 3 neighbour rebuild. */

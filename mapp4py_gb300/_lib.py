@@ -26,6 +26,7 @@ _HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_longlong)
 SIGNATURES = {
     "mappg_last_error": (C.c_char_p, []),
     "mappg_device_info": (C.c_int, [C.c_char_p, C.c_int, _I]),
+    "mappg_batch_autotune": (C.c_int, [_VP, _I, _I, _I, _D]),
     "mappg_fp64_fma_rate": (C.c_int, [C.c_int, C.c_int, _D]),
     "mappg_ff_setfl": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
     "mappg_ff_fs": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
@@ -557,6 +558,22 @@ class Batch(System):
         """Per-cell views of a concatenated per-atom array."""
         return [a[self.offsets[c]:self.offsets[c + 1]] for c in range(self.ncell)]
 
+
+    def autotune(self):
+        """(lanes per atom, entries per step, {(chunk atoms, lanes, entries): ms})
+        over atoms per chunk 128/256/512 and the lanes/entries candidates;
+        the chosen chunk size is in self.chunk_atoms."""
+        tpa, unroll, chunk = C.c_int(), C.c_int(), C.c_int()
+        ms = np.zeros(21)
+        check(load().mappg_batch_autotune(self.h, C.byref(tpa), C.byref(unroll), C.byref(chunk), dptr(ms)))
+        keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2), (32, 1))
+        self.chunk_atoms = chunk.value
+        out = {}
+        for q, ch in enumerate((128, 256, 512)):
+            for k, v in zip(keys, ms[7 * q:7 * q + 7]):
+                if v > 0:
+                    out[(ch,) + k] = v
+        return tpa.value, unroll.value, out
     def force(self):
         pe = np.zeros(self.ncell)
         vir = np.zeros((self.ncell, 6))

@@ -568,6 +568,44 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
     });
 }
 
+// a batch of cells: atoms per chunk (the atoms one block works through
+// before it takes the next chunk: 128, 256, 512) together with the lanes
+// per atom and entries per loop step of mappg_sys_autotune, each candidate
+// timed on the batch's own cells and lists; ms_out: 3 x 7 timings
+int mappg_batch_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, int* chunk_out, double* ms_out) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (s->ncell <= 1) throw Error{MAPPG_ERR_ARG, "mappg_batch_autotune takes a batch of cells"};
+        const int chunks[3] = {128, 256, 512};
+        double best = 1e30;
+        int bt = s->tpa, bu = s->unroll, bc = s->chunk_atoms;
+        for (int k = 0; k < 3; k++) {
+            sys_rechunk(s, chunks[k]);
+            double ms[7] = {0, 0, 0, 0, 0, 0, 0};
+            int t = 0, u = 0;
+            int rc = mappg_sys_autotune(s, &t, &u, ms);
+            if (rc != MAPPG_OK) throw Error{rc, mappg_last_error()};
+            for (int c = 0; c < 7; c++) {
+                if (ms_out) ms_out[7 * k + c] = ms[c];
+                if (ms[c] > 0.0 && ms[c] < best) {
+                    best = ms[c];
+                    bc = chunks[k];
+                }
+            }
+            if (bc == chunks[k]) {
+                bt = t;
+                bu = u;
+            }
+        }
+        sys_rechunk(s, bc);
+        s->tpa = bt;
+        s->unroll = bu;
+        if (tpa_out) *tpa_out = bt;
+        if (unroll_out) *unroll_out = bu;
+        if (chunk_out) *chunk_out = bc;
+    });
+}
+
 int mappg_create_temp(int natoms, const unsigned char* elem, const double* masses, double T, double kB, int seed,
                       double* v) {
     return mappg_create_temp_dof(natoms, elem, masses, nullptr, T, kB, seed, v);

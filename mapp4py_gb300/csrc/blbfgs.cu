@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(256) k_bl_step(BlArgs a, int st, int mode, int
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
         const BlCell& c = a.cs[a.chunk_cell[ch]];
         const bool on = c.state == st;
+        if (!on) continue;  // uniform per block: the chunk's partial is not read
         double coef = 0.0;
         int su = 0, sn = 0;
         if (on) {
@@ -192,6 +193,7 @@ __global__ void __launch_bounds__(256) k_bl_prep(BlArgs a, int st) {
     const int n = a.n;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
         const bool on = st < 0 || a.cs[a.chunk_cell[ch]].state == st;
+        if (!on) continue;
         double v[4] = {0.0, 0.0, 0.0, 0.0};
         for (int ii = a.chunk_begin[ch] + threadIdx.x; on && ii < a.chunk_begin[ch + 1]; ii += blockDim.x)
             for (int q = 0; q < 3; q++) {
@@ -337,6 +339,7 @@ __global__ void __launch_bounds__(256) k_bl_hist(BlArgs a) {
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
         const BlCell& c = a.cs[a.chunk_cell[ch]];
         const bool on = c.state == BL_ACCEPT;
+        if (!on) continue;
         const int hd = (c.head + 1) % a.m;
         double v[4] = {0.0, 0.0, 0.0, 0.0};
         for (int ii = a.chunk_begin[ch] + threadIdx.x; on && ii < a.chunk_begin[ch + 1]; ii += blockDim.x)
@@ -450,6 +453,7 @@ __global__ void __launch_bounds__(256) k_bl_dx(BlArgs a) {
     const int n = a.n;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
         const bool on = a.cs[a.chunk_cell[ch]].state == BL_LS;
+        if (!on) continue;
         double v[1] = {0.0};
         for (int ii = a.chunk_begin[ch] + threadIdx.x; on && ii < a.chunk_begin[ch + 1]; ii += blockDim.x)
             for (int q = 0; q < 3; q++) {
@@ -472,6 +476,25 @@ __global__ void k_bl_cells_bound(BlArgs a) {
     if (cs.state != BL_LS) return;
     cs.dxmax = dx;
     if (!(1.7320508075688772 * (cs.a * cs.hmax + dx) < a.skin_half)) atomicAdd(a.count, 1);
+}
+
+// counts the searching cells whose next trial moves an atom by a quarter of
+// the skin or more (a search of FP32 energy differences goes over to energy
+// differences once none does)
+__global__ void k_bl_count_long(BlArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    const BlCell& cs = a.cs[c];
+    if (cs.state == BL_LS && !(1.7320508075688772 * cs.a * cs.hmax < 0.5 * a.skin_half)) atomicAdd(a.count, 1);
+}
+
+// the searching cells back at x0
+__global__ void k_bl_restore_ls(BlArgs a) {
+    const int n = a.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (a.cs[a.cell_of[i]].state != BL_LS) continue;
+        for (int q = 0; q < 3; q++) a.x[(size_t)q * n + i] = a.x0[(size_t)q * n + i];
+    }
 }
 
 // per-cell trial steps for the energy-difference pass; FP32 energies of x0
@@ -671,7 +694,10 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
                     k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
                     launch_energy32(s, eam_args(s));
                 } else {
+                    k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
+                    s->cell_active = a.active;
                     launch_energy64(s);
+                    s->cell_active = nullptr;
                 }
             }
             MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
@@ -680,16 +706,37 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
             MAPPG_CUDA(cudaMemcpyAsync(&left, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
             MAPPG_CUDA(cudaStreamSynchronize(st));
             if (left == 0) break;
+            if (a.emode == BL_E32DIFF) {
+                // once every remaining trial is short, differences of FP32
+                // energies would drown in their rounding: back to x0 (and a
+                // list around it) and on with energy differences
+                MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+                k_bl_count_long<<<gb, 256, 0, st>>>(a);
+                int longer = 0;
+                MAPPG_CUDA(cudaMemcpyAsync(&longer, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+                MAPPG_CUDA(cudaStreamSynchronize(st));
+                if (longer == 0) {
+                    k_bl_restore_ls<<<ga, 256, 0, st>>>(a);
+                    lb_update(s);
+                    MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+                    k_bl_dx<<<gc, 256, 0, st>>>(a);
+                    k_bl_cells_bound<<<gw, 256, 0, st>>>(a);
+                    int wide = 0;
+                    MAPPG_CUDA(cudaMemcpyAsync(&wide, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    MAPPG_CUDA(cudaStreamSynchronize(st));
+                    if (wide == 0) {
+                        a.emode = BL_EDELTA;
+                        k_lb_h32b<<<ga, 256, 0, st>>>(n, a.h, h32);
+                        MAPPG_CUDA(cudaGetLastError());
+                    }
+                }
+            }
         }
         k_bl_restore<<<ga, 256, 0, st>>>(a);
         lb_update(s);
         // force pass of the cells that took a step, tolerances and history
-        if (mixed && !s->force64) {
-            k_bl_active<<<gb, 256, 0, st>>>(a, BL_ACCEPT);
-            s->cell_active = a.active;
-        } else {
-            s->cell_active = nullptr;
-        }
+        k_bl_active<<<gb, 256, 0, st>>>(a, BL_ACCEPT);
+        s->cell_active = a.active;
         launch_force(s);
         sync_forces64(s);
         s->cell_active = nullptr;

@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(256) k_density64b(EamArgs a, const int* __rest
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         double eacc = 0.0;
         for (int i0 = lo; i0 < hi; i0 += apb) {
@@ -323,6 +324,7 @@ __global__ void __launch_bounds__(256) k_force64b(EamArgs a, const int* __restri
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         double ep = 0;
         double w[6] = {0, 0, 0, 0, 0, 0};
@@ -494,6 +496,7 @@ __global__ void __launch_bounds__(256) k_energy64b(EamArgs a, const int* __restr
     const int lane = threadIdx.x % TPA;
     const int apb = blockDim.x / TPA;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        if (a.cell_active && !a.cell_active[a.chunk_cell[ch]]) continue;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         double ep = 0.0, eacc = 0.0;
         for (int i0 = lo; i0 < hi; i0 += apb) {

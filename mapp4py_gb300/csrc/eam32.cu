@@ -198,7 +198,7 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
         const float cut0 = S.cut_sq[0];
-        auto pair = [&](int e, const float4& q) {
+        auto pair = [&](int e, const float4& q) -> bool {
             const int ej = entry_elem(e);
             float4 o;
             image_offset(e, o);
@@ -216,26 +216,34 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
                 else
                     c = __ldg(a.rho32 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m);
                 kahan_add(acc, acc_c, fmaf(fmaf(fmaf(c.w, fr, c.z), fr, c.y), fr, c.x));
+                return true;
             }
+            return false;
         };
+        // bit t of `bits`: this lane's t-th entry (row slot lane + t TPA) is
+        // inside the cutoff
+        unsigned bits = 0u;
         if (U == 1) {
-            for (int k = lane; k < nn; k += TPA) {
+            int t = 0;
+            for (int k = lane; k < nn; k += TPA, t++) {
                 const int e = __ldg(row + k);
-                pair(e, __ldg(a.p32 + entry_j(e)));
+                if (pair(e, __ldg(a.p32 + entry_j(e))) && t < 32) bits |= 1u << t;
             }
         } else {
             // two entries per step: both gathers are in flight together;
             // the additions keep the order of the one-entry loop
-            for (int k = lane; k < nn; k += 2 * TPA) {
+            int t = 0;
+            for (int k = lane; k < nn; k += 2 * TPA, t += 2) {
                 const bool v1 = k + TPA < nn;
                 const int e0 = __ldg(row + k);
                 const int e1 = v1 ? __ldg(row + k + TPA) : e0;
                 const float4 q0 = __ldg(a.p32 + entry_j(e0));
                 const float4 q1 = __ldg(a.p32 + entry_j(e1));
-                pair(e0, q0);
-                if (v1) pair(e1, q1);
+                if (pair(e0, q0) && t < 32) bits |= 1u << t;
+                if (v1 && pair(e1, q1) && t + 1 < 32) bits |= 1u << (t + 1);
             }
         }
+        if (a.cutmask && nn <= 32 * TPA) a.cutmask[(size_t)i * TPA + lane] = bits;
     }
     const double rho = lane_sum64<TPA>(acc, acc_c);
     if (active && lane == 0) {
@@ -387,7 +395,34 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 kahan_add(w[5], wc[5], fdz * dz);
             }
         };
-        if (U == 1) {
+        if (a.cutmask && nn <= 32 * TPA) {
+            // only the entries the density pass found inside the cutoff (the
+            // same positions), in the same order: the skin shell's entries
+            // cost no gather and no geometry here
+            unsigned bits = __ldg(a.cutmask + (size_t)i * TPA + lane);
+            if (U == 1) {
+                while (bits) {
+                    const int t = __ffs(bits) - 1;
+                    bits &= bits - 1u;
+                    const int e = __ldg(row + lane + t * TPA);
+                    pair(e, __ldg(a.q32 + entry_j(e)));
+                }
+            } else {
+                while (bits) {
+                    const int t0 = __ffs(bits) - 1;
+                    bits &= bits - 1u;
+                    const bool v1 = bits != 0u;
+                    const int t1 = v1 ? __ffs(bits) - 1 : t0;
+                    if (v1) bits &= bits - 1u;
+                    const int e0 = __ldg(row + lane + t0 * TPA);
+                    const int e1 = v1 ? __ldg(row + lane + t1 * TPA) : e0;
+                    const float4 q0 = __ldg(a.q32 + entry_j(e0));
+                    const float4 q1 = __ldg(a.q32 + entry_j(e1));
+                    pair(e0, q0);
+                    if (v1) pair(e1, q1);
+                }
+            }
+        } else if (U == 1) {
             for (int k = lane; k < nn; k += TPA) {
                 const int e = __ldg(row + k);
                 pair(e, __ldg(a.q32 + entry_j(e)));

@@ -37,6 +37,7 @@ struct LbScal {
     double fh, hh, hmax, fmax;
     double tau;    // scale of the learned diagonal, (s.y)/(y.P.y)
     double dxmax;  // max |x - x_build| component (list validity of line-search trials)
+    unsigned long long dxbits;  // the same by k_lb_dxmax (bits of a non-negative double)
 };
 
 __device__ __forceinline__ void warp_sum(double& t) {
@@ -197,6 +198,18 @@ __global__ void __launch_bounds__(256) k_lb_prep(int N, const double* __restrict
     }
 }
 
+// max |x - xb| over components into *out (the bits of a non-negative double
+// order as the values do, so an integer maximum of the bits is the maximum)
+__global__ void k_lb_dxmax(int N, const double* __restrict__ x, const double* __restrict__ xb,
+                           unsigned long long* out) {
+    double m = 0.0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N; q += gridDim.x * blockDim.x)
+        m = fmax(m, fabs(x[q] - xb[q]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
 // the search direction as one float4 per atom (Cartesian) for k_de32
 __global__ void k_lb_h32(int n, const double* __restrict__ h, float4* __restrict__ h32) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -326,10 +339,15 @@ struct TrialLine {
     const double* xs;  // x0
     const double* h;
     long long* n_en;
+    LbScal* L;
     Mode mode = E64;
     double e0 = 0.0;     // energy of x0 (DELTA, E32DIFF)
     double e0_32 = 0.0;  // FP32 energy of x0 (E32DIFF)
+    double hmax = 0.0;   // max |h_c| of the direction
     double F(double a) {
+        // an E32DIFF search whose trials have become short goes over to
+        // energy differences (FP32 differences would drown in rounding)
+        if (mode == E32DIFF && 1.7320508075688772 * a * hmax < 0.25 * s->skin) to_delta(a);
         k_lb_trial<<<grid, 256, 0, s->stream>>>(N, s->x, xs, h, a);
         (*n_en)++;
         if (mode == E64) return lb_energy(s);
@@ -345,6 +363,20 @@ struct TrialLine {
     void reset() {
         MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, s->stream));
         if (mode != DELTA) lb_update(s);
+    }
+    // back at x0 with a list around it; DELTA when the trial of step a then
+    // stays within half the skin
+    void to_delta(double a) {
+        MAPPG_CUDA(cudaMemcpyAsync(s->x, xs, sizeof(double) * N, cudaMemcpyDeviceToDevice, s->stream));
+        lb_update(s);
+        MAPPG_CUDA(cudaMemsetAsync(&L->dxbits, 0, sizeof(unsigned long long), s->stream));
+        k_lb_dxmax<<<grid, 256, 0, s->stream>>>(N, s->x, s->x0, &L->dxbits);
+        unsigned long long bits = 0;
+        MAPPG_CUDA(cudaMemcpyAsync(&bits, &L->dxbits, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        double dx;
+        memcpy(&dx, &bits, sizeof(dx));
+        if (1.7320508075688772 * (a * hmax + dx) < 0.5 * s->skin) mode = DELTA;
     }
     // skin test, gated rebuild, then the FP32 energy
     static double energy32(mappg_sys* s) {
@@ -469,7 +501,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
         }
         MAPPG_CUDA(cudaGetLastError());
     };
-    TrialLine line{s, N, grid, xs, h, &n_en};
+    TrialLine line{s, N, grid, xs, h, &n_en, L};
     LineSearch<TrialLine> search(ls, line);
     int istep = 0;
     for (; err == LS_S; istep++) {
@@ -508,11 +540,12 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
         line.mode = TrialLine::E64;
         if (mixed && !s->force64 && dfa < 0.0 && max_a > 0.0) {
             line.e0 = e_curr;
+            line.hmax = hmax;
+            k_lb_h32<<<grid_for(s, s->n, 256), 256, 0, st>>>(s->n, h, s->h32);
+            MAPPG_CUDA(cudaGetLastError());
             const double a1 = std::min(max_a, 1.0);
             if (1.7320508075688772 * (a1 * hmax + dxmax) < 0.5 * s->skin) {
                 line.mode = TrialLine::DELTA;
-                k_lb_h32<<<grid_for(s, s->n, 256), 256, 0, st>>>(s->n, h, s->h32);
-                MAPPG_CUDA(cudaGetLastError());
             } else {
                 line.mode = TrialLine::E32DIFF;
                 line.e0_32 = TrialLine::energy32(s);
@@ -697,7 +730,7 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsPar
     read_prep(&fh, &hh, &hmax, &fmaxv);
     if (err == LS_S && f_tol > 0.0 && fmaxv < f_tol) err = MIN_S_FTOL;
     double f0_f0 = fh;  // f.f with h = f
-    TrialLine line{s, N, grid, xs, h, &n_en};
+    TrialLine line{s, N, grid, xs, h, &n_en, L};
     LineSearch<TrialLine> search(ls, line);  // prev_val starts at -1 (LineSearch::reset)
     double alpha = 0.0;
     struct Promote {

@@ -709,6 +709,11 @@ struct NvtRun {
     MdArgs a;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
+    // batches: the planned steps (up to kBatchGraphSteps) as one graph, so a
+    // whole run of every cell is one launch
+    cudaGraphExec_t exec_many = nullptr;
+    cudaGraph_t graph_many = nullptr;
+    long long many = 0;
     int L = 3;
     long long planned = 0;
     long long done = 0;
@@ -720,6 +725,8 @@ static void run_clear(mappg_sys* s) {
     if (!r) return;
     if (r->exec) cudaGraphExecDestroy(r->exec);
     if (r->graph) cudaGraphDestroy(r->graph);
+    if (r->exec_many) cudaGraphExecDestroy(r->exec_many);
+    if (r->graph_many) cudaGraphDestroy(r->graph_many);
     delete r;
     s->run = nullptr;
 }
@@ -731,6 +738,8 @@ void sys_join_side(mappg_sys* s);  // system.cu
 // runs this short launch their steps' kernels directly: capturing and
 // instantiating the step graph costs more than it saves over a few steps
 constexpr long long kGraphMinSteps = 8;
+// longest run of batch steps captured as one graph (about 14 nodes a step)
+constexpr long long kBatchGraphSteps = 512;
 
 // MDNVT::init + the opening force call of MDNVT::run, then the step graph
 void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int L, int niters, long long nsteps,
@@ -795,17 +804,22 @@ void nvt_begin(mappg_sys* s, double T, double dt, double kB, double t_relax, int
         k_mvv_init_b<<<std::min(s->nchunk, s->sm_count * 8), 256, 0, s->stream>>>(a);
         k_cells_begin<<<(s->ncell * 32 + 255) / 256, 256, 0, s->stream>>>(a);
         MAPPG_CUDA(cudaGetLastError());
-        MAPPG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            launch_step32b(s, a);
-        } catch (...) {
-            cudaGraph_t g2 = nullptr;
-            cudaStreamEndCapture(s->stream, &g2);
-            if (g2) cudaGraphDestroy(g2);
-            throw;
-        }
-        MAPPG_CUDA(cudaStreamEndCapture(s->stream, &r->graph));
-        MAPPG_CUDA(cudaGraphInstantiate(&r->exec, r->graph, 0));
+        auto capture = [&](long long k, cudaGraph_t* gr, cudaGraphExec_t* ex) {
+            MAPPG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                for (long long q = 0; q < k; q++) launch_step32b(s, a);
+            } catch (...) {
+                cudaGraph_t g2 = nullptr;
+                cudaStreamEndCapture(s->stream, &g2);
+                if (g2) cudaGraphDestroy(g2);
+                throw;
+            }
+            MAPPG_CUDA(cudaStreamEndCapture(s->stream, gr));
+            MAPPG_CUDA(cudaGraphInstantiate(ex, *gr, 0));
+        };
+        capture(1, &r->graph, &r->exec);
+        r->many = std::min(nsteps, kBatchGraphSteps);
+        if (r->many >= kGraphMinSteps) capture(r->many, &r->graph_many, &r->exec_many);
         return;
     }
     double eta_h[kMaxChain] = {0};
@@ -853,7 +867,10 @@ void nvt_steps(mappg_sys* s, long long nsteps) {
     NvtRun* r = (NvtRun*)s->run;
     if (!r) throw Error{MAPPG_ERR_ARG, "no NVT run has begun on this system"};
     if (r->done + nsteps > r->planned) throw Error{MAPPG_ERR_ARG, "more steps than the run was begun with"};
-    for (long long st = 0; st < nsteps; st++) {
+    long long st = 0;
+    if (r->exec_many)
+        for (; nsteps - st >= r->many; st += r->many) MAPPG_CUDA(cudaGraphLaunch(r->exec_many, s->stream));
+    for (; st < nsteps; st++) {
         if (r->exec)
             MAPPG_CUDA(cudaGraphLaunch(r->exec, s->stream));
         else if (s->precision == MAPPG_MIXED)

@@ -101,6 +101,8 @@ void sys_set_box(mappg_sys* s, const double* H) {
 
 // a batch: every cell gets its own box, bins (a block of global bin ids) and
 // frame; the system-level box fields keep cell 0's for code that reads them
+static void chunk_cells(mappg_sys* s);
+
 void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) {
     s->ncell = ncell;
     s->cells.assign(ncell, CellGeo());
@@ -136,12 +138,17 @@ void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) 
     s->nbins = bins;
     s->band = band;
     s->cells_ortho = all_ortho;
-    // chunks of at most kChunk atoms, never across cells
+    chunk_cells(s);
+}
+
+// chunks of at most s->chunk_atoms atoms, never across cells (host arrays)
+static void chunk_cells(mappg_sys* s) {
+    const int ncell = s->ncell;
     s->chunk_begin_h.clear();
     s->cell_chunk_h.assign(ncell + 1, 0);
     std::vector<int> chunk_cell;
     for (int c = 0; c < ncell; c++) {
-        for (int a = s->cell_begin[c]; a < s->cell_begin[c + 1]; a += kChunk) {
+        for (int a = s->cell_begin[c]; a < s->cell_begin[c + 1]; a += s->chunk_atoms) {
             s->chunk_begin_h.push_back(a);
             chunk_cell.push_back(c);
         }
@@ -150,6 +157,37 @@ void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H) 
     s->nchunk = (int)s->chunk_begin_h.size();
     s->chunk_begin_h.push_back(s->cell_begin[ncell]);
     s->cells_chunk_cell_h = chunk_cell;
+}
+
+// device copies of the chunk arrays and the per-chunk sums
+static void upload_chunks(mappg_sys* s) {
+    const int nc = s->ncell, nk = s->nchunk;
+    void* old[] = {s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp};
+    for (void* p : old)
+        if (p) cudaFree(p);
+    MAPPG_CUDA(cudaMalloc((void**)&s->chunk_begin, sizeof(int) * (nk + 1)));
+    MAPPG_CUDA(cudaMalloc((void**)&s->chunk_cell, sizeof(int) * nk));
+    MAPPG_CUDA(cudaMalloc((void**)&s->cell_chunk, sizeof(int) * (nc + 1)));
+    MAPPG_CUDA(cudaMalloc((void**)&s->chunk_part, sizeof(double) * kChunkSlots * (size_t)nk));
+    MAPPG_CUDA(cudaMalloc((void**)&s->chunk_disp, sizeof(double) * 4 * (size_t)nk));
+    MAPPG_CUDA(cudaMemsetAsync(s->chunk_part, 0, sizeof(double) * kChunkSlots * (size_t)nk, s->stream));
+    MAPPG_CUDA(cudaMemsetAsync(s->chunk_disp, 0, sizeof(double) * 4 * (size_t)nk, s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(s->chunk_begin, s->chunk_begin_h.data(), sizeof(int) * (nk + 1), cudaMemcpyHostToDevice,
+                               s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(s->chunk_cell, s->cells_chunk_cell_h.data(), sizeof(int) * nk, cudaMemcpyHostToDevice,
+                               s->stream));
+    MAPPG_CUDA(cudaMemcpyAsync(s->cell_chunk, s->cell_chunk_h.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice,
+                               s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+void sys_rechunk(mappg_sys* s, int chunk_atoms) {
+    if (s->ncell <= 1) return;
+    if (chunk_atoms < 32) throw Error{MAPPG_ERR_ARG, "chunks hold at least 32 atoms"};
+    if (chunk_atoms == s->chunk_atoms) return;
+    s->chunk_atoms = chunk_atoms;
+    chunk_cells(s);
+    upload_chunks(s);
 }
 
 int grid_for(mappg_sys* s, long long threads, int block) {
@@ -809,6 +847,7 @@ EamArgs eam_args(mappg_sys* s) {
     a.h32 = s->h32;
     a.alpha = 0.0;
     a.cell_active = s->cell_active;
+    a.cutmask = s->cutmask;
     a.dF = s->dF;
     a.rho32out = s->rho32;
     a.f = s->f;
@@ -847,7 +886,7 @@ void sys_free(mappg_sys* s) {
                     s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
                     s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev, s->cells_dev, s->cell_of,
                     s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp, s->cmd,
-                    s->cell_out, s->dof, s->stage2};
+                    s->cell_out, s->dof, s->stage2, s->cutmask};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->ev_main) cudaEventDestroy(s->ev_main);
@@ -915,6 +954,7 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
     dev_alloc((void**)&s->f32, sizeof(float) * 3 * (size_t)n);
     dev_alloc((void**)&s->v32, sizeof(float) * 3 * (size_t)n);
     dev_alloc((void**)&s->rho32, sizeof(float) * n);
+    if (s->precision == MAPPG_MIXED) dev_alloc((void**)&s->cutmask, sizeof(unsigned) * 32 * (size_t)n);
     dev_alloc((void**)&s->binc, sizeof(int) * n);
     dev_alloc((void**)&s->binid, sizeof(int) * n);
     dev_alloc((void**)&s->bin_atoms, sizeof(int) * 2 * (size_t)n);
@@ -935,24 +975,13 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
             for (int i = s->cell_begin[c]; i < s->cell_begin[c + 1]; i++) cell_of[i] = c;
         dev_alloc((void**)&s->cells_dev, sizeof(CellGeo) * nc);
         dev_alloc((void**)&s->cell_of, sizeof(int) * n);
-        dev_alloc((void**)&s->chunk_begin, sizeof(int) * (nk + 1));
-        dev_alloc((void**)&s->chunk_cell, sizeof(int) * nk);
-        dev_alloc((void**)&s->cell_chunk, sizeof(int) * (nc + 1));
-        dev_alloc((void**)&s->chunk_part, sizeof(double) * kChunkSlots * (size_t)nk);
-        dev_alloc((void**)&s->chunk_disp, sizeof(double) * 4 * (size_t)nk);
         dev_alloc((void**)&s->cmd, sizeof(CellMd) * nc);
         dev_alloc((void**)&s->cell_out, sizeof(double) * 8 * nc);
         MAPPG_CUDA(cudaMemsetAsync(s->cmd, 0, sizeof(CellMd) * nc, s->stream));
-        MAPPG_CUDA(cudaMemsetAsync(s->chunk_part, 0, sizeof(double) * kChunkSlots * (size_t)nk, s->stream));
         MAPPG_CUDA(cudaMemcpyAsync(s->cells_dev, s->cells.data(), sizeof(CellGeo) * nc, cudaMemcpyHostToDevice,
                                    s->stream));
         MAPPG_CUDA(cudaMemcpyAsync(s->cell_of, cell_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
-        MAPPG_CUDA(cudaMemcpyAsync(s->chunk_begin, s->chunk_begin_h.data(), sizeof(int) * (nk + 1),
-                                   cudaMemcpyHostToDevice, s->stream));
-        MAPPG_CUDA(cudaMemcpyAsync(s->chunk_cell, s->cells_chunk_cell_h.data(), sizeof(int) * nk,
-                                   cudaMemcpyHostToDevice, s->stream));
-        MAPPG_CUDA(cudaMemcpyAsync(s->cell_chunk, s->cell_chunk_h.data(), sizeof(int) * (nc + 1),
-                                   cudaMemcpyHostToDevice, s->stream));
+        upload_chunks(s);
     }
     MAPPG_CUDA(cudaStreamSynchronize(s->stream));
 }

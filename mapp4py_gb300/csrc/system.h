@@ -179,6 +179,10 @@ struct EamArgs {
     const int* chunk_cell;
     double* chunk_part;       // nchunk x kChunkSlots
     const uint8_t* cell_active;  // batch minimizers: cells the chunk kernels work on (null: all)
+    // mixed kernels: per atom and lane, bit t set when the lane's t-th row
+    // entry is inside the cutoff (written by the density pass, read by the
+    // force pass; rows longer than 32 x lanes are scanned in full)
+    unsigned* cutmask;
     const double* cell_alpha;    // batch energy differences: trial step per cell
 };
 
@@ -217,6 +221,7 @@ struct mappg_sys {
     float* f32 = nullptr;
     float* v32 = nullptr;
     float* rho32 = nullptr;
+    unsigned* cutmask = nullptr;  // mixed: 32 words per atom (any lanes-per-atom choice)
     int* binc = nullptr;
     int* binid = nullptr;
     int* bin_count = nullptr;
@@ -240,6 +245,7 @@ struct mappg_sys {
     std::vector<int> cell_chunk_h;       // ncell + 1 chunk offsets
     std::vector<int> cells_chunk_cell_h; // cell of each chunk
     int nchunk = 0;
+    int chunk_atoms = mappg::kChunk;     // atoms per chunk (batch autotuner: 128, 256, 512)
     mappg::CellGeo* cells_dev = nullptr;
     int* cell_of = nullptr;              // per atom
     int* chunk_begin = nullptr;
@@ -285,6 +291,7 @@ namespace mappg {
 // system.cu
 void sys_set_box(mappg_sys* s, const double* H);
 void sys_set_cells(mappg_sys* s, int ncell, const int* natoms, const double* H);  // a batch
+void sys_rechunk(mappg_sys* s, int chunk_atoms);  // a batch's chunks of at most chunk_atoms atoms
 void launch_rebuild_chain(mappg_sys* s);   // kernels gated by sc->rebuild
 void request_rebuild(mappg_sys* s);        // host sets the gate
 void launch_shadow(mappg_sys* s, bool gated);

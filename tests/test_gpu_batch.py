@@ -94,6 +94,36 @@ def test_batch_nvt_follows_single_cell_runs(ff):
         assert np.max(np.abs(vb[k] - v1)) < 1e-5 * np.max(np.abs(v1))
 
 
+def test_batch_autotune_keeps_forces_and_runs(ff):
+    """The batch autotuner (atoms per chunk x lanes per atom x entries per
+    step) changes how the work is cut, not the result: per-atom forces are
+    the same bits, totals agree to rounding; an NVT run of more than 8 steps
+    (its steps captured as one graph) equals the same steps run one by one."""
+    cells, T = _cells()
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
+    pe0, vir0 = b.force()
+    f0 = b.get_f()
+    tpa, unroll, tune = b.autotune()
+    assert b.chunk_atoms in (128, 256, 512) and len(tune) == 21
+    pe1, vir1 = b.force()
+    assert np.array_equal(b.get_f(), f0)
+    assert np.max(np.abs(pe1 - pe0) / np.abs(pe0)) < 1e-12
+    v = np.concatenate([c.v for c in cells])
+    runs = []
+    for k in (12, None):
+        c = _lib.Batch(ff, [(q.H, q.x, q.elem) for q in cells], cells[0].masses)
+        c.set_v(v)
+        if k is None:
+            c.nvt_begin(T, synth.FS, synth.KB, 12)
+            for _ in range(12):
+                c.nvt_steps(1)
+            c.nvt_end(12)
+        else:
+            c.nvt_run(T, synth.FS, synth.KB, k)
+        runs.append((c.get_x(), c.get_v()))
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+
+
 def test_batch_refuses_single_cell_calls(ff):
     cells, _ = _cells()
     b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells[:2]], cells[0].masses)

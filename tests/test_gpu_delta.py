@@ -48,8 +48,10 @@ def test_energy_delta_refuses_steps_beyond_the_skin(potentials):
     path, _ = potentials[("A", "B")]
     c = synth.alloy((6, 6, 6), xB=0.5, sigma=0.05, seed=6)
     m = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
-    h = np.ones_like(c.x)
+    h = np.random.default_rng(7).uniform(-1.0, 1.0, c.x.shape)
     assert abs(m.energy_delta(h, 1e-3)) > 0.0
+    # a rigid translation changes nothing
+    assert abs(m.energy_delta(np.ones_like(c.x), 1e-3)) < 1e-9 * c.natoms
     with pytest.raises(_lib.MappgError, match="skin"):
         m.energy_delta(h, 0.2)
     f64 = _lib.System(_lib.ForceField.setfl(path), c.H, c.x, c.elem, c.masses)

@@ -12,8 +12,9 @@ density is extrapolated, md.nvt/NVE trajectories and md.min_lbfgs iterates.
 
 Tolerances: FP64 forces 1e-10 relative to the largest force component,
 energy 1e-12 relative, stress 1e-11 relative; mixed precision force RMS
-<= 1e-5 eV/A (or 3e-6 of the RMS force, for the compressed cell) and energy
-<= 1e-7 eV/atom against the reference; trajectories
+<= 1e-5 eV/A and energy <= 1e-7 eV/atom against the reference (for the
+compressed cell, whose stiffness scales the FP32 distance rounding up: 3e-6
+of the RMS force and 3e-8 eV/atom per eV/A of it); trajectories
 1e-9 A after 40-100 steps; L-BFGS iterates 1e-8 A after up to 20 iterations.
 """
 import numpy as np
@@ -87,7 +88,7 @@ def test_reference_potential_files(tmp_path, pot, precision):
             rms = np.sqrt(np.mean(np.sum((s.get_f() - f_r) ** 2, axis=1)))
             frms = np.sqrt(np.mean(np.sum(f_r ** 2, axis=1)))
             assert rms <= max(1e-5, 3e-6 * frms), (cell, rms, frms)
-            assert abs(pe - pe_r) / x.shape[0] <= 1e-7, (cell, pe - pe_r)
+            assert abs(pe - pe_r) / x.shape[0] <= max(1e-7, 3e-8 * frms), (cell, pe - pe_r)
 
 
 @pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
