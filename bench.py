@@ -245,36 +245,66 @@ def run_batch(args, ff, torch):
 
 def run_lbfgs(args, ff):
     """L-BFGS time to max|F| < 1e-4 eV/A, the learned diagonal initial inverse
-    Hessian against plain L-BFGS (scalar gamma), m = 10, back-tracking line
-    search, mixed precision (FP64 line-search energies, FP64 forces once FP32
-    forces stall).  Two cells of the same recipe (A/B alloy, 1 % vacancies,
-    0.15 A noise, seed 3): the 253,489-atom FCC 40^3 cell with an iteration
-    cap, and a 3,954-atom FCC 10^3 cell run to the tolerance."""
+    Hessian against plain L-BFGS (scalar gamma); m = 10, back-tracking line
+    search, mixed precision (FP32 forces; line-search energy differences
+    formed pair by pair, FP32 energy differences for steps beyond the skin).
+      c4: the 253,489-atom cell (A/B alloy, FCC 40^3, 1 % vacancies, 0.15 A
+          noise, seed 3), to the tolerance or args.lbfgs_cap iterations
+      c5: args.c5_cells cells of 1,000-16,000 atoms (log-uniform), random
+          composition, 0-3 % vacancies, strain up to +-2 %, noise
+          U(0.05, 0.2) A, relaxed together as one batch, each cell to the
+          tolerance or args.c5_cap iterations
+    max_dx (the largest atom move of a step, MinLBFGS's max_dx) is
+    args.lbfgs_dx for both."""
     from mapp4py_gb300 import _lib, precond, synth
 
     net = precond.load()
+    dx = args.lbfgs_dx
 
-    def one(cells, cap):
-        c = synth.alloy((cells,) * 3, xB=0.5, sigma=0.15, vac=0.01, seed=3)
-        res = {"natoms": c.natoms, "iteration_cap": cap}
+    def c4(cap):
+        c = synth.alloy((args.lbfgs_n,) * 3, xB=0.5, sigma=0.15, vac=0.01, seed=3)
+        res = {"natoms": c.natoms, "iteration_cap": cap, "max_dx": dx}
         for name in ("plain", "learned"):
             s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
             s.build()
             s.sync()
             t0 = time.perf_counter()
             if name == "plain":
-                r = s.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=cap)
+                r = s.lbfgs_run(m=10, e_tol=0.0, max_dx=dx, f_tol=1e-4, nsteps=cap)
             else:
-                r = _lib.lbfgs_run_precond(s, net, m=10, e_tol=0.0, f_tol=1e-4, nsteps=cap)
-            dt = time.perf_counter() - t0
-            res[name] = {"seconds": dt, "converged": r["err"] == 100, "iterations": r["niter"],
-                         "fmax": r["fmax"], "energy_calls": r["n_energy"], "force_calls": r["n_force"]}
+                r = _lib.lbfgs_run_precond(s, net, m=10, e_tol=0.0, max_dx=dx, f_tol=1e-4, nsteps=cap)
+            secs = time.perf_counter() - t0
+            res[name] = {"seconds": secs, "converged": r["err"] == 100, "iterations": r["niter"],
+                         "fmax": r["fmax"], "energy_calls": r["n_energy"], "force_calls": r["n_force"],
+                         "ms_per_iteration": 1000.0 * secs / max(1, r["niter"])}
         res["wall_ratio_plain_over_learned"] = res["plain"]["seconds"] / res["learned"]["seconds"]
         return res
 
-    return {"metric": "L-BFGS time to max|F| < 1e-4 eV/A, learned vs plain", "unit": "s",
-            "network": "33-64-64-3 BF16 MLP trained on 201,814 FD Hessian diagonals (precond_net.npz)",
-            "cell_253k": one(40, args.lbfgs_cap), "cell_4k": one(10, 5 * args.lbfgs_cap)}
+    def c5(ncell, cap):
+        cells, _ = synth.batch_cells(ncell, seed=11, nmin=1000, nmax=16000, vac=(0.0, 0.03), sigma=(0.05, 0.2),
+                                     strain=0.02)
+        res = {"cells": ncell, "natoms": int(sum(x.natoms for x in cells)), "iteration_cap": cap, "max_dx": dx}
+        for name in ("plain", "learned"):
+            b = _lib.Batch(ff, [(x.H, x.x, x.elem) for x in cells], cells[0].masses)
+            b.sync()
+            t0 = time.perf_counter()
+            r = b.lbfgs_run(m=10, max_dx=dx, f_tol=1e-4, nsteps=cap, net=None if name == "plain" else net)
+            secs = time.perf_counter() - t0
+            its = np.array([q["niter"] for q in r])
+            res[name] = {"seconds": secs, "cells_converged": int(sum(q["err"] == 100 for q in r)),
+                         "iterations_max": int(its.max()), "iterations_median": float(np.median(its)),
+                         "energy_calls": int(sum(q["n_energy"] for q in r)),
+                         "force_calls": int(sum(q["n_force"] for q in r))}
+        res["wall_ratio_plain_over_learned"] = res["plain"]["seconds"] / res["learned"]["seconds"]
+        return res
+
+    out = {"metric": "L-BFGS time to max|F| < 1e-4 eV/A, learned vs plain", "unit": "s",
+           "network": "33-64-64-3 BF16 MLP trained on 201,814 FD Hessian diagonals (precond_net.npz)"}
+    if args.lbfgs_cap > 0:
+        out["c4"] = c4(args.lbfgs_cap)
+    if args.c5_cells > 0:
+        out["c5"] = c5(args.c5_cells, args.c5_cap)
+    return out
 
 
 def run_accuracy(args, ff, path, cell, torch):
@@ -498,7 +528,7 @@ def run_gpu(args, rank, world, local_rank):
                    "call, as MDNVT::run"}
 
     batched = None if args.batch_steps <= 0 else run_batch(args, ff, torch)
-    lbfgs = None if args.lbfgs_cap <= 0 else run_lbfgs(args, ff)
+    lbfgs = None if args.lbfgs_cap <= 0 and args.c5_cells <= 0 else run_lbfgs(args, ff)
     extras = None
     if args.extras and rank == 0:
         extras = run_accuracy(args, ff, path, cell, torch)
@@ -553,8 +583,12 @@ def main():
                     help="skip the FP64 run, the mixed-vs-FP64 error, the NVE drift and the 4,000-atom case")
     ap.add_argument("--nve-ps", type=float, default=50.0,
                     help="length of the mixed-precision NVE drift run in ps (1 fs steps)")
-    ap.add_argument("--lbfgs-cap", type=int, default=1000,
-                    help="iteration cap of the 253k-atom L-BFGS comparison (0 skips the L-BFGS part)")
+    ap.add_argument("--lbfgs-cap", type=int, default=20000,
+                    help="iteration cap of the 253,489-atom L-BFGS comparison (0 skips it)")
+    ap.add_argument("--lbfgs-n", type=int, default=40, help="FCC repeats per side of that cell")
+    ap.add_argument("--lbfgs-dx", type=float, default=1.0, help="max_dx of the L-BFGS runs (A)")
+    ap.add_argument("--c5-cells", type=int, default=1024, help="cells of the batched L-BFGS comparison (0 skips it)")
+    ap.add_argument("--c5-cap", type=int, default=8000, help="iteration cap per cell of the batched comparison")
     ap.add_argument("--cells", type=int, default=N_CELLS[0],
                     help="FCC repeats per side (80 = the 2,048,000-atom workload; smaller for profiling)")
     args = ap.parse_args()

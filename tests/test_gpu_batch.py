@@ -96,9 +96,11 @@ def test_batch_nvt_follows_single_cell_runs(ff):
 
 def test_batch_autotune_keeps_forces_and_runs(ff):
     """The batch autotuner (atoms per chunk x lanes per atom x entries per
-    step) changes how the work is cut, not the result: per-atom forces are
-    the same bits, totals agree to rounding; an NVT run of more than 8 steps
-    (its steps captured as one graph) equals the same steps run one by one."""
+    step) changes how the work is cut, not the result: forces agree to FP32
+    rounding (another lanes-per-atom choice sums each row in other lane
+    partials), totals to rounding; an NVT run of more than 8 steps (its steps
+    captured as one graph) equals the same steps run one by one, bit for
+    bit."""
     cells, T = _cells()
     b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in cells], cells[0].masses)
     pe0, vir0 = b.force()
@@ -106,8 +108,8 @@ def test_batch_autotune_keeps_forces_and_runs(ff):
     tpa, unroll, tune = b.autotune()
     assert b.chunk_atoms in (128, 256, 512) and len(tune) == 21
     pe1, vir1 = b.force()
-    assert np.array_equal(b.get_f(), f0)
-    assert np.max(np.abs(pe1 - pe0) / np.abs(pe0)) < 1e-12
+    assert np.max(np.abs(b.get_f() - f0)) <= 1e-5 * max(1.0, np.max(np.abs(f0)))
+    assert np.max(np.abs(pe1 - pe0) / np.abs(pe0)) < 1e-9
     v = np.concatenate([c.v for c in cells])
     runs = []
     for k in (12, None):
