@@ -480,6 +480,12 @@ int mappg_sys_descriptors(mappg_sys* sys, float* feat);
  * the cutoff.  FP64 systems. */
 int mappg_sys_hessian_diag(mappg_sys* sys, const int* color, double h, double* out);
 
+/* With a learned preconditioner, recompute its diagonal from the current
+ * configuration every `every` L-BFGS iterations (0, the default: once, at
+ * the start).  Applies to mappg_lbfgs_run_precond and
+ * mappg_batch_lbfgs_run_precond.  No counterpart in the reference. */
+int mappg_mlp_set_refresh(mappg_mlp* net, int every);
+
 /* mappg_lbfgs_run with H0 = diag(1/y), y the network's prediction for the
  * starting configuration; a non-descent direction falls back to plain
  * L-BFGS (gamma*I) for that iteration.  stats: 7 doubles, the six of

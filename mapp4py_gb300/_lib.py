@@ -27,6 +27,7 @@ SIGNATURES = {
     "mappg_last_error": (C.c_char_p, []),
     "mappg_device_info": (C.c_int, [C.c_char_p, C.c_int, _I]),
     "mappg_batch_autotune": (C.c_int, [_VP, _I, _I, _I, _D]),
+    "mappg_mlp_set_refresh": (C.c_int, [_VP, C.c_int]),
     "mappg_fp64_fma_rate": (C.c_int, [C.c_int, C.c_int, _D]),
     "mappg_ff_setfl": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
     "mappg_ff_fs": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(_VP)]),
@@ -666,6 +667,11 @@ class Mlp:
         loss = C.c_double()
         check(load().mappg_mlp_grad(self.h, fptr(feat), fptr(target), feat.shape[0], fptr(g), C.byref(loss)))
         return loss.value, g
+
+    def set_refresh(self, every):
+        """L-BFGS runs with this network recompute the diagonal every `every`
+        iterations (0: once, at the start)."""
+        check(load().mappg_mlp_set_refresh(self.h, int(every)))
 
     def predict(self, feat):
         feat = f32(feat, (-1, 33))

@@ -643,7 +643,10 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
         MAPPG_CUDA(cudaStreamSynchronize(st));
         if (nrev == 0) break;
     }
+    long long bit = 0;
     while (count(BL_RUN) > 0) {
+        if (P && s->precond_every > 0 && bit > 0 && bit % s->precond_every == 0) s->precond_refresh();
+        bit++;
         // direction: learned (or plain) two-loop for the running cells
         two_loop(BL_RUN, P != nullptr);
         k_bl_prep<<<gc, 256, 0, st>>>(a, BL_RUN);

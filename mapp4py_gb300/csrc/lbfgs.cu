@@ -505,6 +505,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
     LineSearch<TrialLine> search(ls, line);
     int istep = 0;
     for (; err == LS_S; istep++) {
+        if (P && s->precond_every > 0 && istep > 0 && istep % s->precond_every == 0) s->precond_refresh();
         MAPPG_CUDA(cudaMemcpyAsync(xs, s->x, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         MAPPG_CUDA(cudaMemcpyAsync(f0, s->f, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
         two_loop(P != nullptr);

@@ -490,6 +490,7 @@ struct mappg_mlp {
     uint16_t* X = nullptr;  // training inputs, [n][64] bf16
     float* Y = nullptr;     // training targets, [n][3]
     int n = 0;
+    int refresh_every = 0;  // L-BFGS: recompute the diagonal every this many iterations (0: once)
 };
 
 namespace mappg {
@@ -998,17 +999,30 @@ static void run_precond(mappg_sys* s, mappg_mlp* net, int m, double e_tol, doubl
             MAPPG_CUDA(cudaMalloc(&y, sizeof(float) * 3 * (size_t)n));
             MAPPG_CUDA(cudaMalloc(&X, sizeof(uint16_t) * kIn * (size_t)n));
             MAPPG_CUDA(cudaMalloc(&P, sizeof(double) * 3 * (size_t)n));
-            launch_descriptors(s, feat);
-            const int g = std::max(1, std::min(1024, (n + 255) / 256));
-            k_pack_inputs<<<g, 256, 0, s->stream>>>(n, feat, nullptr, norm_of(net), X);
-            MAPPG_CUDA(cudaMemsetAsync(net->err, 0, sizeof(int), s->stream));
-            mlp_forward(net, X, n, y, s->stream);
-            k_precond<<<g, 256, 0, s->stream>>>(n, y, P);
-            MAPPG_CUDA(cudaGetLastError());
-            int e = 0;
-            MAPPG_CUDA(cudaMemcpyAsync(&e, net->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-            MAPPG_CUDA(cudaStreamSynchronize(s->stream));
-            if (e) throw Error{MAPPG_ERR_TIMEOUT, "tensor-core MMA did not complete"};
+            // features of the current configuration -> network -> diagonal
+            auto predict = [&] {
+                launch_descriptors(s, feat);
+                const int g = std::max(1, std::min(1024, (n + 255) / 256));
+                k_pack_inputs<<<g, 256, 0, s->stream>>>(n, feat, nullptr, norm_of(net), X);
+                MAPPG_CUDA(cudaMemsetAsync(net->err, 0, sizeof(int), s->stream));
+                mlp_forward(net, X, n, y, s->stream);
+                k_precond<<<g, 256, 0, s->stream>>>(n, y, P);
+                MAPPG_CUDA(cudaGetLastError());
+                int e = 0;
+                MAPPG_CUDA(cudaMemcpyAsync(&e, net->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+                MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+                if (e) throw Error{MAPPG_ERR_TIMEOUT, "tensor-core MMA did not complete"};
+            };
+            predict();
+            struct Refresh {
+                mappg_sys* s;
+                ~Refresh() {
+                    s->precond_refresh = nullptr;
+                    s->precond_every = 0;
+                }
+            } refresh{s};
+            s->precond_refresh = predict;
+            s->precond_every = net->refresh_every;
             if (batch) {
                 batch_lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, P, stats);
             } else {
@@ -1029,6 +1043,13 @@ static void run_precond(mappg_sys* s, mappg_mlp* net, int m, double e_tol, doubl
             throw;
         }
         release();
+}
+
+int mappg_mlp_set_refresh(mappg_mlp* net, int every) {
+    return guarded([&] {
+        if (!net || every < 0) throw Error{MAPPG_ERR_ARG, "bad argument"};
+        net->refresh_every = every;
+    });
 }
 
 int mappg_lbfgs_run_precond(mappg_sys* s, mappg_mlp* net, int m, double e_tol, double max_dx, double f_tol,

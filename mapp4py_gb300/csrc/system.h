@@ -24,6 +24,8 @@
 // pairs either.
 #pragma once
 
+#include <functional>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -267,6 +269,10 @@ struct mappg_sys {
     // (rho) and h32 holds the search direction for energy differences
     bool keep_rho64 = false;
     float4* h32 = nullptr;
+    // learned preconditioner in progress: recompute its diagonal from the
+    // current configuration every precond_every iterations (0: never)
+    std::function<void()> precond_refresh;
+    int precond_every = 0;
     // called by the minimizers after every hook_every-th iteration's force
     // call (mappg_sys_set_hook)
     int (*hook)(void* user, long long iteration) = nullptr;
