@@ -270,9 +270,20 @@ int mappg_sys_sync(mappg_sys* sys);
  * the choice is kept for the system.  tpa, unroll (may be NULL) receive it,
  * ms (7 doubles, may be NULL) the density+force time of each candidate
  * (4,1) (8,1) (16,1) (4,2) (8,2) (16,2) (32,1); FP64 systems try the
- * one-entry forms only (the others stay 0).  No counterpart in the
- * reference. */
+ * one-entry forms only (the others stay 0).  Single mixed cells also time
+ * each candidate with both force-record sources (mappg_sys_force_tables);
+ * ms then holds the faster.  No counterpart in the reference. */
 int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
+
+/* The mixed force pass's record source: mode 0 reads the force records
+ * through L1 (k_force32); mode k > 0 copies the records of one element group
+ * at a time into k KB of shared memory (k_force32s; single cells of mixed
+ * precision; the knots nearest the cutoff that fit, clamped to the largest
+ * budget a block may opt in to; nearer pairs read global memory); mode -1
+ * only queries.  *active receives the mode in use.  mappg_sys_autotune
+ * times 0, 64 KB, 128 KB and the largest budget and keeps the fastest; the
+ * forces are the same in every mode.  No counterpart in the reference. */
+int mappg_sys_force_tables(mappg_sys* sys, int mode, int* active);
 
 /* A batch of cells (mappg_batch_create): the atoms per chunk (128, 256 or
  * 512: the atoms a block of the batch kernels works through before it takes

@@ -94,6 +94,7 @@ SIGNATURES = {
     "mappg_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_int, _D]),
     "mappg_sys_autotune": (C.c_int, [_VP, _I, _I, _D]),
+    "mappg_sys_force_tables": (C.c_int, [_VP, C.c_int, _I]),
     "mappg_cg_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                C.c_int, _D]),
     "mappg_batch_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -446,6 +447,15 @@ class System:
         check(load().mappg_sys_autotune(self.h, C.byref(tpa), C.byref(unroll), dptr(ms)))
         keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2), (32, 1))
         return tpa.value, unroll.value, {k: v for k, v in zip(keys, ms) if v > 0}
+
+    def force_tables(self, mode=None):
+        """The mixed force pass's record source: 0 through L1, k > 0 the
+        records of one element group at a time in k KB of shared memory
+        (clamped to the largest budget); None only queries.  Returns the mode
+        in use."""
+        act = C.c_int()
+        check(load().mappg_sys_force_tables(self.h, -1 if mode is None else int(mode), C.byref(act)))
+        return act.value
 
     def enqueue(self, what):
         check(load().mappg_sys_enqueue(self.h, int(what)))

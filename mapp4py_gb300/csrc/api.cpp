@@ -326,6 +326,7 @@ int mappg_sys_create(const mappg_ff* ff, int natoms, const double* H, const doub
             cudaDeviceProp p;
             MAPPG_CUDA(cudaGetDeviceProperties(&p, s->device));
             s->sm_count = p.multiProcessorCount;
+            s->smem_optin = (int)p.sharedMemPerBlockOptin;
             sys_set_box(s, H);
             sys_alloc(s, x);
             sys_alloc_bins(s);
@@ -338,6 +339,21 @@ int mappg_sys_create(const mappg_ff* ff, int natoms, const double* H, const doub
             std::vector<uint8_t> es(natoms);
             for (int i = 0; i < natoms; i++) es[i] = elem[s->host_id[i]];
             MAPPG_CUDA(cudaMemcpyAsync(s->elem, es.data(), natoms, cudaMemcpyHostToDevice, s->stream));
+            // the atoms of each element in bin order (k_force32s works one
+            // element's force records at a time)
+            s->grp_begin[0] = 0;
+            for (int g = 0; g < ne; g++)
+                s->grp_begin[g + 1] = s->grp_begin[g] + (int)std::count(es.begin(), es.end(), (uint8_t)g);
+            std::vector<int> grp;
+            if (ne > 1) {
+                grp.reserve(natoms);
+                for (int g = 0; g < ne; g++)
+                    for (int i = 0; i < natoms; i++)
+                        if (es[i] == g) grp.push_back(i);
+                MAPPG_CUDA(cudaMalloc(&s->grp_atoms, sizeof(int) * (size_t)natoms));
+                MAPPG_CUDA(cudaMemcpyAsync(s->grp_atoms, grp.data(), sizeof(int) * (size_t)natoms,
+                                           cudaMemcpyHostToDevice, s->stream));
+            }
             MAPPG_CUDA(cudaStreamSynchronize(s->stream));
         } catch (...) {
             sys_free(s);
@@ -528,28 +544,42 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
         MAPPG_CUDA(cudaEventCreate(&e0));
         MAPPG_CUDA(cudaEventCreate(&e1));
         double best = 1e30;
-        int best_tpa = s->tpa, best_u = s->unroll;
+        int best_tpa = s->tpa, best_u = s->unroll, best_sm = s->force_smem;
+        // a single mixed cell also tries the force pass with its records in
+        // shared memory (k_force32s) at three budgets: the budget takes L1
+        // from the neighbour-position gathers; ms_out[c] is the fastest
+        int modes[4] = {0, 0, 0, 0}, nmodes = 1;
+        if (mixed && force_smem_available(s)) {
+            const int mx = force_smem_max_kb(s);
+            for (int kb : {64, 128, mx})
+                if (kb <= mx && kb > modes[nmodes - 1]) modes[nmodes++] = kb;
+        }
         try {
             for (int c = 0; c < 7; c++) {
                 if (!mixed && cand[c][1] != 1) continue;
                 s->tpa = cand[c][0];
                 s->unroll = cand[c][1];
-                launch_density_only(s);  // warm-up (and first-use set-up)
-                launch_force_only(s);
-                MAPPG_CUDA(cudaEventRecord(e0, s->stream));
-                for (int r = 0; r < 3; r++) {
-                    launch_density_only(s);
+                for (int mi = 0; mi < nmodes; mi++) {
+                    const int mode = modes[mi];
+                    s->force_smem = mode;
+                    launch_density_only(s);  // warm-up (and first-use set-up)
                     launch_force_only(s);
-                }
-                MAPPG_CUDA(cudaEventRecord(e1, s->stream));
-                MAPPG_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms_out) ms_out[c] = ms / 3.0;
-                if (ms < best) {
-                    best = ms;
-                    best_tpa = cand[c][0];
-                    best_u = cand[c][1];
+                    MAPPG_CUDA(cudaEventRecord(e0, s->stream));
+                    for (int r = 0; r < 3; r++) {
+                        launch_density_only(s);
+                        launch_force_only(s);
+                    }
+                    MAPPG_CUDA(cudaEventRecord(e1, s->stream));
+                    MAPPG_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms_out && (mi == 0 || ms / 3.0 < ms_out[c])) ms_out[c] = ms / 3.0;
+                    if (ms < best) {
+                        best = ms;
+                        best_tpa = cand[c][0];
+                        best_u = cand[c][1];
+                        best_sm = mode;
+                    }
                 }
             }
         } catch (...) {
@@ -557,14 +587,31 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
             cudaEventDestroy(e1);
             s->tpa = best_tpa;
             s->unroll = best_u;
+            s->force_smem = best_sm;
             throw;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         s->tpa = best_tpa;
         s->unroll = best_u;
+        s->force_smem = best_sm;
         if (tpa_out) *tpa_out = best_tpa;
         if (unroll_out) *unroll_out = best_u;
+    });
+}
+
+int mappg_sys_force_tables(mappg_sys* s, int mode, int* active) {
+    return guard([&] {
+        if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
+        if (mode < -1) throw Error{MAPPG_ERR_ARG, "mode must be -1, 0 or a budget in KB"};
+        if (mode > 0) {
+            if (!force_smem_available(s))
+                throw Error{MAPPG_ERR_UNSUPP, "shared-memory force records need a single mixed-precision cell"};
+            s->force_smem = std::min(mode, force_smem_max_kb(s));
+        } else if (mode == 0) {
+            s->force_smem = 0;
+        }
+        if (active) *active = s->force_smem;
     });
 }
 

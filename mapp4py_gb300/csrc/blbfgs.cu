@@ -71,6 +71,8 @@ struct BlArgs {
     double skin_half;
     uint8_t* active;        // per cell: the chunk kernels work on it
     double* alpha_cell;     // per cell trial step (energy differences)
+    uint8_t* cell_reb;      // per cell: rebuild its list at the next list check
+    DevScalars* sc;
 };
 
 __device__ __forceinline__ int slot_of(const BlCell& c, int i, int m) { return (c.head - i + m) % m; }
@@ -478,6 +480,32 @@ __global__ void k_bl_cells_bound(BlArgs a) {
     if (!(1.7320508075688772 * (cs.a * cs.hmax + dx) < a.skin_half)) atomicAdd(a.count, 1);
 }
 
+// the searching cells that fail that bound only through the distance their
+// atoms moved since their list was built: their lists are rebuilt at the
+// search start (the batch rebuilds cells one by one, so a cell's list can be
+// older than its neighbours' in the batch); counts them
+__global__ void k_bl_refresh(BlArgs a) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    const BlCell& cs = a.cs[c];
+    if (cs.state != BL_LS) return;
+    const double step = 1.7320508075688772 * cs.a * cs.hmax;
+    if (step < a.skin_half && !(step + 1.7320508075688772 * cs.dxmax < a.skin_half)) {
+        a.cell_reb[c] = 1;
+        a.sc->rebuild = 1;
+        atomicAdd(a.count, 1);
+    }
+}
+
+// the search start of the searching cells after a rebuild wrapped x
+__global__ void k_bl_restart(BlArgs a) {
+    const int n = a.n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (a.cs[a.cell_of[i]].state != BL_LS) continue;
+        for (int q = 0; q < 3; q++) a.x0[(size_t)q * n + i] = a.x[(size_t)q * n + i];
+    }
+}
+
 // counts the searching cells whose next trial moves an atom by a quarter of
 // the skin or more (a search of FP32 energy differences goes over to energy
 // differences once none does)
@@ -519,6 +547,17 @@ __global__ void k_bl_count(BlArgs a, int st) {
 }
 
 // ------------------------------------------------------------------ host
+// the rebuild chain for the cells flagged in s->cell_reb (the gate set by
+// k_bl_refresh), the frame positions, and the capacity check of lb_update
+static void bl_rebuild_flagged(mappg_sys* s) {
+    launch_rebuild_chain(s);
+    launch_shadow(s, false);
+    int ov = 0;
+    MAPPG_CUDA(cudaMemcpyAsync(&ov, &s->sc->overflow, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+    if (ov) sys_build(s);
+}
+
 void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, double c_ls, double rho_ls,
                      double min_alpha, int nsteps, const double* P, double* stats) {
     if (m < 1 || m > kBlMaxHist) throw Error{MAPPG_ERR_ARG, "m must be in 1..32 for a batch"};
@@ -573,6 +612,8 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
     a.skin_half = 0.5 * s->skin;
     a.active = (uint8_t*)dalloc(nc);
     a.alpha_cell = (double*)dalloc(sizeof(double) * nc);
+    a.cell_reb = s->cell_reb;
+    a.sc = s->sc;
     const bool mixed = s->precision == MAPPG_MIXED;
     float4* h32 = mixed ? (float4*)dalloc(sizeof(float4) * (size_t)n) : nullptr;
     // the masks and the kept density belong to this run only
@@ -674,6 +715,25 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
             int wide = 0;
             MAPPG_CUDA(cudaMemcpyAsync(&wide, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
             MAPPG_CUDA(cudaStreamSynchronize(st));
+            if (wide > 0) {
+                // cells held back only by an old list: rebuild those at the
+                // search start (x does not move; the rebuild may wrap it,
+                // so the start is taken again) and test the bound again
+                MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+                k_bl_refresh<<<g1, 256, 0, st>>>(a);
+                int nref = 0;
+                MAPPG_CUDA(cudaMemcpyAsync(&nref, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+                MAPPG_CUDA(cudaStreamSynchronize(st));
+                if (nref > 0) {
+                    bl_rebuild_flagged(s);
+                    k_bl_restart<<<ga, 256, 0, st>>>(a);
+                    MAPPG_CUDA(cudaMemsetAsync(a.count, 0, sizeof(int), st));
+                    k_bl_dx<<<gc, 256, 0, st>>>(a);
+                    k_bl_cells_bound<<<gw, 256, 0, st>>>(a);
+                    MAPPG_CUDA(cudaMemcpyAsync(&wide, a.count, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    MAPPG_CUDA(cudaStreamSynchronize(st));
+                }
+            }
             a.emode = wide == 0 ? BL_EDELTA : BL_E32DIFF;
             k_bl_active<<<gb, 256, 0, st>>>(a, BL_LS);
             s->cell_active = a.active;

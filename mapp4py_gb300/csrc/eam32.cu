@@ -10,13 +10,17 @@
 //                gather plus the record
 //   k_energy32   energy only (line-search trials)
 //
-// Precision: every per-pair term is computed in FP32; every sum of them is
+// Precision: every per-pair term is computed in FP32; the sums of them are
 // accumulated with compensation (Kahan: an FP32 sum and an FP32 correction
 // holding its lost low part), which carries the sum of FP32 terms as an FP64
 // accumulator would: per-atom density, force and pair energy within a lane,
-// the virial across all pairs a thread visits.  Lane partials are reduced in
-// FP64 (shuffles of doubles), block and grid totals in FP64 in a fixed
-// order.  The embedding takes the FP64 density.  Constants shared by many
+// and the energy across all atoms a thread visits.  The virial is summed in
+// plain FP32 per thread (a few hundred pair terms: six more compensated sums
+// per pair cost 6 % of the force pass) and in FP64 across threads, which
+// keeps the stress within ~1e-7 of its scale.  Lane partials are combined
+// with exact two-sums (the correction keeps every rounding error), block and
+// grid totals are FP64 in a fixed order.  The embedding takes the density as
+// an FP64 value (sum minus correction).  Constants shared by many
 // pairs (1/dr, the frame-to-Cartesian scale, the spline constant terms) are
 // carried as head + tail so their rounding does not bias the totals.
 //
@@ -114,14 +118,29 @@ struct Consts32 {
     }
 };
 
-// a lane's compensated partial (s, c), reduced over the TPA lanes of one
-// atom in FP64
+// s + e == a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// a lane's compensated partial (s, c), whose value is s - c, summed over the
+// TPA lanes of one atom: the rounding error of every addition goes into the
+// correction, so lane 0 ends with (s, c) of the whole sum; FP32 instructions
+// only (GB300's FP64 pipe is narrow, and per-lane FP64 shuffles and
+// conversions took a quarter of it)
 template <int TPA>
-__device__ __forceinline__ double lane_sum64(float s, float c) {
-    double v = (double)s - (double)c;
+__device__ __forceinline__ void lane_sum_comp(float& s, float& c) {
 #pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, TPA);
-    return v;
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o, TPA);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c, o, TPA);
+        float t, e;
+        two_sum(s, s2, t, e);
+        s = t;
+        c = (c + c2) - e;
+    }
 }
 
 // embedding F and F' of the FP64 density: knot and fraction from rho/drho
@@ -245,8 +264,9 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
         }
         if (a.cutmask && nn <= 32 * TPA) a.cutmask[(size_t)i * TPA + lane] = bits;
     }
-    const double rho = lane_sum64<TPA>(acc, acc_c);
+    lane_sum_comp<TPA>(acc, acc_c);
     if (active && lane == 0) {
+        const double rho = (double)acc - (double)acc_c;
         float Fv, dFv;
         embed32(a, ei, rho, Fv, dFv);
         a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
@@ -340,11 +360,14 @@ __global__ void __launch_bounds__(256) k_density32b(EamArgs a) {
     }
 }
 
-// one atom's force row (TPA lanes): force, pair energy and virial
-template <int TPA, bool ORTHO, int U, class FR>
+// one atom's force row (TPA lanes): force, pair energy and virial;
+// SM: the records of knots from a.fs_mlo on come from the shared-memory copy
+// stab of atom i's element group (k_force32s), lower knots from global
+// memory; both hold the same values, so the forces are the same
+template <int TPA, bool ORTHO, int U, class FR, bool SM = false>
 __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, const Consts32& K, const FR& fr,
                                            int i, int lane, bool active, float& es, float& ec, float (&w)[6],
-                                           float (&wc)[6]) {
+                                           const float4* stab = nullptr) {
     float fx = 0.f, fy = 0.f, fz = 0.f, ep = 0.f;
     float fxc = 0.f, fyc = 0.f, fzc = 0.f, epc = 0.f;
     int ei = 0;
@@ -356,7 +379,8 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         const int* row = a.nbr + (size_t)i * a.maxnbr;
         const float cut0 = S.cut_sq[0];
         auto pair = [&](int e, const float4& q) {
-            const int t = ei * a.ne + entry_elem(e);
+            const int ej = entry_elem(e);
+            const int t = ei * a.ne + ej;
             float4 o;
             image_offset(e, o);
             float dx, dy, dz;
@@ -368,12 +392,29 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 float fr;
                 const int m = knot32(fmaf(r, K.dri, r * K.dri_lo), a.nr - 2, fr);
                 const size_t kt = (size_t)t * a.nr + m;
+                const int ms = m - a.fs_mlo;
+                const bool in_smem = SM && ms >= 0 && ms < a.fs_w;
                 float4 r0, r1;
-                ldg8(a.ftab + 2 * kt, r0, r1);
+                if (in_smem) {
+                    const float4 z = stab[ej * a.fs_w + ms];
+                    const float4 d = stab[(a.ne + ej) * a.fs_w + ms];
+                    r0 = make_float4(d.x, d.y, d.z, z.w);
+                    r1 = make_float4(z.x, z.y, z.z, d.w);
+                } else {
+                    ldg8(a.ftab + 2 * kt, r0, r1);
+                }
                 const float der_i = fmaf(fmaf(r0.z, fr, r0.y), fr, r0.x);
                 float der_j = der_i;
-                if (entry_elem(e) != ei) {
-                    const float4 r2 = __ldg(a.fjtab + kt);
+                if (ej != ei) {
+                    float4 r2;
+                    if (in_smem) {
+                        // rho'_{g->ej}: with one density function per source
+                        // element it is the group's own rho'_{g->g} record
+                        const int rj = a.rho_ei ? 2 * a.ne + (ej < ei ? ej : ej - 1) : a.ne + ei;
+                        r2 = stab[rj * a.fs_w + ms];
+                    } else {
+                        r2 = __ldg(a.fjtab + kt);
+                    }
                     der_j = fmaf(fmaf(r2.z, fr, r2.y), fr, r2.x);
                 }
                 const float zpoly = fmaf(fmaf(r1.z, fr, r1.y), fr, r1.x);
@@ -387,12 +428,12 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 kahan_add(fy, fyc, fdy);
                 kahan_add(fz, fzc, fdz);
                 kahan_add(ep, epc, phi);
-                kahan_add(w[0], wc[0], fdx * dx);
-                kahan_add(w[1], wc[1], fdx * dy);
-                kahan_add(w[2], wc[2], fdx * dz);
-                kahan_add(w[3], wc[3], fdy * dy);
-                kahan_add(w[4], wc[4], fdy * dz);
-                kahan_add(w[5], wc[5], fdz * dz);
+                w[0] = fmaf(fdx, dx, w[0]);
+                w[1] = fmaf(fdx, dy, w[1]);
+                w[2] = fmaf(fdx, dz, w[2]);
+                w[3] = fmaf(fdy, dy, w[3]);
+                w[4] = fmaf(fdy, dz, w[4]);
+                w[5] = fmaf(fdz, dz, w[5]);
             }
         };
         if (a.cutmask && nn <= 32 * TPA) {
@@ -442,11 +483,13 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         kahan_add(es, ec, ep);
         ec += epc;  // the atom's own correction (small): the thread total is es - ec
     }
-    const double gx = lane_sum64<TPA>(fx, fxc), gy = lane_sum64<TPA>(fy, fyc), gz = lane_sum64<TPA>(fz, fzc);
+    lane_sum_comp<TPA>(fx, fxc);
+    lane_sum_comp<TPA>(fy, fyc);
+    lane_sum_comp<TPA>(fz, fzc);
     if (active && lane == 0) {
-        a.f32[i] = (float)gx;
-        a.f32[a.n + i] = (float)gy;
-        a.f32[2 * a.n + i] = (float)gz;
+        a.f32[i] = fx - fxc;
+        a.f32[a.n + i] = fy - fyc;
+        a.f32[2 * a.n + i] = fz - fzc;
     }
 }
 
@@ -459,15 +502,15 @@ __global__ void __launch_bounds__(256, 4) k_force32(EamArgs a) {
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
     const int stride = (gridDim.x * blockDim.x) / TPA;
     float es = 0.f, ec = 0.f;  // pair energy, compensated
-    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, wc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // virial
+    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // virial: plain FP32 per thread
     for (int base = 0;; base += stride) {
         const int i = gid + base;
         const bool active = i < a.n;
         if (!__any_sync(0xffffffffu, active)) break;
-        force_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec, w, wc);
+        force_atom<TPA, ORTHO, U>(a, S, K, a.fr, i, lane, active, es, ec, w);
     }
     auto sum_k = [&](int k) -> double {
-        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * ((double)w[k - 1] - (double)wc[k - 1]);
+        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1];
     };
     __shared__ double tot[7];
     if (block_partials_fn<7>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
@@ -478,6 +521,84 @@ __global__ void __launch_bounds__(256, 4) k_force32(EamArgs a) {
             for (int k = 0; k < 6; k++) sc->virial[k] = tot[k + 1];
             sc->counter[0] = 0;
         }
+    }
+}
+
+// k_force32 with the force records in shared memory: one 1024-thread block
+// per SM works through the atoms one element group at a time, each group
+// with its own records (r*phi of the group's pair types and the density
+// derivatives they need) copied into shared memory first, so that a pair's
+// records cost shared-memory reads instead of L1/L2 traffic
+template <int TPA, bool ORTHO, int U>
+__global__ void __launch_bounds__(1024, 1) k_force32s(EamArgs a) {
+    extern __shared__ float4 ftab_s[];
+    __shared__ Smem32 S;
+    S.fill(a);  // ends with __syncthreads
+    const Consts32 K(a);
+    const int lane = threadIdx.x % TPA;
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / TPA;
+    const int stride = (gridDim.x * blockDim.x) / TPA;
+    const int nrec = a.fs_rec * a.fs_w;
+    float es = 0.f, ec = 0.f;
+    float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int g = 0; g < a.ne; g++) {
+        const int lo = a.grp_begin[g], hi = a.grp_begin[g + 1];
+        if (lo == hi) continue;
+        __syncthreads();  // every thread is done with the previous group's records
+        const float4* src = a.fs_tab + (size_t)g * a.fs_rec * a.fs_stride + a.fs_off;
+        for (int k = threadIdx.x; k < nrec; k += blockDim.x) {
+            const int r = k / a.fs_w;
+            ftab_s[k] = __ldg(src + (size_t)r * a.fs_stride + (k - r * a.fs_w));
+        }
+        __syncthreads();
+        for (int base = lo;; base += stride) {
+            const int q = base + gid;
+            const bool active = q < hi;
+            if (!__any_sync(0xffffffffu, active)) break;
+            const int i = !active ? 0 : (a.grp_atoms ? a.grp_atoms[q] : q);
+            force_atom<TPA, ORTHO, U, Frame, true>(a, S, K, a.fr, i, lane, active, es, ec, w, ftab_s);
+        }
+    }
+    auto sum_k = [&](int k) -> double {
+        return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1];
+    };
+    __shared__ double tot[7];
+    if (block_partials_fn<7>(sum_k, a.partials, 0, &a.sc->counter[0]) && threadIdx.x < 32) {
+        final_sums_smem<7>(a.partials, gridDim.x, tot);
+        if (threadIdx.x == 0) {
+            DevScalars* sc = a.sc;
+            sc->energy = tot[0] + sc->e_embed;
+            for (int k = 0; k < 6; k++) sc->virial[k] = tot[k + 1];
+            sc->counter[0] = 0;
+        }
+    }
+}
+
+// the group records of k_force32s from the global force records (same
+// values): out[(g * R + r) * W + w] for knot mlo + w
+__global__ void k_fs_fill(EamArgs a, float4* __restrict__ out, int R, int W, int mlo) {
+    const long long total = (long long)a.ne * R * W;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(idx % W);
+        const int r = (int)((idx / W) % R);
+        const int g = (int)(idx / ((long long)W * R));
+        const int m = mlo + w;
+        float4 v;
+        if (r < a.ne) {
+            const size_t kt = (size_t)(g * a.ne + r) * a.nr + m;
+            const float4 r0 = a.ftab[2 * kt], r1 = a.ftab[2 * kt + 1];
+            v = make_float4(r1.x, r1.y, r1.z, r0.w);
+        } else if (r < 2 * a.ne) {
+            const size_t kt = (size_t)(g * a.ne + (r - a.ne)) * a.nr + m;
+            const float4 r0 = a.ftab[2 * kt], r1 = a.ftab[2 * kt + 1];
+            v = make_float4(r0.x, r0.y, r0.z, r1.w);
+        } else {
+            const int k = r - 2 * a.ne;
+            const int ej = k < g ? k : k + 1;
+            v = a.fjtab[(size_t)(g * a.ne + ej) * a.nr + m];
+        }
+        out[idx] = v;
     }
 }
 
@@ -494,14 +615,14 @@ __global__ void __launch_bounds__(256, 4) k_force32b(EamArgs a) {
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const CellFrame fr = cell_frame<ORTHO>(a.cells + a.chunk_cell[ch]);
         float es = 0.f, ec = 0.f;
-        float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, wc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (int i0 = lo; i0 < hi; i0 += apb) {
             const int i = i0 + (int)threadIdx.x / TPA;
-            force_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec, w, wc);
+            force_atom<TPA, ORTHO, U>(a, S, K, fr, i, lane, i < hi, es, ec, w);
         }
         chunk_store<7>(
             [&](int k) -> double {
-                return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * ((double)w[k - 1] - (double)wc[k - 1]);
+                return k == 0 ? 0.5 * ((double)es - (double)ec) : 0.5 * (double)w[k - 1];
             },
             a.chunk_part + (size_t)ch * kChunkSlots);
     }
@@ -543,12 +664,13 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
             }
         }
     }
-    const double rho = lane_sum64<TPA>(acc, acc_c);
+    lane_sum_comp<TPA>(acc, acc_c);
     if (active) {
         kahan_add(es, ec, ep);
         ec += epc;
     }
     if (active && lane == 0) {
+        const double rho = (double)acc - (double)acc_c;
         float Fv, dFv;
         embed32(a, ei, rho, Fv, dFv);
         kahan_add(es, ec, Fv);
@@ -736,12 +858,13 @@ __device__ __forceinline__ void de_atom(const EamArgs& a, const Smem32& S, const
             kahan_add(dp, dpc, dphi);
         }
     }
-    const double drho_i = lane_sum64<TPA>(dr, drc);
+    lane_sum_comp<TPA>(dr, drc);
     if (active) {
         kahan_add(es, ec, 0.5f * dp);
         ec += 0.5f * dpc;
     }
     if (active && lane == 0) {
+        const double drho_i = (double)dr - (double)drc;
         const double r0 = a.rho0[i];
         const double dF = embed64(a, ei, r0 + drho_i) - embed64(a, ei, r0);
         // dF carries FP64 precision; added as head and tail
@@ -868,6 +991,17 @@ static void density_t(mappg_sys* s, const EamArgs& a) {
 
 template <int TPA, bool ORTHO, int U>
 static void force_t(mappg_sys* s, const EamArgs& a) {
+    if (s->force_smem > 0 && a.fs_tab) {
+        static bool attr = false;
+        if (!attr) {
+            MAPPG_CUDA(cudaFuncSetAttribute(k_force32s<TPA, ORTHO, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            s->smem_optin - (int)kForceSmemReserve));
+            attr = true;
+        }
+        const size_t bytes = sizeof(float4) * (size_t)a.fs_rec * a.fs_w;
+        k_force32s<TPA, ORTHO, U><<<s->sm_count, 1024, bytes, s->stream>>>(a);
+        return;
+    }
     static int grid = 0;
     if (!grid) grid = occupancy_grid(s, k_force32<TPA, ORTHO, U>, 256);
     k_force32<TPA, ORTHO, U><<<grid, 256, 0, s->stream>>>(a);
@@ -961,6 +1095,32 @@ void launch_density32(mappg_sys* s, const EamArgs& a) {
     else
         MAPPG_TPA32(density_t);
 }
+// the group records of k_force32s for as many knots as fit in the shared
+// memory a block may opt in to, from the knot of the cutoff down (a table
+// may reach beyond the cutoff; knots there are never read)
+bool force_smem_available(mappg_sys* s) {
+    if (s->ncell > 1 || s->precision != MAPPG_MIXED || s->ne > kMaxElem) return false;
+    if (s->fs_tab) return true;
+    const int nr = s->ff->dev.nr;
+    const int R = s->ff->dev.rho_ei ? 3 * s->ne - 1 : 2 * s->ne;
+    const long long budget = (long long)s->smem_optin - (long long)kForceSmemReserve;
+    const int mhi = std::min(nr - 2, (int)((s->max_cut - s->skin) * s->ff->dev.dr_inv) + 1);
+    const int W = (int)std::min<long long>(mhi + 1, budget / ((long long)sizeof(float4) * R));
+    if (W < 16) return false;
+    MAPPG_CUDA(cudaMalloc(&s->fs_tab, sizeof(float4) * (size_t)s->ne * R * W));
+    EamArgs a = eam_args(s);
+    k_fs_fill<<<256, 256, 0, s->stream>>>(a, s->fs_tab, R, W, mhi + 1 - W);
+    MAPPG_CUDA(cudaGetLastError());
+    s->fs_rec = R;
+    s->fs_w = W;
+    s->fs_mlo = mhi + 1 - W;
+    return true;
+}
+
+int force_smem_max_kb(const mappg_sys* s) {
+    return s->fs_rec > 0 ? (int)(((long long)sizeof(float4) * s->fs_rec * s->fs_w + 1023) / 1024) : 0;
+}
+
 void launch_force32(mappg_sys* s, const EamArgs& a) {
     if (s->ncell > 1) {
         MAPPG_TPA32B(force_b);

@@ -81,6 +81,7 @@ struct MdArgs {
     double* chunk_part;
     double* chunk_disp;
     CellMd* cmd;
+    uint8_t* cell_reb;  // per cell: an atom moved beyond skin/2 (rebuild that cell)
 };
 
 // NHC parameters of one cell of a batch: its own target and dof
@@ -495,6 +496,7 @@ __global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
     const int n = a.n;
     int moved = 0;
     for (int ch = blockIdx.x; ch < a.nchunk; ch += gridDim.x) {
+        int moved_ch = 0;
         const int lo = a.chunk_begin[ch], hi = a.chunk_begin[ch + 1];
         const int c = a.chunk_cell[ch];
         const CellGeo& g = a.cells[c];
@@ -535,7 +537,12 @@ __global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
             const float cx = da * g.G[0][0] + db * g.G[1][0] + dc * g.G[2][0];
             const float cy = db * g.G[1][1] + dc * g.G[2][1];
             const float cz = dc * g.G[2][2];
-            moved |= fmaf(cx, cx, fmaf(cy, cy, cz * cz)) > a.skin_sq32;
+            moved_ch |= fmaf(cx, cx, fmaf(cy, cy, cz * cz)) > a.skin_sq32;
+        }
+        // the chunk's cell is rebuilt at the next list check
+        if (__syncthreads_or(moved_ch)) {
+            moved = 1;
+            if (threadIdx.x == 0) a.cell_reb[c] = 1;
         }
         chunk_store<3>(
             [&](int k) -> double { return k == 0 ? (double)dsum0 : (k == 1 ? (double)dsum1 : (double)dsum2); },
@@ -655,6 +662,7 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
     a.chunk_part = s->chunk_part;
     a.chunk_disp = s->chunk_disp;
     a.cmd = s->cmd;
+    a.cell_reb = s->cell_reb;
     return a;
 }
 

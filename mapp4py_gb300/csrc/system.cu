@@ -284,13 +284,16 @@ __global__ void k_wrap_bin(int n, double* __restrict__ x, double* __restrict__ s
 }
 
 // batch variant of step 1: each atom uses its cell's box, bins and drift
+// (cells without their rebuild flag keep their wrap, bins and rows)
 __global__ void k_wrap_bin_b(int n, double* __restrict__ x, double* __restrict__ s, const CellGeo* __restrict__ cells,
                              const int* __restrict__ cell_of, const CellMd* __restrict__ cmd, int* __restrict__ binc,
-                             int* __restrict__ binid, int* __restrict__ bin_count, DevScalars* sc) {
+                             int* __restrict__ binid, int* __restrict__ bin_count, const uint8_t* __restrict__ cell_reb,
+                             DevScalars* sc) {
     if (!sc->rebuild) return;
     int bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int c = cell_of[i];
+        if (!cell_reb[c]) continue;
         const CellGeo& g = cells[c];
         const double* dr = cmd[c].drift;
         double x0 = dsub(x[i], dr[0]), x1 = dsub(x[n + i], dr[1]), x2 = dsub(x[2 * n + i], dr[2]);
@@ -349,11 +352,51 @@ __global__ void k_scan_bins(int nbins, int* __restrict__ bin_count, int* __restr
     }
 }
 
-// rebuild step 3: scatter atom indices into their bins (order fixed next)
+// batch variant of step 2: one warp per flagged cell scans its own bins,
+// from the cell's first atom (a cell's bins hold exactly its atoms, so the
+// other cells' bin starts stay valid)
+__global__ void k_scan_bins_b(int ncell, int n, int nbins, const CellGeo* __restrict__ cells,
+                              const uint8_t* __restrict__ cell_reb, int* __restrict__ bin_count,
+                              int* __restrict__ bin_start, DevScalars* sc) {
+    if (!sc->rebuild) return;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        bin_start[nbins] = n;
+        sc->maxrow = 0;
+        sc->sumrow = 0;
+    }
+    for (int c = warp; c < ncell; c += nw) {
+        if (!cell_reb[c]) continue;
+        const CellGeo& g = cells[c];
+        const int nb = g.nb[0] * g.nb[1] * g.nb[2], base = g.bin_base;
+        int run = g.begin;
+        for (int k0 = 0; k0 < nb; k0 += 32) {
+            const int k = k0 + lane;
+            const int v = k < nb ? bin_count[base + k] : 0;
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            if (k < nb) {
+                bin_start[base + k] = run + incl - v;
+                bin_count[base + k] = 0;
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+}
+
+// rebuild step 3: scatter atom indices into their bins (order fixed next);
+// a batch scatters the atoms of flagged cells only
 __global__ void k_scatter_bins(int n, const int* __restrict__ binid, const int* __restrict__ bin_start,
-                               int* __restrict__ bin_count, int* __restrict__ bin_tmp, DevScalars* sc) {
+                               int* __restrict__ bin_count, int* __restrict__ bin_tmp, const int* __restrict__ cell_of,
+                               const uint8_t* __restrict__ cell_reb, DevScalars* sc) {
     if (!sc->rebuild) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (cell_reb && !cell_reb[cell_of[i]]) continue;
         int b = binid[i];
         int slot = atomicAdd(&bin_count[b], 1);
         bin_tmp[bin_start[b] + slot] = i;
@@ -363,13 +406,17 @@ __global__ void k_scatter_bins(int n, const int* __restrict__ binid, const int* 
 // rebuild step 4: one warp per bin ranks its atoms by index (deterministic
 // order), counts zeroed for the next rebuild
 __global__ void k_sort_bins(int nbins, const int* __restrict__ bin_start, const int* __restrict__ bin_tmp,
-                            int* __restrict__ bin_atoms, int* __restrict__ bin_count, DevScalars* sc) {
+                            int* __restrict__ bin_atoms, int* __restrict__ bin_count, const int* __restrict__ cell_of,
+                            const uint8_t* __restrict__ cell_reb, DevScalars* sc) {
     if (!sc->rebuild) return;
     int lane = threadIdx.x & 31;
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int nw = (gridDim.x * blockDim.x) >> 5;
     for (int b = warp; b < nbins; b += nw) {
         int lo = bin_start[b], hi = bin_start[b + 1];
+        // a batch bin's slots lie in its cell's atom range, so the cell of a
+        // non-empty bin is the cell of atom index lo
+        if (cell_reb && lo < hi && !cell_reb[cell_of[lo]]) continue;
         for (int k = lo + lane; k < hi; k += 32) {
             int a = bin_tmp[k];
             int r = 0;
@@ -407,9 +454,11 @@ __global__ void k_shadow(int n, const double* __restrict__ x, const int* __restr
 
 __global__ void k_shadow_b(int n, const double* __restrict__ x, const int* __restrict__ binc,
                            const CellGeo* __restrict__ cells, const int* __restrict__ cell_of,
-                           float4* __restrict__ p32, float4* __restrict__ p0, int gated, DevScalars* sc) {
+                           float4* __restrict__ p32, float4* __restrict__ p0, int gated,
+                           const uint8_t* __restrict__ cell_reb, DevScalars* sc) {
     if (gated && !sc->rebuild) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (gated && !cell_reb[cell_of[i]]) continue;
         const CellGeo& cg = cells[cell_of[i]];
         Geo g;
         for (int k = 0; k < 6; k++) g.bs[k] = cg.bs[k];
@@ -436,6 +485,7 @@ struct BuildArgs {
     double cut_sk_sq[kMaxElem * kMaxElem];
     const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
     const int* cell_of;
+    const uint8_t* cell_reb;  // batch: the cells to rebuild
 };
 
 // frame displacement to Cartesian: dx' G with G as head + tail
@@ -510,7 +560,9 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
         const int a0 = a.bin_start[b];
         const int na = a.bin_start[b + 1] - a0;
         if (na == 0) continue;
-        const CellGeo* cg = BATCH ? a.cells + a.cell_of[a.bin_atoms[a0]] : nullptr;
+        const int cell = BATCH ? a.cell_of[a0] : 0;  // a batch bin's slots lie in its cell's atom range
+        if (BATCH && !a.cell_reb[cell]) continue;
+        const CellGeo* cg = BATCH ? a.cells + cell : nullptr;
         const int nbx = BATCH ? cg->nb[0] : a.g.nb[0], nby = BATCH ? cg->nb[1] : a.g.nb[1],
                   nbz = BATCH ? cg->nb[2] : a.g.nb[2];
         const int bin_base = BATCH ? cg->bin_base : 0;
@@ -648,10 +700,13 @@ __global__ void k_rebuild_done(DevScalars* sc) {
     sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
 }
 
-__global__ void k_rebuild_done_b(DevScalars* sc, CellMd* cmd, int ncell) {
+__global__ void k_rebuild_done_b(DevScalars* sc, CellMd* cmd, uint8_t* cell_reb, int ncell) {
     if (!sc->rebuild) return;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        if (!cell_reb[c]) continue;
         cmd[c].drift[0] = cmd[c].drift[1] = cmd[c].drift[2] = 0.0;
+        cell_reb[c] = 0;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         sc->nrebuild++;
         sc->drift[0] = sc->drift[1] = sc->drift[2] = 0.0;
@@ -667,6 +722,21 @@ __global__ void k_skin(int n, const double* __restrict__ x, const double* __rest
         double d0 = dsub(x0[i], x[i]), d1 = dsub(x0[n + i], x[n + i]), d2 = dsub(x0[2 * n + i], x[2 * n + i]);
         double r = dadd(dmul(d0, d0), dadd(dmul(d1, d1), dmul(d2, d2)));
         moved |= r > skin_sq;
+    }
+    if (__syncthreads_or(moved) && threadIdx.x == 0) sc->rebuild = 1;
+}
+
+// batch: the same test, flagging the cells whose atoms moved
+__global__ void k_skin_b(int n, const double* __restrict__ x, const double* __restrict__ x0, double skin_sq,
+                         const int* __restrict__ cell_of, uint8_t* __restrict__ cell_reb, DevScalars* sc) {
+    int moved = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d0 = dsub(x0[i], x[i]), d1 = dsub(x0[n + i], x[n + i]), d2 = dsub(x0[2 * n + i], x[2 * n + i]);
+        double r = dadd(dmul(d0, d0), dadd(dmul(d1, d1), dmul(d2, d2)));
+        if (r > skin_sq) {
+            cell_reb[cell_of[i]] = 1;
+            moved = 1;
+        }
     }
     if (__syncthreads_or(moved) && threadIdx.x == 0) sc->rebuild = 1;
 }
@@ -711,12 +781,13 @@ void sync_forces64(mappg_sys* s) {
 void request_rebuild(mappg_sys* s) {
     k_set_rebuild<<<1, 1, 0, s->stream>>>(s->sc, 1);
     MAPPG_CUDA(cudaGetLastError());
+    if (s->cell_reb) MAPPG_CUDA(cudaMemsetAsync(s->cell_reb, 1, s->ncell, s->stream));
 }
 
 void launch_shadow(mappg_sys* s, bool gated) {
     if (s->ncell > 1) {
         k_shadow_b<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->binc, s->cells_dev, s->cell_of,
-                                                                   s->p32, s->p0, gated ? 1 : 0, s->sc);
+                                                                   s->p32, s->p0, gated ? 1 : 0, s->cell_reb, s->sc);
         MAPPG_CUDA(cudaGetLastError());
         return;
     }
@@ -731,18 +802,27 @@ void launch_rebuild_chain(mappg_sys* s) {
     const int B = 256;
     int gb = grid_for(s, s->n, B);
     const bool batch = s->ncell > 1;
-    if (batch)
+    // a batch rebuilds the cells whose flag is set (cell_reb), a single cell
+    // all of its atoms
+    const uint8_t* reb = batch ? s->cell_reb : nullptr;
+    if (batch) {
         k_wrap_bin_b<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, s->cells_dev, s->cell_of, s->cmd, s->binc, s->binid,
-                                              s->bin_count, s->sc);
-    else
+                                              s->bin_count, s->cell_reb, s->sc);
+        k_scan_bins_b<<<(s->ncell * 32 + B - 1) / B, B, 0, s->stream>>>(s->ncell, s->n, s->nbins, s->cells_dev,
+                                                                         s->cell_reb, s->bin_count, s->bin_start,
+                                                                         s->sc);
+    } else {
         k_wrap_bin<<<gb, B, 0, s->stream>>>(s->n, s->x, s->s, g, s->binc, s->binid, s->bin_count, s->sc);
-    k_scan_bins<<<1, 1024, 0, s->stream>>>(s->nbins, s->bin_count, s->bin_start, s->sc);
+        k_scan_bins<<<1, 1024, 0, s->stream>>>(s->nbins, s->bin_count, s->bin_start, s->sc);
+    }
     int* bin_tmp = s->bin_atoms + s->n;
-    k_scatter_bins<<<gb, B, 0, s->stream>>>(s->n, s->binid, s->bin_start, s->bin_count, bin_tmp, s->sc);
-    k_sort_bins<<<grid_for(s, (long long)s->nbins * 32, B), B, 0, s->stream>>>(s->nbins, s->bin_start, bin_tmp,
-                                                                               s->bin_atoms, s->bin_count, s->sc);
+    k_scatter_bins<<<gb, B, 0, s->stream>>>(s->n, s->binid, s->bin_start, s->bin_count, bin_tmp, s->cell_of, reb,
+                                            s->sc);
+    k_sort_bins<<<grid_for(s, (long long)s->nbins * 32, B), B, 0, s->stream>>>(
+        s->nbins, s->bin_start, bin_tmp, s->bin_atoms, s->bin_count, s->cell_of, reb, s->sc);
     if (batch)
-        k_shadow_b<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->cells_dev, s->cell_of, s->p32, s->p0, 1, s->sc);
+        k_shadow_b<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->cells_dev, s->cell_of, s->p32, s->p0, 1,
+                                            s->cell_reb, s->sc);
     else
         k_shadow<<<gb, B, 0, s->stream>>>(s->n, s->x, s->binc, s->p32, s->p0, g, 1, s->sc);
     BuildArgs a;
@@ -767,6 +847,7 @@ void launch_rebuild_chain(mappg_sys* s) {
     a.fr = s->frame;
     a.cells = s->cells_dev;
     a.cell_of = s->cell_of;
+    a.cell_reb = reb;
     const int gbins = grid_for(s, (long long)s->nbins * 32, B);
     bool uni = true;
     for (int p = 1; p < s->ne * s->ne; p++) uni = uni && a.lo2[p] == a.lo2[0] && a.hi2[p] == a.hi2[0];
@@ -785,7 +866,7 @@ void launch_rebuild_chain(mappg_sys* s) {
             by_uni(std::true_type(), std::true_type());
         else
             by_uni(std::true_type(), std::false_type());
-        k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->ncell);
+        k_rebuild_done_b<<<(s->ncell + 255) / 256, 256, 0, s->stream>>>(s->sc, s->cmd, s->cell_reb, s->ncell);
     } else {
         if (s->frame.ortho)
             by_uni(std::false_type(), std::true_type());
@@ -798,7 +879,11 @@ void launch_rebuild_chain(mappg_sys* s) {
 
 void launch_skin_test(mappg_sys* s) {
     double skin_sq = 0.25 * s->skin * s->skin;
-    k_skin<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->x0, skin_sq, s->sc);
+    if (s->cell_reb)
+        k_skin_b<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->x0, skin_sq, s->cell_of, s->cell_reb,
+                                                                s->sc);
+    else
+        k_skin<<<grid_for(s, s->n, 256), 256, 0, s->stream>>>(s->n, s->x, s->x0, skin_sq, s->sc);
     MAPPG_CUDA(cudaGetLastError());
 }
 
@@ -848,6 +933,18 @@ EamArgs eam_args(mappg_sys* s) {
     a.alpha = 0.0;
     a.cell_active = s->cell_active;
     a.cutmask = s->cutmask;
+    a.fs_tab = s->fs_tab;
+    a.fs_rec = s->fs_rec;
+    a.fs_stride = s->fs_w;
+    a.fs_w = s->fs_w;
+    if (s->force_smem > 0 && s->fs_rec > 0) {
+        const long long fit = (long long)s->force_smem * 1024 / ((long long)sizeof(float4) * s->fs_rec);
+        a.fs_w = (int)std::min<long long>(s->fs_w, fit);
+    }
+    a.fs_off = s->fs_w - a.fs_w;
+    a.fs_mlo = s->fs_mlo + a.fs_off;
+    a.grp_atoms = s->grp_atoms;
+    for (int g = 0; g <= s->ne; g++) a.grp_begin[g] = s->grp_begin[g];
     a.dF = s->dF;
     a.rho32out = s->rho32;
     a.f = s->f;
@@ -886,7 +983,7 @@ void sys_free(mappg_sys* s) {
                     s->rho32, s->binc, s->binid, s->bin_count, s->bin_start, s->bin_atoms, s->nbr, s->nnbr,
                     s->rho, s->dF, s->partials, s->sc, s->stage, s->thermo_dev, s->cells_dev, s->cell_of,
                     s->chunk_begin, s->chunk_cell, s->cell_chunk, s->chunk_part, s->chunk_disp, s->cmd,
-                    s->cell_out, s->dof, s->stage2, s->cutmask};
+                    s->cell_out, s->dof, s->stage2, s->cutmask, s->fs_tab, s->grp_atoms, s->cell_reb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->ev_main) cudaEventDestroy(s->ev_main);
@@ -977,6 +1074,8 @@ void sys_alloc(mappg_sys* s, const double* x_host) {
         dev_alloc((void**)&s->cell_of, sizeof(int) * n);
         dev_alloc((void**)&s->cmd, sizeof(CellMd) * nc);
         dev_alloc((void**)&s->cell_out, sizeof(double) * 8 * nc);
+        dev_alloc((void**)&s->cell_reb, nc);
+        MAPPG_CUDA(cudaMemsetAsync(s->cell_reb, 1, nc, s->stream));
         MAPPG_CUDA(cudaMemsetAsync(s->cmd, 0, sizeof(CellMd) * nc, s->stream));
         MAPPG_CUDA(cudaMemcpyAsync(s->cells_dev, s->cells.data(), sizeof(CellGeo) * nc, cudaMemcpyHostToDevice,
                                    s->stream));

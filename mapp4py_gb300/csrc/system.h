@@ -127,6 +127,9 @@ constexpr int kMaxCells = 1 << 16;
 // shared memory given to the density tables of k_density32s: the rest of
 // the SM's 256 KB stays L1 for the neighbour-position gathers
 constexpr size_t kDensSmemBytes = 94 * 1024;
+// static shared memory of k_force32s (frame offsets, cutoffs, block sums),
+// kept out of its dynamic table budget
+constexpr size_t kForceSmemReserve = 4 * 1024;
 
 struct EamArgs {
     int n, maxnbr, ne, nr, nrho;
@@ -186,6 +189,21 @@ struct EamArgs {
     // force pass; rows longer than 32 x lanes are scanned in full)
     unsigned* cutmask;
     const double* cell_alpha;    // batch energy differences: trial step per cell
+    // k_force32s: the force records of one element group at a time in shared
+    // memory.  fs_tab holds, per group g (the element of atom i), fs_rec
+    // records of fs_stride knots ending at the cutoff's knot, record-major:
+    //   r <  ne       (z1, z2, z3, z0 head) of r*phi for the pair (g, r)
+    //   r <  2 ne     (rho'_{r->g} x3, z0 tail of (g, r - ne))
+    //   r >= 2 ne     rho'_{g->e} for e != g (per-pair densities only)
+    // The kernel copies the top fs_w knots of each record (from fs_off in
+    // its row; knots fs_mlo .. fs_mlo + fs_w - 1), as many as the shared
+    // memory budget allows.  grp_atoms lists the atoms of each element in
+    // bin order, group g at grp_begin[g] .. grp_begin[g + 1] (null for one
+    // element)
+    const float4* fs_tab;
+    int fs_rec, fs_w, fs_mlo, fs_stride, fs_off;
+    const int* grp_atoms;
+    int grp_begin[kMaxElem + 1];
 };
 
 }  // namespace mappg
@@ -224,6 +242,17 @@ struct mappg_sys {
     float* v32 = nullptr;
     float* rho32 = nullptr;
     unsigned* cutmask = nullptr;  // mixed: 32 words per atom (any lanes-per-atom choice)
+    // mixed force pass with the force records in shared memory (k_force32s):
+    // force_smem is its budget in KB (0: the L1 kernel k_force32; set by the
+    // autotuner); fs_tab is built on first use for the fs_w knots (from knot
+    // fs_mlo) of fs_rec records per element group that the largest budget
+    // holds
+    int force_smem = 0;
+    int smem_optin = 0;  // shared memory a block may opt in to
+    float4* fs_tab = nullptr;
+    int fs_rec = 0, fs_w = 0, fs_mlo = 0;
+    int* grp_atoms = nullptr;
+    int grp_begin[mappg::kMaxElem + 1] = {0};
     int* binc = nullptr;
     int* binid = nullptr;
     int* bin_count = nullptr;
@@ -255,6 +284,10 @@ struct mappg_sys {
     int* cell_chunk = nullptr;           // ncell + 1
     double* chunk_part = nullptr;
     uint8_t* cell_active = nullptr;      // batch minimizer in progress: cells still working (null: all)
+    // batch: per cell, set when one of its atoms moved more than skin/2 since
+    // the cell's last build (or a full build was requested); the rebuild
+    // chain rebuilds only these cells and clears their flags
+    uint8_t* cell_reb = nullptr;
     double* chunk_disp = nullptr;        // nchunk x 4 (integrator displacement sums)
     mappg::CellMd* cmd = nullptr;        // per-cell MD state
     double* cell_out = nullptr;          // ncell x 8 (pe, virial6, spare) staging
@@ -317,5 +350,7 @@ void launch_force_only(mappg_sys* s);      // the force kernel alone (timing; ne
 void launch_density32(mappg_sys* s, const EamArgs& a);
 void launch_force32(mappg_sys* s, const EamArgs& a);
 void launch_energy32(mappg_sys* s, const EamArgs& a);
+bool force_smem_available(mappg_sys* s);   // builds the k_force32s records on first use
+int force_smem_max_kb(const mappg_sys* s); // the largest shared-memory budget of k_force32s
 
 }  // namespace mappg

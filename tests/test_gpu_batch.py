@@ -94,6 +94,46 @@ def test_batch_nvt_follows_single_cell_runs(ff):
         assert np.max(np.abs(vb[k] - v1)) < 1e-5 * np.max(np.abs(v1))
 
 
+def _cell_keys(b, k):
+    """cell k's neighbour set in its own atom numbering"""
+    cnt, ent = b.neighbors()
+    off = b.offsets
+    sel = slice(off[k], off[k + 1])
+    first = int(cnt[:off[k]].sum())
+    ek = ent[first:first + int(cnt[sel].sum())].copy()
+    ek[:, 0] -= off[k]
+    return _keys(cnt[sel], ek)
+
+
+def test_batch_rebuilds_only_cells_that_moved(ff):
+    """A hot cell that needs list rebuilds does not rebuild a cold cell of
+    the same batch: the cold cell keeps the list of its start positions
+    (still valid: no atom moved skin/2), although a list built at its final
+    positions differs.  The single-cell runs rebuild the same way."""
+    hot = synth.alloy((5, 5, 5), xB=0.5, sigma=0.05, T=2500.0, seed=41)
+    # the cold cell's fifth neighbour shell sits at the list radius (a sqrt(5/2)
+    # = 6.0 A = cutoff + skin), so any motion changes which pairs a fresh list
+    # holds, while at 20 K no atom moves skin/2 in 40 steps
+    cold = synth.alloy((6, 5, 5), a=6.0 / np.sqrt(2.5), xB=0.5, sigma=0.02, T=20.0, seed=42)
+    b = _lib.Batch(ff, [(c.H, c.x, c.elem) for c in (hot, cold)], hot.masses)
+    b.build()
+    k_hot0, k_cold0 = _cell_keys(b, 0), _cell_keys(b, 1)
+    b.set_v(np.concatenate([hot.v, cold.v]))
+    b.nvt_run(np.array([2500.0, 20.0]), synth.FS, synth.KB, 40)
+    assert not np.array_equal(_cell_keys(b, 0), k_hot0)  # the hot cell was rebuilt
+    assert np.array_equal(_cell_keys(b, 1), k_cold0)  # the cold one kept its list
+    xc = b.split(b.get_x())[1]
+    fresh = _lib.System(ff, cold.H, xc, cold.elem, cold.masses, precision=_lib.MIXED)
+    assert not np.array_equal(_keys(*fresh.neighbors()), k_cold0)  # the test has teeth
+    s = _lib.System(ff, cold.H, cold.x, cold.elem, cold.masses, precision=_lib.MIXED)
+    s.set_v(cold.v)
+    s.nvt_run(20.0, synth.FS, synth.KB, 40)
+    assert np.array_equal(_keys(*s.neighbors()), k_cold0)
+    d = xc - s.get_x()
+    d -= np.round(d @ np.linalg.inv(cold.H)) @ cold.H
+    assert np.max(np.abs(d)) < 1e-5
+
+
 def test_batch_autotune_keeps_forces_and_runs(ff):
     """The batch autotuner (atoms per chunk x lanes per atom x entries per
     step) changes how the work is cut, not the result: forces agree to FP32
