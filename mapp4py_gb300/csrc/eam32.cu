@@ -171,6 +171,41 @@ __device__ __forceinline__ void embed32(const EamArgs& a, int ei, double rho, fl
     Fv = c.x + (__ldg(a.F32lo + k) + fr * fmaf(fmaf(c.w, fr, c.z), fr, c.y));
 }
 
+// F and F' of the density s - c (a compensated FP32 pair) without FP64
+// arithmetic: p = rho/drho as head ph + tail pl (the exact error of the head
+// product by an FMA, plus the tails of s*(1/drho) and of c), m = floor(ph)
+// corrected by the tail, fr = (ph - m) + pl (ph - m is exact).  The last
+// knot interval and the extrapolation above rho_max take embed32's FP64
+// route.  The density pass's lane 0 per atom runs this; on GB300's narrow
+// FP64 pipe the FP64 form cost 1 % of the pass
+__device__ __forceinline__ void embed32f(const EamArgs& a, int ei, float s, float c, float& Fv, float& dFv) {
+    const float dhi = (float)a.drho_inv;
+    const float dlo = (float)(a.drho_inv - (double)dhi);
+    const float ph = s * dhi;
+    const float pl = fmaf(s, dlo, fmaf(-c, dhi, fmaf(s, dhi, -ph)));
+    if (!(ph < (float)(a.nrho - 2))) {
+        embed32(a, ei, (double)s - (double)c, Fv, dFv);
+        return;
+    }
+    int m = (int)ph;
+    float fr = (ph - (float)m) + pl;
+    if (fr < 0.f) {
+        m -= 1;
+        fr += 1.f;
+    } else if (fr >= 1.f) {
+        m += 1;
+        fr -= 1.f;
+    }
+    if (m < 0) {
+        m = 0;
+        fr = 0.f;
+    }
+    const size_t k = (size_t)ei * a.nrho + m;
+    const float4 cc = __ldg(a.F32 + k);
+    dFv = fmaf(fmaf(3.0f * cc.w, fr, 2.0f * cc.z), fr, cc.y) * dhi;
+    Fv = cc.x + (__ldg(a.F32lo + k) + fr * fmaf(fmaf(cc.w, fr, cc.z), fr, cc.y));
+}
+
 // per-kernel persistent grid: as many blocks as fit on the GPU at once
 template <class Kern>
 static int occupancy_grid(mappg_sys* s, Kern k, int block) {
@@ -266,12 +301,11 @@ __device__ __forceinline__ void density_atom(const EamArgs& a, const Smem32& S, 
     }
     lane_sum_comp<TPA>(acc, acc_c);
     if (active && lane == 0) {
-        const double rho = (double)acc - (double)acc_c;
         float Fv, dFv;
-        embed32(a, ei, rho, Fv, dFv);
+        embed32f(a, ei, acc, acc_c, Fv, dFv);
         a.q32[i] = make_float4(pi.x, pi.y, pi.z, dFv);
-        a.rho32out[i] = (float)rho;
-        if (a.rho_keep) a.rho_keep[i] = rho;
+        a.rho32out[i] = acc - acc_c;
+        if (a.rho_keep) a.rho_keep[i] = (double)acc - (double)acc_c;
         kahan_add(es, ec, Fv);
     }
 }

@@ -389,6 +389,13 @@ struct TrialLine {
     }
 };
 
+// grid of the FP64 vector kernels with grid-wide sums: two blocks per SM, so
+// that each thread adds up N / (2 x SMs x 256) components (~10 for 250,000
+// atoms) before the block and last-block reductions, whose FP64 shuffle
+// trees would otherwise cost more than the components themselves (the order
+// stays fixed for a given N)
+static int lb_grid(mappg_sys* s, int N) { return std::max(1, std::min((N + 255) / 256, 2 * s->sm_count)); }
+
 // a mixed-precision search that fails may be FP32 force noise, not a minimum
 static bool ls_failed(int err) { return err == LS_MIN_ALPHA || err == B_F_DOWNHILL; }
 
@@ -399,7 +406,7 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
     if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     const int N = 3 * s->n;
-    const int grid = grid_for(s, N, 256);
+    const int grid = lb_grid(s, N);
     std::vector<void*> owned;
     auto dalloc = [&](size_t bytes) {
         void* p = nullptr;
@@ -684,7 +691,7 @@ void cg_run(mappg_sys* s, double e_tol, double max_dx, double f_tol, const LsPar
     if (!(e_tol >= 0.0)) throw Error{MAPPG_ERR_ARG, "e_tol must be >= 0"};
     if (nsteps < 0) throw Error{MAPPG_ERR_ARG, "nsteps must be >= 0"};
     const int N = 3 * s->n;
-    const int grid = grid_for(s, N, 256);
+    const int grid = lb_grid(s, N);
     std::vector<void*> owned;
     auto dalloc = [&](size_t bytes) {
         void* p = nullptr;
