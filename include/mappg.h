@@ -504,6 +504,18 @@ int mappg_mlp_set_refresh(mappg_mlp* net, int every);
 int mappg_lbfgs_run_precond(mappg_sys* sys, mappg_mlp* net, int m, double e_tol, double max_dx, double f_tol,
                             double c, double rho, double min_alpha, int nsteps, double* stats);
 
+/* mappg_lbfgs_run (one cell) or mappg_batch_lbfgs_run (a batch) with
+ * H0 = diag(1/d), d the caller's Hessian diagonal (n x 3 in the caller's
+ * atom order, eV/A^2, every entry positive and finite), scaled each
+ * iteration by (s.y)/(y.P.y) of the newest pair as the learned diagonal
+ * is; a non-descent direction falls back to plain L-BFGS.  For a diagonal
+ * from elsewhere (finite differences, a model of one's own), and the bound
+ * the network's prediction is measured against.  stats as
+ * mappg_lbfgs_run_precond (a batch: ncell x 7).  No counterpart in the
+ * reference. */
+int mappg_lbfgs_run_diag(mappg_sys* sys, const double* hdiag, int m, double e_tol, double max_dx, double f_tol,
+                         double c, double rho, double min_alpha, int nsteps, double* stats);
+
 /* L-BFGS over a batch of cells: every cell runs mappg_lbfgs_run's
  * iteration with its own history, line search and stopping state; the
  * kernels of each phase cover all cells.  m in 1..32.  stats: ncell x 7

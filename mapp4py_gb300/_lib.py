@@ -95,6 +95,8 @@ SIGNATURES = {
                                   C.c_double, C.c_int, _D]),
     "mappg_sys_autotune": (C.c_int, [_VP, _I, _I, _D]),
     "mappg_sys_force_tables": (C.c_int, [_VP, C.c_int, _I]),
+    "mappg_lbfgs_run_diag": (C.c_int, [_VP, _D, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.c_int, _D]),
     "mappg_cg_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                C.c_int, _D]),
     "mappg_batch_lbfgs_run": (C.c_int, [_VP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -724,6 +726,23 @@ def lbfgs_run_precond(system, net, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.
                                                    dptr(st)))
     return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]), "n_energy": int(st[4]),
             "n_force": int(st[5]), "fallbacks": int(st[6])}
+
+
+def lbfgs_run_diag(system, hdiag, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0,
+                   nsteps=100000):
+    """L-BFGS with H0 = diag(1/hdiag), hdiag the (n, 3) Hessian diagonal in the
+    caller's atom order; a Batch relaxes every cell (a list of stats)."""
+    hd = f64(hdiag).reshape(-1, 3)
+    if hd.shape[0] != system.n:
+        raise ValueError("hdiag must be (n, 3)")
+    batch = getattr(system, "ncell", 1) > 1
+    st = np.zeros((system.ncell, 7)) if batch else np.zeros(7)
+    system._checked(load().mappg_lbfgs_run_diag(system.h, dptr(hd), int(m), float(e_tol), float(max_dx),
+                                                float(f_tol), float(c), float(rho), float(min_alpha), int(nsteps),
+                                                dptr(st)))
+    keys = ("niter", "pe", "fmax", "err", "n_energy", "n_force", "fallbacks")
+    conv = lambda r: {k: (r[i] if k in ("pe", "fmax") else int(r[i])) for i, k in enumerate(keys)}
+    return [conv(r) for r in st] if batch else conv(st)
 
 
 def create_temp_dof(elem, masses, dof, T, kB, seed, v):

@@ -1045,6 +1045,72 @@ static void run_precond(mappg_sys* s, mappg_mlp* net, int m, double e_tol, doubl
         release();
 }
 
+}  // extern "C"
+
+namespace mappg {
+void sys_upload(mappg_sys* s, const double* host, double* dev);  // system.cu
+}  // namespace mappg
+
+// P = 1/d, d the caller's Hessian diagonal (bin order, SoA)
+__global__ void k_inv_diag(int n3, double* __restrict__ P, int* __restrict__ bad) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n3; q += gridDim.x * blockDim.x) {
+        const double d = P[q];
+        if (!(d > 0.0) || !isfinite(d)) {
+            *bad = 1;
+            P[q] = 1.0;
+        } else {
+            P[q] = 1.0 / d;
+        }
+    }
+}
+
+extern "C" {
+
+int mappg_lbfgs_run_diag(mappg_sys* s, const double* hdiag, int m, double e_tol, double max_dx, double f_tol,
+                         double c, double rho, double min_alpha, int nsteps, double* stats) {
+    return guarded([&] {
+        if (!s || !hdiag) throw Error{MAPPG_ERR_ARG, "null argument"};
+        const int n = s->n;
+        double* P = nullptr;
+        int* bad = nullptr;
+        struct Release {
+            double*& P;
+            int*& bad;
+            ~Release() {
+                if (P) cudaFree(P);
+                if (bad) cudaFree(bad);
+            }
+        } release{P, bad};
+        MAPPG_CUDA(cudaMalloc(&P, sizeof(double) * 3 * (size_t)n));
+        MAPPG_CUDA(cudaMalloc(&bad, sizeof(int)));
+        MAPPG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s->stream));
+        sys_upload(s, hdiag, P);
+        const int g = std::max(1, std::min(1024, (3 * n + 255) / 256));
+        k_inv_diag<<<g, 256, 0, s->stream>>>(3 * n, P, bad);
+        MAPPG_CUDA(cudaGetLastError());
+        int hb = 0;
+        MAPPG_CUDA(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        MAPPG_CUDA(cudaStreamSynchronize(s->stream));
+        if (hb) throw Error{MAPPG_ERR_ARG, "the Hessian diagonal must be positive and finite"};
+        sys_build(s);
+        if (s->ncell > 1) {
+            batch_lbfgs_run(s, m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, P, stats);
+        } else {
+            long long nfb = 0;
+            double st6[6];
+            LsParams ls;
+            ls.c = c;
+            ls.rho = rho;
+            ls.min_alpha = min_alpha;
+            lbfgs_run(s, m, e_tol, max_dx, f_tol, ls, nsteps, st6, P, &nfb);
+            if (stats) {
+                for (int k = 0; k < 6; k++) stats[k] = st6[k];
+                stats[6] = (double)nfb;
+            }
+        }
+    });
+}
+
 int mappg_mlp_set_refresh(mappg_mlp* net, int every) {
     return guarded([&] {
         if (!net || every < 0) throw Error{MAPPG_ERR_ARG, "bad argument"};

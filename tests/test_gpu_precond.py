@@ -82,3 +82,28 @@ def test_training_and_preconditioned_lbfgs(ff):
         learned += r1["n_force"] + r1["n_energy"]
     print("force+energy evaluations, plain %d, learned %d" % (plain, learned))
     assert learned < plain
+
+
+def test_lbfgs_with_a_callers_hessian_diagonal(ff):
+    """mappg_lbfgs_run_diag: H0 from a Hessian diagonal the caller supplies
+    (here the exact finite-difference one), one cell and a batch; a diagonal
+    that is not positive is refused."""
+    rng = np.random.default_rng(17)
+    masses = np.array([synth.MASS, synth.MASS])
+    cells = [precond.alloy_cell((4, 4, 8), rng, 0.4, 0.01, 0.1), precond.alloy_cell((8, 4, 4), rng, 0.7, 0.02, 0.1)]
+    hds = []
+    for H, x, elem, col in cells:
+        s = _lib.System(ff, H, x, elem, masses)
+        s.build()
+        hds.append(_lib.hessian_diag(s, col, 1e-4))
+    H, x, elem, _ = cells[0]
+    s = _lib.System(ff, H, x, elem, masses, precision=_lib.MIXED)
+    r = _lib.lbfgs_run_diag(s, np.maximum(hds[0], 0.5), m=10, f_tol=1e-4, nsteps=5000)
+    assert r["err"] == 100 and r["fmax"] < 1e-4
+    b = _lib.Batch(ff, [(c[0], c[1], c[2]) for c in cells], masses)
+    rb = _lib.lbfgs_run_diag(b, np.maximum(np.concatenate(hds), 0.5), m=10, f_tol=1e-4, nsteps=5000)
+    assert len(rb) == 2 and all(q["err"] == 100 and q["fmax"] < 1e-4 for q in rb)
+    bad = np.maximum(hds[0], 0.5)
+    bad[3, 1] = 0.0
+    with pytest.raises(_lib.MappgError, match="positive"):
+        _lib.lbfgs_run_diag(s, bad)
