@@ -173,8 +173,11 @@ __device__ __forceinline__ void force64_lane(const EamArgs& a, const Smem64& S, 
         double rsq = dx * dx + dy * dy + dz * dz;
         if (rsq < S.cut_sq[ei * a.ne + ej]) {
             const int j = entry_j(e);
-            const double r = sqrt(rsq);
-            const double rinv = 1.0 / r;
+            // 1/r from the FP64 reciprocal square root and r = rsq/r: one
+            // root instead of a root and a division, within an ulp or two of
+            // sqrt and 1/sqrt (GB300's FP64 pipe bounds this kernel)
+            const double rinv = rsqrt(rsq);
+            const double r = rsq * rinv;
             double p;
             const int m = knot64(r, a, p);
             const double der_i = spl_der(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p) * dri;
@@ -184,18 +187,19 @@ __device__ __forceinline__ void force64_lane(const EamArgs& a, const Smem64& S, 
             const double z = spl_val(cz, p);
             const double zp = spl_der(cz, p) * dri;
             const double phi = z * rinv;
-            const double dphi = zp * rinv - phi * rinv;
+            const double dphi = (zp - phi) * rinv;
             const double fp = -(dphi + dFi * der_i + __ldg(a.dF + j) * der_j) * rinv;
-            fx += fp * dx;
-            fy += fp * dy;
-            fz += fp * dz;
+            const double fdx = fp * dx, fdy = fp * dy, fdz = fp * dz;
+            fx += fdx;
+            fy += fdy;
+            fz += fdz;
             ep += phi;
-            w[0] += fp * dx * dx;
-            w[1] += fp * dx * dy;
-            w[2] += fp * dx * dz;
-            w[3] += fp * dy * dy;
-            w[4] += fp * dy * dz;
-            w[5] += fp * dz * dz;
+            w[0] += fdx * dx;
+            w[1] += fdx * dy;
+            w[2] += fdx * dz;
+            w[3] += fdy * dy;
+            w[4] += fdy * dz;
+            w[5] += fdz * dz;
         }
     }
 }
@@ -460,11 +464,11 @@ __global__ void __launch_bounds__(256) k_energy64(EamArgs a) {
                 P.delta(a, S.sh, e, dx, dy, dz);
                 double rsq = dx * dx + dy * dy + dz * dz;
                 if (rsq < S.cut_sq[ei * a.ne + ej]) {
-                    const double r = sqrt(rsq);
+                    const double rinv = rsqrt(rsq);  // as in force64_lane
                     double p;
-                    const int m = knot64(r, a, p);
+                    const int m = knot64(rsq * rinv, a, p);
                     acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
-                    ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
+                    ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) * rinv;
                 }
             }
         }
@@ -517,11 +521,11 @@ __global__ void __launch_bounds__(256) k_energy64b(EamArgs a, const int* __restr
                     P.delta(a, nullptr, e, dx, dy, dz);
                     const double rsq = dx * dx + dy * dy + dz * dz;
                     if (rsq < S.cut_sq[ei * a.ne + ej]) {
-                        const double r = sqrt(rsq);
+                        const double rinv = rsqrt(rsq);  // as in force64_lane
                         double p;
-                        const int m = knot64(r, a, p);
+                        const int m = knot64(rsq * rinv, a, p);
                         acc += spl_val(ldg4(a.rho64 + (size_t)(ej * a.ne + ei * a.rho_ei) * a.nr + m), p);
-                        ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) / r;
+                        ep += spl_val(ldg4(a.rphi64 + (size_t)(ei * a.ne + ej) * a.nr + m), p) * rinv;
                     }
                 }
             }
