@@ -740,7 +740,10 @@ void batch_lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_
             if (a.emode == BL_EDELTA) {
                 k_lb_h32b<<<ga, 256, 0, st>>>(n, a.h, h32);
             } else {
-                launch_energy32(s, eam_args(s));
+                // each searching cell's FP32 energy of x0 is its last force
+                // call's (CellMd::energy): every searching cell took a step
+                // and a force call in the previous iteration (or is at the
+                // opening force call)
                 k_bl_e0_32<<<gb, 256, 0, st>>>(a);
             }
             MAPPG_CUDA(cudaGetLastError());

@@ -555,8 +555,10 @@ void lbfgs_run(mappg_sys* s, int m, double e_tol, double max_dx, double f_tol, c
             if (1.7320508075688772 * (a1 * hmax + dxmax) < 0.5 * s->skin) {
                 line.mode = TrialLine::DELTA;
             } else {
+                // the FP32 energy of x0 is the last force call's: the same
+                // pair terms and compensated sums as the trials' energy pass
                 line.mode = TrialLine::E32DIFF;
-                line.e0_32 = TrialLine::energy32(s);
+                line.e0_32 = pe_force;
             }
         }
         if (dfa == 0.0)
