@@ -8,7 +8,11 @@
 //                (pair type, knot) (plus a 16-byte one for unlike pairs);
 //                F'_j rides in q32[j].w, so a neighbour costs one 16-byte
 //                gather plus the record
+//   k_force32s   k_force32 with one element group's records in shared
+//                memory at a time (an autotuner candidate)
 //   k_energy32   energy only (line-search trials)
+//   k_de32       energy differences E(x0 + alpha h) - E(x0) pair by pair
+//                (line-search trials within half the skin)
 //
 // Precision: every per-pair term is computed in FP32; the sums of them are
 // accumulated with compensation (Kahan: an FP32 sum and an FP32 correction
@@ -19,8 +23,9 @@
 // per pair cost 6 % of the force pass) and in FP64 across threads, which
 // keeps the stress within ~1e-7 of its scale.  Lane partials are combined
 // with exact two-sums (the correction keeps every rounding error), block and
-// grid totals are FP64 in a fixed order.  The embedding takes the density as
-// an FP64 value (sum minus correction).  Constants shared by many
+// grid totals are FP64 in a fixed order.  The embedding's knot index and
+// fraction come from the density's sum and correction without rounding them
+// to one FP32 value (embed32f).  Constants shared by many
 // pairs (1/dr, the frame-to-Cartesian scale, the spline constant terms) are
 // carried as head + tail so their rounding does not bias the totals.
 //
