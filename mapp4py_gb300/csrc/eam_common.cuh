@@ -152,6 +152,29 @@ __device__ __forceinline__ void chunk_store(Get get, double* out) {
     __syncthreads();
 }
 
+// chunk_store for FP32 per-thread values (streaming MD sums): FP32 warp
+// sums (a warp holds a few dozen terms), FP64 across the block's warps; the
+// FP64 shuffle tree of chunk_store costs more than the chunk's atoms here
+template <int K>
+__device__ __forceinline__ void chunk_store_f32(const float (&v)[K], double* out) {
+    __shared__ double red[8][K];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[w][k] = (double)t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int q = 0; q < nw; q++) t += red[q][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
 // sums of the first K partial slots over nblk blocks by one warp, in a fixed
 // order (lane-strided, then a shuffle tree): every lane gets the totals
 template <int K>

@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(256) k_ke32b(MdArgs a) {
             k[4] = fmaf(my, vz, k[4]);
             k[5] = fmaf(mz, vz, k[5]);
         }
-        chunk_store<6>([&](int q) { return (double)k[q]; }, a.chunk_part + (size_t)ch * kChunkSlots + 7);
+        chunk_store_f32<6>(k, a.chunk_part + (size_t)ch * kChunkSlots + 7);
     }
 }
 
@@ -544,9 +544,8 @@ __global__ void __launch_bounds__(256) k_integrate32b(MdArgs a) {
             moved = 1;
             if (threadIdx.x == 0) a.cell_reb[c] = 1;
         }
-        chunk_store<3>(
-            [&](int k) -> double { return k == 0 ? (double)dsum0 : (k == 1 ? (double)dsum1 : (double)dsum2); },
-            a.chunk_disp + (size_t)ch * 4);
+        const float ds[3] = {dsum0, dsum1, dsum2};
+        chunk_store_f32<3>(ds, a.chunk_disp + (size_t)ch * 4);
     }
     if (__syncthreads_or(moved) && threadIdx.x == 0) a.sc->rebuild = 1;
 }
