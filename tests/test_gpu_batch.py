@@ -134,6 +134,28 @@ def test_batch_rebuilds_only_cells_that_moved(ff):
     assert np.max(np.abs(d)) < 1e-5
 
 
+def test_batch_capacity_grows_and_cells_keep_their_lists(ff):
+    """A dense slab in one cell overflows the rows sized from the batch's
+    mean density: the build regrows them for every cell, and each cell's
+    neighbour set and forces equal the cell's own run alone."""
+    masses = np.array([synth.MASS, synth.MASS])
+    normal = synth.alloy((4, 4, 4), xB=0.5, sigma=0.05, seed=51)
+    _, xs = synth.fcc((4, 4, 4), a=3.0)  # a dense slab in a box 4x longer
+    Hs = np.diag([48.0, 12.0, 12.0])
+    es = np.zeros(len(xs), np.uint8)
+    cells = [(normal.H, normal.x, normal.elem), (Hs, xs, es)]
+    b = _lib.Batch(ff, cells, masses)
+    cap0 = b.stats()["capacity"]
+    b.force()
+    assert b.stats()["capacity"] > cap0
+    f = b.split(b.get_f())
+    for k, (H, x, elem) in enumerate(cells):
+        s = _lib.System(ff, H, x, elem, masses, precision=_lib.MIXED)
+        s.force()
+        assert np.array_equal(_cell_keys(b, k), _keys(*s.neighbors()))
+        assert np.array_equal(f[k], s.get_f())
+
+
 def test_batch_autotune_keeps_forces_and_runs(ff):
     """The batch autotuner (atoms per chunk x lanes per atom x entries per
     step) changes how the work is cut, not the result: forces agree to FP32
