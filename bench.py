@@ -281,6 +281,7 @@ def run_lbfgs(args, ff):
         for name in ("plain", "learned"):
             s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.MIXED)
             s.build()
+            s.autotune()  # as md.atoms does for a mixed system of 50,000 atoms or more
             s.sync()
             t0 = time.perf_counter()
             if name == "plain":
@@ -300,6 +301,7 @@ def run_lbfgs(args, ff):
         res = {"cells": ncell, "natoms": int(sum(x.natoms for x in cells)), "iteration_cap": cap, "max_dx": dx}
         for name in ("plain", "learned"):
             b = _lib.Batch(ff, [(x.H, x.x, x.elem) for x in cells], cells[0].masses)
+            b.autotune()  # chunk, lanes per atom and unrolling for the batch's own cells
             b.sync()
             t0 = time.perf_counter()
             r = b.lbfgs_run(m=10, max_dx=dx, f_tol=1e-4, nsteps=cap, net=None if name == "plain" else net)

@@ -709,9 +709,8 @@ __device__ __forceinline__ void energy_atom(const EamArgs& a, const Smem32& S, c
         ec += epc;
     }
     if (active && lane == 0) {
-        const double rho = (double)acc - (double)acc_c;
         float Fv, dFv;
-        embed32(a, ei, rho, Fv, dFv);
+        embed32f(a, ei, acc, acc_c, Fv, dFv);  // as the density pass (line searches compare the two)
         kahan_add(es, ec, Fv);
     }
 }

@@ -62,6 +62,7 @@ struct MdArgs {
     double masses[kMaxElem];
     double dtm[kMaxElem];  // dt2/m
     float dtm32[kMaxElem];
+    float m32[kMaxElem];   // masses as floats (the kinetic tensors' FP32 products)
     double dt, dt2, skin_sq;
     float dt32, skin_sq32;
     double bs[6];          // x -> scaled frame
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(256) k_close32(MdArgs a) {
     float k0 = 0.f, k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f, k5 = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int e = a.elem[i];
-        const float dtm = a.dtm32[e], m = (float)a.masses[e];
+        const float dtm = a.dtm32[e], m = a.m32[e];
         float vx = fmaf(a.f32[i], dtm, a.v32[i]);
         float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
         float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(256) k_ke32b(MdArgs a) {
         float k[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             const int e = a.elem[i];
-            const float dtm = a.dtm32[e], m = (float)a.masses[e];
+            const float dtm = a.dtm32[e], m = a.m32[e];
             const float vx = fmaf(a.f32[i], dtm, a.v32[i]);
             const float vy = fmaf(a.f32[n + i], dtm, a.v32[n + i]);
             const float vz = fmaf(a.f32[2 * n + i], dtm, a.v32[2 * n + i]);
@@ -618,6 +619,7 @@ static MdArgs md_args(mappg_sys* s, double T, double dt, double kB, double t_rel
         a.masses[e] = s->masses[e];
         a.dtm[e] = a.dt2 / s->masses[e];
         a.dtm32[e] = (float)a.dtm[e];
+        a.m32[e] = (float)a.masses[e];
     }
     a.skin_sq = 0.25 * s->skin * s->skin;
     // the FP32 skin test triggers a little early rather than late
