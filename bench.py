@@ -269,7 +269,8 @@ def run_lbfgs(args, ff):
           U(0.05, 0.2) A, relaxed together as one batch, each cell to the
           tolerance or args.c5_cap iterations
     max_dx (the largest atom move of a step, MinLBFGS's max_dx) is
-    args.lbfgs_dx for both."""
+    args.lbfgs_dx for both.  Each system is autotuned before its timed run,
+    as md.atoms tunes mixed systems of 50,000 atoms or more."""
     from mapp4py_gb300 import _lib, precond, synth
 
     net = precond.load()
