@@ -267,8 +267,10 @@ int mappg_sys_sync(mappg_sys* sys);
 /* Choose the lanes per atom (4, 8 or 16; 256/lanes atoms per block) and the
  * neighbour entries per loop step (1 or 2, mixed kernels) of the density and
  * force kernels by timing them on this system's atoms and neighbour list;
- * the choice is kept for the system.  tpa, unroll (may be NULL) receive it,
- * ms (7 doubles, may be NULL) the density+force time of each candidate
+ * the two passes share the lanes per atom and each takes its own entries per
+ * step; the choice is kept for the system.  tpa, unroll (may be NULL)
+ * receive it (unroll: the density pass's), ms (7 doubles, may be NULL) the
+ * density+force time of each candidate
  * (4,1) (8,1) (16,1) (4,2) (8,2) (16,2) (32,1); FP64 systems try the
  * one-entry forms only (the others stay 0).  Single mixed cells also time
  * each candidate with both force-record sources (mappg_sys_force_tables);

@@ -543,57 +543,81 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
         cudaEvent_t e0, e1;
         MAPPG_CUDA(cudaEventCreate(&e0));
         MAPPG_CUDA(cudaEventCreate(&e1));
-        double best = 1e30;
-        int best_tpa = s->tpa, best_u = s->unroll, best_sm = s->force_smem;
-        // a single mixed cell also tries the force pass with its records in
-        // shared memory (k_force32s) at three budgets: the budget takes L1
-        // from the neighbour-position gathers; ms_out[c] is the fastest
+        // density and force are timed apart: they share the lanes per atom
+        // (the force pass walks the density pass's per-lane cutoff bits) but
+        // each keeps its own entries per loop step; a single mixed cell also
+        // tries the force pass with its records in shared memory
+        // (k_force32s) at three budgets
         int modes[4] = {0, 0, 0, 0}, nmodes = 1;
         if (mixed && force_smem_available(s)) {
             const int mx = force_smem_max_kb(s);
             for (int kb : {64, 128, mx})
                 if (kb <= mx && kb > modes[nmodes - 1]) modes[nmodes++] = kb;
         }
+        const int tpa0 = s->tpa, u0 = s->unroll, uf0 = s->unroll_force, sm0 = s->force_smem;
+        double td[7], tf[7];
+        int tf_mode[7];
+        auto time_ms = [&](auto&& launch) {
+            launch();  // warm-up (and first-use set-up)
+            MAPPG_CUDA(cudaEventRecord(e0, s->stream));
+            for (int r = 0; r < 3; r++) launch();
+            MAPPG_CUDA(cudaEventRecord(e1, s->stream));
+            MAPPG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            return ms / 3.0;
+        };
         try {
             for (int c = 0; c < 7; c++) {
+                td[c] = tf[c] = 0.0;
+                tf_mode[c] = 0;
                 if (!mixed && cand[c][1] != 1) continue;
                 s->tpa = cand[c][0];
                 s->unroll = cand[c][1];
+                s->unroll_force = 0;
+                td[c] = time_ms([&] { launch_density_only(s); });
+                tf[c] = 1e30;
                 for (int mi = 0; mi < nmodes; mi++) {
-                    const int mode = modes[mi];
-                    s->force_smem = mode;
-                    launch_density_only(s);  // warm-up (and first-use set-up)
-                    launch_force_only(s);
-                    MAPPG_CUDA(cudaEventRecord(e0, s->stream));
-                    for (int r = 0; r < 3; r++) {
-                        launch_density_only(s);
-                        launch_force_only(s);
-                    }
-                    MAPPG_CUDA(cudaEventRecord(e1, s->stream));
-                    MAPPG_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                    if (ms_out && (mi == 0 || ms / 3.0 < ms_out[c])) ms_out[c] = ms / 3.0;
-                    if (ms < best) {
-                        best = ms;
-                        best_tpa = cand[c][0];
-                        best_u = cand[c][1];
-                        best_sm = mode;
+                    s->force_smem = modes[mi];
+                    const double t = time_ms([&] { launch_force_only(s); });
+                    if (t < tf[c]) {
+                        tf[c] = t;
+                        tf_mode[c] = modes[mi];
                     }
                 }
+                if (ms_out) ms_out[c] = td[c] + tf[c];
             }
         } catch (...) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            s->tpa = best_tpa;
-            s->unroll = best_u;
-            s->force_smem = best_sm;
+            s->tpa = tpa0;
+            s->unroll = u0;
+            s->unroll_force = uf0;
+            s->force_smem = sm0;
             throw;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        // per lanes per atom: the best density unroll plus the best force
+        // unroll and record source
+        double best = 1e30;
+        int best_tpa = tpa0, best_u = u0, best_uf = 0, best_sm = sm0;
+        for (int c = 0; c < 7; c++) {
+            if (td[c] <= 0.0) continue;
+            for (int c2 = 0; c2 < 7; c2++) {
+                if (tf[c2] <= 0.0 || cand[c2][0] != cand[c][0]) continue;
+                if (td[c] + tf[c2] < best) {
+                    best = td[c] + tf[c2];
+                    best_tpa = cand[c][0];
+                    best_u = cand[c][1];
+                    best_uf = cand[c2][1];
+                    best_sm = tf_mode[c2];
+                }
+            }
+        }
         s->tpa = best_tpa;
         s->unroll = best_u;
+        s->unroll_force = best_uf == best_u ? 0 : best_uf;
         s->force_smem = best_sm;
         if (tpa_out) *tpa_out = best_tpa;
         if (unroll_out) *unroll_out = best_u;
@@ -625,7 +649,7 @@ int mappg_batch_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, int* chunk
         if (s->ncell <= 1) throw Error{MAPPG_ERR_ARG, "mappg_batch_autotune takes a batch of cells"};
         const int chunks[3] = {128, 256, 512};
         double best = 1e30;
-        int bt = s->tpa, bu = s->unroll, bc = s->chunk_atoms;
+        int bt = s->tpa, bu = s->unroll, bf = s->unroll_force, bc = s->chunk_atoms;
         for (int k = 0; k < 3; k++) {
             sys_rechunk(s, chunks[k]);
             double ms[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -642,11 +666,13 @@ int mappg_batch_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, int* chunk
             if (bc == chunks[k]) {
                 bt = t;
                 bu = u;
+                bf = s->unroll_force;
             }
         }
         sys_rechunk(s, bc);
         s->tpa = bt;
         s->unroll = bu;
+        s->unroll_force = bf;
         if (tpa_out) *tpa_out = bt;
         if (unroll_out) *unroll_out = bu;
         if (chunk_out) *chunk_out = bc;

@@ -417,7 +417,10 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
         const int nn = __ldg(a.nnbr + i);
         const int* row = a.nbr + (size_t)i * a.maxnbr;
         const float cut0 = S.cut_sq[0];
-        auto pair = [&](int e, const float4& q) {
+        // inside: the entry is known to lie inside the cutoff (a set bit of the
+        // density pass's mask: the same positions and arithmetic give the same
+        // test), so the test is left out
+        auto pair = [&](int e, const float4& q, bool inside) {
             const int ej = entry_elem(e);
             const int t = ei * a.ne + ej;
             float4 o;
@@ -425,7 +428,7 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
             float dx, dy, dz;
             cart<ORTHO>(fr, (pi.x - q.x) + o.x, (pi.y - q.y) + o.y, (pi.z - q.z) + o.z, dx, dy, dz);
             const float rsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (rsq < (a.cut_uniform ? cut0 : S.cut_sq[t])) {
+            if (inside || rsq < (a.cut_uniform ? cut0 : S.cut_sq[t])) {
                 const float rinv = inv_sqrt(rsq);
                 const float r = rsq * rinv;
                 float fr;
@@ -485,7 +488,7 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                     const int t = __ffs(bits) - 1;
                     bits &= bits - 1u;
                     const int e = __ldg(row + lane + t * TPA);
-                    pair(e, __ldg(a.q32 + entry_j(e)));
+                    pair(e, __ldg(a.q32 + entry_j(e)), true);
                 }
             } else {
                 while (bits) {
@@ -498,14 +501,14 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                     const int e1 = v1 ? __ldg(row + lane + t1 * TPA) : e0;
                     const float4 q0 = __ldg(a.q32 + entry_j(e0));
                     const float4 q1 = __ldg(a.q32 + entry_j(e1));
-                    pair(e0, q0);
-                    if (v1) pair(e1, q1);
+                    pair(e0, q0, true);
+                    if (v1) pair(e1, q1, true);
                 }
             }
         } else if (U == 1) {
             for (int k = lane; k < nn; k += TPA) {
                 const int e = __ldg(row + k);
-                pair(e, __ldg(a.q32 + entry_j(e)));
+                pair(e, __ldg(a.q32 + entry_j(e)), false);
             }
         } else {
             // two entries per step, sums in the order of the one-entry loop
@@ -515,8 +518,8 @@ __device__ __forceinline__ void force_atom(const EamArgs& a, const Smem32& S, co
                 const int e1 = v1 ? __ldg(row + k + TPA) : e0;
                 const float4 q0 = __ldg(a.q32 + entry_j(e0));
                 const float4 q1 = __ldg(a.q32 + entry_j(e1));
-                pair(e0, q0);
-                if (v1) pair(e1, q1);
+                pair(e0, q0, false);
+                if (v1) pair(e1, q1, false);
             }
         }
         kahan_add(es, ec, ep);
@@ -1103,11 +1106,11 @@ static void pick_ortho(bool o, F&& fn) {
 }
 
 // dispatch on the system's lanes per atom, unroll and frame shape
-#define MAPPG_DISPATCH32(FN, ORTHO_EXPR)                                                              \
+#define MAPPG_DISPATCH32U(FN, ORTHO_EXPR, UNROLL)                                                     \
     do {                                                                                              \
         const bool o = (ORTHO_EXPR);                                                                  \
         auto call = [&](auto T, auto O, auto U) { FN<decltype(T)::value, decltype(O)::value, decltype(U)::value>(s, a); }; \
-        const bool u2 = s->unroll == 2;                                                               \
+        const bool u2 = (UNROLL) == 2;                                                                \
         switch (s->tpa) {                                                                             \
             case 4: u2 ? pick_ortho<4, 2>(o, call) : pick_ortho<4, 1>(o, call); break;                \
             case 16: u2 ? pick_ortho<16, 2>(o, call) : pick_ortho<16, 1>(o, call); break;            \
@@ -1117,8 +1120,11 @@ static void pick_ortho(bool o, F&& fn) {
         MAPPG_CUDA(cudaGetLastError());                                                               \
     } while (0)
 
+#define MAPPG_DISPATCH32(FN, ORTHO_EXPR) MAPPG_DISPATCH32U(FN, ORTHO_EXPR, s->unroll)
 #define MAPPG_TPA32(FN) MAPPG_DISPATCH32(FN, a.fr.ortho != 0)
 #define MAPPG_TPA32B(FN) MAPPG_DISPATCH32(FN, all_ortho(s))
+// the force pass's entries per loop step (it may differ from the density pass's)
+#define MAPPG_FORCE_U (s->unroll_force ? s->unroll_force : s->unroll)
 
 static void cells_done(mappg_sys* s, const EamArgs& a, int what) {
     k_cells_done<<<(s->ncell * 32 + 255) / 256, 256, 0, s->stream>>>(a, s->cell_chunk, s->cmd, what);
@@ -1161,10 +1167,10 @@ int force_smem_max_kb(const mappg_sys* s) {
 
 void launch_force32(mappg_sys* s, const EamArgs& a) {
     if (s->ncell > 1) {
-        MAPPG_TPA32B(force_b);
+        MAPPG_DISPATCH32U(force_b, all_ortho(s), MAPPG_FORCE_U);
         cells_done(s, a, 0);
     } else {
-        MAPPG_TPA32(force_t);
+        MAPPG_DISPATCH32U(force_t, a.fr.ortho != 0, MAPPG_FORCE_U);
     }
 }
 // E(x0 + alpha h) - E(x0) into sc->de (one cell; p32, rows and rho of x0,

@@ -217,6 +217,7 @@ struct mappg_sys {
     int sm_count = 0;
     int tpa = 8;
     int unroll = 1;  // neighbour entries per loop step of the mixed kernels (1 or 2)
+    int unroll_force = 0;  // the force pass's own entries per loop step (0: unroll)
     double skin = 0.5;
     double max_cut = 0.0;  // max cut + skin
     double cut_sq[mappg::kMaxElem * mappg::kMaxElem];
