@@ -254,6 +254,7 @@ def run_batch(args, ff, torch):
             "value": b.n * K / (ms / 1000.0), "unit": "atom-steps/s", "steps": K, "ms_per_step": ms / K,
             "graph_launches": 1 if K <= 512 else -(-K // 512), "rebuilds_in_run": st["rebuilds"],
             "lanes_per_atom": tpa, "entries_per_step": unroll, "atoms_per_chunk": b.chunk_atoms,
+            "force_entries_per_step": b.tuning()["force_entries_per_step"],
             "autotune_ms": {"%d,%d,%d" % k: round(v, 4) for k, v in tune.items()}}
 
 
@@ -558,8 +559,8 @@ def run_gpu(args, rank, world, local_rank):
                 "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "precision": args.precision,
                 "data": "synthetic",
                 "config": workload_config(N, args.cells, world),
-                "tuning": {"lanes_per_atom": tpa, "entries_per_step": unroll,
-                           "autotune_ms": {"%d,%d" % k: round(v, 4) for k, v in tune_ms.items()}},
+                "tuning": dict(sysm.tuning(), entries_per_step=unroll,
+                               autotune_ms={"%d,%d" % k: round(v, 4) for k, v in tune_ms.items()}),
                 "roofline": roof, "clocks": clk, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP[args.precision] * K,
                 "neighbor": {"rebuilds_in_run": st["rebuilds"], "max_row": st["max_row"], "capacity": st["capacity"]}}
         if batched is not None:

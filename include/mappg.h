@@ -277,6 +277,13 @@ int mappg_sys_sync(mappg_sys* sys);
  * ms then holds the faster.  No counterpart in the reference. */
 int mappg_sys_autotune(mappg_sys* sys, int* tpa, int* unroll, double* ms);
 
+/* The kernel shape in use (set by mappg_sys_autotune / mappg_batch_autotune):
+ * out[0] lanes per atom, out[1] entries per loop step of the density pass,
+ * out[2] of the force pass, out[3] the force pass's shared-memory budget in
+ * KB (mappg_sys_force_tables), out[4] atoms per chunk of a batch (0 for one
+ * cell).  No counterpart in the reference. */
+int mappg_sys_tuning(mappg_sys* sys, int* out);
+
 /* The mixed force pass's record source: mode 0 reads the force records
  * through L1 (k_force32); mode k > 0 copies the records of one element group
  * at a time into k KB of shared memory (k_force32s; single cells of mixed

@@ -95,6 +95,7 @@ SIGNATURES = {
                                   C.c_double, C.c_int, _D]),
     "mappg_sys_autotune": (C.c_int, [_VP, _I, _I, _D]),
     "mappg_sys_force_tables": (C.c_int, [_VP, C.c_int, _I]),
+    "mappg_sys_tuning": (C.c_int, [_VP, _I]),
     "mappg_lbfgs_run_diag": (C.c_int, [_VP, _D, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_int, _D]),
     "mappg_cg_run": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -449,6 +450,15 @@ class System:
         check(load().mappg_sys_autotune(self.h, C.byref(tpa), C.byref(unroll), dptr(ms)))
         keys = ((4, 1), (8, 1), (16, 1), (4, 2), (8, 2), (16, 2), (32, 1))
         return tpa.value, unroll.value, {k: v for k, v in zip(keys, ms) if v > 0}
+
+    def tuning(self):
+        """The kernel shape in use: lanes per atom, the density and force
+        passes' entries per loop step, the force records' shared-memory
+        budget (KB) and a batch's atoms per chunk."""
+        out = (C.c_int * 5)()
+        check(load().mappg_sys_tuning(self.h, out))
+        return dict(zip(("lanes_per_atom", "density_entries_per_step", "force_entries_per_step",
+                         "force_smem_kb", "atoms_per_chunk"), list(out)))
 
     def force_tables(self, mode=None):
         """The mixed force pass's record source: 0 through L1, k > 0 the

@@ -624,6 +624,17 @@ int mappg_sys_autotune(mappg_sys* s, int* tpa_out, int* unroll_out, double* ms_o
     });
 }
 
+int mappg_sys_tuning(mappg_sys* s, int* out) {
+    return guard([&] {
+        if (!s || !out) throw Error{MAPPG_ERR_ARG, "null argument"};
+        out[0] = s->tpa;
+        out[1] = s->unroll;
+        out[2] = s->unroll_force ? s->unroll_force : s->unroll;
+        out[3] = s->force_smem;
+        out[4] = s->ncell > 1 ? s->chunk_atoms : 0;
+    });
+}
+
 int mappg_sys_force_tables(mappg_sys* s, int mode, int* active) {
     return guard([&] {
         if (!s) throw Error{MAPPG_ERR_ARG, "null handle"};
