@@ -52,8 +52,8 @@ struct Pos64 {
     // dx = x_i - (x_j + n*H)
     __device__ __forceinline__ void delta(const EamArgs& a, const double (*sh)[3], int e, double& dx, double& dy,
                                           double& dz) const {
-        const int j = entry_j(e), c = entry_code(e);
-        int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
+        const int j = entry_j(e);
+        const int d0 = entry_step(e, 0), d1 = entry_step(e, 1), d2 = entry_step(e, 2);
         int n0 = (d0 < 0 && lo[0]) ? -1 : ((d0 > 0 && hi[0]) ? 1 : 0);
         int n1 = (d1 < 0 && lo[1]) ? -1 : ((d1 > 0 && hi[1]) ? 1 : 0);
         int n2 = (d2 < 0 && lo[2]) ? -1 : ((d2 > 0 && hi[2]) ? 1 : 0);
@@ -85,8 +85,8 @@ struct PosCell {
     }
     __device__ __forceinline__ void delta(const EamArgs& a, const double (*)[3], int e, double& dx, double& dy,
                                           double& dz) const {
-        const int j = entry_j(e), c = entry_code(e);
-        const int d0 = c % 3 - 1, d1 = (c / 3) % 3 - 1, d2 = c / 9 - 1;
+        const int j = entry_j(e);
+        const int d0 = entry_step(e, 0), d1 = entry_step(e, 1), d2 = entry_step(e, 2);
         const int n0 = (d0 < 0 && lo[0]) ? -1 : ((d0 > 0 && hi[0]) ? 1 : 0);
         const int n1 = (d1 < 0 && lo[1]) ? -1 : ((d1 > 0 && hi[1]) ? 1 : 0);
         const int n2 = (d2 < 0 && lo[2]) ? -1 : ((d2 > 0 && hi[2]) ? 1 : 0);

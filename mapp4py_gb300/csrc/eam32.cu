@@ -53,20 +53,17 @@ struct Smem32 {
     }
 };
 
-// frame offset -8 d of a neighbour image from its entry's bin-step code
-// c = (d0+1) + 3(d1+1) + 9(d2+1), by integer arithmetic (c/9 = (57 c) >> 9
-// and r/3 = (11 r) >> 5 hold for c < 27, r < 9) and an exact int-to-float
-// through the float bits of 2^23 + k; cheaper on the L1 data pipe, which
-// bounds these kernels, than a table in shared memory
+// frame offset -8 d of a neighbour image from its entry's bin steps: with
+// k_q = d_q + 1 in bits 2q..2q+1, the float whose bits are 0x4B000000 | (e &
+// (3 << 2q)) is 2^23 + 4^q k_q, and one FMA takes it to 8 - 8 k_q:
+// (2^23 + 4^q k) (-8 / 4^q) + (2^26 / 4^q + 8).  Every value involved is a
+// multiple of 8 / 4^q below 2^27 / 4^q, so the product and the sum are exact.
+// Two instructions per axis (a LOP3 and an FFMA): the density pass is bound
+// by instruction issue
 __device__ __forceinline__ void image_offset(int e, float4& o) {
-    const int c = entry_code(e);
-    const int k2 = (c * 57) >> 9;
-    const int r = c - 9 * k2;
-    const int k1 = (r * 11) >> 5;
-    const int k0 = r - 3 * k1;
-    o.x = fmaf(__int_as_float(0x4B000000 + k0) - 8388608.0f, -8.0f, 8.0f);
-    o.y = fmaf(__int_as_float(0x4B000000 + k1) - 8388608.0f, -8.0f, 8.0f);
-    o.z = fmaf(__int_as_float(0x4B000000 + k2) - 8388608.0f, -8.0f, 8.0f);
+    o.x = fmaf(__int_as_float(0x4B000000 | (e & 3)), -8.0f, 67108872.0f);
+    o.y = fmaf(__int_as_float(0x4B000000 | (e & 12)), -2.0f, 16777224.0f);
+    o.z = fmaf(__int_as_float(0x4B000000 | (e & 48)), -0.5f, 4194312.0f);
     o.w = 0.f;
 }
 

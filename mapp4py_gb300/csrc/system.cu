@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                     qy = pj.y - o.y;
                     qz = pj.z - o.z;
                 }
-                const int ent = valid ? (j << kEntryShift) | (ej << 5) | c : 0;
+                const int ent = valid ? make_entry(j, ej, c) : 0;
                 for (int q = 0; q < ng; q++) {
                     const float4 pq = s_at[wib][q];
                     const int iw = __float_as_int(pq.w);
@@ -1208,8 +1208,8 @@ void sys_neighbors(mappg_sys* s, int* counts, int* entries, long long* total) {
         int* out = entries + 4 * uoff[u];
         for (int k = 0; k < nn[i]; k++) {
             int e = rows[(size_t)i * s->maxnbr + k];
-            int j = entry_j(e), c = entry_code(e);
-            int d[3] = {c % 3 - 1, (c / 3) % 3 - 1, c / 9 - 1};
+            int j = entry_j(e);
+            int d[3] = {entry_step(e, 0), entry_step(e, 1), entry_step(e, 2)};
             out[4 * k] = s->host_id[j];
             const int* nbq = s->ncell > 1 ? s->cells[cell_of_host(s, i)].nb : s->nb;
             for (int q = 0; q < 3; q++) {

@@ -10,8 +10,10 @@
 //   q32              float4 per atom: p32.xyz and F'(rho) in .w, written by
 //                    the mixed density kernel and gathered by the force kernel
 //   nbr              full neighbour list, row i holds nnbr[i] entries
-//                    (j << 8 | e_j << 5 | code), code = (d0+1)+3(d1+1)+9(d2+1)
-//                    the bin step from atom i's bin to the neighbour image's bin
+//                    (j << 9 | e_j << 6 | k), k = k0 | k1 << 2 | k2 << 4 with
+//                    k_d = d_d + 1, d the bin step from atom i's bin to the
+//                    neighbour image's bin (j < 2^23: the entry is read as
+//                    unsigned)
 //   f32, v32         FP32 copies for the mixed path (forces out of the force
 //                    kernel; velocities for its kinetic-energy epilogue)
 //
@@ -36,13 +38,20 @@ namespace mappg {
 constexpr int kRedSlots = 16;    // doubles per block partial
 constexpr int kMaxBlocks = 4096; // partial slots
 constexpr int kMaxChain = 16;    // NHC chain length
-constexpr int kEntryShift = 8;   // j << 8 | element << 5 | code
+constexpr int kEntryShift = 9;   // j << 9 | element << 6 | bin steps
 constexpr int kMaxAtoms = 1 << 23;
 constexpr float kBinW = 8.0f;    // bin width in the scaled frame
 
-__host__ __device__ inline int entry_j(int e) { return e >> kEntryShift; }
-__host__ __device__ inline int entry_elem(int e) { return (e >> 5) & 7; }
-__host__ __device__ inline int entry_code(int e) { return e & 31; }
+__host__ __device__ inline int entry_j(int e) { return (int)((unsigned)e >> kEntryShift); }
+__host__ __device__ inline int entry_elem(int e) { return (e >> 6) & 7; }
+// bin step d_q in {-1, 0, 1} along axis q
+__host__ __device__ inline int entry_step(int e, int q) { return ((e >> (2 * q)) & 3) - 1; }
+// the entry of neighbour j (element ej) reached by stencil bin c = (d0+1) +
+// 3(d1+1) + 9(d2+1) of atom i's bin
+__host__ __device__ inline int make_entry(int j, int ej, int c) {
+    const unsigned k = (unsigned)(c % 3) | (unsigned)((c / 3) % 3) << 2 | (unsigned)(c / 9) << 4;
+    return (int)((unsigned)j << kEntryShift | (unsigned)ej << 6 | k);
+}
 
 struct Box {
     double H[3][3], B[3][3], h6[6], b6[6], vol, depth_inv[3];
