@@ -482,6 +482,7 @@ struct BuildArgs {
     Geo g;
     Frame fr;
     float lo2[kMaxElem * kMaxElem], hi2[kMaxElem * kMaxElem];
+    float in2[kMaxElem * kMaxElem];  // pair cutoff squared: entries below it lead their row
     double cut_sk_sq[kMaxElem * kMaxElem];
     const CellGeo* cells;  // batch: per-cell geometry, indexed by cell_of
     const int* cell_of;
@@ -528,10 +529,16 @@ __device__ __forceinline__ bool exact_keep(const BuildArgs& a, const double* h6,
 // stencil are read 32 at a time, once for all atoms of the bin, and every
 // atom of the bin tests them in turn, so a candidate's gathers and its place
 // in the bin sequence are paid once per bin instead of once per atom.  A
-// row lists its atom's neighbours in (bin step, bin order) order, bin steps
-// c = (d0+1) + 3(d1+1) + 9(d2+1); lanes test candidates and a ballot keeps
-// their order.  A batch finds the bin's cell through its first atom (the
-// bins of a cell hold only that cell's atoms).
+// row holds first its atom's neighbours inside the pair cutoff at build time,
+// in (bin step, bin order) order, bin steps c = (d0+1) + 3(d1+1) + 9(d2+1),
+// then those of the skin shell, in the reverse of that order: the shell's
+// entries are written backwards from the row's end and moved behind the
+// inner ones once the bin's candidates are done.  Lanes test candidates and
+// ballots keep their order.  With the inner entries in front, the lanes of
+// an atom (slots lane, lane + TPA, ...) get equal shares of the pairs inside
+// the cutoff, and the density pass's lanes reach the shell together.  A
+// batch finds the bin's cell through its first atom (the bins of a cell hold
+// only that cell's atoms).
 // ORTHO: every cell orthorhombic (one product per axis to Cartesian).
 // UNI: every pair type has the same list cutoff (thresholds in registers).
 template <bool BATCH, bool ORTHO, bool UNI>
@@ -540,12 +547,13 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
     __shared__ float4 off[27];
     __shared__ int s_pre[8][32], s_lo[8][32], s_img[8][32];  // per warp: the bin's 27 stencil bins
     __shared__ float4 s_at[8][32];  // per warp: the bin's atoms (frame position, w = index << 3 | element)
-    __shared__ float s_lo2[kMaxElem * kMaxElem], s_hi2[kMaxElem * kMaxElem];
+    __shared__ float s_lo2[kMaxElem * kMaxElem], s_hi2[kMaxElem * kMaxElem], s_in2[kMaxElem * kMaxElem];
     if (threadIdx.x < 27)
         off[threadIdx.x] = make_float4(a.fr.off[threadIdx.x][0], a.fr.off[threadIdx.x][1], a.fr.off[threadIdx.x][2], 0.f);
     if (threadIdx.x < a.ne * a.ne) {
         s_lo2[threadIdx.x] = a.lo2[threadIdx.x];
         s_hi2[threadIdx.x] = a.hi2[threadIdx.x];
+        s_in2[threadIdx.x] = a.in2[threadIdx.x];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -553,7 +561,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int n = a.n;
-    const float lo2u = a.lo2[0], hi2u = a.hi2[0];
+    const float lo2u = a.lo2[0], hi2u = a.hi2[0], in2u = a.in2[0];
     int maxrow = 0, overflow = 0;
     long long sumrow = 0;
     for (int b = warp; b < nbins; b += nw) {
@@ -605,7 +613,8 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                 s_at[wib][lane] = p;
             }
             __syncwarp();
-            int mycnt = 0;  // lane q: entries so far of the group's atom q
+            int mycnt = 0;  // lane q: inner entries so far of the group's atom q (row front)
+            int myout = 0;  // lane q: shell entries so far (row end, backwards)
             int c = 0, cpre = 0, cnext = s_pre[wib][1], clo = s_lo[wib][0], cimg = s_img[wib][0];
             for (int t0 = 0; t0 < total; t0 += 32) {
                 const int t = t0 + lane;
@@ -637,7 +646,7 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                     const float4 pq = s_at[wib][q];
                     const int iw = __float_as_int(pq.w);
                     const int i = iw >> 3;
-                    bool keep = false;
+                    bool keep = false, inner = false;
                     if (valid && q != selfq) {
                         float dx, dy, dz;
                         if (ORTHO) {
@@ -656,24 +665,55 @@ __global__ void __launch_bounds__(256) k_build_bins(BuildArgs a, int nbins, DevS
                         else if (r2 <= (UNI ? hi2u : s_hi2[pe]))
                             keep = exact_keep(a, h6, a.x[i], a.x[n + i], a.x[2 * n + i], j, im,
                                               UNI ? (iw & 7) * a.ne + ej : pe);
+                        inner = keep && r2 < (UNI ? in2u : s_in2[pe]);
                     }
                     const unsigned m = __ballot_sync(0xffffffffu, keep);
                     if (m) {
-                        const int cnt = __shfl_sync(0xffffffffu, mycnt, q);
+                        const unsigned mi = __ballot_sync(0xffffffffu, inner);
+                        const unsigned mo = m & ~mi;
+                        const unsigned below = (1u << lane) - 1u;
+                        const int cin = __shfl_sync(0xffffffffu, mycnt, q);
+                        const int cout = __shfl_sync(0xffffffffu, myout, q);
                         if (keep) {
-                            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                            if (pos < a.maxnbr) a.nbr[(size_t)i * a.maxnbr + pos] = ent;
+                            // both streams stay inside the row; where they
+                            // meet the row has overflowed and is built again
+                            // with a larger capacity
+                            const int pos = inner ? cin + __popc(mi & below)
+                                                  : a.maxnbr - 1 - (cout + __popc(mo & below));
+                            if (pos >= 0 && pos < a.maxnbr) a.nbr[(size_t)i * a.maxnbr + pos] = ent;
                         }
-                        if (lane == q) mycnt = cnt + __popc(m);
+                        if (lane == q) {
+                            mycnt = cin + __popc(mi);
+                            myout = cout + __popc(mo);
+                        }
                     }
+                }
+            }
+            // each row's shell entries move from the row's end to follow its
+            // inner ones: a move to lower slots, 32 entries at a time, each
+            // batch read before it is written (the gap is never negative)
+            __syncwarp();
+            for (int q = 0; q < ng; q++) {
+                const int cin = __shfl_sync(0xffffffffu, mycnt, q);
+                const int cout = __shfl_sync(0xffffffffu, myout, q);
+                if (cout == 0 || cin + cout > a.maxnbr) continue;
+                int* row = a.nbr + (size_t)(__float_as_int(s_at[wib][q].w) >> 3) * a.maxnbr;
+                const int src = a.maxnbr - cout;
+                for (int k0 = 0; k0 < cout; k0 += 32) {
+                    const int k = k0 + lane;
+                    const int v = k < cout ? row[src + k] : 0;
+                    __syncwarp();
+                    if (k < cout) row[cin + k] = v;
+                    __syncwarp();
                 }
             }
             if (lane < ng) {
                 const int i = __float_as_int(s_at[wib][lane].w) >> 3;
-                a.nnbr[i] = min(mycnt, a.maxnbr);
-                if (mycnt > a.maxnbr) overflow = 1;
-                maxrow = max(maxrow, mycnt);
-                sumrow += mycnt;
+                const int tot = mycnt + myout;
+                a.nnbr[i] = min(tot, a.maxnbr);
+                if (tot > a.maxnbr) overflow = 1;
+                maxrow = max(maxrow, tot);
+                sumrow += tot;
                 a.x0[i] = a.x[i];
                 a.x0[n + i] = a.x[n + i];
                 a.x0[2 * n + i] = a.x[2 * n + i];
@@ -843,6 +883,7 @@ void launch_rebuild_chain(mappg_sys* s) {
         a.cut_sk_sq[p] = s->cut_sk_sq[p];
         a.lo2[p] = (float)(s->cut_sk_sq[p] - s->band);
         a.hi2[p] = (float)(s->cut_sk_sq[p] + s->band);
+        a.in2[p] = (float)s->cut_sq[p];
     }
     a.fr = s->frame;
     a.cells = s->cells_dev;
