@@ -132,6 +132,14 @@ def throughput(natoms, steps, world, ms):
     return natoms * steps * world / (ms / 1000.0)
 
 
+def guarded(leg):
+    """leg() or, if it raises, {"error": <type: message>}."""
+    try:
+        return leg()
+    except Exception as ex:
+        return {"error": "%s: %s" % (type(ex).__name__, ex)}
+
+
 def workload_config(natoms, cells, world):
     """The workload both arms run (the arithmetic is the line's `precision`
     and `dtype`, outside the config, so the two arms' configs compare equal)."""
@@ -545,13 +553,17 @@ def run_gpu(args, rank, world, local_rank):
                    "(list rebuilt when an atom moved more than skin/2) + opening force call + one step per "
                    "call, as MDNVT::run"}
 
-    batched = None if args.batch_steps <= 0 else run_batch(args, ff, torch)
-    lbfgs = None if args.lbfgs_cap <= 0 and args.c5_cells <= 0 else run_lbfgs(args, ff)
+    # the legs beside the headline: each reports its own failure in the line
+    # instead of taking the measured headline down with it
+    batched = None if args.batch_steps <= 0 else guarded(lambda: run_batch(args, ff, torch))
+    lbfgs = None if args.lbfgs_cap <= 0 and args.c5_cells <= 0 else guarded(lambda: run_lbfgs(args, ff))
     extras = None
     if args.extras and rank == 0:
-        extras = run_accuracy(args, ff, path, cell, torch)
+        extras = guarded(lambda: run_accuracy(args, ff, path, cell, torch))
+        if "error" in extras:
+            extras = {"accuracy_error": extras["error"]}
         if not args.no_cpu:
-            extras["c1"] = run_c1(args, path, torch)
+            extras["c1"] = guarded(lambda: run_c1(args, path, torch))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
