@@ -299,7 +299,7 @@ def run_lbfgs(args, ff):
             else:
                 r = _lib.lbfgs_run_precond(s, net, m=10, e_tol=0.0, max_dx=dx, f_tol=1e-4, nsteps=cap)
             secs = time.perf_counter() - t0
-            res[name] = {"seconds": secs, "converged": r["err"] == 100, "iterations": r["niter"],
+            res[name] = {"seconds": secs, "converged": r["err"] == 100, "stop_code": r["err"], "iterations": r["niter"],
                          "fmax": r["fmax"], "energy_calls": r["n_energy"], "force_calls": r["n_force"],
                          "ms_per_iteration": 1000.0 * secs / max(1, r["niter"])}
         res["wall_ratio_plain_over_learned"] = res["plain"]["seconds"] / res["learned"]["seconds"]
@@ -317,7 +317,10 @@ def run_lbfgs(args, ff):
             r = b.lbfgs_run(m=10, max_dx=dx, f_tol=1e-4, nsteps=cap, net=None if name == "plain" else net)
             secs = time.perf_counter() - t0
             its = np.array([q["niter"] for q in r])
-            res[name] = {"seconds": secs, "cells_converged": int(sum(q["err"] == 100 for q in r)),
+            codes = {}
+            for q in r:
+                codes[str(q["err"])] = codes.get(str(q["err"]), 0) + 1
+            res[name] = {"seconds": secs, "cells_converged": int(sum(q["err"] == 100 for q in r)), "stop_codes": codes,
                          "iterations_max": int(its.max()), "iterations_median": float(np.median(its)),
                          "energy_calls": int(sum(q["n_energy"] for q in r)),
                          "force_calls": int(sum(q["n_force"] for q in r))}
@@ -325,6 +328,10 @@ def run_lbfgs(args, ff):
         return res
 
     out = {"metric": "L-BFGS time to max|F| < 1e-4 eV/A, learned vs plain", "unit": "s",
+           "stop_code_legend": {"100": "max|F| below the tolerance", "5": "iteration cap",
+                                "3": "line search: step below min_alpha", "1": "line search: not downhill",
+                                "2": "line search: zero gradient", "4": "energy change below e_tol",
+                                "8": "bracketing: not downhill"},
            "network": "33-64-64-3 BF16 MLP trained on 201,814 FD Hessian diagonals (precond_net.npz)"}
     if args.lbfgs_cap > 0:
         out["c4"] = c4(args.lbfgs_cap)
