@@ -331,6 +331,7 @@ def run_lbfgs(args, ff):
            "stop_code_legend": {"100": "max|F| below the tolerance", "5": "iteration cap",
                                 "3": "line search: step below min_alpha", "1": "line search: not downhill",
                                 "2": "line search: zero gradient", "4": "energy change below e_tol",
+                                "7": "bracketing: step above its maximum",
                                 "8": "bracketing: not downhill"},
            "network": "33-64-64-3 BF16 MLP trained on 201,814 FD Hessian diagonals (precond_net.npz)"}
     if args.lbfgs_cap > 0:
