@@ -32,6 +32,13 @@ REF_BUDGET_S = 60  # CPU seconds of the reference arm's timed sample
 # kernels in one step's CUDA graph: FP64 step_open, kick_drift, com_skin, 7 rebuild-chain, density,
 # force, kick2; mixed step_open32, integrate32, 7 rebuild-chain, density32, force32, close32
 KERNELS_PER_STEP = {"fp64": 13, "mixed": 12}
+# how the sums of the pair terms are carried (the line's dtype in words)
+ACCUMULATION = {
+    "mixed": "FP32 pair terms; per-atom density, force and pair energy in compensated FP32 (Kahan) "
+             "within a lane, exact FP32 two-sums across an atom's lanes, FP64 per atom and across "
+             "blocks; virial in plain FP32 per thread (a few hundred terms), FP64 across threads",
+    "fp64": "FP64 throughout",
+}
 
 
 def env_int(k, d):
@@ -577,6 +584,7 @@ def run_gpu(args, rank, world, local_rank):
         line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32+f64acc" if prec == _lib.MIXED else "f64", "precision": args.precision,
+                "accumulation": ACCUMULATION[args.precision],
                 "data": "synthetic",
                 "config": workload_config(N, args.cells, world),
                 "tuning": dict(sysm.tuning(), entries_per_step=unroll,
