@@ -370,6 +370,11 @@ def run_accuracy(args, ff, path, cell, torch):
     ms = e0.elapsed_time(e1) / K
     s64.nvt_end(K + 3)
     out["fp64"] = {"value": cell.natoms / (ms / 1000.0), "unit": "atom-steps/s", "ms_per_step": ms, "steps": K}
+    # the FP64 path's own roof: its pair kernels are bound by the FP64 pipe,
+    # not by HBM
+    out["fp64"]["roof"] = guarded(lambda: {
+        "bound": "fp64 pipe", "fma_rate_tflops": _lib.fp64_fma_rate(),
+        "source": "mappg_fp64_fma_rate: independent FP64 FMA chains on every SM, CUDA events"})
     # error of the mixed path against FP64 on the starting configuration
     a = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, precision=_lib.FP64)
     b = _lib.System(ff, cell.H, cell.x, cell.elem, cell.masses, precision=_lib.MIXED)
