@@ -68,3 +68,19 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
 
     bench.run_reference(A(), rank=1, world=2)
     assert capsys.readouterr().out == ""
+
+
+def test_side_legs_report_their_failure_in_the_line():
+    """A leg beside the headline that raises leaves an error entry instead of
+    ending the run; a leg that succeeds returns its result unchanged."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.guarded(lambda: {"value": 1.0}) == {"value": 1.0}
+
+    def broken():
+        raise RuntimeError("leg failed")
+
+    assert bench.guarded(broken) == {"error": "RuntimeError: leg failed"}
+    assert set(bench.ACCUMULATION) == {"mixed", "fp64"}
+    assert "FP32 per thread" in bench.ACCUMULATION["mixed"]
