@@ -39,11 +39,21 @@ extern "C" int mappg_fp64_fma_rate(int iters, int reps, double* tflops) {
         int dev = 0, sms = 0;
         MAPPG_CUDA(cudaGetDevice(&dev));
         MAPPG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        double* sink = nullptr;
-        MAPPG_CUDA(cudaMalloc(&sink, sizeof(double)));
-        cudaEvent_t e0, e1;
-        MAPPG_CUDA(cudaEventCreate(&e0));
-        MAPPG_CUDA(cudaEventCreate(&e1));
+        // released on every return, including a failed CUDA call
+        struct Held {
+            double* sink = nullptr;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            ~Held() {
+                if (e0) cudaEventDestroy(e0);
+                if (e1) cudaEventDestroy(e1);
+                if (sink) cudaFree(sink);
+            }
+        } held;
+        MAPPG_CUDA(cudaMalloc(&held.sink, sizeof(double)));
+        MAPPG_CUDA(cudaEventCreate(&held.e0));
+        MAPPG_CUDA(cudaEventCreate(&held.e1));
+        double* sink = held.sink;
+        cudaEvent_t e0 = held.e0, e1 = held.e1;
         const int grid = sms * 8, block = 256;
         k_fma64<<<grid, block>>>(iters, 0.999999, 1e-7, sink);
         MAPPG_CUDA(cudaGetLastError());
@@ -57,9 +67,6 @@ extern "C" int mappg_fp64_fma_rate(int iters, int reps, double* tflops) {
             MAPPG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             best = std::min(best, ms);
         }
-        MAPPG_CUDA(cudaEventDestroy(e0));
-        MAPPG_CUDA(cudaEventDestroy(e1));
-        cudaFree(sink);
         const double flops = 2.0 * kChains * (double)iters * grid * block;
         *tflops = flops / (best * 1e-3) / 1e12;
         return MAPPG_OK;
