@@ -856,36 +856,40 @@ extern "C" int mappg_sys_energy_delta(mappg_sys* s, const double* h, double alph
         const int n = s->n;
         double* hd = nullptr;
         float4* h32 = nullptr;
-        MAPPG_CUDA(cudaMalloc(&hd, sizeof(double) * 3 * (size_t)n));
-        MAPPG_CUDA(cudaMalloc(&h32, sizeof(float4) * (size_t)n));
+        LbScal* L = nullptr;
+        unsigned* counter = nullptr;
+        // released on every return, including a failed allocation or launch
         struct Free {
-            double* a;
-            float4* b;
+            double*& a;
+            float4*& b;
+            LbScal*& l;
+            unsigned*& c;
             mappg_sys* s;
             ~Free() {
-                cudaFree(a);
-                cudaFree(b);
+                if (a) cudaFree(a);
+                if (b) cudaFree(b);
+                if (l) cudaFree(l);
+                if (c) cudaFree(c);
                 s->h32 = nullptr;
                 s->keep_rho64 = false;
             }
-        } fr{hd, h32, s};
+        } fr{hd, h32, L, counter, s};
+        MAPPG_CUDA(cudaMalloc(&hd, sizeof(double) * 3 * (size_t)n));
+        MAPPG_CUDA(cudaMalloc(&h32, sizeof(float4) * (size_t)n));
         // the list must hold every pair inside the cutoff at x and at x + alpha h
         double hmax = 0.0;
         for (size_t q = 0; q < 3 * (size_t)n; q++) hmax = std::max(hmax, std::fabs(h[q]));
         lb_update(s);
         sys_upload(s, h, hd);
         const int N = 3 * n, grid = grid_for(s, N, 256);
-        LbScal* L = nullptr;
-        unsigned* counter = nullptr;
         MAPPG_CUDA(cudaMalloc(&L, sizeof(LbScal)));
         MAPPG_CUDA(cudaMalloc(&counter, sizeof(unsigned)));
         MAPPG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s->stream));
         k_lb_prep<<<grid, 256, 0, s->stream>>>(N, hd, hd, s->x, s->x0, L, s->partials, counter);
+        MAPPG_CUDA(cudaGetLastError());
         double dxmax = 0.0;
         MAPPG_CUDA(cudaMemcpyAsync(&dxmax, &L->dxmax, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         MAPPG_CUDA(cudaStreamSynchronize(s->stream));
-        cudaFree(L);
-        cudaFree(counter);
         if (!(1.7320508075688772 * (std::fabs(alpha) * hmax + dxmax) < 0.5 * s->skin))
             throw Error{MAPPG_ERR_ARG, "alpha*h moves atoms beyond the neighbour list's skin"};
         s->keep_rho64 = true;

@@ -665,6 +665,19 @@ uint16_t* upload_inputs(mappg_mlp* net, const float* feat, int n, const std::vec
     float* df = nullptr;
     int* dord = nullptr;
     uint16_t* X = nullptr;
+    // the staging arrays go on every return; X only on a failed one (the
+    // caller owns it otherwise)
+    struct Held {
+        float*& df;
+        int*& dord;
+        uint16_t*& X;
+        bool keep_x = false;
+        ~Held() {
+            if (df) cudaFree(df);
+            if (dord) cudaFree(dord);
+            if (X && !keep_x) cudaFree(X);
+        }
+    } held{df, dord, X};
     MAPPG_CUDA(cudaMalloc(&df, sizeof(float) * 33 * (size_t)n));
     MAPPG_CUDA(cudaMalloc(&X, sizeof(uint16_t) * kIn * (size_t)n));
     MAPPG_CUDA(cudaMemcpyAsync(df, feat, sizeof(float) * 33 * (size_t)n, cudaMemcpyHostToDevice, net->stream));
@@ -675,8 +688,7 @@ uint16_t* upload_inputs(mappg_mlp* net, const float* feat, int n, const std::vec
     k_pack_inputs<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, net->stream>>>(n, df, dord, norm_of(net), X);
     MAPPG_CUDA(cudaGetLastError());
     MAPPG_CUDA(cudaStreamSynchronize(net->stream));
-    cudaFree(df);
-    if (dord) cudaFree(dord);
+    held.keep_x = true;
     return X;
 }
 
