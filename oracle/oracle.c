@@ -1922,9 +1922,53 @@ static int ls_min(const orc_ls* p, orc_line* L, double dfa, double max_a, double
  * after each accepted step).  stats out: [niter, pe, max|F|, err, n_energy,
  * n_force].  Returns 0 on success.
  */
+static int lbfgs_core(orc_sys* s, int m, double e_tol, double max_dx, double f_tol, const orc_ls* ls, int nsteps,
+                      double* stats, const double* P, long* n_fallback);
+
 int orc_lbfgs_run_ls(void* p, int m, double e_tol, double max_dx, double f_tol, const orc_ls* ls, int nsteps,
                      double* stats) {
+    return lbfgs_core((orc_sys*)p, m, e_tol, max_dx, f_tol, ls, nsteps, stats, NULL, NULL);
+}
+
+/*
+ * L-BFGS with a diagonal initial inverse Hessian, as the library's
+ * mappg_lbfgs_run_diag runs it (the learned-preconditioner path; no
+ * counterpart in the reference): hdiag is the per-component Hessian
+ * diagonal in atom order (x, y, z per atom), P = 1/hdiag, and the two-loop
+ * recursion's middle step is h <- tau P h instead of gamma h, with tau =
+ * (s.y)/(y.P.y) of the newest pair (1 before the first).  A direction that
+ * is not a descent direction is recomputed with gamma (counted in
+ * stats[6]), then replaced by f as in the plain run.  A pair without
+ * positive curvature takes no part in the recursion (rho = 0) and leaves
+ * gamma and tau as they were.  hdiag must be positive and finite.
+ * stats out: [niter, pe, max|F|, err, n_energy, n_force, fallbacks].
+ */
+int orc_lbfgs_run_diag(void* p, const double* hdiag, int m, double e_tol, double max_dx, double f_tol, double c_ls,
+                       double rho_ls, double min_alpha, int nsteps, double* stats) {
     orc_sys* s = (orc_sys*)p;
+    int n3 = 3 * s->natms;
+    double* P = (double*)malloc(sizeof(double) * (n3 ? n3 : 1));
+    for (int q = 0; q < n3; q++) {
+        if (!(hdiag[q] > 0.0) || !isfinite(hdiag[q])) {
+            free(P);
+            return fail("the Hessian diagonal must be positive and finite");
+        }
+        P[q] = 1.0 / hdiag[q];
+    }
+    orc_ls ls = {0, c_ls, rho_ls, min_alpha, 0.0, 0, 0, 0.0};
+    long nfb = 0;
+    double st[6];
+    int r = lbfgs_core(s, m, e_tol, max_dx, f_tol, &ls, nsteps, st, P, &nfb);
+    free(P);
+    if (stats && r == 0) {
+        for (int k = 0; k < 6; k++) stats[k] = st[k];
+        stats[6] = (double)nfb;
+    }
+    return r;
+}
+
+static int lbfgs_core(orc_sys* s, int m, double e_tol, double max_dx, double f_tol, const orc_ls* ls, int nsteps,
+                      double* stats, const double* P, long* n_fallback) {
     int n3 = 3 * s->natms;
     if (orc_sys_init_dynamic(s)) return -1;
     double* f0 = (double*)malloc(sizeof(double) * n3);
@@ -1940,7 +1984,7 @@ int orc_lbfgs_run_ls(void* p, int m, double e_tol, double max_dx, double f_tol, 
     double* alpha = (double*)calloc(m ? m : 1, sizeof(double));
     long n_en = 0, n_fc = 1;
     force_calc(s);
-    double e_prev, e_curr = s->pe, alpha_m = 0.0, gamma = 1.0;
+    double e_prev, e_curr = s->pe, alpha_m = 0.0, gamma = 1.0, tau = 1.0;
     int k = 0;
     int err = nsteps == 0 ? MIN_F_MAX_ITER : LS_S;
     if (err == LS_S && f_tol > 0.0 && max_abs_f(s) < f_tol) err = MIN_S_FTOL;
@@ -1949,15 +1993,24 @@ int orc_lbfgs_run_ls(void* p, int m, double e_tol, double max_dx, double f_tol, 
     for (; err == LS_S; istep++) {
         memcpy(x0, s->x, sizeof(double) * n3);
         memcpy(f0, s->f, sizeof(double) * n3);
-        memcpy(h, s->f, sizeof(double) * n3);
-        for (int i = 0; i < k; i++) {
-            alpha[i] = -rho[i] * vdot(sv[i], h, n3);
-            for (int q = 0; q < n3; q++) h[q] += alpha[i] * yv[i][q];
-        }
-        for (int q = 0; q < n3; q++) h[q] *= gamma;
-        for (int i = k - 1; i > -1; i--) {
-            double scl0 = -alpha[i] - rho[i] * vdot(yv[i], h, n3);
-            for (int q = 0; q < n3; q++) h[q] += scl0 * sv[i][q];
+        /* the two-loop recursion, min_l-bfgs.h:148-170; a diagonal P
+           replaces gamma*I by tau*diag(P) */
+        for (int pass = P ? 0 : 1; pass < 2; pass++) {
+            memcpy(h, s->f, sizeof(double) * n3);
+            for (int i = 0; i < k; i++) {
+                alpha[i] = -rho[i] * vdot(sv[i], h, n3);
+                for (int q = 0; q < n3; q++) h[q] += alpha[i] * yv[i][q];
+            }
+            if (pass == 0)
+                for (int q = 0; q < n3; q++) h[q] *= tau * P[q];
+            else
+                for (int q = 0; q < n3; q++) h[q] *= gamma;
+            for (int i = k - 1; i > -1; i--) {
+                double scl0 = -alpha[i] - rho[i] * vdot(yv[i], h, n3);
+                for (int q = 0; q < n3; q++) h[q] += scl0 * sv[i][q];
+            }
+            if (pass == 1 || vdot(s->f, h, n3) >= 0.0) break;
+            if (n_fallback) (*n_fallback)++; /* not a descent direction: gamma instead */
         }
         e_prev = e_curr;
         double f_h = vdot(s->f, h, n3);
@@ -2019,8 +2072,18 @@ int orc_lbfgs_run_ls(void* p, int m, double e_tol, double max_dx, double f_tol, 
             }
             double inner0 = vdot(sv[0], yv[0], n3);
             double inner1 = vdot(yv[0], yv[0], n3);
-            gamma = inner0 / inner1;
-            rho[0] = 1.0 / inner0;
+            if (!P) {
+                gamma = inner0 / inner1;
+                rho[0] = 1.0 / inner0;
+            } else if (inner0 > 0.0 && inner1 > 0.0) {
+                double inner2 = 0.0;
+                for (int q = 0; q < n3; q++) inner2 += yv[0][q] * yv[0][q] * P[q];
+                gamma = inner0 / inner1;
+                rho[0] = 1.0 / inner0;
+                if (inner2 > 0.0) tau = inner0 / inner2;
+            } else {
+                rho[0] = 0.0;
+            }
         } else {
             gamma = alpha_m * (vdot(h, f0, n3) - vdot(h, s->f, n3)) /
                     (vdot(s->f, s->f, n3) + vdot(f0, f0, n3) - 2.0 * vdot(s->f, f0, n3));

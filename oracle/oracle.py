@@ -68,6 +68,8 @@ def lib():
         L.orc_lbfgs_run_ls.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
                                        C.POINTER(OrcLs), C.c_int, _D]
         L.orc_cg_run_ls.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(OrcLs), C.c_int, _D]
+        L.orc_lbfgs_run_diag.argtypes = [C.c_void_p, _D, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_int, _D]
         L.orc_min_box_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int),
                                       C.c_int, C.POINTER(OrcLs), C.c_int, _D]
         L.orc_sys_get_box.argtypes = [C.c_void_p, _D]
@@ -263,6 +265,19 @@ class System:
         self.initialized = True
         return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
                 "n_energy": int(st[4]), "n_force": int(st[5])}
+
+    def lbfgs_run_diag(self, hdiag, m=10, e_tol=0.0, max_dx=1.0, f_tol=1e-4, c=0.4, rho=0.5, min_alpha=0.0,
+                       nsteps=10000):
+        """L-BFGS with H0 = tau diag(1/hdiag) (hdiag: (n, 3) Hessian diagonal),
+        as the library's mappg_lbfgs_run_diag."""
+        hd = np.ascontiguousarray(hdiag, dtype=np.float64).reshape(-1, 3)
+        st = np.zeros(7)
+        r = lib().orc_lbfgs_run_diag(self.h, _dp(hd), m, e_tol, max_dx, f_tol, c, rho, min_alpha, nsteps, _dp(st))
+        if r != 0:
+            raise RuntimeError("oracle: " + _err())
+        self.initialized = True
+        return {"niter": int(st[0]), "pe": st[1], "fmax": st[2], "err": int(st[3]),
+                "n_energy": int(st[4]), "n_force": int(st[5]), "fallbacks": int(st[6])}
 
     def min_box_run(self, ls, H_dof, affine=False, method="lbfgs", m=10, e_tol=0.0, max_dx=1.0, nsteps=10000):
         """L-BFGS or CG with box degrees of freedom (H_dof: 3x3 mask, lower

@@ -110,3 +110,30 @@ def test_lbfgs_with_a_callers_hessian_diagonal(ff):
     bad[3, 1] = 0.0
     with pytest.raises(_lib.MappgError, match="positive"):
         _lib.lbfgs_run_diag(s, bad)
+
+
+@pytest.mark.parametrize("diag", ["mild", "wide"])
+def test_diagonal_lbfgs_follows_oracle(ff, potentials, diag):
+    """mappg_lbfgs_run_diag against the oracle's restatement of the same
+    recursion (H0 = tau diag(1/h), tau = s.y / y.P.y of the newest pair): in
+    FP64, over five iterations and over a full relaxation, the same
+    iterations, energy and force calls, energies and relaxed positions.  The
+    diagonals are synthetic: a mild one (3-9) and one spread over two
+    decades (e^-2 - e^2); this cell's relaxation under either does not move
+    when its start moves by 1e-11 A."""
+    path = potentials[("A", "B")][0]
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+    k = np.arange(3 * c.natoms)
+    hd = (6.0 + 3.0 * np.cos(0.7 * k) if diag == "mild" else np.exp(2.0 * np.sin(1.3 * k))).reshape(-1, 3)
+    for nsteps in (5, 5000):
+        o = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses, skin=0.5)
+        ro = o.lbfgs_run_diag(hd, m=10, e_tol=0.0, f_tol=1e-4, nsteps=nsteps)
+        s = _lib.System(ff, c.H, c.x, c.elem, c.masses, skin=0.5, precision=_lib.FP64)
+        r = _lib.lbfgs_run_diag(s, hd, m=10, e_tol=0.0, f_tol=1e-4, nsteps=nsteps)
+        for key in ("niter", "err", "n_energy", "n_force", "fallbacks"):
+            assert r[key] == ro[key], (nsteps, key, r, ro)
+        assert abs(r["pe"] - ro["pe"]) <= 1e-11 * abs(ro["pe"])
+        d = s.get_x() - o.x
+        d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
+        assert np.max(np.abs(d)) < 1e-8
+    assert ro["err"] == 100

@@ -138,6 +138,25 @@ def test_lbfgs_reaches_force_tolerance(potentials):
     assert r["pe"] == float(g["pe"]) and r["niter"] == int(g["niter"])
 
 
+def test_lbfgs_with_a_unit_diagonal_is_plain_lbfgs(potentials):
+    """The diagonal-H0 restatement (the library's mappg_lbfgs_run_diag): a unit
+    Hessian diagonal makes tau*diag(1/h) equal gamma*I, so the run retraces
+    plain L-BFGS step for step; a diagonal that is not positive is refused."""
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+    path = potentials[("A", "B")][0]
+    a = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses)
+    b = O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses)
+    r0 = a.lbfgs_run(m=10, e_tol=0.0, f_tol=1e-4, nsteps=400)
+    r1 = b.lbfgs_run_diag(np.ones((c.natoms, 3)), m=10, e_tol=0.0, f_tol=1e-4, nsteps=400)
+    keys = ("niter", "err", "n_energy", "n_force", "pe")
+    assert [r1[k] for k in keys] == [r0[k] for k in keys]
+    assert r1["fallbacks"] == 0 and np.array_equal(a.x, b.x)
+    bad = np.ones((c.natoms, 3))
+    bad[3, 1] = 0.0
+    with pytest.raises(RuntimeError, match="positive"):
+        O.System(O.Eam.setfl(path), c.H, c.x, c.elem, c.masses).lbfgs_run_diag(bad)
+
+
 def test_cg_reaches_force_tolerance(potentials):
     path, _ = potentials[("A", "B")]
     c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
