@@ -73,3 +73,43 @@ def loss_grad(w, X, T):
     g2 = dz2.T @ H1.astype(np.float64)
     g1 = dz1.T @ X.astype(np.float64)
     return loss, np.concatenate([g1.ravel(), g2.ravel(), g3.ravel()])
+
+
+# the network's per-atom inputs (k_descriptors)
+DESC_R, DESC_RC, DESC_W = 16, 5.5, 0.3
+DESC_CENTRES = 2.0 + 3.5 * np.arange(DESC_R) / 15.0
+
+
+def descriptors(H, x, elem, rho):
+    """Per-atom inputs as k_descriptors forms them, in FP64: 16 Gaussian
+    radial functions (centres 2.0-5.5 A in 15 equal steps, width 0.3 A)
+    times the cosine cutoff 0.5 (1 + cos(pi r / 5.5)), summed over the
+    neighbours of element 0 (columns 0-15) and of element 1 (columns 16-31)
+    within 5.5 A, every periodic image counted; column 32 is the host
+    density rho (passed in: the oracle's per-atom EAM density).  H: rows are
+    the cell vectors.  Brute force over images: for test-sized cells."""
+    H = np.asarray(H, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    elem = np.asarray(elem)
+    n = len(x)
+    # image range per cell vector: the spacing of its lattice planes
+    vol = abs(np.linalg.det(H))
+    reach = []
+    for k in range(3):
+        a, b = H[(k + 1) % 3], H[(k + 2) % 3]
+        reach.append(int(np.ceil(DESC_RC / (vol / np.linalg.norm(np.cross(a, b))))) + 1)
+    shifts = np.array([(i, j, k) for i in range(-reach[0], reach[0] + 1) for j in range(-reach[1], reach[1] + 1)
+                       for k in range(-reach[2], reach[2] + 1)], dtype=np.float64) @ H
+    out = np.zeros((n, 2 * DESC_R + 1))
+    for i in range(n):
+        d = x[i][None, None, :] - (x[None, :, :] + shifts[:, None, :])  # [shift][j][3]
+        r = np.sqrt(np.sum(d * d, axis=2))
+        keep = (r < DESC_RC) & (r > 0.0)
+        sh, j = np.nonzero(keep)
+        rr = r[sh, j]
+        fc = 0.5 * (1.0 + np.cos(np.pi * rr / DESC_RC))
+        g = np.exp(-(rr[:, None] - DESC_CENTRES[None, :]) ** 2 / (2.0 * DESC_W * DESC_W)) * fc[:, None]
+        for e in (0, 1):
+            out[i, e * DESC_R:(e + 1) * DESC_R] = g[elem[j] == e].sum(axis=0)
+    out[:, 2 * DESC_R] = rho
+    return out

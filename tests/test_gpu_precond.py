@@ -137,3 +137,25 @@ def test_diagonal_lbfgs_follows_oracle(ff, potentials, diag):
         d -= np.round(d @ np.linalg.inv(c.H)) @ c.H
         assert np.max(np.abs(d)) < 1e-8
     assert ro["err"] == 100
+
+
+@pytest.mark.parametrize("cells", [(4, 4, 4), (2, 2, 5)])
+def test_descriptors_match_restatement(ff, potentials, cells):
+    """k_descriptors (mappg_sys_descriptors), the network's inputs, against
+    the numpy restatement (mlp_ref.descriptors): the 32 radial functions
+    within FP32 rounding, the host density to the oracle's FP64 density.  The
+    (2, 2, 5) cell is thinner than twice the 5.5 A range, so an atom sees
+    several images of one neighbour."""
+    rng = np.random.default_rng(4)
+    H, x, elem, _ = precond.alloy_cell(cells, rng, 0.5, 0.0, 0.1)
+    masses = [synth.MASS, synth.MASS]
+    s = _lib.System(ff, H, x, elem, masses)
+    s.build()
+    feat = _lib.descriptors(s)
+    o = O.System(O.Eam.setfl(potentials[("A", "B")][0]), H, x, elem, masses)
+    o.force()
+    rho, _ = o.rho_dF()
+    ref = R.descriptors(H, x, elem, rho)
+    scale = max(1.0, np.max(np.abs(ref[:, :32])))
+    assert np.max(np.abs(feat[:, :32] - ref[:, :32])) <= 1e-5 * scale
+    assert np.max(np.abs(feat[:, 32] - ref[:, 32])) <= 1e-6 * np.max(ref[:, 32])

@@ -9,6 +9,7 @@ import os
 import numpy as np
 import pytest
 
+import mlp_ref as R
 import oracle as O
 from conftest import REF_ROOT, golden, golden_potential
 from mapp4py_gb300 import synth
@@ -359,3 +360,19 @@ def test_x_dof_with_nst(potentials):
     t.v = c.v
     with pytest.raises(RuntimeError, match="degree freedom"):
         t.nst_run(S, 300.0, synth.FS, synth.KB, 1)
+
+
+def test_descriptor_restatement_on_a_perfect_lattice():
+    """The network inputs' restatement (mlp_ref.descriptors) on a perfect
+    single-element FCC crystal: every atom's 16 radial functions equal the
+    shell sum of the four neighbour shells inside 5.5 A (12 at a/sqrt2, 6 at
+    a, 24 at a sqrt(3/2), 12 at a sqrt2); no element-1 neighbours."""
+    a = 3.615
+    H, x = synth.fcc((3, 3, 3), a=a)
+    f = R.descriptors(H, x, np.zeros(len(x), np.uint8), np.full(len(x), 7.0))
+    want = np.zeros(16)
+    for count, r in ((12, a / np.sqrt(2.0)), (6, a), (24, a * np.sqrt(1.5)), (12, a * np.sqrt(2.0))):
+        fc = 0.5 * (1.0 + np.cos(np.pi * r / 5.5))
+        want += count * np.exp(-((r - R.DESC_CENTRES) ** 2) / (2.0 * 0.3 ** 2)) * fc
+    assert np.max(np.abs(f[:, :16] - want)) < 1e-12
+    assert np.all(f[:, 16:32] == 0.0) and np.all(f[:, 32] == 7.0)
