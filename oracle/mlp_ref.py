@@ -1,8 +1,9 @@
 """CPU restatement of the preconditioner network's forward pass, loss and
 gradient, with the BF16 roundings of the tensor-core kernels (inputs,
 weights, hidden activations and backpropagated errors rounded to BF16;
-products accumulated in FP32 or wider).  TEST INFRASTRUCTURE ONLY: the
-checker of mappg_mlp_grad / mappg_mlp_predict.
+products accumulated in FP32 or wider), and of its per-atom inputs
+(descriptors).  TEST INFRASTRUCTURE ONLY: the checker of mappg_mlp_grad,
+mappg_mlp_predict and mappg_sys_descriptors.
 
 Layout of the parameter vector (10496 floats): W1 [64][64] | W2 [64][80] |
 W3 [16][80], row-major [unit][input]; input 33 of W1 and input 64 of W2, W3
