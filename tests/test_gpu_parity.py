@@ -306,3 +306,36 @@ def test_autotune_keeps_the_forces(potentials, precision):
     tol = 1e-10 if precision == _lib.FP64 else 1e-5
     assert np.max(np.abs(f1 - f0)) <= tol * max(1.0, np.max(np.abs(f0)))
     assert abs(pe1 - pe0) <= (1e-12 if precision == _lib.FP64 else 1e-7) * abs(pe0)
+
+
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+def test_set_box_then_forces_match_oracle(potentials, precision):
+    """mappg_sys_set_box: the same system carried through three boxes (a
+    small strain, a tilt, and a 25 % expansion that changes the number of
+    bins), with the atoms mapped affinely each time.  Forces, energy and
+    virial match the oracle built in that box (FP64 to the parity bars,
+    mixed within its error budget).  A batch's boxes are fixed."""
+    path, _ = potentials[("A", "B")]
+    c = synth.alloy((6, 6, 6), xB=0.4, sigma=0.05, seed=9)
+    s = make(path, dict(H=c.H, x=c.x, elem=c.elem, masses=c.masses), precision=precision)
+    s.force()  # a list in the first box
+    tilt = c.H.copy()
+    tilt[1, 0] += 0.3 * c.H[1, 1]
+    tilt[2, 1] -= 0.2 * c.H[2, 2]
+    for H1 in (c.H @ np.diag([1.02, 0.99, 1.0]), tilt, 1.25 * c.H):
+        x1 = c.x @ np.linalg.inv(c.H) @ H1
+        s.set_box(H1)
+        s.set_x(x1)
+        pe, vir = s.force()
+        o = O.System(O.Eam.setfl(path), H1, x1, c.elem, c.masses, skin=0.5)
+        pe_o, vir_o = o.force()
+        f = s.get_f()
+        if precision == _lib.FP64:
+            assert abs(pe - pe_o) <= 1e-12 * abs(pe_o)
+            assert np.max(np.abs(vir - vir_o)) <= 1e-11 * np.max(np.abs(vir_o))
+            assert_forces(f, o.f)
+        else:
+            assert np.sqrt(np.mean(np.sum((f - o.f) ** 2, axis=1))) <= 1e-5
+            assert abs(pe - pe_o) / c.natoms <= 1e-7
+    b = _lib.Batch(_lib.ForceField.setfl(path), [(c.H, c.x, c.elem)] * 2, c.masses)
+    assert _lib.load().mappg_sys_set_box(b.h, _lib.dptr(np.ascontiguousarray(c.H))) == -8  # MAPPG_ERR_UNSUPP

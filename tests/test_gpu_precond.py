@@ -159,3 +159,34 @@ def test_descriptors_match_restatement(ff, potentials, cells):
     scale = max(1.0, np.max(np.abs(ref[:, :32])))
     assert np.max(np.abs(feat[:, :32] - ref[:, :32])) <= 1e-5 * scale
     assert np.max(np.abs(feat[:, 32] - ref[:, 32])) <= 1e-6 * np.max(ref[:, 32])
+
+
+def test_refresh_of_the_learned_diagonal(ff):
+    """mappg_mlp_set_refresh: a refresh period longer than the run leaves the
+    run exactly as without refresh; a period of five iterations recomputes
+    the diagonal from the moved atoms, takes another path and still
+    converges; a negative period is refused.  The network is untrained
+    (seeded weights, inputs standardised on this cell): the refresh
+    mechanics do not depend on what it predicts."""
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=2, vac=0.01)
+    s = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.FP64)
+    s.build()
+    feat = _lib.descriptors(s)
+    net = _lib.Mlp(seed=3)
+    w, _, _ = net.params()
+    net.set_params(w, feat.mean(axis=0), feat.std(axis=0) + 1e-3)
+
+    def run(every):
+        net.set_refresh(every)
+        q = _lib.System(ff, c.H, c.x, c.elem, c.masses, precision=_lib.FP64)
+        r = _lib.lbfgs_run_precond(q, net, m=10, f_tol=1e-4, nsteps=5000)
+        return r, q.get_x()
+
+    r0, x0 = run(0)
+    rl, xl = run(100000)
+    r5, x5 = run(5)
+    assert r0["err"] == 100 and r5["err"] == 100
+    assert rl == r0 and np.array_equal(xl, x0)
+    assert (r5["niter"], r5["n_energy"], r5["pe"]) != (r0["niter"], r0["n_energy"], r0["pe"])
+    with pytest.raises(_lib.MappgError):
+        net.set_refresh(-1)
