@@ -188,6 +188,26 @@ class RefSystem:
         mn.run(self.sim, nsteps)
         return self.state()
 
+    def minimize(self, method, nsteps, ls="bt", m=10, e_tol=0.0, max_dx=1.0, bracket=True):
+        """md.min_lbfgs(m, e_tol, max_dx) or md.min_cg_new(e_tol, max_dx)
+        (MinCG, min_cg.h:454-536) with mapp4py.ls_bt(), ls_golden() or
+        ls_brent() at their defaults (bracket set as given): nsteps
+        iterations."""
+        M = module()
+        if method == "lbfgs":
+            mn = M.md.min_lbfgs(m=m, e_tol=e_tol, max_dx=max_dx)
+        elif method == "cg":
+            mn = M.md.min_cg_new(e_tol=e_tol, max_dx=max_dx)
+        else:
+            raise ValueError(method)
+        search = {"bt": M.ls_bt, "golden": M.ls_golden, "brent": M.ls_brent}[ls]()
+        if ls != "bt":
+            search.bracket = bool(bracket)
+        mn.ls = search
+        mn.ntally = 0
+        mn.run(self.sim, nsteps)
+        return self.state()
+
     def create_temp(self, T, seed):
         """atoms.create_temp(T, seed): the velocities it draws, caller order."""
         self.sim.create_temp(T, seed)

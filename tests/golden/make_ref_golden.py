@@ -13,6 +13,9 @@ Fixtures:
   ref_synth.npz      the analytic-potential cases of make_golden.py (forces,
                      energy, stress), the 256-atom NVT run's end state, the
                      first L-BFGS iterates of two cells, create_temp draws
+  ref_min.npz        iterates of md.min_cg_new (back-tracking) and of
+                     md.min_lbfgs / md.min_cg_new with ls_golden and ls_brent
+                     on a 256-atom alloy cell
   ref_extrap.npz     an FCC cell whose host densities exceed rho_max
                      (linear extrapolation of F, ff_eam.cpp:188-189)
   ref_pot_<name>.npz the knot values of a potential file shipped with the
@@ -129,6 +132,33 @@ def synth_cases(tmp):
     return out
 
 
+def minimizer_cases(tmp):
+    """Iterates of md.min_cg_new with back-tracking and of md.min_lbfgs and
+    md.min_cg_new with the golden-section and Brent line searches (bracketing
+    on and off), on the 256-atom alloy cell of the L-BFGS case."""
+    out = {}
+    path, digest = make_golden.potential(tmp, ("A", "B"))
+    cell = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, seed=51)
+    runs = {
+        "cg_bt": ("cg", "bt", True, (1, 5, 20)),
+        "lbfgs_golden": ("lbfgs", "golden", True, (1, 5)),
+        "lbfgs_brent": ("lbfgs", "brent", True, (1, 5)),
+        "cg_golden": ("cg", "golden", True, (1, 5)),
+        "cg_brent_nobracket": ("cg", "brent", False, (1, 3)),
+    }
+    for name, (method, ls, bracket, iters) in runs.items():
+        for it in iters:
+            r = refmod.RefSystem(cell.H, cell.x, cell.elem, cell.masses, ["A", "B"], path)
+            H, x, v = r.minimize(method, it, ls=ls, m=10, e_tol=0.0, bracket=bracket)
+            out["%s/x_%d" % (name, it)] = x
+            out["%s/pe_%d" % (name, it)] = r.force()[0]
+        out[name + "/iters"] = np.array(iters)
+        out[name + "/spec"] = np.array([method, ls, str(bool(bracket))])
+        print(name, [out["%s/pe_%d" % (name, it)] for it in iters])
+    out.update({"H": cell.H, "x": cell.x, "elem": cell.elem, "masses": cell.masses, "sha256_AB": np.array(digest)})
+    return out
+
+
 def extrap_case(tmp):
     path = os.path.join(tmp, "A_extrap.setfl")
     synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
@@ -187,6 +217,7 @@ def main():
     with tempfile.TemporaryDirectory() as tmp:
         np.savez_compressed(os.path.join(HERE, "ref_synth.npz"), **synth_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_extrap.npz"), **extrap_case(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_min.npz"), **minimizer_cases(tmp))
         for name in POTENTIALS:
             np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
 

@@ -6,7 +6,9 @@ from its own sources (oracle/ref.mk) and driven through its Python API
 ForceFieldMD::force_calc on the analytic potential and on the four
 potential files shipped with the reference's examples (setfl with one and
 two elements, per-pair cutoffs, Finnis-Sinclair), host densities beyond
-rho_max, md.nvt trajectories, md.min_lbfgs iterates and create_temp draws.
+rho_max, md.nvt trajectories, md.min_lbfgs and md.min_cg_new iterates (with
+the back-tracking, golden-section and Brent line searches) and create_temp
+draws.
 The oracle must reproduce them to rounding.  Where the compiled reference
 module is present (oracle/_ref), further seeded cases run live against it.
 """
@@ -112,6 +114,41 @@ def test_oracle_lbfgs_iterates_match_reference(potentials, ref, name):
         tol = 1e-12 if r["niter"] == it else 1e-6
         assert np.max(np.abs(d)) <= tol, (it, np.max(np.abs(d)))
         assert abs(r["pe"] - ref["%s/pe_%d" % (name, it)]) <= 1e-12 * abs(r["pe"])
+
+
+@pytest.mark.parametrize("name", ["cg_bt", "lbfgs_golden", "lbfgs_brent", "cg_golden", "cg_brent_nobracket"])
+def test_oracle_minimizer_iterates_match_reference(potentials, name):
+    """md.min_cg_new (MinCG) with ls_bt, and md.min_lbfgs / md.min_cg_new
+    with ls_golden and ls_brent (bracketing on and off), e_tol = 0:
+    positions and energy after k iterations of each.  Back-tracking follows
+    the reference to rounding.  Golden section and Brent refine the step
+    until the bracket is tol |alpha| wide (tol = sqrt(2 eps)), where the
+    energies they compare differ by less than their rounding; the oracle's
+    energies agree with the reference's to ~1e-14, so it may settle
+    elsewhere inside that last bracket (at most tol * max_dx = 2e-8 A after
+    one step), and L-BFGS carries the difference on.  Measured: golden 1e-11
+    A after five iterations, Brent 2e-9 A after one and 2e-7 A after five;
+    the energies stay within 1e-12."""
+    tol_x = {"bt": 1e-11, "golden": 1e-9, "brent": 1e-6}
+    g = golden("ref_min")
+    path, digest = potentials[("A", "B")]
+    assert str(g["sha256_AB"]) == digest
+    e = O.Eam.setfl(path)
+    H = g["H"]
+    method, ls, bracket = (str(v) for v in g[name + "/spec"])
+    search = O.line_search(ls, bracket=bracket == "True")
+    for it in g[name + "/iters"]:
+        s = O.System(e, H, g["x"], g["elem"], g["masses"])
+        if method == "lbfgs":
+            r = s.lbfgs_run_ls(search, m=10, e_tol=0.0, f_tol=0.0, nsteps=int(it))
+        else:
+            r = s.cg_run_ls(search, e_tol=0.0, f_tol=0.0, nsteps=int(it))
+        d = s.x - g["%s/x_%d" % (name, it)]
+        ds = d @ np.linalg.inv(H)
+        d = (ds - np.round(ds)) @ H  # the reference leaves x unwrapped
+        assert r["niter"] == it
+        assert np.max(np.abs(d)) <= tol_x[ls], (it, np.max(np.abs(d)))
+        assert abs(r["pe"] - g["%s/pe_%d" % (name, it)]) <= 1e-12 * abs(r["pe"])
 
 
 def test_create_temp_matches_reference(ref):
