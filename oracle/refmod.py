@@ -188,7 +188,21 @@ class RefSystem:
         mn.run(self.sim, nsteps)
         return self.state()
 
-    def minimize(self, method, nsteps, ls="bt", m=10, e_tol=0.0, max_dx=1.0, bracket=True):
+    def nst(self, S, T, dt, nsteps, L=3, niters=1):
+        """md.nst(S, T, dt).run(atoms, nsteps) (MDNST::run) as a user calls
+        it; S: 3x3 with NaN where the box entry has no degree of freedom
+        (passed to the reference in its triangular form, None for NaN)."""
+        S = np.asarray(S, dtype=np.float64).reshape(3, 3)
+        tri = [[None if np.isnan(S[i][j]) else float(S[i][j]) for j in range(i + 1)] for i in range(3)]
+        nst = module().md.nst(tri, T, dt)
+        nst.L = L
+        nst.niters = niters
+        nst.ntally = 0
+        nst.run(self.sim, nsteps)
+        return self.state()
+
+    def minimize(self, method, nsteps, ls="bt", m=10, e_tol=0.0, max_dx=1.0, bracket=True, H_dof=None,
+                 affine=False):
         """md.min_lbfgs(m, e_tol, max_dx) or md.min_cg_new(e_tol, max_dx)
         (MinCG, min_cg.h:454-536) with mapp4py.ls_bt(), ls_golden() or
         ls_brent() at their defaults (bracket set as given): nsteps
@@ -200,6 +214,9 @@ class RefSystem:
             mn = M.md.min_cg_new(e_tol=e_tol, max_dx=max_dx)
         else:
             raise ValueError(method)
+        if H_dof is not None:
+            mn.H_dof = [[bool(H_dof[i][j]) for j in range(3)] for i in range(3)]
+            mn.affine = bool(affine)
         search = {"bt": M.ls_bt, "golden": M.ls_golden, "brent": M.ls_brent}[ls]()
         if ls != "bt":
             search.bracket = bool(bracket)

@@ -16,6 +16,9 @@ Fixtures:
   ref_min.npz        iterates of md.min_cg_new (back-tracking) and of
                      md.min_lbfgs / md.min_cg_new with ls_golden and ls_brent
                      on a 256-atom alloy cell
+  ref_box.npz        md.nst states of an expanded alloy cell at zero stress,
+                     and md.min_lbfgs / md.min_cg_new iterates with box
+                     degrees of freedom (H_dof), atoms free or affine
   ref_extrap.npz     an FCC cell whose host densities exceed rho_max
                      (linear extrapolation of F, ff_eam.cpp:188-189)
   ref_pot_<name>.npz the knot values of a potential file shipped with the
@@ -159,6 +162,36 @@ def minimizer_cases(tmp):
     return out
 
 
+def box_cases(tmp):
+    """md.nst (MDNST::run) at zero stress on the diagonal from an expanded
+    256-atom alloy at 300 K, states after 5 and 30 steps; md.min_lbfgs and
+    md.min_cg_new with box degrees of freedom (H_dof on the diagonal, atoms
+    free or affine), states after a few iterations."""
+    out = {}
+    path, digest = make_golden.potential(tmp, ("A", "B"))
+    c = synth.alloy((4, 4, 4), a=3.7, xB=0.3, sigma=0.02, T=300.0, seed=4)
+    nan = float("nan")
+    S = np.array([[0.0, nan, nan], [nan, 0.0, nan], [nan, nan, 0.0]])
+    for it in (5, 30):
+        r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A", "B"], path, v=c.v, kB=synth.KB)
+        H, x, v = r.nst(S, 300.0, synth.FS, it)
+        out.update({"nst/H_%d" % it: H, "nst/x_%d" % it: x, "nst/v_%d" % it: v})
+        print("nst", it, np.diag(H))
+    out.update({"nst/iters": np.array([5, 30]), "nst/S": S, "nst/v": c.v})
+    H_dof = np.eye(3, dtype=bool)
+    runs = {"box_lbfgs": ("lbfgs", False, (1, 5, 20)), "box_cg_affine": ("cg", True, (1, 5))}
+    for name, (method, affine, iters) in runs.items():
+        for it in iters:
+            r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A", "B"], path)
+            H, x, _ = r.minimize(method, it, ls="bt", m=10, e_tol=0.0, H_dof=H_dof, affine=affine)
+            out.update({"%s/H_%d" % (name, it): H, "%s/x_%d" % (name, it): x, "%s/pe_%d" % (name, it): r.force()[0]})
+        out[name + "/iters"] = np.array(iters)
+        out[name + "/spec"] = np.array([method, str(affine)])
+        print(name, [out["%s/pe_%d" % (name, it)] for it in iters])
+    out.update({"H": c.H, "x": c.x, "elem": c.elem, "masses": c.masses, "sha256_AB": np.array(digest)})
+    return out
+
+
 def extrap_case(tmp):
     path = os.path.join(tmp, "A_extrap.setfl")
     synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
@@ -218,6 +251,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_synth.npz"), **synth_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_extrap.npz"), **extrap_case(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_min.npz"), **minimizer_cases(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_box.npz"), **box_cases(tmp))
         for name in POTENTIALS:
             np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
 

@@ -6,9 +6,9 @@ from its own sources (oracle/ref.mk) and driven through its Python API
 ForceFieldMD::force_calc on the analytic potential and on the four
 potential files shipped with the reference's examples (setfl with one and
 two elements, per-pair cutoffs, Finnis-Sinclair), host densities beyond
-rho_max, md.nvt trajectories, md.min_lbfgs and md.min_cg_new iterates (with
-the back-tracking, golden-section and Brent line searches) and create_temp
-draws.
+rho_max, md.nvt trajectories, md.nst states, md.min_lbfgs and md.min_cg_new
+iterates (with the back-tracking, golden-section and Brent line searches, and
+with box degrees of freedom) and create_temp draws.
 The oracle must reproduce them to rounding.  Where the compiled reference
 module is present (oracle/_ref), further seeded cases run live against it.
 """
@@ -148,6 +148,56 @@ def test_oracle_minimizer_iterates_match_reference(potentials, name):
         d = (ds - np.round(ds)) @ H  # the reference leaves x unwrapped
         assert r["niter"] == it
         assert np.max(np.abs(d)) <= tol_x[ls], (it, np.max(np.abs(d)))
+        assert abs(r["pe"] - g["%s/pe_%d" % (name, it)]) <= 1e-12 * abs(r["pe"])
+
+
+def _wrapped(d, H):
+    ds = d @ np.linalg.inv(H)
+    return (ds - np.round(ds)) @ H
+
+
+def test_oracle_nst_matches_reference(potentials):
+    """md.nst (MDNST::run) at zero stress on the diagonal, from an expanded
+    alloy cell at 300 K: after 5 and 30 steps the box and the velocities
+    follow the reference to rounding, and the positions up to one rigid
+    translation.  The translation comes from the mean displacement that each
+    step removes (md_nst.cpp:120-127): it includes the affine part x.V_H,
+    which depends on the periodic image an atom is stored as, and the
+    reference re-wraps atoms only at its skin-triggered rebuilds while the
+    oracle (and libmappg) rebuild, and so wrap, at every step.  Forces and
+    the dynamics do not depend on it."""
+    g = golden("ref_box")
+    path, digest = potentials[("A", "B")]
+    assert str(g["sha256_AB"]) == digest
+    e = O.Eam.setfl(path)
+    for it in g["nst/iters"]:
+        o = O.System(e, g["H"], g["x"], g["elem"], g["masses"], skin=0.5)
+        o.v = g["nst/v"]
+        o.nst_run(g["nst/S"], 300.0, synth.FS, synth.KB, int(it))
+        H = o.box()
+        assert np.max(np.abs(H - g["nst/H_%d" % it])) <= 1e-12 * np.max(np.abs(H))
+        assert np.max(np.abs(o.v - g["nst/v_%d" % it])) <= 1e-12 * np.max(np.abs(o.v))
+        d = _wrapped(o.x - g["nst/x_%d" % it], H)
+        assert np.max(np.abs(d - d.mean(axis=0))) <= 1e-11
+
+
+@pytest.mark.parametrize("name", ["box_lbfgs", "box_cg_affine"])
+def test_oracle_box_minimizers_match_reference(potentials, name):
+    """md.min_lbfgs and md.min_cg_new with H_dof on the diagonal (atoms free,
+    or affine), ls_bt, e_tol = 0: box, positions and energy after k
+    iterations."""
+    g = golden("ref_box")
+    path, _ = potentials[("A", "B")]
+    e = O.Eam.setfl(path)
+    method, affine = (str(v) for v in g[name + "/spec"])
+    for it in g[name + "/iters"]:
+        o = O.System(e, g["H"], g["x"], g["elem"], g["masses"], skin=0.5)
+        r = o.min_box_run(O.line_search("bt"), np.eye(3, dtype=bool), affine == "True", method, m=10, e_tol=0.0,
+                          nsteps=int(it))
+        H = o.box()
+        assert r["niter"] == it
+        assert np.max(np.abs(H - g["%s/H_%d" % (name, it)])) <= 1e-10
+        assert np.max(np.abs(_wrapped(o.x - g["%s/x_%d" % (name, it)], H))) <= 1e-10
         assert abs(r["pe"] - g["%s/pe_%d" % (name, it)]) <= 1e-12 * abs(r["pe"])
 
 
