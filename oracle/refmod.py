@@ -188,6 +188,17 @@ class RefSystem:
         mn.run(self.sim, nsteps)
         return self.state()
 
+    def set_dof(self, dof):
+        """atoms.x_dof through atoms.do, as the reference's examples set it:
+        dof (n, 3) bool in caller order, True where the component is free."""
+        dof = np.asarray(dof, dtype=bool).reshape(-1, 3)
+        by_id = dof[self.order]  # ids follow the CFG rows
+
+        def put(id, x_dof):
+            x_dof[:] = by_id[int(id[0])]
+
+        self.sim.do(put)
+
     def nst(self, S, T, dt, nsteps, L=3, niters=1):
         """md.nst(S, T, dt).run(atoms, nsteps) (MDNST::run) as a user calls
         it; S: 3x3 with NaN where the box entry has no degree of freedom

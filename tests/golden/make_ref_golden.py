@@ -19,6 +19,8 @@ Fixtures:
   ref_box.npz        md.nst states of an expanded alloy cell at zero stress,
                      and md.min_lbfgs / md.min_cg_new iterates with box
                      degrees of freedom (H_dof), atoms free or affine
+  ref_dof.npz        md.nvt and md.min_lbfgs with frozen components
+                     (atoms.x_dof)
   ref_extrap.npz     an FCC cell whose host densities exceed rho_max
                      (linear extrapolation of F, ff_eam.cpp:188-189)
   ref_pot_<name>.npz the knot values of a potential file shipped with the
@@ -192,6 +194,37 @@ def box_cases(tmp):
     return out
 
 
+def dof_cases(tmp):
+    """atoms.x_dof (set through atoms.do): an NVT run (md_nvt.cpp:144-215)
+    and md.min_lbfgs iterates of a 256-atom alloy with some components and
+    some whole atoms frozen."""
+    out = {}
+    path, digest = make_golden.potential(tmp, ("A", "B"))
+    c = synth.alloy((4, 4, 4), xB=0.3, sigma=0.1, T=600.0, seed=2)
+    k = np.arange(c.natoms)
+    dof = np.ones((c.natoms, 3), dtype=bool)
+    dof[k % 5 == 0, 0] = False
+    dof[k % 7 == 0, 2] = False
+    dof[k % 11 == 0] = False
+    v = c.v.copy()
+    for it in (10, 40):
+        r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A", "B"], path, v=v, kB=synth.KB)
+        r.set_dof(dof)
+        H, x, vv = r.nvt(600.0, synth.FS, it, t_relax=20.0 * synth.FS)
+        out.update({"nvt/x_%d" % it: x, "nvt/v_%d" % it: vv})
+    out["nvt/iters"] = np.array([10, 40])
+    for it in (1, 5, 20):
+        r = refmod.RefSystem(c.H, c.x, c.elem, c.masses, ["A", "B"], path)
+        r.set_dof(dof)
+        H, x, _ = r.minimize("lbfgs", it, ls="bt", m=10, e_tol=0.0)
+        out.update({"lbfgs/x_%d" % it: x, "lbfgs/pe_%d" % it: r.force()[0]})
+    out["lbfgs/iters"] = np.array([1, 5, 20])
+    out.update({"H": c.H, "x": c.x, "v": v, "elem": c.elem, "masses": c.masses, "dof": dof,
+                "sha256_AB": np.array(digest)})
+    print("dof", out["lbfgs/pe_20"])
+    return out
+
+
 def extrap_case(tmp):
     path = os.path.join(tmp, "A_extrap.setfl")
     synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
@@ -252,6 +285,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_extrap.npz"), **extrap_case(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_min.npz"), **minimizer_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_box.npz"), **box_cases(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_dof.npz"), **dof_cases(tmp))
         for name in POTENTIALS:
             np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
 

@@ -8,7 +8,8 @@ potential files shipped with the reference's examples (setfl with one and
 two elements, per-pair cutoffs, Finnis-Sinclair), host densities beyond
 rho_max, md.nvt trajectories, md.nst states, md.min_lbfgs and md.min_cg_new
 iterates (with the back-tracking, golden-section and Brent line searches, and
-with box degrees of freedom) and create_temp draws.
+with box degrees of freedom), runs with frozen components (atoms.x_dof) and
+create_temp draws.
 The oracle must reproduce them to rounding.  Where the compiled reference
 module is present (oracle/_ref), further seeded cases run live against it.
 """
@@ -199,6 +200,32 @@ def test_oracle_box_minimizers_match_reference(potentials, name):
         assert np.max(np.abs(H - g["%s/H_%d" % (name, it)])) <= 1e-10
         assert np.max(np.abs(_wrapped(o.x - g["%s/x_%d" % (name, it)], H))) <= 1e-10
         assert abs(r["pe"] - g["%s/pe_%d" % (name, it)]) <= 1e-12 * abs(r["pe"])
+
+
+def test_oracle_frozen_components_match_reference(potentials):
+    """atoms.x_dof set through atoms.do on some components and some whole
+    atoms: md.nvt positions and velocities after 10 and 40 steps, and
+    md.min_lbfgs positions and energy after 1, 5 and 20 iterations, to
+    rounding."""
+    g = golden("ref_dof")
+    path, digest = potentials[("A", "B")]
+    assert str(g["sha256_AB"]) == digest
+    e = O.Eam.setfl(path)
+    H = g["H"]
+    for it in g["nvt/iters"]:
+        o = O.System(e, H, g["x"], g["elem"], g["masses"])
+        o.set_dof(g["dof"])
+        o.v = g["v"]
+        o.nvt_run(600.0, synth.FS, synth.KB, int(it), t_relax=20.0 * synth.FS)
+        assert np.max(np.abs(_wrapped(o.x - g["nvt/x_%d" % it], H))) <= 1e-12
+        assert np.max(np.abs(o.v - g["nvt/v_%d" % it])) <= 1e-12 * np.max(np.abs(o.v))
+    for it in g["lbfgs/iters"]:
+        o = O.System(e, H, g["x"], g["elem"], g["masses"])
+        o.set_dof(g["dof"])
+        r = o.lbfgs_run(m=10, e_tol=0.0, f_tol=0.0, nsteps=int(it))
+        assert r["niter"] == it
+        assert np.max(np.abs(_wrapped(o.x - g["lbfgs/x_%d" % it], H))) <= 1e-12
+        assert abs(r["pe"] - g["lbfgs/pe_%d" % it]) <= 1e-12 * abs(r["pe"])
 
 
 def test_create_temp_matches_reference(ref):
