@@ -21,6 +21,8 @@ Fixtures:
                      degrees of freedom (H_dof), atoms free or affine
   ref_dof.npz        md.nvt and md.min_lbfgs with frozen components
                      (atoms.x_dof)
+  ref_funcfl.npz     forces, energy and stress through ff_eam_funcfl on two
+                     seeded funcfl files with different grids
   ref_extrap.npz     an FCC cell whose host densities exceed rho_max
                      (linear extrapolation of F, ff_eam.cpp:188-189)
   ref_pot_<name>.npz the knot values of a potential file shipped with the
@@ -225,6 +227,23 @@ def dof_cases(tmp):
     return out
 
 
+def funcfl_case(tmp):
+    """ff_eam_funcfl on two seeded funcfl files with different grids
+    (potfile.write_funcfl_pair): the reference's forces, energy and stress on
+    a 256-atom A/B alloy."""
+    paths = potfile.write_funcfl_pair(tmp)
+    c = synth.alloy((4, 4, 4), xB=0.4, sigma=0.1, seed=81)
+    _, res = ref_force(c.H, c.x, c.elem, c.masses, ["A", "B"], paths, "funcfl")
+    out = {"H": c.H, "x": c.x, "elem": c.elem, "masses": c.masses}
+    out.update(res)
+    import hashlib
+    for k, p in enumerate(paths):
+        with open(p, "rb") as fh:
+            out["sha256_%d" % k] = np.array(hashlib.sha256(fh.read()).hexdigest())
+    print("funcfl pe", res["pe"])
+    return out
+
+
 def extrap_case(tmp):
     path = os.path.join(tmp, "A_extrap.setfl")
     synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
@@ -286,6 +305,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_min.npz"), **minimizer_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_box.npz"), **box_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_dof.npz"), **dof_cases(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_funcfl.npz"), **funcfl_case(tmp))
         for name in POTENTIALS:
             np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
 

@@ -105,3 +105,34 @@ def from_fixture(g, prefix="pot_"):
     out["names"] = [str(n) for n in out["names"]]
     out["lattice"] = [str(n) for n in out["lattice"]]
     return out
+
+
+def write_funcfl_pair(dirname):
+    """Two seeded single-element DYNAMO funcfl files on different grids
+    (import_eam.h:68-346: a comment line; "Z mass a lattice"; "nrho drho nr
+    dr rc"; F on the rho grid, the effective charge Z on the r grid, the
+    density on the r grid), so that reading both resamples them onto the
+    coarser grid.  Returns the two paths."""
+    import os
+
+    specs = (("A", 29, 63.5, 3.615, 500, 0.05, 600, 0.01, 1.0, 1.2),
+             ("B", 28, 58.7, 3.52, 400, 0.06, 500, 0.012, 0.8, 1.5))
+    paths = []
+    for name, Z, mass, a, nrho, drho, nr, dr, z0, F0 in specs:
+        r = np.arange(nr) * dr
+        rc = 5.5
+        sw = np.where(r < rc, (1.0 - r / rc) ** 3, 0.0)
+        Zr = z0 * np.exp(-0.9 * r) * sw
+        dens = np.exp(-3.0 * (r / 2.55 - 1.0)) * sw
+        rh = np.arange(nrho) * drho
+        F = -F0 * np.sqrt(rh)
+        p = os.path.join(dirname, "%s.funcfl" % name)
+        with open(p, "w") as fh:
+            fh.write("seeded funcfl test potential %s\n" % name)
+            fh.write("%d %.17g %.17g fcc\n" % (Z, mass, a))
+            fh.write("%d %.17g %d %.17g %.17g\n" % (nrho, drho, nr, dr, rc))
+            for arr in (F, Zr, dens):
+                for k in range(0, len(arr), 5):
+                    fh.write(" ".join("%.17g" % v for v in arr[k:k + 5]) + "\n")
+        paths.append(p)
+    return paths
