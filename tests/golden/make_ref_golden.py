@@ -23,6 +23,8 @@ Fixtures:
                      (atoms.x_dof)
   ref_funcfl.npz     forces, energy and stress through ff_eam_funcfl on two
                      seeded funcfl files with different grids
+  ref_cfg.npz        files written by md.export_cfg (an alloy with its
+                     velocities, a triclinic cell)
   ref_extrap.npz     an FCC cell whose host densities exceed rho_max
                      (linear extrapolation of F, ff_eam.cpp:188-189)
   ref_pot_<name>.npz the knot values of a potential file shipped with the
@@ -244,6 +246,37 @@ def funcfl_case(tmp):
     return out
 
 
+def cfg_cases(tmp):
+    """Files written by the reference's md.export_cfg (ExportCFGMD,
+    export_cfg_md.cpp) called as (atoms, file): an alloy with its
+    velocities as an extra vector, and a triclinic cell with the default
+    vectors.  The atoms are stored in the file's (id) order."""
+    out = {}
+    path, _ = make_golden.potential(tmp, ("A", "B"))
+    M = refmod.module()
+    tric = synth.alloy((3, 3, 3), xB=0.4, sigma=0.05, T=300.0, seed=3)
+    Ht = tric.H.copy()
+    Ht[1, 0] += 2.1
+    Ht[2, 0] -= 1.3
+    Ht[2, 1] += 0.8
+    cases = {"alloy_v": (synth.alloy((3, 3, 3), xB=0.4, sigma=0.05, T=300.0, seed=2), None, ["x_d"]),
+             "tric": (tric, Ht, [])}
+    for name, (c, H, extra) in cases.items():
+        H = c.H if H is None else H
+        x = c.x @ np.linalg.inv(c.H) @ H
+        r = refmod.RefSystem(H, x, c.elem, c.masses, ["A", "B"], path, v=c.v)
+        e = M.md.export_cfg("", 1, extra_vecs=extra) if extra else M.md.export_cfg("", 1)
+        f = os.path.join(tmp, name + ".cfg")
+        e(r.sim, f)
+        Hs, xs, vs = r.state()
+        o = r.order
+        with open(f, "rb") as fh:
+            out[name + "/text"] = np.array(fh.read().decode())
+        out.update({name + "/H": Hs, name + "/x": xs[o], name + "/v": vs[o], name + "/elem": c.elem[o],
+                    name + "/masses": c.masses, name + "/with_v": np.array(bool(extra))})
+    return out
+
+
 def extrap_case(tmp):
     path = os.path.join(tmp, "A_extrap.setfl")
     synth.write_setfl(path, ("A",), drho=EXTRAP_DRHO)
@@ -306,6 +339,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "ref_box.npz"), **box_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_dof.npz"), **dof_cases(tmp))
         np.savez_compressed(os.path.join(HERE, "ref_funcfl.npz"), **funcfl_case(tmp))
+        np.savez_compressed(os.path.join(HERE, "ref_cfg.npz"), **cfg_cases(tmp))
         for name in POTENTIALS:
             np.savez_compressed(os.path.join(HERE, "ref_pot_%s.npz" % name), **potential_case(tmp, name, root))
 

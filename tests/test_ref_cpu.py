@@ -368,3 +368,18 @@ def test_library_tables_equal_oracle_on_reference_files(tmp_path, pot):
     ff = _lib.ForceField.setfl(path) if d["kind"] == "setfl" else _lib.ForceField.fs(path)
     for a, b in zip(ff.tables(), oracle_eam(d, path).tables()):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["alloy_v", "tric"])
+def test_library_cfg_writer_matches_reference(tmp_path, name):
+    """The CFG files md.export_cfg of the reference wrote (ExportCFGMD,
+    export_cfg_md.cpp): libmappg's writer (mappg_cfg_write, host code) gives
+    the same bytes for the same box, atoms, masses and velocities, in an
+    orthorhombic alloy cell with velocities and in a triclinic cell."""
+    g = golden("ref_cfg")
+    _lib.load()
+    p = str(tmp_path / (name + ".cfg"))
+    vecs = (("x_d", g[name + "/v"]),) if bool(g[name + "/with_v"]) else ()
+    _lib.write_cfg(p, g[name + "/H"], g[name + "/x"], g[name + "/elem"], g[name + "/masses"], ["A", "B"], vecs=vecs)
+    with open(p) as fh:
+        assert fh.read() == str(g[name + "/text"])
