@@ -28,6 +28,15 @@ STATIC = ["fcc_a_256", "alloy_ab_475", "thin_a_32", "tric_ab_240"]
 POTS = ["cu", "nial", "feh", "feh_fs"]
 
 
+@pytest.fixture(scope="module")
+def built():
+    """libmappg.so, built here if it is not yet (its host code only is used)."""
+    from mapp4py_gb300 import build
+
+    build.build()
+    return _lib.load()
+
+
 def voigt_to_stress(vir, H):
     """F_H (Voigt xx, xy, xz, yy, yz, zz) -> S_pe = -F_H / V (ff_md.cpp:129-134)."""
     F = np.array([[vir[0], vir[1], vir[2]], [vir[1], vir[3], vir[4]], [vir[2], vir[4], vir[5]]])
@@ -228,7 +237,7 @@ def test_oracle_frozen_components_match_reference(potentials):
         assert abs(r["pe"] - g["lbfgs/pe_%d" % it]) <= 1e-12 * abs(r["pe"])
 
 
-def test_library_funcfl_tables_match_reference(tmp_path):
+def test_library_funcfl_tables_match_reference(built, tmp_path):
     """ff_eam_funcfl (import_eam.h:68-346) on two funcfl files with
     different grids: libmappg's host table builder (mappg_ff_funcfl, no GPU
     involved) resamples them onto the common grid; the oracle, given those
@@ -371,7 +380,7 @@ def test_library_tables_equal_oracle_on_reference_files(tmp_path, pot):
 
 
 @pytest.mark.parametrize("name", ["alloy_v", "tric"])
-def test_library_cfg_writer_matches_reference(tmp_path, name):
+def test_library_cfg_writer_matches_reference(built, tmp_path, name):
     """The CFG files md.export_cfg of the reference wrote (ExportCFGMD,
     export_cfg_md.cpp): libmappg's writer (mappg_cfg_write, host code) gives
     the same bytes for the same box, atoms, masses and velocities, in an
